@@ -1,0 +1,83 @@
+"""Loader of libghostlight_gb300.so, the C-ABI of include/ghostlight_gb300.h.
+
+There is no fallback: if the shared library is missing or fails to load, every
+entry point raises.  ``load()`` builds it in-tree first when the sources are
+newer (nvcc cross-compiles without a GPU).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import threading
+
+from . import _abi
+from ._abi import (gl_filter_params, gl_flare_source, gl_ghost_pair, gl_ghost_render_params,
+                   gl_pupil_sample, gl_sampler_params, gl_spectral_sample, gl_surface)
+
+_lock = threading.Lock()
+_lib = None
+
+
+class GhostlightError(RuntimeError):
+    """A CUDA / device failure reported by the C-ABI."""
+
+
+def _declare(lib):
+    P = C.POINTER
+    i, f, vp = C.c_int, C.c_float, C.c_void_p
+    lib.gl_last_error.restype = C.c_char_p
+    lib.gl_version.restype = i
+    lib.gl_last_launch_count.restype = i
+    lib.gl_finalize_z.argtypes = [P(gl_surface), i]
+    lib.gl_enumerate_ghost_pairs.argtypes = [P(gl_surface), i, P(gl_ghost_pair), i, P(i)]
+    lib.gl_build_aperture_samples.argtypes = [P(gl_surface), i, P(gl_sampler_params),
+                                              P(gl_pupil_sample), i, P(i)]
+    lib.gl_build_spectral_table.argtypes = [i, i, P(f), P(gl_spectral_sample), P(f)]
+    lib.gl_color_matrices.argtypes = [i, P(f), i, P(f), P(f), P(f)]
+    lib.gl_filter_ghost_pairs.argtypes = [P(gl_surface), i, f, f, P(gl_filter_params),
+                                          P(gl_ghost_pair), P(f), i, P(i), P(i)]
+    lib.gl_trace_rays.argtypes = [P(gl_surface), i, i, i, vp, i, vp, vp]
+    render_args = [P(gl_surface), i, P(gl_ghost_pair), P(f), P(C.c_int32), i,
+                   P(gl_flare_source), i, P(gl_pupil_sample), P(C.c_int32), i,
+                   P(gl_spectral_sample), i, P(gl_ghost_render_params)]
+    lib.gl_render_ghosts.argtypes = render_args + [vp, vp, vp, vp]
+    lib.gl_ghost_plan_create.argtypes = render_args + [P(vp)]
+    lib.gl_ghost_plan_execute.argtypes = [vp, vp, vp, vp, vp]
+    lib.gl_ghost_plan_info.argtypes = [vp, P(C.c_longlong), P(i), P(i)]
+    lib.gl_ghost_plan_destroy.argtypes = [vp]
+    for name in dir(lib):
+        pass
+    return lib
+
+
+def load():
+    """Return the loaded library, building it first if it is stale."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    with _lock:
+        if _lib is None:
+            from . import build as _build
+            path = _build.build()
+            _lib = _declare(C.CDLL(str(path)))
+    return _lib
+
+
+def lib_path():
+    from . import build as _build
+    return _build.LIB
+
+
+def check(rc: int, what: str = "") -> None:
+    """Map a GL_* status to the reference's exception types."""
+    if rc == _abi.GL_OK:
+        return
+    msg = (_lib.gl_last_error() or b"").decode(errors="replace") if _lib is not None else ""
+    if what and not msg.startswith(what):
+        msg = "%s: %s" % (what, msg)
+    if rc in (_abi.GL_ERR_INVALID, _abi.GL_ERR_UNSUPPORTED):
+        raise ValueError(msg)
+    raise GhostlightError(msg)
+
+
+def last_launch_count() -> int:
+    return int(load().gl_last_launch_count())

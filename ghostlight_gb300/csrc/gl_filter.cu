@@ -1,0 +1,201 @@
+// gl_filter.cu — ghost-pair enumerator and energy culler on the device.
+//
+// Replaces filter_ghost_pairs (ghostlight/src/ghost.cpp:105-138).  One block
+// per enumerated pair traces the reference's probes — three axial rays at
+// 650/550/450 nm for the intensity estimate (ghost.cpp:34-50) and the 8x8
+// green probe for the area boost (ghost.cpp:53-102) — in one launch instead of
+// 67 host traces per pair.
+//
+// This translation unit is compiled IEEE-exact (-fmad=false, IEEE division
+// and square root, no flush-to-zero), so its float arithmetic equals the
+// reference host build's except inside cosf / atan2f / fmodf, which may differ
+// in the last place.  A keep/drop decision whose estimate lies within a guard
+// band of the threshold is therefore re-evaluated on the host with the
+// identical code compiled by the host compiler; the surviving set and its
+// order are the reference's bit for bit.
+#include "gl_internal.h"
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+namespace gl {
+
+namespace {
+
+constexpr int kProbeThreads = 96;   // 3 intensity rays + 64 spread probes, padded
+
+struct ProbeOut {
+    float w[3];        // per-wavelength weight of the axial ray
+    int wok[3];        // 1 when that ray reached the sensor
+    float mnx, mxx, mny, mxy;
+    int valid;
+};
+
+__global__ void __launch_bounds__(kProbeThreads)
+filter_probe_kernel(const SurfRec* __restrict__ recs, int n, const float* __restrict__ ior_at3,
+                    const float* __restrict__ ior_bf3, const int2* __restrict__ pairs,
+                    float front_R, float start_z, ProbeOut* __restrict__ out)
+{
+    __shared__ SurfRec lens[kMaxSurfaces];
+    __shared__ float at[3 * kMaxSurfaces], bf[3 * kMaxSurfaces];
+    __shared__ float px[64], py[64];
+    __shared__ int ok[64];
+    const int tid = threadIdx.x;
+    {
+        const int words = n * (int)(sizeof(SurfRec) / 4);
+        const int* src = reinterpret_cast<const int*>(recs);
+        int* dst = reinterpret_cast<int*>(lens);
+        for (int i = tid; i < words; i += blockDim.x) dst[i] = src[i];
+        for (int i = tid; i < 3 * n; i += blockDim.x) { at[i] = ior_at3[i]; bf[i] = ior_bf3[i]; }
+    }
+    __syncthreads();
+    const int2 p = pairs[blockIdx.x];
+    const float lams[3] = {650.0f, 550.0f, 450.0f};
+    ProbeOut* o = out + blockIdx.x;
+    if (tid < 3)
+    {
+        TraceOut r = trace_ghost(lens, n, at + tid * n, bf + tid * n, v3(0.0f, 0.0f, start_z),
+                                 v3(0.0f, 0.0f, 1.0f), lams[tid], p.x, p.y);
+        o->w[tid] = r.w;
+        o->wok[tid] = (r.status == 0);
+    }
+    else if (tid < 67)
+    {
+        const int k = tid - 3, gx = k % 8, gy = k / 8;
+        const float u = ((gx + 0.5f) / 8) * 2.0f - 1.0f;
+        const float v = ((gy + 0.5f) / 8) * 2.0f - 1.0f;
+        int good = 0;
+        if (!(u * u + v * v > 1.0f))
+        {
+            TraceOut r = trace_ghost(lens, n, at + n, bf + n, v3(u * front_R, v * front_R, start_z),
+                                     v3(0.0f, 0.0f, 1.0f), 550.0f, p.x, p.y);
+            if (r.status == 0) { px[k] = r.x; py[k] = r.y; good = 1; }
+        }
+        ok[k] = good;
+    }
+    __syncthreads();
+    if (tid == 0)
+    {
+        float mnx = 1e30f, mxx = -1e30f, mny = 1e30f, mxy = -1e30f;
+        int valid = 0;
+        for (int k = 0; k < 64; ++k)
+        {
+            if (!ok[k]) continue;
+            mnx = fminf(mnx, px[k]); mxx = fmaxf(mxx, px[k]);
+            mny = fminf(mny, py[k]); mxy = fmaxf(mxy, py[k]);
+            ++valid;
+        }
+        o->mnx = mnx; o->mxx = mxx; o->mny = mny; o->mxy = mxy; o->valid = valid;
+    }
+}
+
+}  // namespace
+}  // namespace gl
+
+using namespace gl;
+
+extern "C" int gl_filter_ghost_pairs(const gl_surface* surfaces, int n, float hw, float hh,
+                                     const gl_filter_params* prm, gl_ghost_pair* out_pairs,
+                                     float* out_boosts, int cap, int* n_out, int* n_rechecked)
+{
+    if (!surfaces || n <= 0 || !prm || !n_out) return fail(GL_ERR_INVALID, "filter_ghost_pairs: bad arguments");
+    std::vector<SurfRec> recs((size_t)n);
+    int rc = pack_lens(surfaces, n, recs.data());
+    if (rc) return rc;
+
+    // Enumerate (ghost.cpp:17-31) and apply the IOR-contrast test
+    // (ghost.cpp:118-125) — exact float comparisons, done here.
+    std::vector<int2> cand;
+    for (int a = 0; a < n; ++a)
+    {
+        if (!surfaces[a].is_active) continue;
+        for (int b = a + 1; b < n; ++b)
+        {
+            if (!surfaces[b].is_active) continue;
+            float iba = ior_before_nd(surfaces, a), iaa = surfaces[a].ior;
+            float ibb = ior_before_nd(surfaces, b), iab = surfaces[b].ior;
+            if (std::abs(iba - iaa) < 0.001f || std::abs(ibb - iab) < 0.001f) continue;
+            cand.push_back(make_int2(a, b));
+        }
+    }
+    int rechecked = 0;
+    int kept = 0;
+    if (!cand.empty())
+    {
+        const float lams[3] = {650.0f, 550.0f, 450.0f};
+        std::vector<float> at(3 * (size_t)n), bf(3 * (size_t)n);
+        build_ior_tables(surfaces, n, lams, 3, at.data(), bf.data());
+        const int np = (int)cand.size();
+        SurfRec* d_recs = nullptr; float* d_at = nullptr; float* d_bf = nullptr;
+        int2* d_pairs = nullptr; ProbeOut* d_out = nullptr;
+        std::vector<ProbeOut> res((size_t)np);
+        cudaError_t e = cudaSuccess;
+        auto chk = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
+        chk(cudaMalloc(&d_recs, sizeof(SurfRec) * n));
+        chk(cudaMalloc(&d_at, sizeof(float) * 3 * n));
+        chk(cudaMalloc(&d_bf, sizeof(float) * 3 * n));
+        chk(cudaMalloc(&d_pairs, sizeof(int2) * np));
+        chk(cudaMalloc(&d_out, sizeof(ProbeOut) * np));
+        if (e == cudaSuccess)
+        {
+            chk(cudaMemcpy(d_recs, recs.data(), sizeof(SurfRec) * n, cudaMemcpyHostToDevice));
+            chk(cudaMemcpy(d_at, at.data(), sizeof(float) * 3 * n, cudaMemcpyHostToDevice));
+            chk(cudaMemcpy(d_bf, bf.data(), sizeof(float) * 3 * n, cudaMemcpyHostToDevice));
+            chk(cudaMemcpy(d_pairs, cand.data(), sizeof(int2) * np, cudaMemcpyHostToDevice));
+        }
+        if (e == cudaSuccess)
+        {
+            const float front_R = surfaces[0].semi_aperture;
+            const float start_z = surfaces[0].z - kSpawnOffset;
+            filter_probe_kernel<<<np, kProbeThreads>>>(d_recs, n, d_at, d_bf, d_pairs, front_R, start_z, d_out);
+            chk(cudaGetLastError());
+            chk(cudaMemcpy(res.data(), d_out, sizeof(ProbeOut) * np, cudaMemcpyDeviceToHost));
+        }
+        cudaFree(d_recs); cudaFree(d_at); cudaFree(d_bf); cudaFree(d_pairs); cudaFree(d_out);
+        if (e != cudaSuccess)
+            return fail(e == cudaErrorMemoryAllocation ? GL_ERR_OOM : GL_ERR_CUDA,
+                        std::string("filter_ghost_pairs: ") + cudaGetErrorString(e));
+        g_last_launches = 1;
+
+        const float thr = prm->min_ghost_intensity;
+        for (int i = 0; i < np; ++i)
+        {
+            const ProbeOut& r = res[i];
+            // estimate_ghost_intensity's sum order: total += w650, w550, w450
+            float total = 0.0f;
+            for (int ch = 0; ch < 3; ++ch)
+                if (r.wok[ch]) total += r.w[ch];
+            float est = total / 3.0f;
+            const float band = 1e-4f * std::fabs(thr);
+            if (!(std::fabs(est - thr) > band))
+            {
+                est = host_intensity_estimate(surfaces, recs.data(), n, cand[i].x, cand[i].y);
+                ++rechecked;
+            }
+            if (est < thr) continue;
+            float boost = 1.0f;
+            if (prm->ghost_normalize)
+            {
+                if (r.valid >= 2)
+                {
+                    float gw = std::max(r.mxx - r.mnx, 0.01f), gh = std::max(r.mxy - r.mny, 0.01f);
+                    float area = (gw * gh) / ((2.0f * hw) * (2.0f * hh));
+                    boost = (area < 1.0f) ? 1.0f : (prm->max_area_boost < area) ? prm->max_area_boost : area;
+                }
+            }
+            if (out_pairs && kept < cap)
+            {
+                out_pairs[kept] = {cand[i].x, cand[i].y};
+                if (out_boosts) out_boosts[kept] = boost;
+            }
+            ++kept;
+        }
+    }
+    *n_out = kept;
+    if (n_rechecked) *n_rechecked = rechecked;
+    if (out_pairs && kept > cap) return fail(GL_ERR_INVALID, "filter_ghost_pairs: capacity too small");
+    return GL_OK;
+}

@@ -1,0 +1,52 @@
+// gl_internal.h — declarations shared by the translation units of
+// libghostlight_gb300 (host builders, culler, render, starburst, conv).
+#pragma once
+
+#include "ghostlight_gb300.h"
+#include "gl_trace.cuh"
+
+#include <string>
+#include <vector>
+
+namespace gl {
+
+extern thread_local std::string g_last_error;
+extern thread_local int g_last_launches;
+int fail(int code, const std::string& msg);
+
+// Entrance-pupil silhouette (aperture_sampler.h:49-83), plain polygon form.
+struct PupilMask {
+    float aspect = 1.0f;
+    int n_blades = 0;
+    float rot_rad = 0.0f;
+    float apothem = 1.0f;
+    float sector = 1.0f;
+};
+
+int pack_lens(const gl_surface* in, int n, SurfRec* out);
+float ior_at(const gl_surface& s, float lam);
+float ior_before_nd(const gl_surface* s, int idx);
+void build_ior_tables(const gl_surface* s, int n, const float* lambdas, int n_lam, float* at, float* bf);
+PupilMask resolve_pupil_mask(const gl_surface* surfs, int n, int blades_override, float rotation_deg);
+bool pupil_contains(const PupilMask& m, float u, float v);
+int build_aperture_samples(const gl_surface* surfs, int n, const gl_sampler_params& p,
+                           std::vector<gl_pupil_sample>& out);
+int output_matrix(int cs, const float* custom, float M[9]);
+int input_matrix(int cs, const float* custom, float M[9]);
+std::vector<gl_spectral_sample> spectral_table(int n, float lmin, float lmax, const float M[9]);
+void spectral_correction(const std::vector<gl_spectral_sample>& tn, float lmin, float lmax,
+                         const float M[9], float C[9]);
+float host_intensity_estimate(const gl_surface* s, const SurfRec* recs, int n, int a, int b);
+float host_spread_boost(const gl_surface* s, const SurfRec* recs, int n, int a, int b,
+                        float hw, float hh, float max_boost);
+
+}  // namespace gl
+
+#define GL_CUDA_TRY(expr)                                                          \
+    do {                                                                           \
+        cudaError_t _e = (expr);                                                   \
+        if (_e != cudaSuccess)                                                     \
+            return ::gl::fail(_e == cudaErrorMemoryAllocation ? GL_ERR_OOM         \
+                                                              : GL_ERR_CUDA,       \
+                              std::string(#expr) + ": " + cudaGetErrorString(_e)); \
+    } while (0)

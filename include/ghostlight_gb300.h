@@ -1,0 +1,243 @@
+/*
+ * ghostlight_gb300.h — C-ABI of the GB300 flare hot path.
+ *
+ * Plain C: fixed-layout structs, raw pointers and sizes, int status codes.
+ * Device pointers are CUDA global-memory addresses (for example a torch
+ * tensor's data_ptr()); `stream` is a cudaStream_t passed as void*.
+ * The library never frees caller memory.  Every entry point returns GL_OK (0)
+ * or a negative GL_ERR_* code; gl_last_error() gives the message of the last
+ * failure on the calling thread.
+ *
+ * Each declaration names the reference interface it replaces
+ * (JaydenB/ghostlight, path within that project, file:line).
+ */
+#ifndef GHOSTLIGHT_GB300_H
+#define GHOSTLIGHT_GB300_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define GL_OK                0
+#define GL_ERR_INVALID      -1   /* bad argument (maps to ValueError)        */
+#define GL_ERR_OOM          -2   /* device allocation failed                 */
+#define GL_ERR_CUDA         -3   /* CUDA launch / runtime error              */
+#define GL_ERR_TIMEOUT      -4   /* a bounded device wait gave up            */
+#define GL_ERR_BUDGET       -5   /* request above the admission budget       */
+#define GL_ERR_NO_DEVICE    -6   /* no CUDA device                           */
+#define GL_ERR_UNSUPPORTED  -7   /* feature outside the implemented path     */
+
+/* ---- enums (values match ghostlight/src/optical_system.h:54-97) ---------- */
+#define GL_FORM_SPHERE        0
+#define GL_FORM_ASPHERE       1
+#define GL_FORM_CYLINDRICAL   2
+#define GL_CYL_AXIS_X         0
+#define GL_CYL_AXIS_Y         1
+#define GL_APERTURE_CIRCLE    0
+#define GL_APERTURE_POLYGON   1
+#define GL_APERTURE_IMAGE     2
+#define GL_DISP_AIR           0
+#define GL_DISP_ABBE          1
+#define GL_DISP_SELLMEIER     2
+#define GL_COATING_SIMPLE     0
+#define GL_COATING_ATTENUATOR 4
+#define GL_COATING_ARTIST     5
+
+/* TraceStatus, ghostlight/src/trace_event.h:13-19 */
+#define GL_TRACE_OK             0
+#define GL_TRACE_VIGNETTED      1
+#define GL_TRACE_TIR            2
+#define GL_TRACE_MISSED_SURFACE 3
+#define GL_TRACE_INVALID_INPUT  4
+
+/* Output colour spaces, ghostlight/src/spectral.h:24-31 */
+#define GL_CS_ACESCG      0
+#define GL_CS_SRGB_LINEAR 1
+#define GL_CS_P3_D65      2
+#define GL_CS_P3_D60      3
+#define GL_CS_XYZ         4
+#define GL_CS_CUSTOM      5
+/* Input colour spaces, ghostlight/src/spectral.h:18-22 */
+#define GL_CS_INPUT_ACESCG      0
+#define GL_CS_INPUT_SRGB_LINEAR 1
+#define GL_CS_INPUT_CUSTOM      2
+
+/* ---- data formats ------------------------------------------------------- */
+
+/* One sequential surface.  Field meaning follows struct Surface,
+ * ghostlight/src/optical_system.h:157-249 (the trace-facing subset: table and
+ * image-backed coatings/apertures are not part of this path).  All fields are
+ * 4 bytes so the layout is identical in C, C++, CUDA and ctypes. */
+typedef struct gl_surface {
+    float   radius;                 /* signed radius (mm), 0 = flat          */
+    float   thickness;              /* axial gap to the next surface (mm)    */
+    float   ior;                    /* n_d of the medium after the surface   */
+    float   abbe_v;                 /* V_d of the medium after the surface   */
+    float   semi_aperture;          /* clear semi-diameter (mm)              */
+    float   z;                      /* world vertex z (mm); sensor at z = 0  */
+    int32_t is_stop;
+    int32_t is_active;
+    int32_t aperture_shape;         /* GL_APERTURE_*                         */
+    int32_t aperture_blades;
+    float   aperture_rotation_rad;
+    float   aperture_aspect;
+    float   aperture_curvature;     /* blade shape; all 0 = plain polygon    */
+    float   aperture_twist;
+    float   aperture_notch_rad;
+    float   aperture_notch_angle_rad;
+    float   decenter_x, decenter_y;
+    float   rot[9];                 /* row-major local->world rotation       */
+    int32_t form;                   /* GL_FORM_*                             */
+    float   conic_k;
+    float   asphere_terms[8];       /* A4, A6, ... A18                       */
+    int32_t n_asphere_terms;
+    int32_t cyl_axis;               /* GL_CYL_AXIS_*                         */
+    int32_t disp_model;             /* GL_DISP_*                             */
+    float   sellmeier_B[3];
+    float   sellmeier_C[3];         /* um^2                                  */
+    int32_t coating_model;          /* GL_COATING_*                          */
+    int32_t ar_layers;              /* SIMPLE: 0 bare, 1 MgF2, 2+ multi      */
+    float   tint_r, tint_g, tint_b, tint_strength;        /* ARTIST          */
+    float   gauss_sigma, gauss_background, gauss_peak;    /* ATTENUATOR      */
+    float   gauss_decenter_x, gauss_decenter_y;
+} gl_surface;
+
+/* GPUSpectralSample, ghostlight/src/spectral.h:46-50 */
+typedef struct gl_spectral_sample { float lambda, cmf_r, cmf_g, cmf_b; } gl_spectral_sample;
+/* ApertureSample, ghostlight/src/aperture_sampler.h:21 */
+typedef struct gl_pupil_sample { float u, v; } gl_pupil_sample;
+/* GhostPair, ghostlight/src/ghost.h:12-16 */
+typedef struct gl_ghost_pair { int32_t surf_a, surf_b; } gl_ghost_pair;
+/* FlareSource, ghostlight/src/ghost.h:18-23 (angles in radians) */
+typedef struct gl_flare_source { float angle_x, angle_y, r, g, b; } gl_flare_source;
+
+/* ApertureSamplerParams, ghostlight/src/aperture_sampler.h:28-42 */
+typedef struct gl_sampler_params {
+    int32_t ray_grid;
+    int32_t pupil_jitter;           /* 0 regular, 1 wang hash, 2 Halton      */
+    int32_t jitter_seed;
+    int32_t blades_override;        /* 0 = derive from the stop              */
+    float   rotation_deg;
+} gl_sampler_params;
+
+/* The FlareConfig fields filter_ghost_pairs reads,
+ * ghostlight/src/render_config.h:281-284 */
+typedef struct gl_filter_params {
+    float   min_ghost_intensity;
+    int32_t ghost_normalize;
+    float   max_area_boost;
+} gl_filter_params;
+
+/* ---- errors ------------------------------------------------------------- */
+const char* gl_last_error(void);
+int         gl_version(void);
+
+/* ---- host builders (no GPU) -------------------------------------------- */
+
+/* OpticalSystem::finalize, ghostlight/src/optical_system.cpp:1425 —
+ * lays z so the chain ends at the sensor (z = 0). */
+int gl_finalize_z(gl_surface* surfaces, int n);
+
+/* enumerate_ghost_pairs, ghostlight/src/ghost.cpp:17-31 */
+int gl_enumerate_ghost_pairs(const gl_surface* surfaces, int n,
+                             gl_ghost_pair* out, int cap, int* n_out);
+
+/* build_aperture_samples, ghostlight/src/aperture_sampler.h:180-223 */
+int gl_build_aperture_samples(const gl_surface* surfaces, int n,
+                              const gl_sampler_params* p,
+                              gl_pupil_sample* out, int cap, int* n_out);
+
+/* build_spectral_table + compute_spectral_correction,
+ * ghostlight/src/spectral.cpp:317-369 and :419 (CIE 1931 sensor).
+ * correction_out (9 floats, row-major) may be NULL. */
+int gl_build_spectral_table(int n_samples, int output_cs,
+                            const float* custom_xyz_to_output /* 9 or NULL */,
+                            gl_spectral_sample* out, float* correction_out);
+
+/* resolve_input_matrix / resolve_output_matrix, ghostlight/src/spectral.cpp:186,247 */
+int gl_color_matrices(int input_cs, const float* custom_in, int output_cs,
+                      const float* custom_out, float* m_in9, float* m_out9);
+
+/* ---- device entry points ------------------------------------------------ */
+
+/* filter_ghost_pairs, ghostlight/src/ghost.cpp:105-138 (+ the estimators at
+ * :34-102).  The per-pair probe traces run as one device launch; decisions
+ * whose device estimate lies within a guard band of the threshold are
+ * re-evaluated on the host in the reference's own FP32 arithmetic, so the
+ * surviving set and its order are the reference's.  Synchronous. */
+int gl_filter_ghost_pairs(const gl_surface* surfaces, int n,
+                          float sensor_half_w, float sensor_half_h,
+                          const gl_filter_params* params,
+                          gl_ghost_pair* out_pairs, float* out_boosts,
+                          int cap, int* n_out, int* n_rechecked);
+
+/* trace_ghost_ray / trace_primary_ray, ghostlight/src/trace.cpp:171,243,
+ * batched.  d_rays: n_rays x 7 floats (ox,oy,oz, dx,dy,dz, lambda_nm);
+ * d_out: n_rays x 5 floats (x,y,z, weight, status).  bounce_b < 0 traces a
+ * primary ray.  Asynchronous on `stream`. */
+int gl_trace_rays(const gl_surface* surfaces, int n,
+                  int bounce_a, int bounce_b,
+                  const float* d_rays, int n_rays, float* d_out, void* stream);
+
+/* Ghost render: the main scatter of launch_ghost_render,
+ * ghostlight/src/ghost_render.cu:630-1442 (kernel :209-491, colour
+ * correction :610-622).  All pairs x sources are traced by ONE persistent
+ * launch (or, with plain_per_pair, one launch per pair — the reference's
+ * per-ghost loop shape, ghost_render.cu:1544-1557, kept as a baseline).
+ * pair_grid[i] selects which pupil grid pair i samples (adaptive grids);
+ * grid_offsets has n_grids+1 entries into `samples`.
+ * Outputs are planar float32 W x H, overwritten.  Asynchronous. */
+typedef struct gl_ghost_render_params {
+    int32_t width, height;
+    int32_t fmt_w, fmt_h, fmt_x0, fmt_y0;
+    float   sensor_half_w, sensor_half_h;
+    float   flare_gain;
+    int32_t apply_correction;
+    float   correction[9];
+    int32_t plain_per_pair;          /* 1 = one launch per pair (baseline)  */
+    int32_t splat_mode;              /* 0 = bilinear point splat (reference) */
+} gl_ghost_render_params;
+
+int gl_render_ghosts(const gl_surface* surfaces, int n_surfaces,
+                     const gl_ghost_pair* pairs, const float* area_boosts,
+                     const int32_t* pair_grid, int n_pairs,
+                     const gl_flare_source* sources, int n_sources,
+                     const gl_pupil_sample* samples, const int32_t* grid_offsets,
+                     int n_grids,
+                     const gl_spectral_sample* spec, int n_spec,
+                     const gl_ghost_render_params* params,
+                     float* d_out_r, float* d_out_g, float* d_out_b,
+                     void* stream);
+
+/* The same render split into a resident plan (all uploads, synchronous) and
+ * an execute step that only enqueues kernels on `stream` (so it can be
+ * captured in a CUDA graph and replayed).  Same arguments as
+ * gl_render_ghosts.  A plan may be executed any number of times; executes
+ * of one plan must not overlap on the device (they share its accumulator). */
+typedef struct gl_ghost_plan gl_ghost_plan;
+int gl_ghost_plan_create(const gl_surface* surfaces, int n_surfaces,
+                         const gl_ghost_pair* pairs, const float* area_boosts,
+                         const int32_t* pair_grid, int n_pairs,
+                         const gl_flare_source* sources, int n_sources,
+                         const gl_pupil_sample* samples, const int32_t* grid_offsets,
+                         int n_grids,
+                         const gl_spectral_sample* spec, int n_spec,
+                         const gl_ghost_render_params* params, gl_ghost_plan** out);
+int gl_ghost_plan_execute(gl_ghost_plan* plan, float* d_out_r, float* d_out_g,
+                          float* d_out_b, void* stream);
+/* rays = ray-wavelength traces per execute; n_items = 256-sample work items;
+ * grid = CTAs of the persistent launch. */
+int gl_ghost_plan_info(const gl_ghost_plan* plan, long long* rays, int* n_items, int* grid);
+int gl_ghost_plan_destroy(gl_ghost_plan* plan);
+
+/* Number of kernel launches issued by the last device call on this thread. */
+int gl_last_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GHOSTLIGHT_GB300_H */
