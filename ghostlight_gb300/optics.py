@@ -1,0 +1,268 @@
+"""Lens data model mirroring the reference bindings (bind_geometry.cpp,
+bind_trace.cpp): Surface, Coating, OpticalSystem, Ray, Vec3f, TraceResult
+and the enums, with the same attribute names.  A Surface is a view of one
+plain-C ``gl_surface`` record, so a lens is handed to the C-ABI as one
+contiguous array without conversion.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import enum
+from typing import List
+
+import numpy as np
+
+from ._abi import default_surface, gl_surface
+
+
+class SurfaceForm(enum.IntEnum):
+    SPHERE = 0
+    ASPHERE = 1
+    CYLINDRICAL = 2
+
+
+class CylinderAxis(enum.IntEnum):
+    X = 0
+    Y = 1
+
+
+class ApertureShape(enum.IntEnum):
+    CIRCLE = 0
+    POLYGON = 1
+    IMAGE = 2
+
+
+class DispersionModel(enum.IntEnum):
+    AIR = 0
+    ABBE = 1
+    SELLMEIER = 2
+
+
+class CoatingModel(enum.IntEnum):
+    SIMPLE = 0
+    SPECTRAL = 1
+    ANGULAR = 2
+    SPECTRAL_ANGULAR = 3
+    ATTENUATOR_GAUSS = 4
+    ARTIST = 5
+
+
+class TraceStatus(enum.IntEnum):
+    OK = 0
+    VIGNETTED = 1
+    TIR = 2
+    MISSED_SURFACE = 3
+    INVALID_INPUT = 4
+
+
+class Vec3f:
+    __slots__ = ("x", "y", "z")
+
+    def __init__(self, x=0.0, y=0.0, z=0.0):
+        self.x, self.y, self.z = float(x), float(y), float(z)
+
+    def __iter__(self):
+        return iter((self.x, self.y, self.z))
+
+    def __repr__(self):
+        return "Vec3f(%g, %g, %g)" % (self.x, self.y, self.z)
+
+
+class Ray:
+    """Ray (ray.h): origin, normalised direction, wavelength in nm."""
+
+    def __init__(self, origin=None, dir=None, lambda_=587.56):
+        self.origin = origin if origin is not None else Vec3f()
+        self.dir = dir if dir is not None else Vec3f(0.0, 0.0, 1.0)
+        self.lambda_ = float(lambda_)
+
+    # `lambda` is a Python keyword; the reference binding exposes it as .lambda_
+    @property
+    def wavelength(self):
+        return self.lambda_
+
+
+class TraceResult:
+    __slots__ = ("position", "weight", "status")
+
+    def __init__(self, position, weight, status):
+        self.position, self.weight, self.status = position, float(weight), TraceStatus(int(status))
+
+    def __repr__(self):
+        return "TraceResult(status=%d, weight=%g)" % (int(self.status), self.weight)
+
+
+class Coating:
+    """View of the coating fields of one surface record (optical_system.h:109-147)."""
+
+    _MAP = {"ar_layers": "ar_layers", "tint_r": "tint_r", "tint_g": "tint_g", "tint_b": "tint_b",
+            "tint_strength": "tint_strength", "gauss_sigma": "gauss_sigma",
+            "gauss_background": "gauss_background", "gauss_peak": "gauss_peak",
+            "gauss_decenter_x": "gauss_decenter_x", "gauss_decenter_y": "gauss_decenter_y"}
+
+    def __init__(self, rec: gl_surface):
+        object.__setattr__(self, "_rec", rec)
+
+    @property
+    def model(self):
+        return CoatingModel(self._rec.coating_model)
+
+    @model.setter
+    def model(self, v):
+        self._rec.coating_model = int(v)
+
+    def __getattr__(self, k):
+        if k in Coating._MAP:
+            return getattr(self._rec, Coating._MAP[k])
+        raise AttributeError(k)
+
+    def __setattr__(self, k, v):
+        if k == "model":
+            self._rec.coating_model = int(v)
+        elif k in Coating._MAP:
+            setattr(self._rec, Coating._MAP[k], v)
+        else:
+            raise AttributeError("Coating has no field %r" % k)
+
+
+class Surface:
+    """One sequential surface (optical_system.h:157-249)."""
+
+    def __init__(self, rec: gl_surface | None = None):
+        object.__setattr__(self, "_rec", rec if rec is not None else default_surface())
+
+    @property
+    def coating(self) -> Coating:
+        return Coating(self._rec)
+
+    @property
+    def record(self) -> gl_surface:
+        return self._rec
+
+    def ior_at(self, lambda_nm: float) -> float:
+        """Surface::ior_at (optical_system.h:230-235), float32 arithmetic."""
+        f = np.float32
+        r = self._rec
+        lam = f(lambda_nm)
+        if r.disp_model == DispersionModel.SELLMEIER:
+            l = lam * f(1e-3)
+            l2 = l * l
+            n2 = f(1.0)
+            for k in range(3):
+                n2 = f(n2 + f(r.sellmeier_B[k]) * l2 / (l2 - f(r.sellmeier_C[k])))
+            return float(np.sqrt(n2)) if n2 > 0 else 1.0
+        nd, vd = f(r.ior), f(r.abbe_v)
+        if vd < f(0.1) or nd <= f(1.0001):
+            return float(nd)
+        lF, lC, ld = f(486.13), f(656.27), f(587.56)
+        dn = (nd - f(1.0)) / vd
+        B = dn / (f(1.0) / (lF * lF) - f(1.0) / (lC * lC))
+        A = nd - B * (f(1.0) / (ld * ld))
+        return float(A + B / (lam * lam))
+
+    def __getattr__(self, k):
+        return getattr(object.__getattribute__(self, "_rec"), k)
+
+    def __setattr__(self, k, v):
+        rec = object.__getattribute__(self, "_rec")
+        if not hasattr(rec, k):
+            raise AttributeError("Surface has no field %r" % k)
+        if k in ("is_stop", "is_active"):
+            v = int(bool(v))
+        elif isinstance(v, enum.IntEnum):
+            v = int(v)
+        setattr(rec, k, v)
+
+    def copy(self) -> "Surface":
+        r = gl_surface()
+        C.pointer(r)[0] = self._rec
+        return Surface(r)
+
+
+class OpticalSystem:
+    """Flat sequential lens (optical_system.h:305-416): sensor at z = 0,
+    light travelling in +z."""
+
+    def __init__(self, surfaces=None, name: str = "", focal_length: float = 0.0):
+        self.name = name
+        self.focal_length = float(focal_length)
+        self.surfaces: List[Surface] = []
+        for s in surfaces or []:
+            self.surfaces.append(s if isinstance(s, Surface) else Surface(s))
+        self._calib = None
+        self._calib_key = None
+
+    @classmethod
+    def from_records(cls, recs, name: str = "", focal_length: float = 0.0):
+        out = cls(name=name, focal_length=focal_length)
+        for r in recs:
+            rr = gl_surface()
+            C.pointer(rr)[0] = r
+            out.surfaces.append(Surface(rr))
+        return out
+
+    def num_surfaces(self) -> int:
+        return len(self.surfaces)
+
+    def to_array(self):
+        arr = (gl_surface * len(self.surfaces))()
+        for i, s in enumerate(self.surfaces):
+            arr[i] = s.record
+        return arr
+
+    def records(self):
+        return [s.record for s in self.surfaces]
+
+    def state_key(self) -> bytes:
+        return bytes(self.to_array())
+
+    def finalize(self) -> bool:
+        """OpticalSystem::finalize (optical_system.cpp:1425)."""
+        if not self.surfaces:
+            return False
+        from . import _native
+        arr = self.to_array()
+        _native.check(_native.load().gl_finalize_z(arr, len(arr)), "finalize")
+        for i, s in enumerate(self.surfaces):
+            s.z = arr[i].z
+        return True
+
+    def ior_before(self, idx: int, lambda_nm: float | None = None) -> float:
+        """OpticalSystem::ior_before (optical_system.h:385-402)."""
+        idx = min(idx, len(self.surfaces))
+        for k in range(idx - 1, -1, -1):
+            if self.surfaces[k].is_active:
+                s = self.surfaces[k]
+                return float(np.float32(s.ior)) if lambda_nm is None else s.ior_at(lambda_nm)
+        return 1.0
+
+    # Cached helpers mirroring ghostlight/bindings/python/ghostlight/optical_system.py
+    def calibration(self, *, d_line_nm: float = 587.56):
+        from .calibration import calibrate_lens
+        key = (self.state_key(), d_line_nm)
+        if self._calib is None or self._calib_key != key:
+            self._calib = calibrate_lens(self, d_line_nm)
+            self._calib_key = key
+        return self._calib
+
+    def ghost_pairs(self):
+        from .flare import enumerate_ghost_pairs
+        return enumerate_ghost_pairs(self)
+
+    def filter_ghosts(self, config, *, calib=None):
+        from .flare import filter_ghost_pairs
+        cal = calib if calib is not None else self.calibration()
+        return filter_ghost_pairs(self, cal.sensor_half_w, cal.sensor_half_h, config)
+
+    def render_point_flare(self, width, height, config, *, calib=None):
+        from .flare import render_point_flare
+        cal = calib if calib is not None else self.calibration()
+        return render_point_flare(width, height, self, cal, config)
+
+    def render_source_flare(self, offsets, width, height, config, *, calib=None):
+        from .flare import render_source_flare
+        cal = calib if calib is not None else self.calibration()
+        return render_source_flare(offsets, width, height, self, cal, config)
+
+    def __repr__(self):
+        return "OpticalSystem(name=%r, surfaces=%d)" % (self.name, len(self.surfaces))

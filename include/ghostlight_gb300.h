@@ -173,6 +173,7 @@ int gl_filter_ghost_pairs(const gl_surface* surfaces, int n,
                           float sensor_half_w, float sensor_half_h,
                           const gl_filter_params* params,
                           gl_ghost_pair* out_pairs, float* out_boosts,
+                          float* out_footprint_mm /* 2 per pair or NULL */,
                           int cap, int* n_out, int* n_rechecked);
 
 /* trace_ghost_ray / trace_primary_ray, ghostlight/src/trace.cpp:171,243,

@@ -1,0 +1,215 @@
+"""GPU parity of the flare path: device culler, device trace, batched
+render, against the reference's recorded outputs and the FP64 oracle.
+
+Tolerances (stated by the benchmark spec): ghost set and pupil mask bit-exact;
+FP32 images within 1e-3 relative L2 of the FP64 oracle.
+"""
+import numpy as np
+import pytest
+
+from conftest import LENS_NAMES, lens_from_pins, rel_l2
+from oracle import oracle as O
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+IMG_TOL = 1e-3
+
+
+def _lens(pins, name):
+    from ghostlight_gb300.optics import OpticalSystem
+    return OpticalSystem.from_records(lens_from_pins(pins, name))
+
+
+@pytest.mark.parametrize("name", LENS_NAMES)
+def test_device_trace_matches_reference_rays(pins, name):
+    import ghostlight_gb300 as gl
+    lens = _lens(pins, name)
+    k = 0
+    while "%s/rays_%d/ab" % (name, k) in pins:
+        a, b = (int(x) for x in pins["%s/rays_%d/ab" % (name, k)])
+        rays = torch.from_numpy(pins["%s/rays_%d/in" % (name, k)]).cuda()
+        want = pins["%s/rays_%d/out" % (name, k)]
+        got = gl.trace_rays(lens, rays, a, b).cpu().numpy()
+        agree = (got[:, 4] == want[:, 4]).mean()
+        assert agree >= 0.99, (name, k, agree)
+        ok = (got[:, 4] == 0) & (want[:, 4] == 0)
+        if ok.any():
+            d = np.abs(got[ok, :2].astype(np.float64) - want[ok, :2])
+            assert np.median(d) < 1e-3 and np.percentile(d, 99) < 5e-2, (name, k)
+            rw = np.abs(got[ok, 3] - want[ok, 3]) / np.maximum(np.abs(want[ok, 3]), 1e-30)
+            assert np.median(rw) < 1e-4
+        k += 1
+
+
+@pytest.mark.parametrize("name", LENS_NAMES)
+@pytest.mark.parametrize("thr", ["1e-7", "1e-6", "1e-4", "0"])
+def test_device_culler_ghost_set_bit_exact(pins, meta, name, thr):
+    from ghostlight_gb300 import FlareConfig
+    from ghostlight_gb300.flare import filter_ghosts_device
+    lens = _lens(pins, name)
+    cal = meta[name]["calibration"]
+    cfg = FlareConfig(min_ghost_intensity=float(thr))
+    r = filter_ghosts_device(lens, cal["sensor_half_w"], cal["sensor_half_h"], cfg)
+    np.testing.assert_array_equal(r.pairs, pins["%s/filter_%s/pairs" % (name, thr)])
+    want_b = pins["%s/filter_%s/boosts" % (name, thr)]
+    np.testing.assert_allclose(r.boosts, want_b, rtol=1e-5)
+
+
+def _plan_vs_oracle(lens, cal, pairs, boosts, grids, pair_grid, spec, W, H, src, gain=1000.0,
+                    plain=False, correction=False):
+    from ghostlight_gb300.flare import GhostRenderPlan, spectral_table
+    hw, hh = cal["sensor_half_w"], cal["sensor_half_h"]
+    _, corr = spectral_table(len(spec))
+    plan = GhostRenderPlan(lens, pairs, boosts, src, grids, pair_grid, spec, corr, W, H, hw, hh, gain,
+                           apply_correction=correction, plain_per_pair=plain)
+    out = [torch.zeros((H, W), dtype=torch.float32, device="cuda") for _ in range(3)]
+    plan.execute(*out)
+    torch.cuda.synchronize()
+    got = np.stack([o.cpu().numpy() for o in out])
+    want = O.render(lens.records(), pairs, boosts, src, grids, spec, hw, hh, W, H, gain,
+                    pair_grid=pair_grid, fp64=True)
+    if correction:
+        want = np.einsum("ij,jhw->ihw", corr.astype(np.float64), want)
+    plan.close()
+    return got, want
+
+
+def test_render_cfg1_matches_fp64_oracle(pins, meta, ref_images):
+    """Configuration 1 (12-surface double Gauss, 30 non-crossing pairs, 8
+    wavelengths, 10 deg source) at 128^2 pupil samples, 512^2 output."""
+    lens = _lens(pins, "cfg1_double_gauss_12")
+    cal = meta["cfg1_double_gauss_12"]["calibration"]
+    pairs, boosts = ref_images["cfg1_small/pairs"], ref_images["cfg1_small/boosts"]
+    spec = ref_images["cfg1_small/spec"]
+    grid = O.aperture_samples(lens.records(), 128, 0)
+    src = ref_images["cfg1_small/source"]
+    got, want = _plan_vs_oracle(lens, cal, pairs, boosts, [grid], np.zeros(len(pairs), np.int32), spec,
+                                512, 512, src)
+    assert want.sum() > 0
+    assert rel_l2(got, want) < IMG_TOL
+
+
+def test_render_correction_and_plain_mode(pins, meta, ref_images):
+    lens = _lens(pins, "cfg1_double_gauss_12")
+    cal = meta["cfg1_double_gauss_12"]["calibration"]
+    pairs, boosts = ref_images["cfg1_small/pairs"], ref_images["cfg1_small/boosts"]
+    spec = ref_images["cfg1_small/spec"]
+    grid = O.aperture_samples(lens.records(), 96, 1, 3)
+    src = np.array([[0.12, -0.05, 1.0, 0.7, 0.4]], np.float32)
+    got_c, want_c = _plan_vs_oracle(lens, cal, pairs, boosts, [grid], np.zeros(len(pairs), np.int32), spec,
+                                    301, 203, src, correction=True)
+    assert rel_l2(got_c, want_c) < IMG_TOL
+    got_p, want_p = _plan_vs_oracle(lens, cal, pairs, boosts, [grid], np.zeros(len(pairs), np.int32), spec,
+                                    301, 203, src, correction=True, plain=True)
+    assert rel_l2(got_p, got_c) < 1e-5
+
+
+def test_render_adaptive_grids_cfg2_matches_oracle(pins, meta):
+    """Configuration 2 lens (24 surfaces, two aspheres) with uneven per-pair
+    pupil grids in one persistent launch."""
+    import ghostlight_gb300 as gl
+    from ghostlight_gb300.flare import filter_ghosts_device, pupil_grid, spectral_table
+    lens = _lens(pins, "cfg2_wide_angle_24")
+    cal = meta["cfg2_wide_angle_24"]["calibration"]
+    cfg = gl.FlareConfig(min_ghost_intensity=1e-6)
+    fr = filter_ghosts_device(lens, cal["sensor_half_w"], cal["sensor_half_h"], cfg)
+    pairs, boosts = fr.pairs[::5], fr.boosts[::5]
+    sizes = [16, 32, 48, 64]
+    grids = [pupil_grid(lens, g) for g in sizes]
+    pair_grid = np.arange(len(pairs), dtype=np.int32) % len(sizes)
+    spec, _ = spectral_table(31)
+    src = np.array([[np.radians(15.0), 0.0, 1.0, 1.0, 1.0]], np.float32)
+    got, want = _plan_vs_oracle(lens, cal, pairs, boosts, grids, pair_grid, spec, 256, 256, src)
+    assert want.sum() > 0
+    assert rel_l2(got, want) < IMG_TOL
+
+
+@pytest.mark.parametrize("golden", ["refgpu_pfs_dg_axial_c0", "refgpu_ab_dg_axial", "refgpu_ab_hex_axial"])
+def test_render_matches_reference_gpu_golden(pins, meta, ref_images, golden):
+    """Against the reference renderer's own GPU output (validation/goldens,
+    concentration off): same lens, sampling, spectral table and gain."""
+    import ghostlight_gb300 as gl
+    m = meta[golden]
+    lens = _lens(pins, m["lens"])
+    cal = gl.LensCalibration.from_dict(meta[m["lens"]]["calibration"])
+    cfg = gl.PointFlareConfig(ray_grid=m["ray_grid"], spectral_samples=m["spectral_samples"],
+                              pupil_jitter=m["pupil_jitter"], jitter_seed=m["jitter_seed"],
+                              flare_gain=m["flare_gain"], min_ghost_intensity=m["min_ghost_intensity"],
+                              source_r=m["source_rgb"], source_g=m["source_rgb"], source_b=m["source_rgb"])
+    if m["sensor_half"] != "calib":
+        cfg.sensor_half_w = cfg.sensor_half_h = float(m["sensor_half"])
+    else:
+        cfg.sensor_half_w, cfg.sensor_half_h = cal.sensor_half_w, cal.sensor_half_h
+    out = gl.render_point_flare(m["W"], m["H"], lens, cal, cfg, source_angle=(0.0, 0.0))
+    got = np.stack([out[k].cpu().numpy() for k in ("ghost_r", "ghost_g", "ghost_b")], -1)
+    want = ref_images[golden + "/image"]
+    assert got.shape == want.shape
+    assert rel_l2(got, want) < IMG_TOL
+
+
+def test_graph_capture_replays_plan(pins, meta, ref_images):
+    from ghostlight_gb300.flare import GhostRenderPlan
+    lens = _lens(pins, "cfg1_double_gauss_12")
+    cal = meta["cfg1_double_gauss_12"]["calibration"]
+    pairs, boosts = ref_images["cfg1_small/pairs"], ref_images["cfg1_small/boosts"]
+    spec, corr = ref_images["cfg1_small/spec"], ref_images["cfg1_small/corr"]
+    grid = O.aperture_samples(lens.records(), 64, 0)
+    src = ref_images["cfg1_small/source"]
+    plan = GhostRenderPlan(lens, pairs, boosts, src, [grid], None, spec, corr, 256, 256,
+                           cal["sensor_half_w"], cal["sensor_half_h"], 1000.0)
+    eager = [torch.zeros((256, 256), device="cuda") for _ in range(3)]
+    plan.execute(*eager)
+    torch.cuda.synchronize()
+    outs = [torch.zeros((256, 256), device="cuda") for _ in range(3)]
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(s):
+        plan.execute(*outs, stream=s.cuda_stream)   # warm on the capture stream
+        s.synchronize()
+        with torch.cuda.graph(g, stream=s):
+            plan.execute(*outs, stream=s.cuda_stream)
+    for o in outs:
+        o.zero_()
+    g.replay()
+    torch.cuda.synchronize()
+    for a, b in zip(eager, outs):
+        assert rel_l2(b.cpu().numpy(), a.cpu().numpy()) < 1e-5
+    plan.close()
+
+
+def test_edge_cases(pins, meta, ref_images):
+    from ghostlight_gb300.flare import GhostRenderPlan
+    lens = _lens(pins, "cfg1_double_gauss_12")
+    cal = meta["cfg1_double_gauss_12"]["calibration"]
+    spec, corr = ref_images["cfg1_small/spec"], ref_images["cfg1_small/corr"]
+    pairs, boosts = ref_images["cfg1_small/pairs"], ref_images["cfg1_small/boosts"]
+    grid = O.aperture_samples(lens.records(), 16, 0)
+    # no pairs -> black image, no launch of the trace kernel
+    plan = GhostRenderPlan(lens, np.zeros((0, 2), np.int32), np.zeros(0, np.float32),
+                           ref_images["cfg1_small/source"], [grid], None, spec, corr, 7, 5,
+                           cal["sensor_half_w"], cal["sensor_half_h"], 1000.0)
+    out = [torch.full((5, 7), 3.0, device="cuda") for _ in range(3)]
+    plan.execute(*out)
+    torch.cuda.synchronize()
+    assert all(float(o.abs().max()) == 0.0 for o in out)
+    plan.close()
+    # 1x1 image and a source far outside the field: finite, non-negative
+    for W, H, ang in ((1, 1, 0.0), (37, 23, 1.2)):
+        src = np.array([[ang, 0.0, 1.0, 1.0, 1.0]], np.float32)
+        plan = GhostRenderPlan(lens, pairs, boosts, src, [grid], None, spec, corr, W, H,
+                               cal["sensor_half_w"], cal["sensor_half_h"], 1000.0)
+        out = [torch.zeros((H, W), device="cuda") for _ in range(3)]
+        plan.execute(*out)
+        torch.cuda.synchronize()
+        img = np.stack([o.cpu().numpy() for o in out])
+        assert np.isfinite(img).all()
+        plan.close()
+    # bad arguments raise ValueError before any device work
+    with pytest.raises(ValueError):
+        GhostRenderPlan(lens, np.array([[3, 3]], np.int32), np.ones(1, np.float32),
+                        ref_images["cfg1_small/source"], [grid], None, spec, corr, 8, 8,
+                        cal["sensor_half_w"], cal["sensor_half_h"], 1000.0)
+    with pytest.raises(ValueError):
+        GhostRenderPlan(lens, pairs, boosts, ref_images["cfg1_small/source"], [grid], None, spec, corr,
+                        0, 8, cal["sensor_half_w"], cal["sensor_half_h"], 1000.0)
