@@ -183,8 +183,11 @@ def run_gpu(args, rank, world):
     with ClockSampler(dev.index) as clk:
         t_batched = timed(graph.replay, args.steps, args.warmup)
     torch.cuda.synchronize()
-    t_plain = timed(lambda: plain.execute(*outs, stream=stream.cuda_stream), max(2, min(args.steps, 5)),
-                    max(1, min(args.warmup, 2)))
+    if args.quick:
+        t_plain = [float("nan")]
+    else:
+        t_plain = timed(lambda: plain.execute(*outs, stream=stream.cuda_stream), max(2, min(args.steps, 5)),
+                        max(1, min(args.warmup, 2)))
 
     # ---- e2e through the public API: host inputs in, host image out ----
     host_out = torch.empty((3, H, W), dtype=torch.float32).pin_memory()
@@ -199,12 +202,12 @@ def run_gpu(args, rank, world):
         return p
 
     with torch.cuda.stream(stream):
-        e2e_step()
         te = []
-        for _ in range(max(3, min(args.steps, 10))):
+        for _ in range(0 if args.quick else max(3, min(args.steps, 10)) + 1):
             t0 = time.perf_counter()
-            pe = e2e_step()
+            e2e_step()
             te.append(time.perf_counter() - t0)
+        te = te[1:] or [float("nan")]
     h2d = int(lens.num_surfaces() * 192 + 2 * N_SPEC * lens.num_surfaces() * 4 + N_SPEC * 16 +
               sum(len(g) for g in plan.grids) * 8 + plan.n_items * 16 + len(plan.pairs) * 16 + 32)
     d2h = 3 * W * H * 4
@@ -227,8 +230,7 @@ def run_gpu(args, rank, world):
                                "after the 1e-6 culler, adaptive pupil grids 16^2-256^2, %d wavelengths, "
                                "source %.0f deg, %dx%d float32 RGB, one graph-replayed persistent launch"
                                % (len(plan.pairs), N_SPEC, SOURCE_DEG, W, H),
-                   "pairs": int(len(plan.pairs)), "grids": sorted(int(round(math.sqrt(len(g) / 0.87)))
-                                                                 for g in plan.grids),
+                   "pairs": int(len(plan.pairs)), "grid_sides": plan.grid_sides,
                    "l2": "flushed (512 MB write) between timed steps", "parallelism": "replicas"},
         "rays_per_s": rays_per_s,
         "ray_lambda_traces_per_frame": plan.rays,
@@ -269,25 +271,31 @@ def cpu_baseline(plan, lens, cal, budget_s=8.0):
             "rays_per_s": rps}
 
 
+def reference_workload(lens, cal):
+    """The same frame for the CPU arm: the reference-exact filter (oracle),
+    the same adaptive grid rule on its probe footprints, the same spectral
+    table."""
+    from ghostlight_gb300.flare import adaptive_grid_size, spectral_table
+    from oracle import oracle as O
+    hw, hh = cal["sensor_half_w"], cal["sensor_half_h"]
+    pairs, boosts, fps = O.filter_pairs(lens.records(), hw, hh, MIN_INTENSITY, footprint=True)
+    sizes = [adaptive_grid_size(fp, hw, hh, W, H, 16, 256) for fp in fps]
+    uniq = sorted(set(sizes))
+    grids = [O.aperture_samples(lens.records(), g, 0) for g in uniq]
+    pair_grid = np.asarray([uniq.index(x) for x in sizes], np.int32)
+    spec, _ = spectral_table(N_SPEC)
+    rays = sum(len(grids[g]) for g in pair_grid) * N_SPEC
+    return pairs, boosts, grids, pair_grid, spec, rays
+
+
 def run_reference(args):
     """CPU reference arm: the reference's own trace code when it was built
-    here (oracle/_ref), else the oracle port; bounded sample per step."""
-    import ghostlight_gb300 as gl  # noqa: F401
-    from ghostlight_gb300.flare import pupil_grid, spectral_table, adaptive_grid_size
+    here (oracle/_ref), else the oracle port; every step traces a bounded
+    sample of the frame's pairs and is scaled to the full frame."""
+    from oracle import oracle as O
     lens, cal = _workload()
     hw, hh = cal["sensor_half_w"], cal["sensor_half_h"]
-    pins = np.load(GOLDEN / "ref_pins.npz")
-    pairs = pins["cfg2_wide_angle_24/filter_1e-6/pairs"]
-    boosts = pins["cfg2_wide_angle_24/filter_1e-6/boosts"]
-    spec, _ = spectral_table(N_SPEC)
-    # grid sizes: same adaptive rule on the reference filter's own output
-    from oracle import oracle as O
-    grids_by = {}
-    total_rays = 0
-    sizes = []
-    for a, b in pairs:
-        sizes.append(64)
-    kind = "port"
+    pairs, boosts, grids, pair_grid, spec, total_rays = reference_workload(lens, cal)
     use_ref = False
     try:
         from oracle import ref as R
@@ -295,35 +303,36 @@ def run_reference(args):
     except Exception:
         use_ref = False
     n_threads = os.cpu_count() or 1
-    grid = O.aperture_samples(lens.records(), 64, 0)
-    total_rays = len(pairs) * len(grid) * N_SPEC
-    sel = np.arange(0, len(pairs), max(1, len(pairs) // 16))
-    rays = len(sel) * len(grid) * N_SPEC
+    sel = np.arange(0, len(pairs), max(1, len(pairs) // 12))
+    rays = sum(len(grids[pair_grid[i]]) for i in sel) * N_SPEC
     ts = []
     for it in range(args.warmup + args.steps):
         t0 = time.perf_counter()
         if use_ref:
-            R.render_ghosts_cpu(lens.records(), pairs[sel], boosts[sel], _sources(), grid, spec, hw, hh,
-                                512, 512, 1000.0, n_threads=n_threads)
-            kind = "reference"
+            for i in sel:   # the harness takes one grid per call
+                R.render_ghosts_cpu(lens.records(), pairs[i:i + 1], boosts[i:i + 1], _sources(),
+                                    grids[pair_grid[i]], spec, hw, hh, 512, 512, 1000.0, n_threads=n_threads)
         else:
-            O.render(lens.records(), pairs[sel], boosts[sel], _sources(), [grid], spec, hw, hh, 512, 512,
-                     1000.0, fp64=False, n_threads=n_threads)
+            O.render(lens.records(), pairs[sel], boosts[sel], _sources(), grids, spec, hw, hh, 512, 512,
+                     1000.0, pair_grid=pair_grid[sel], fp64=False, n_threads=n_threads)
         if it >= args.warmup:
             ts.append(time.perf_counter() - t0)
-    rps = rays / (sum(ts) / len(ts))
+    step = sum(ts) / len(ts)
+    rps = rays / step
     fps = rps / total_rays
+    kind = "reference" if use_ref else "port"
     return {"metric": METRIC, "value": fps, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1e3 * sum(ts) / len(ts), "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": 1e3 * step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "impl": "reference",
-            "config": {"workload": "cfg2 ghost layer (24-surface wide-angle, %d pairs, 31 wavelengths, "
-                                   "64^2 pupil grid per pair), reference CPU trace per ray; each step "
-                                   "traces a %d-pair sample and is scaled to the frame" % (len(pairs), len(sel))},
+            "config": {"workload": "cfg2 ghost layer (24-surface wide-angle, %d pairs, adaptive grids, "
+                                   "%d wavelengths, 2048^2); each step traces %d of the pairs on the CPU "
+                                   "and is scaled to the full frame (%d ray-wavelength traces)"
+                                   % (len(pairs), N_SPEC, len(sel), total_rays)},
             "rays_per_s": rps,
             "cpu_baseline": {"value": fps, "unit": UNIT, "cores": n_threads, "kind": kind,
-                             "sample": "%d of %d pairs x %d pupil samples x %d wavelengths per step"
-                                       % (len(sel), len(pairs), len(grid), N_SPEC)},
+                             "sample": "%d of %d pairs per step (%d ray-wavelength traces)"
+                                       % (len(sel), len(pairs), rays)},
             "e2e": {"value": fps, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
@@ -334,6 +343,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--quick", action="store_true",
+                    help="batched timing only (no plain / e2e / CPU legs): for profiler runs")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -348,7 +359,7 @@ def main():
     res, plan = run_gpu(args, rank, world)
     if rank == 0:
         lens, cal = _workload()
-        if not args.no_cpu_baseline:
+        if not (args.no_cpu_baseline or args.quick):
             res["cpu_baseline"] = cpu_baseline(plan, lens, cal)
         res["roofline"] = roofline(res, plan)
         print(json.dumps(res))

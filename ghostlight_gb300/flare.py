@@ -302,11 +302,13 @@ def prepare_ghost_render(lens: OpticalSystem, sources, width: int, height: int, 
         grids = [pupil_grid(lens, g, jitter, seed, bo, rot) for g in uniq]
         pair_grid = np.asarray([uniq.index(s) for s in sizes], np.int32)
     else:
+        uniq = [int(config.ray_grid)]
         grids = [pupil_grid(lens, int(config.ray_grid), jitter, seed, bo, rot)]
         pair_grid = np.zeros(len(pairs), np.int32)
     plan = GhostRenderPlan(lens, pairs, boosts, sources, grids, pair_grid, spec, corr, width, height,
                            sensor_half_w, sensor_half_h, config.flare_gain, apply_corr, plain_per_pair)
     plan.pairs, plan.boosts, plan.grids, plan.pair_grid = pairs, boosts, grids, pair_grid
+    plan.grid_sides = list(uniq)
     plan.spec, plan.correction, plan.apply_correction = spec, corr, apply_corr
     return plan
 

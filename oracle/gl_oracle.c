@@ -125,7 +125,7 @@ static float ior_before_nd(const gl_surface* S, int idx)
 
 /* filter_ghost_pairs, ghost.cpp:105-138, in the reference's float arithmetic */
 int orc_filter(const gl_surface* S, int N, float hw, float hh, float min_int, int normalize,
-               float max_boost, int* out_ab, float* out_boost, int cap)
+               float max_boost, int* out_ab, float* out_boost, float* out_fp, int cap)
 {
     static const float lams[3] = {650.0f, 550.0f, 450.0f};
     const float start_z = S[0].z - 20.0f;
@@ -147,8 +147,7 @@ int orc_filter(const gl_surface* S, int N, float hw, float hh, float min_int, in
             }
             float est = total / 3.0f;
             if (est < min_int) continue;
-            float boost = 1.0f;
-            if (normalize)
+            float boost = 1.0f, fpw = 0.0f, fph = 0.0f;
             {
                 float mnx = 1e30f, mxx = -1e30f, mny = 1e30f, mxy = -1e30f;
                 int valid = 0;
@@ -165,7 +164,8 @@ int orc_filter(const gl_surface* S, int N, float hw, float hh, float min_int, in
                         mny = r.y < mny ? r.y : mny; mxy = r.y > mxy ? r.y : mxy;
                         ++valid;
                     }
-                if (valid >= 2)
+                if (valid >= 2) { fpw = mxx - mnx; fph = mxy - mny; }
+                if (normalize && valid >= 2)
                 {
                     float gw = (mxx - mnx) > 0.01f ? (mxx - mnx) : 0.01f;
                     float gh = (mxy - mny) > 0.01f ? (mxy - mny) : 0.01f;
@@ -173,7 +173,11 @@ int orc_filter(const gl_surface* S, int N, float hw, float hh, float min_int, in
                     boost = (area < 1.0f) ? 1.0f : (max_boost < area ? max_boost : area);
                 }
             }
-            if (kept < cap) { out_ab[2 * kept] = a; out_ab[2 * kept + 1] = b; out_boost[kept] = boost; }
+            if (kept < cap)
+            {
+                out_ab[2 * kept] = a; out_ab[2 * kept + 1] = b; out_boost[kept] = boost;
+                if (out_fp) { out_fp[2 * kept] = fpw; out_fp[2 * kept + 1] = fph; }
+            }
             ++kept;
         }
     }

@@ -28,7 +28,7 @@ def _load():
         P, i, f, d = C.POINTER, C.c_int, C.c_float, C.c_double
         lib.orc_trace.argtypes = [P(gl_surface), i, i, i, P(f), i, i, P(d)]
         lib.orc_enumerate.argtypes = [P(gl_surface), i, P(i), i]
-        lib.orc_filter.argtypes = [P(gl_surface), i, f, f, f, i, f, P(i), P(f), i]
+        lib.orc_filter.argtypes = [P(gl_surface), i, f, f, f, i, f, P(i), P(f), P(f), i]
         lib.orc_aperture_samples.argtypes = [P(gl_surface), i, i, i, i, i, f, P(f), i]
         lib.orc_render.argtypes = [P(gl_surface), i, P(i), P(f), P(i), i, P(f), i, P(f), P(i),
                                    P(f), i, f, f, i, i, f, i, i, P(d)]
@@ -65,13 +65,18 @@ def enumerate_pairs(surfs):
     return out[:n].copy()
 
 
-def filter_pairs(surfs, hw, hh, min_int=1e-7, normalize=True, max_boost=100.0):
+def filter_pairs(surfs, hw, hh, min_int=1e-7, normalize=True, max_boost=100.0, footprint=False):
+    """Reference-exact filter; with footprint=True also the (n,2) green-probe
+    footprint in mm that sizes adaptive pupil grids."""
     lib = _load()
     cap = len(surfs) ** 2
     ab = np.zeros((cap, 2), np.int32)
     bo = np.zeros(cap, np.float32)
+    fp = np.zeros((cap, 2), np.float32)
     n = lib.orc_filter(surface_array(surfs), len(surfs), hw, hh, min_int, int(normalize), max_boost,
-                       _ip(ab), _fp(bo), cap)
+                       _ip(ab), _fp(bo), _fp(fp), cap)
+    if footprint:
+        return ab[:n].copy(), bo[:n].copy(), fp[:n].copy()
     return ab[:n].copy(), bo[:n].copy()
 
 
