@@ -79,7 +79,8 @@ class gl_ghost_render_params(C.Structure):
                 ("sensor_half_w", C.c_float), ("sensor_half_h", C.c_float),
                 ("flare_gain", C.c_float), ("apply_correction", C.c_int32),
                 ("correction", C.c_float * 9), ("plain_per_pair", C.c_int32),
-                ("splat_mode", C.c_int32)]
+                ("splat_mode", C.c_int32), ("cull_dead_pairs", C.c_int32),
+                ("blades_override", C.c_int32), ("rotation_deg", C.c_float)]
 
 
 SURFACE_DTYPE = np.dtype([(name, np.float32 if t in (C.c_float,) else np.int32)

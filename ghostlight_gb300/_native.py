@@ -44,6 +44,7 @@ def _declare(lib):
     lib.gl_ghost_plan_execute.argtypes = [vp, vp, vp, vp, vp]
     lib.gl_ghost_plan_info.argtypes = [vp, P(C.c_longlong), P(i), P(i)]
     lib.gl_ghost_plan_destroy.argtypes = [vp]
+    lib.gl_ghost_plan_pair_hits.argtypes = [vp, P(C.c_int32), i]
     return lib
 
 

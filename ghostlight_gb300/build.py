@@ -35,6 +35,10 @@ UNITS = {
     "gl_filter.cu": EXACT,
     "gl_ghost.cu": FAST,
 }
+# Occupancy target of the render kernel (CTAs of 128 threads per SM); an
+# environment override lets a tuning sweep rebuild with another value.
+if os.environ.get("GL_RENDER_MIN_BLOCKS"):
+    UNITS["gl_ghost.cu"] = FAST + ["-DGL_RENDER_MIN_BLOCKS=%d" % int(os.environ["GL_RENDER_MIN_BLOCKS"])]
 
 
 def nvcc() -> str:

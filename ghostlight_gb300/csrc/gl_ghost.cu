@@ -34,9 +34,14 @@
 
 namespace gl {
 
-constexpr int kRenderThreads = 256;
-constexpr int kTile = kRenderThreads;
+constexpr int kRenderThreads = 128;
+#ifndef GL_RENDER_MIN_BLOCKS
+#define GL_RENDER_MIN_BLOCKS 8
+#endif
+constexpr int kRenderMinBlocks = GL_RENDER_MIN_BLOCKS;
+constexpr int kTile = 32;          // pupil samples per work item = one warp
 constexpr int kMaxSpec = 256;
+constexpr unsigned kFull = 0xffffffffu;
 
 struct PairDev {
     int a, b;
@@ -57,117 +62,386 @@ struct RenderArgs {
     const PairDev* pairs;
     const SourceDev* sources;
     const float2* samples;
-    int* counter;             // persistent queue head; null = one item per CTA
+    int* counter;             // persistent queue head; null = static item assignment
     float4* accum;            // RGBA, width x height
+    int* pair_hits;           // off-sensor cull: per-pair probe hits (null = no cull)
     int n_surf, n_spec, n_items, item_base;
     int width, height;
     float fmt_w, fmt_h, fmt_x0, fmt_y0;
     float hw2, hh2, gain, front_R, start_z;
 };
 
-__device__ __forceinline__ void flush_taps(float4* accum, int W, int H, int cx, int cy,
-                                           const float (&acc)[4][3])
+// Per-lane splat footprint kept in shared memory (12 floats, stride 13 so the
+// lanes of a warp fall in distinct banks) together with its 2x2 origin.
+constexpr int kAccStride = 13;
+
+__device__ __forceinline__ void flush_taps(float4* accum, int W, int H, int cx, int cy, const float* acc)
 {
     #pragma unroll
     for (int k = 0; k < 4; ++k)
     {
         const int xi = cx + (k & 1), yi = cy + (k >> 1);
         if (xi < 0 || xi >= W || yi < 0 || yi >= H) continue;
-        if (acc[k][0] == 0.0f && acc[k][1] == 0.0f && acc[k][2] == 0.0f) continue;
-        atomicAdd(accum + ((size_t)yi * W + xi), make_float4(acc[k][0], acc[k][1], acc[k][2], 0.0f));
+        const float r = acc[3 * k], g = acc[3 * k + 1], b = acc[3 * k + 2];
+        if (r == 0.0f && g == 0.0f && b == 0.0f) continue;
+        atomicAdd(accum + ((size_t)yi * W + xi), make_float4(r, g, b, 0.0f));
     }
 }
 
-__device__ __forceinline__ void trace_sample(const RenderArgs& A, const SurfRec* lens, const float* at,
-                                             const float* bf, const float4* spec, const PairDev& P,
-                                             const SourceDev& S, float2 uv)
-{
-    const V3 o = v3(uv.x * A.front_R + S.sdx, uv.y * A.front_R + S.sdy, A.start_z);
-    const V3 d = v3(S.dx, S.dy, S.dz);
-    int cx = INT_MIN, cy = INT_MIN;
-    float acc[4][3];
-    #pragma unroll
-    for (int k = 0; k < 4; ++k) acc[k][0] = acc[k][1] = acc[k][2] = 0.0f;
+// ---- render-path surface interaction --------------------------------------
+// Same physics as trace_surface_step (trace.cpp:84-135), arranged for the
+// render kernel: the common case (untilted sphere or plane, round aperture,
+// single-layer coating) is straight-line code; every rarer case (asphere
+// Newton solve, cylinder, tilted/decentred frame, polygon stop, other coating
+// models) is an out-of-line call so the hot loop stays small in the
+// instruction cache.
 
+// Sphere or plane in the vertex-plane form c*|q|^2 - 2*q_z = 0 (q relative to
+// the vertex, c = 1/R, c = 0 for a plane).  The ray is first moved to the
+// vertex plane, then the root nearest to it is taken in the
+// cancellation-free product form t = -C / (B + sign(B) sqrt(B^2 - A C)).
+// Choosing the root with the smaller |t| is choosing the hit whose z lies
+// nearer the vertex, which is the reference's root rule (trace_core.h:
+// 505-515); unlike b^2 - 4ac about the centre of curvature, this form loses
+// no precision for large radii or rays near the vertex.
+__device__ __forceinline__ bool sphere_hit(V3 o, V3 d, float z_s, float c, float& t_out, V3& q_out)
+{
+    if (fabsf(d.z) < 1e-12f) return false;
+    const float t0 = (z_s - o.z) / d.z;
+    const float px = o.x + d.x * t0, py = o.y + d.y * t0;
+    const float A = c * (d.x * d.x + d.y * d.y + d.z * d.z);
+    const float B = c * (px * d.x + py * d.y) - d.z;
+    const float C = c * (px * px + py * py);
+    const float disc = B * B - A * C;
+    if (disc < 0.0f) return false;
+    const float den = B + copysignf(sqrtf(disc), B);
+    const float ts = (den != 0.0f) ? -C / den : 0.0f;
+    float t = t0 + ts;
+    if (!(t > 1e-6f))
+    {
+        // the near root is behind the ray: the far root, if any, is the hit
+        if (!(A != 0.0f) || !(ts != 0.0f)) return false;
+        const float tb = t0 + (C / A) / ts;
+        if (!(tb > 1e-6f)) return false;
+        t = tb;
+    }
+    t_out = t;
+    q_out = v3(o.x + d.x * t, o.y + d.y * t, o.z + d.z * t - z_s);
+    return true;
+}
+
+__device__ __noinline__ bool check_polygon(float hx, float hy, float h2, const SurfRec& s)
+{
+    float r = sqrtf(h2);
+    if (r < 1e-9f) return true;
+    const float angle = atan2f(hy, hx) - s.rot_rad;
+    float off = fmodf(angle, s.sector);
+    if (off < 0.0f) off += s.sector;
+    off -= 0.5f * s.sector;
+    return r <= s.apothem / cosf(off);
+}
+
+__device__ __forceinline__ bool aperture_ok(float x, float y, const SurfRec& s)
+{
+    const float hx = x / s.aspect, hy = y;
+    const float h2 = hx * hx + hy * hy;
+    if (!(h2 <= s.semi_ap * s.semi_ap)) return false;
+    if (s.shape == 1) return check_polygon(hx, hy, h2, s);
+    return true;
+}
+
+// Everything but an untilted sphere/plane: the shared reference formulation.
+__device__ __noinline__ bool intersect_general(V3 o, V3 d, const SurfRec& s, float& t, V3& nrm)
+{
+    return intersect(o, d, s, t, nrm);
+}
+
+__device__ __noinline__ float weight_general(V3 d, V3 nrm, float n1, float n2, const SurfRec& s,
+                                             float lam, bool reflecting)
+{
+    return surface_weight(d, nrm, n1, n2, s, lam, reflecting);
+}
+
+__device__ __noinline__ float attenuator_general(V3 hit, const SurfRec& s)
+{
+    return surface_attenuator(hit, s);
+}
+
+// The per-step fields of one surface packed into two 16-byte words (two
+// vector shared-memory loads per step instead of a dozen scalar ones).
+struct __align__(16) HotRec {
+    float z, c, sa2, inv_aspect;
+    int bits, ar_layers, pad0, pad1;
+};
+enum HotBits { HB_ACTIVE = 1, HB_GENERAL = 2, HB_POLYGON = 4, HB_SIMPLE = 8, HB_ATTEN = 16 };
+
+__device__ __forceinline__ HotRec make_hot(const SurfRec& s)
+{
+    HotRec h;
+    h.z = s.z;
+    h.c = (fabsf(s.radius) < 1e-6f) ? 0.0f : s.inv_r;
+    h.sa2 = s.semi_ap * s.semi_ap;
+    h.inv_aspect = 1.0f / s.aspect;
+    h.bits = ((s.flags & SF_ACTIVE) ? HB_ACTIVE : 0) |
+             ((s.form != 0 || (s.flags & SF_TRANSFORMED)) ? HB_GENERAL : 0) |
+             ((s.shape == 1) ? HB_POLYGON : 0) | ((s.coating == 0) ? HB_SIMPLE : 0) |
+             ((s.coating == 4) ? HB_ATTEN : 0);
+    h.ar_layers = s.ar_layers;
+    h.pad0 = h.pad1 = 0;
+    return h;
+}
+
+// Single-layer MgF2 reflectance (coating_reflectance / surface_reflectance,
+// fresnel.h:92-178) with the film phase factor 2*pi*n_c*d/lambda supplied per
+// wavelength (kdelta) and cos(2 delta) formed as 2 cos^2(delta) - 1: delta is
+// below pi here, where the SFU cosine is accurate.
+__device__ __forceinline__ float mgf2_reflectance(float cos_i, float n1, float n2, int layers, float kdelta)
+{
+    if (layers <= 0) return fresnel_reflectance(cos_i, n1, n2);
+    const float cn = 1.38f;
+    const float a1 = n1 * (1.0f / cn);
+    const float sin2_c = a1 * a1 * (1.0f - cos_i * cos_i);
+    if (sin2_c >= 1.0f) return fresnel_reflectance(cos_i, n1, n2);
+    const float cos_c = sqrtf(1.0f - sin2_c);
+    const float a2 = cn / n2;
+    const float sin2_2 = a2 * a2 * (1.0f - cos_c * cos_c);
+    if (sin2_2 >= 1.0f) return fresnel_reflectance(cos_i, n1, n2);
+    const float cos_2 = sqrtf(1.0f - sin2_2);
+    const float r01 = (n1 * cos_i - cn * cos_c) / (n1 * cos_i + cn * cos_c);
+    const float r12 = (cn * cos_c - n2 * cos_2) / (cn * cos_c + n2 * cos_2);
+    const float cd = __cosf(kdelta * cos_c);
+    const float c2d = 2.0f * cd * cd - 1.0f;
+    const float x = 2.0f * r01 * r12 * c2d;
+    float R = (r01 * r01 + r12 * r12 + x) / (1.0f + r01 * r01 * r12 * r12 + x);
+    R = fminf(fmaxf(R, 0.0f), 1.0f);
+    for (int i = 1; i < layers; ++i) R *= 0.25f;
+    return R;
+}
+
+// One surface interaction on the lane's ray; false when the ray died.
+__device__ __forceinline__ bool surface_step(V3& o, V3& d, const HotRec& h, const SurfRec& s, float lam,
+                                             float kdelta, float n2, bool reflecting, float reflect_ior,
+                                             float& cur, float& w)
+{
+    float t; V3 nrm;
+    if (!(h.bits & HB_GENERAL))
+    {
+        const float c = h.c;
+        V3 q;
+        if (!sphere_hit(o, d, h.z, c, t, q)) return false;
+        const float hx = q.x * h.inv_aspect, hy = q.y;
+        const float h2 = hx * hx + hy * hy;
+        if (!(h2 <= h.sa2)) return false;
+        if ((h.bits & HB_POLYGON) && !check_polygon(hx, hy, h2, s)) return false;
+        // outward normal (c q_x, c q_y, c q_z - 1), turned to oppose the ray
+        nrm = v3(c * q.x, c * q.y, c * q.z - 1.0f);
+        if (c == 0.0f) nrm = v3(0.0f, 0.0f, -1.0f);
+        if (dot(nrm, d) > 0.0f) nrm = -nrm;
+    }
+    else if (!intersect_general(o, d, s, t, nrm))
+    {
+        return false;
+    }
+    const V3 hit = o + d * t;
+    o = hit;
+    const float n1 = cur;
+    const bool simple = (h.bits & HB_SIMPLE) != 0;
+    if (reflecting)
+    {
+        w *= simple ? mgf2_reflectance(fabsf(dot(nrm, d)), n1, n2, h.ar_layers, kdelta)
+                    : weight_general(d, nrm, n1, n2, s, lam, true);
+        if (h.bits & HB_ATTEN) w *= attenuator_general(hit, s);
+        d = reflect(d, nrm);
+        cur = reflect_ior;
+    }
+    else
+    {
+        V3 nd;
+        if (!refract(d, nrm, n1, n2, nd)) return false;
+        w *= simple ? 1.0f - mgf2_reflectance(fabsf(dot(nrm, d)), n1, n2, h.ar_layers, kdelta)
+                    : weight_general(d, nrm, n1, n2, s, lam, false);
+        if (h.bits & HB_ATTEN) w *= attenuator_general(hit, s);
+        d = nd;
+        cur = n2;
+    }
+    return true;
+}
+
+// The three legs of trace_ghost_ray (trace.cpp:196-233) flattened into one
+// step sequence k = 0 .. L-1 with a single step site.  The warp walks the
+// sequence in lock step for one wavelength at a time: the surface, its form,
+// its aperture shape, reflect-or-refract and the IOR pair are the same for
+// every lane (uniform branches, broadcast shared-memory reads); only the ray
+// state differs.  The walk stops as soon as every lane's ray has died.
+__device__ __forceinline__ void splat_ray(const RenderArgs& A, const PairDev& P, const SourceDev& S,
+                                          const float4& sp, V3 o, V3 d, float w,
+                                          int& cx, int& cy, float* acc)
+{
+    // propagate_to_sensor (trace.cpp:147-162), then the splat (ghost_render.cu:423-463)
+    if (!(fabsf(d.z) >= 1e-12f)) return;
+    const float ts = -o.z / d.z;
+    if (!(ts >= 0.0f)) return;
+    const float rx = o.x + d.x * ts, ry = o.y + d.y * ts;
+    if (!isfinite(rx) || !isfinite(ry)) return;
+    const float base = w * P.w_ray * A.gain * P.boost;
+    if (base < 1e-14f) return;
+    float px = (rx / A.hw2 + 0.5f) * A.fmt_w + A.fmt_x0;
+    float py = (ry / A.hh2 + 0.5f) * A.fmt_h + A.fmt_y0;
+    if (!isfinite(px) || !isfinite(py)) return;
+    px = fmaxf(-2.0e9f, fminf(2.0e9f, px));
+    py = fmaxf(-2.0e9f, fminf(2.0e9f, py));
+    const int x0 = (int)floorf(px - 0.5f), y0 = (int)floorf(py - 0.5f);
+    const float fx = (px - 0.5f) - (float)x0, fy = (py - 0.5f) - (float)y0;
+    const float power = (S.r * sp.y + S.g * sp.z + S.b * sp.w) * base;
+    const float c0 = power * sp.y, c1 = power * sp.z, c2 = power * sp.w;
+    if (x0 != cx || y0 != cy)
+    {
+        if (cx != INT_MIN) flush_taps(A.accum, A.width, A.height, cx, cy, acc);
+        cx = x0; cy = y0;
+        #pragma unroll
+        for (int q = 0; q < 12; ++q) acc[q] = 0.0f;
+    }
+    const float wt[4] = {(1.0f - fx) * (1.0f - fy), fx * (1.0f - fy), (1.0f - fx) * fy, fx * fy};
+    #pragma unroll
+    for (int q = 0; q < 4; ++q)
+    {
+        acc[3 * q] += c0 * wt[q];
+        acc[3 * q + 1] += c1 * wt[q];
+        acc[3 * q + 2] += c2 * wt[q];
+    }
+}
+
+template <bool PROBE>
+__device__ __forceinline__ void trace_warp(const RenderArgs& A, const SurfRec* lens, const HotRec* hot,
+                                           const float* at, const float* bf, const float4* spec,
+                                           const float* kdel, const PairDev& P, const SourceDev& S,
+                                           float2 uv, bool active, float* acc, int pair)
+{
+    const int n = A.n_surf, a = P.a, b = P.b;
+    const int L1 = b + 1, L2 = L1 + (b - a), L = L2 + (n - 1 - a);
+    int cx = INT_MIN, cy = INT_MIN;
+
+    #pragma unroll 1
     for (int li = 0; li < A.n_spec; ++li)
     {
         const float4 sp = spec[li];
-        TraceOut r = trace_ghost(lens, A.n_surf, at + li * A.n_surf, bf + li * A.n_surf, o, d, sp.x, P.a, P.b);
-        if (r.status != 0) continue;
-        if (!isfinite(r.x) || !isfinite(r.y)) continue;
-        const float base = r.w * P.w_ray * A.gain * P.boost;
-        if (base < 1e-14f) continue;
-        float px = (r.x / A.hw2 + 0.5f) * A.fmt_w + A.fmt_x0;
-        float py = (r.y / A.hh2 + 0.5f) * A.fmt_h + A.fmt_y0;
-        if (!isfinite(px) || !isfinite(py)) continue;
-        px = fmaxf(-2.0e9f, fminf(2.0e9f, px));
-        py = fmaxf(-2.0e9f, fminf(2.0e9f, py));
-        const int x0 = (int)floorf(px - 0.5f), y0 = (int)floorf(py - 0.5f);
-        const float fx = (px - 0.5f) - (float)x0, fy = (py - 0.5f) - (float)y0;
-        const float P_l = S.r * sp.y + S.g * sp.z + S.b * sp.w;
-        const float power = P_l * base;
-        const float c0 = power * sp.y, c1 = power * sp.z, c2 = power * sp.w;
-        if (x0 != cx || y0 != cy)
+        const float kdelta = kdel[li];
+        const float* atl = at + li * n;
+        const float* bfl = bf + li * n;
+        V3 o = v3(uv.x * A.front_R + S.sdx, uv.y * A.front_R + S.sdy, A.start_z);
+        V3 d = v3(S.dx, S.dy, S.dz);
+        float w = 1.0f, cur = 1.0f;
+        bool alive = active;
+        #pragma unroll 1
+        for (int k = 0; k < L; ++k)
         {
-            if (cx != INT_MIN) flush_taps(A.accum, A.width, A.height, cx, cy, acc);
-            cx = x0; cy = y0;
-            #pragma unroll
-            for (int k = 0; k < 4; ++k) acc[k][0] = acc[k][1] = acc[k][2] = 0.0f;
+            if (!__any_sync(kFull, alive)) break;
+            int s; float n2; bool refl; bool back = false;
+            if (k < L1)      { s = k;                refl = (s == b); }
+            else if (k < L2) { s = 2 * b - k;        refl = (s == a); back = true; }
+            else             { s = a + 1 + (k - L2); refl = false; }
+            const HotRec hr = hot[s];
+            if (!(hr.bits & HB_ACTIVE)) continue;
+            n2 = back ? bfl[s] : atl[s];
+            const float rior = (back && refl) ? atl[a] : cur;
+            if (alive) alive = surface_step(o, d, hr, lens[s], sp.x, kdelta, n2, refl, rior, cur, w);
         }
-        const float w[4] = {(1.0f - fx) * (1.0f - fy), fx * (1.0f - fy), (1.0f - fx) * fy, fx * fy};
-        #pragma unroll
-        for (int k = 0; k < 4; ++k)
+        if (PROBE)
         {
-            acc[k][0] += c0 * w[k];
-            acc[k][1] += c1 * w[k];
-            acc[k][2] += c2 * w[k];
+            // Off-sensor probe (the STATS pass of ghost_render.cu:402-415 with
+            // the 1.25 margin of :148): did this ray land inside the inflated
+            // frame?  One hit anywhere keeps the pair, so the warp stops at
+            // the first wavelength that produced one.
+            bool hit = false;
+            if (alive && fabsf(d.z) >= 1e-12f)
+            {
+                const float ts = -o.z / d.z;
+                if (ts >= 0.0f)
+                {
+                    const float spx = ((o.x + d.x * ts) / A.hw2 + 0.5f) * A.fmt_w + A.fmt_x0;
+                    const float spy = ((o.y + d.y * ts) / A.hh2 + 0.5f) * A.fmt_h + A.fmt_y0;
+                    hit = isfinite(spx) && isfinite(spy) && spx >= 0.0f && spx < (float)A.width &&
+                          spy >= 0.0f && spy < (float)A.height;
+                }
+            }
+            if (__any_sync(kFull, hit))
+            {
+                if ((threadIdx.x & 31) == 0) atomicAdd(A.pair_hits + pair, 1);
+                return;
+            }
+        }
+        else if (alive)
+        {
+            splat_ray(A, P, S, sp, o, d, w, cx, cy, acc);
         }
     }
-    if (cx != INT_MIN) flush_taps(A.accum, A.width, A.height, cx, cy, acc);
+    if (!PROBE && cx != INT_MIN) flush_taps(A.accum, A.width, A.height, cx, cy, acc);
 }
 
-__global__ void __launch_bounds__(kRenderThreads, 2) ghost_render_kernel(const RenderArgs A)
+template <bool PROBE>
+__global__ void __launch_bounds__(kRenderThreads, kRenderMinBlocks) ghost_render_kernel(const RenderArgs A)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ int s_item;
-    SurfRec* lens = reinterpret_cast<SurfRec*>(smem_raw);
-    float4* spec = reinterpret_cast<float4*>(lens + A.n_surf);
-    float* at = reinterpret_cast<float*>(spec + A.n_spec);
+    HotRec* hot = reinterpret_cast<HotRec*>(smem_raw);
+    float4* spec = reinterpret_cast<float4*>(hot + A.n_surf);
+    float* kdel = reinterpret_cast<float*>(spec + A.n_spec);
+    float* at = kdel + A.n_spec;
     float* bf = at + A.n_spec * A.n_surf;
+    SurfRec* lens = reinterpret_cast<SurfRec*>(bf + A.n_spec * A.n_surf);
+    float* acc_base = reinterpret_cast<float*>(lens + A.n_surf);
     const int tid = threadIdx.x;
+    float* acc = acc_base + tid * kAccStride;   // 13 floats per lane: conflict-free banks
     {
         const int words = A.n_surf * (int)(sizeof(SurfRec) / 4);
         const int* src = reinterpret_cast<const int*>(A.recs);
         int* dst = reinterpret_cast<int*>(lens);
         for (int i = tid; i < words; i += blockDim.x) dst[i] = src[i];
-        for (int i = tid; i < A.n_spec; i += blockDim.x) spec[i] = A.spec[i];
+        for (int i = tid; i < A.n_spec; i += blockDim.x)
+        {
+            spec[i] = A.spec[i];
+            // film phase factor of the MgF2 quarter-wave layer (fresnel.h:103, 168)
+            kdel[i] = 2.0f * kPi * 1.38f * (550.0f / (4.0f * 1.38f)) / A.spec[i].x;
+        }
         const int nt = A.n_spec * A.n_surf;
         for (int i = tid; i < nt; i += blockDim.x) { at[i] = A.ior_at[i]; bf[i] = A.ior_bf[i]; }
     }
     __syncthreads();
+    for (int i = tid; i < A.n_surf; i += blockDim.x) hot[i] = make_hot(lens[i]);
+    __syncthreads();
+    // Warp-granular work: each warp takes one (pair, source, 32-sample) item
+    // at a time, so no CTA-wide barrier sits inside the loop.
+    const int lane = tid & 31;
+    const int gwarp = (int)((blockIdx.x * blockDim.x + tid) >> 5);
+    const int nwarp = (int)((gridDim.x * blockDim.x) >> 5);
+    int next_static = A.item_base + gwarp;
     for (;;)
     {
         int item;
         if (A.counter != nullptr)
         {
-            if (tid == 0) s_item = atomicAdd(A.counter, 1);
-            __syncthreads();
-            item = s_item;
-            __syncthreads();
+            int v = 0;
+            if (lane == 0) v = atomicAdd(A.counter, 1);
+            item = __shfl_sync(kFull, v, 0);
         }
         else
         {
-            item = A.item_base + (int)blockIdx.x;
+            item = next_static;
+            next_static += nwarp;
         }
         if (item >= A.n_items) break;
         const int4 w = A.items[item];
-        if (tid < w.w)
+        if (A.pair_hits != nullptr)
         {
-            const PairDev P = A.pairs[w.x];
-            const SourceDev S = A.sources[w.y];
-            trace_sample(A, lens, at, bf, spec, P, S, A.samples[w.z + tid]);
+            // render: skip pairs the probe found off-sensor; probe passes
+            // after the first: skip pairs already known to be on-sensor
+            const int h = A.pair_hits[w.x];
+            if (PROBE ? (h > 0) : (h == 0)) continue;
         }
-        if (A.counter == nullptr) break;
+        const PairDev P = A.pairs[w.x];
+        const SourceDev S = A.sources[w.y];
+        const bool active = lane < w.w;
+        const float2 uv = active ? A.samples[w.z + lane] : make_float2(0.0f, 0.0f);
+        trace_warp<PROBE>(A, lens, hot, at, bf, spec, kdel, P, S, uv, active, acc, w.x);
     }
 }
 
@@ -235,6 +509,14 @@ struct GhostPlan {
     int grid_persistent = 0;
     long long rays = 0;                 // ray-wavelength traces per execute
     float front_R = 0.0f, start_z = 0.0f;
+    // off-sensor cull (probe passes)
+    bool cull = false;
+    int4* probe_items = nullptr;
+    float2* probe_samples = nullptr;
+    int probe_begin[4] = {0, 0, 0, 0};   // item range of each pass
+    int* pair_hits = nullptr;
+    int* probe_counters = nullptr;
+    long long probe_rays = 0;
 };
 
 static void plan_free(GhostPlan* p)
@@ -243,6 +525,7 @@ static void plan_free(GhostPlan* p)
     cudaFree(p->recs); cudaFree(p->ior_at); cudaFree(p->ior_bf); cudaFree(p->spec);
     cudaFree(p->items); cudaFree(p->pairs); cudaFree(p->sources); cudaFree(p->samples);
     cudaFree(p->counter); cudaFree(p->accum);
+    cudaFree(p->probe_items); cudaFree(p->probe_samples); cudaFree(p->pair_hits); cudaFree(p->probe_counters);
     delete p;
 }
 
@@ -257,7 +540,8 @@ static cudaError_t upload(T** dst, const T* src, size_t count)
 
 static size_t render_smem(int n_surf, int n_spec)
 {
-    return (size_t)n_surf * sizeof(SurfRec) + (size_t)n_spec * 16 + 2 * (size_t)n_spec * n_surf * 4;
+    return (size_t)n_surf * 32 + (size_t)n_spec * 16 + (size_t)n_spec * 4 + 2 * (size_t)n_spec * n_surf * 4 +
+           (size_t)n_surf * sizeof(SurfRec) + (size_t)kRenderThreads * kAccStride * 4;
 }
 
 int plan_create(const gl_surface* surfaces, int n_surf, const gl_ghost_pair* pairs, const float* boosts,
@@ -317,6 +601,39 @@ int plan_create(const gl_surface* surfaces, int n_surf, const gl_ghost_pair* pai
         src[i] = {dir.x, dir.y, dir.z, -kSpawnOffset * bx, -kSpawnOffset * by, sources[i].r, sources[i].g, sources[i].b};
     }
 
+    // Pupil samples of each grid in Morton order over the unit square: 32
+    // consecutive samples (one warp) then cover a compact patch of the pupil,
+    // whose rays tend to vignette together, instead of a strip across it.
+    // The set of samples and each one's weight are unchanged.
+    const int n_samples_all = n_grids > 0 ? grid_offsets[n_grids] : 0;
+    std::vector<gl_pupil_sample> ordered((size_t)n_samples_all);
+    {
+        auto spread = [](uint32_t x) {
+            x &= 0x3ffu;
+            x = (x | (x << 16)) & 0x030000ffu;
+            x = (x | (x << 8)) & 0x0300f00fu;
+            x = (x | (x << 4)) & 0x030c30c3u;
+            x = (x | (x << 2)) & 0x09249249u;
+            return x;
+        };
+        std::vector<std::pair<uint32_t, int>> key;
+        for (int g = 0; g < n_grids; ++g)
+        {
+            const int g0 = grid_offsets[g], g1 = grid_offsets[g + 1];
+            key.clear();
+            for (int i = g0; i < g1; ++i)
+            {
+                const float fu = std::min(std::max((samples[i].u + 1.0f) * 512.0f, 0.0f), 1023.0f);
+                const float fv = std::min(std::max((samples[i].v + 1.0f) * 512.0f, 0.0f), 1023.0f);
+                const uint32_t m = (spread((uint32_t)fu) << 1) | spread((uint32_t)fv);
+                key.push_back({m, i});
+            }
+            std::stable_sort(key.begin(), key.end(),
+                             [](const std::pair<uint32_t, int>& x, const std::pair<uint32_t, int>& y) { return x.first < y.first; });
+            for (int i = g0; i < g1; ++i) ordered[i] = samples[key[i - g0].second];
+        }
+    }
+
     std::vector<PairDev> pd((size_t)n_pairs);
     std::vector<int4> items;
     p->pair_item_begin.assign((size_t)n_pairs + 1, 0);
@@ -333,6 +650,36 @@ int plan_create(const gl_surface* surfaces, int n_surf, const gl_ghost_pair* pai
     }
     p->pair_item_begin[n_pairs] = (int)items.size();
     p->n_items = (int)items.size();
+
+    // Off-sensor probe grids (ghost_render.cu:1022-1027): 40x40, wang-hash
+    // jitter with a fixed seed per pass, the config's blade override.
+    p->cull = prm->cull_dead_pairs && n_pairs > 1 && n_spec != 3 && !prm->plain_per_pair;
+    std::vector<int4> pitems;
+    std::vector<gl_pupil_sample> psamples;
+    if (p->cull)
+    {
+        for (int pass = 0; pass < 3; ++pass)
+        {
+            gl_sampler_params sp;
+            sp.ray_grid = 40;
+            sp.pupil_jitter = 1;
+            sp.jitter_seed = (int)(0x9E3779B9u * (unsigned)(pass + 1));
+            sp.blades_override = prm->blades_override;
+            sp.rotation_deg = prm->rotation_deg;
+            std::vector<gl_pupil_sample> g;
+            int rcs = build_aperture_samples(surfaces, n_surf, sp, g);
+            if (rcs) { plan_free(p); return rcs; }
+            const int base = (int)psamples.size();
+            psamples.insert(psamples.end(), g.begin(), g.end());
+            p->probe_begin[pass] = (int)pitems.size();
+            for (int i = 0; i < n_pairs; ++i)
+                for (int s = 0; s < n_src; ++s)
+                    for (int t = 0; t < (int)g.size(); t += kTile)
+                        pitems.push_back(make_int4(i, s, base + t, std::min(kTile, (int)g.size() - t)));
+            p->probe_rays += (long long)g.size() * n_src * n_pairs * n_spec;
+        }
+        p->probe_begin[3] = (int)pitems.size();
+    }
     const int n_samples = n_grids > 0 ? grid_offsets[n_grids] : 0;
 
     cudaError_t e = cudaSuccess;
@@ -344,14 +691,22 @@ int plan_create(const gl_surface* surfaces, int n_surf, const gl_ghost_pair* pai
     chk(upload(&p->items, items.data(), items.size()));
     chk(upload(&p->pairs, pd.data(), pd.size()));
     chk(upload(&p->sources, src.data(), src.size()));
-    chk(upload(&p->samples, reinterpret_cast<const float2*>(samples), (size_t)n_samples));
+    chk(upload(&p->samples, reinterpret_cast<const float2*>(ordered.data()), (size_t)n_samples));
     chk(cudaMalloc(&p->counter, sizeof(int)));
+    if (p->cull)
+    {
+        chk(upload(&p->probe_items, pitems.data(), pitems.size()));
+        chk(upload(&p->probe_samples, reinterpret_cast<const float2*>(psamples.data()), psamples.size()));
+        chk(cudaMalloc(&p->pair_hits, sizeof(int) * std::max(1, n_pairs)));
+        chk(cudaMalloc(&p->probe_counters, sizeof(int) * 4));
+    }
     chk(cudaMalloc(&p->accum, (size_t)prm->width * prm->height * sizeof(float4)));
     if (e == cudaSuccess) chk(cudaMemset(p->accum, 0, (size_t)prm->width * prm->height * sizeof(float4)));
     p->smem = render_smem(n_surf, n_spec);
-    if (e == cudaSuccess) chk(cudaFuncSetAttribute(ghost_render_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem));
+    if (e == cudaSuccess) chk(cudaFuncSetAttribute(ghost_render_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem));
+    if (e == cudaSuccess) chk(cudaFuncSetAttribute(ghost_render_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem));
     int per_sm = 0, n_sm = 0;
-    if (e == cudaSuccess) chk(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ghost_render_kernel, kRenderThreads, p->smem));
+    if (e == cudaSuccess) chk(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ghost_render_kernel<false>, kRenderThreads, p->smem));
     if (e == cudaSuccess) chk(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, p->device));
     if (e != cudaSuccess)
     {
@@ -359,7 +714,9 @@ int plan_create(const gl_surface* surfaces, int n_surf, const gl_ghost_pair* pai
         return fail(e == cudaErrorMemoryAllocation ? GL_ERR_OOM : GL_ERR_CUDA,
                     std::string("render_ghosts: ") + cudaGetErrorString(e));
     }
-    p->grid_persistent = std::max(1, std::min(p->n_items, std::max(1, per_sm) * n_sm));
+    const int warps_per_block = kRenderThreads / 32;
+    p->grid_persistent = std::max(1, std::min((p->n_items + warps_per_block - 1) / warps_per_block,
+                                              std::max(1, per_sm) * n_sm));
     *out = p;
     return GL_OK;
 }
@@ -381,6 +738,34 @@ int plan_execute(GhostPlan* p, float* d_out_r, float* d_out_g, float* d_out_b, c
     A.hw2 = 2.0f * p->prm.sensor_half_w; A.hh2 = 2.0f * p->prm.sensor_half_h;
     A.gain = p->prm.flare_gain;
     A.front_R = p->front_R; A.start_z = p->start_z;
+    A.pair_hits = nullptr;
+    if (p->cull && p->n_items > 0)
+    {
+        // Probe passes: the frame inflated by CULL_MARGIN = 1.25
+        // (ghost_render.cu:148), persistent launches over the probe items.
+        GL_CUDA_TRY(cudaMemsetAsync(p->pair_hits, 0, sizeof(int) * p->n_pairs, st));
+        GL_CUDA_TRY(cudaMemsetAsync(p->probe_counters, 0, sizeof(int) * 4, st));
+        RenderArgs B = A;
+        B.samples = p->probe_samples;
+        B.items = p->probe_items;
+        B.pair_hits = p->pair_hits;
+        B.hw2 = 2.0f * (p->prm.sensor_half_w * 1.25f);
+        B.hh2 = 2.0f * (p->prm.sensor_half_h * 1.25f);
+        const int warps_per_block = kRenderThreads / 32;
+        for (int pass = 0; pass < 3; ++pass)
+        {
+            const int n_it = p->probe_begin[pass + 1] - p->probe_begin[pass];
+            if (n_it <= 0) continue;
+            B.items = p->probe_items + p->probe_begin[pass];
+            B.n_items = n_it;
+            B.counter = p->probe_counters + pass;
+            const int grid = std::max(1, std::min((n_it + warps_per_block - 1) / warps_per_block, p->grid_persistent));
+            ghost_render_kernel<true><<<grid, kRenderThreads, p->smem, st>>>(B);
+            ++launches;
+        }
+        GL_CUDA_TRY(cudaGetLastError());
+        A.pair_hits = p->pair_hits;
+    }
     if (p->n_items > 0)
     {
         if (p->prm.plain_per_pair)
@@ -392,7 +777,8 @@ int plan_execute(GhostPlan* p, float* d_out_r, float* d_out_g, float* d_out_b, c
                 if (b1 <= b0) continue;
                 A.item_base = b0;
                 A.n_items = b1;
-                ghost_render_kernel<<<b1 - b0, kRenderThreads, p->smem, st>>>(A);
+                const int warps_per_block = kRenderThreads / 32;
+                ghost_render_kernel<false><<<(b1 - b0 + warps_per_block - 1) / warps_per_block, kRenderThreads, p->smem, st>>>(A);
                 ++launches;
             }
             GL_CUDA_TRY(cudaGetLastError());
@@ -401,7 +787,7 @@ int plan_execute(GhostPlan* p, float* d_out_r, float* d_out_g, float* d_out_b, c
         {
             GL_CUDA_TRY(cudaMemsetAsync(p->counter, 0, sizeof(int), st));
             A.counter = p->counter;
-            ghost_render_kernel<<<p->grid_persistent, kRenderThreads, p->smem, st>>>(A);
+            ghost_render_kernel<false><<<p->grid_persistent, kRenderThreads, p->smem, st>>>(A);
             GL_CUDA_TRY(cudaGetLastError());
             ++launches;
         }
@@ -517,9 +903,17 @@ int gl_ghost_plan_execute(gl_ghost_plan* plan, float* d_out_r, float* d_out_g, f
 int gl_ghost_plan_info(const gl_ghost_plan* plan, long long* rays, int* n_items, int* grid)
 {
     if (!plan) return fail(GL_ERR_INVALID, "ghost_plan_info: null plan");
-    if (rays) *rays = plan->p->rays;
+    if (rays) *rays = plan->p->rays + plan->p->probe_rays;
     if (n_items) *n_items = plan->p->n_items;
     if (grid) *grid = plan->p->grid_persistent;
+    return GL_OK;
+}
+
+int gl_ghost_plan_pair_hits(const gl_ghost_plan* plan, int32_t* out, int n)
+{
+    if (!plan || !out || n < plan->p->n_pairs) return fail(GL_ERR_INVALID, "ghost_plan_pair_hits: bad arguments");
+    if (!plan->p->cull) { for (int i = 0; i < plan->p->n_pairs; ++i) out[i] = 1; return GL_OK; }
+    GL_CUDA_TRY(cudaMemcpy(out, plan->p->pair_hits, sizeof(int) * plan->p->n_pairs, cudaMemcpyDeviceToHost));
     return GL_OK;
 }
 

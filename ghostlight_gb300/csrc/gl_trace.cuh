@@ -42,7 +42,7 @@ enum SurfFlags : int32_t {
     SF_ACTIVE = 1, SF_TRANSFORMED = 2, SF_STOP = 4,
 };
 
-// 48 words (192 B).  Field meaning: struct Surface (optical_system.h:157-249).
+// Field meaning: struct Surface (optical_system.h:157-249).
 struct SurfRec {
     float z, radius, semi_ap, aspect;
     float rot_rad, sector, apothem, conic;
@@ -53,9 +53,11 @@ struct SurfRec {
     int32_t coating, ar_layers, blades, cyl_axis;
     float tint_r, tint_g, tint_b, tint_s;
     float g_sigma, g_bg, g_peak, g_dx, g_dy;
-    float pad1[2];
+    float pad1[3];
 };
-static_assert(sizeof(SurfRec) == 192, "SurfRec must stay 192 bytes");
+// 49 words: an odd stride, so lanes reading the same field of different
+// surfaces in shared memory hit different banks.
+static_assert(sizeof(SurfRec) == 196, "SurfRec must stay 196 bytes");
 
 struct V3 {
     float x, y, z;

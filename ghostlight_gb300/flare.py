@@ -209,7 +209,8 @@ class GhostRenderPlan:
 
     def __init__(self, lens: OpticalSystem, pairs, boosts, sources, grids, pair_grid, spec,
                  correction, width, height, sensor_half_w, sensor_half_h, gain,
-                 apply_correction=True, plain_per_pair=False, fmt=None):
+                 apply_correction=True, plain_per_pair=False, fmt=None, cull_dead_pairs=False,
+                 blades_override=0, rotation_deg=0.0):
         lib = _native.load()
         self._lib = lib
         self.width, self.height = int(width), int(height)
@@ -233,6 +234,10 @@ class GhostRenderPlan:
         for k, v in enumerate(np.asarray(correction, np.float32).reshape(-1)):
             prm.correction[k] = float(v)
         prm.plain_per_pair = int(bool(plain_per_pair))
+        prm.cull_dead_pairs = int(bool(cull_dead_pairs))
+        prm.blades_override = int(blades_override)
+        prm.rotation_deg = float(rotation_deg)
+        self.n_pairs = len(pairs)
         P = C.POINTER
         arr = lens.to_array()
         h = C.c_void_p()
@@ -259,6 +264,12 @@ class GhostRenderPlan:
         _native.check(self._lib.gl_ghost_plan_execute(self._h, out_r.data_ptr(), out_g.data_ptr(),
                                                       out_b.data_ptr(), st), "render_ghosts")
         return _native.last_launch_count()
+
+    def pair_hits(self):
+        """Probe hits per pair from the last execute (0 = culled)."""
+        out = (C.c_int32 * max(1, self.n_pairs))()
+        _native.check(self._lib.gl_ghost_plan_pair_hits(self._h, out, max(1, self.n_pairs)), "pair_hits")
+        return np.frombuffer(out, np.int32)[: self.n_pairs].copy()
 
     def close(self):
         if getattr(self, "_h", None):
@@ -306,7 +317,9 @@ def prepare_ghost_render(lens: OpticalSystem, sources, width: int, height: int, 
         grids = [pupil_grid(lens, int(config.ray_grid), jitter, seed, bo, rot)]
         pair_grid = np.zeros(len(pairs), np.int32)
     plan = GhostRenderPlan(lens, pairs, boosts, sources, grids, pair_grid, spec, corr, width, height,
-                           sensor_half_w, sensor_half_h, config.flare_gain, apply_corr, plain_per_pair)
+                           sensor_half_w, sensor_half_h, config.flare_gain, apply_corr, plain_per_pair,
+                           cull_dead_pairs=bool(config.cull_dead_pairs), blades_override=bo,
+                           rotation_deg=rot)
     plan.pairs, plan.boosts, plan.grids, plan.pair_grid = pairs, boosts, grids, pair_grid
     plan.grid_sides = list(uniq)
     plan.spec, plan.correction, plan.apply_correction = spec, corr, apply_corr

@@ -191,6 +191,12 @@ int gl_trace_rays(const gl_surface* surfaces, int n,
  * per-ghost loop shape, ghost_render.cu:1544-1557, kept as a baseline).
  * pair_grid[i] selects which pupil grid pair i samples (adaptive grids);
  * grid_offsets has n_grids+1 entries into `samples`.
+ * With cull_dead_pairs (and more than one pair, and not the three-sample
+ * preview table) the frame first runs the reference's off-sensor probe —
+ * three wang-jittered 40x40 pupil passes over every wavelength with the
+ * frame inflated by 1.25 — on the device, and the render skips every pair no
+ * probe ray landed for; there is no host round trip.  plain_per_pair renders
+ * every pair (the reference's per-pair loop culls nothing, :1000).
  * Outputs are planar float32 W x H, overwritten.  Asynchronous. */
 typedef struct gl_ghost_render_params {
     int32_t width, height;
@@ -201,6 +207,9 @@ typedef struct gl_ghost_render_params {
     float   correction[9];
     int32_t plain_per_pair;          /* 1 = one launch per pair (baseline)  */
     int32_t splat_mode;              /* 0 = bilinear point splat (reference) */
+    int32_t cull_dead_pairs;         /* off-sensor probe cull, ghost_render.cu:976-1238 */
+    int32_t blades_override;         /* sampler override for the probe grids */
+    float   rotation_deg;
 } gl_ghost_render_params;
 
 int gl_render_ghosts(const gl_surface* surfaces, int n_surfaces,
@@ -230,9 +239,13 @@ int gl_ghost_plan_create(const gl_surface* surfaces, int n_surfaces,
                          const gl_ghost_render_params* params, gl_ghost_plan** out);
 int gl_ghost_plan_execute(gl_ghost_plan* plan, float* d_out_r, float* d_out_g,
                           float* d_out_b, void* stream);
-/* rays = ray-wavelength traces per execute; n_items = 256-sample work items;
+/* rays = ray-wavelength traces per execute at most (render + probe passes);
+ * n_items = 32-sample work items;
  * grid = CTAs of the persistent launch. */
 int gl_ghost_plan_info(const gl_ghost_plan* plan, long long* rays, int* n_items, int* grid);
+/* Per-pair probe hit counts of the last execute (0 = culled); all 1 when the
+ * plan does not cull.  Synchronous. */
+int gl_ghost_plan_pair_hits(const gl_ghost_plan* plan, int32_t* out, int n);
 int gl_ghost_plan_destroy(gl_ghost_plan* plan);
 
 /* Number of kernel launches issued by the last device call on this thread. */

@@ -118,6 +118,9 @@ def main():
                                       "jitter_seed": 12345, "flare_gain": 5000.0, "source_rgb": 10.0,
                                       "min_ghost_intensity": 0.0, "source_xy": [0.5, 0.5],
                                       "origin": "validation/goldens/point_flare_sampling/double_gauss_0.5_0.5_b0_c0.npy"}
+    img["refgpu_pfs_dg_axial_c1/image"] = np.load(gold / "point_flare_sampling" / "double_gauss_0.5_0.5_b0_c1.npy")
+    meta["refgpu_pfs_dg_axial_c1"] = dict(meta["refgpu_pfs_dg_axial_c0"], cull=True,
+                                          origin="validation/goldens/point_flare_sampling/double_gauss_0.5_0.5_b0_c1.npy")
     img["refgpu_ab_dg_axial/image"] = np.load(gold / "aperture_baseline" / "double_gauss__ghost_axial.npy")
     meta["refgpu_ab_dg_axial"] = {"lens": "ref_DoubleGauss", "W": 192, "H": 192, "sensor_half": "calib",
                                   "ray_grid": 192, "spectral_samples": 8, "pupil_jitter": 2,

@@ -125,7 +125,8 @@ def test_render_adaptive_grids_cfg2_matches_oracle(pins, meta):
     assert rel_l2(got, want) < IMG_TOL
 
 
-@pytest.mark.parametrize("golden", ["refgpu_pfs_dg_axial_c0", "refgpu_ab_dg_axial", "refgpu_ab_hex_axial"])
+@pytest.mark.parametrize("golden", ["refgpu_pfs_dg_axial_c0", "refgpu_pfs_dg_axial_c1", "refgpu_ab_dg_axial",
+                                    "refgpu_ab_hex_axial"])
 def test_render_matches_reference_gpu_golden(pins, meta, ref_images, golden):
     """Against the reference renderer's own GPU output (validation/goldens,
     concentration off): same lens, sampling, spectral table and gain."""
@@ -136,7 +137,8 @@ def test_render_matches_reference_gpu_golden(pins, meta, ref_images, golden):
     cfg = gl.PointFlareConfig(ray_grid=m["ray_grid"], spectral_samples=m["spectral_samples"],
                               pupil_jitter=m["pupil_jitter"], jitter_seed=m["jitter_seed"],
                               flare_gain=m["flare_gain"], min_ghost_intensity=m["min_ghost_intensity"],
-                              source_r=m["source_rgb"], source_g=m["source_rgb"], source_b=m["source_rgb"])
+                              source_r=m["source_rgb"], source_g=m["source_rgb"], source_b=m["source_rgb"],
+                              cull_dead_pairs=bool(m.get("cull", False)))
     if m["sensor_half"] != "calib":
         cfg.sensor_half_w = cfg.sensor_half_h = float(m["sensor_half"])
     else:
@@ -213,3 +215,30 @@ def test_edge_cases(pins, meta, ref_images):
     with pytest.raises(ValueError):
         GhostRenderPlan(lens, pairs, boosts, ref_images["cfg1_small/source"], [grid], None, spec, corr,
                         0, 8, cal["sensor_half_w"], cal["sensor_half_h"], 1000.0)
+
+
+def test_off_sensor_cull_keeps_the_image(pins, meta):
+    """The device probe cull (three 40^2 wang-jittered passes, 1.25 margin)
+    drops pairs without changing the frame: configuration 2 at 15 deg."""
+    import ghostlight_gb300 as gl
+    from ghostlight_gb300.flare import filter_ghosts_device, prepare_ghost_render
+    lens = _lens(pins, "cfg2_wide_angle_24")
+    cal = meta["cfg2_wide_angle_24"]["calibration"]
+    hw, hh = cal["sensor_half_w"], cal["sensor_half_h"]
+    src = np.array([[np.radians(15.0), 0.0, 1.0, 1.0, 1.0]], np.float32)
+    imgs = {}
+    for cull in (False, True):
+        cfg = gl.FlareConfig(min_ghost_intensity=1e-6, spectral_samples=16, adaptive_grids=True,
+                             adaptive_grid_max=96, cull_dead_pairs=cull)
+        fr = filter_ghosts_device(lens, hw, hh, cfg)
+        plan = prepare_ghost_render(lens, src, 384, 384, cfg, hw, hh, filter_result=fr)
+        out = [torch.zeros((384, 384), device="cuda") for _ in range(3)]
+        plan.execute(*out)
+        torch.cuda.synchronize()
+        imgs[cull] = np.stack([o.cpu().numpy() for o in out])
+        if cull:
+            hits = plan.pair_hits()
+            assert (hits == 0).sum() > len(hits) // 4      # most pairs are off-sensor here
+        plan.close()
+    assert imgs[False].sum() > 0
+    assert rel_l2(imgs[True], imgs[False]) < 1e-4
