@@ -36,6 +36,7 @@ def _declare(lib):
     lib.gl_filter_ghost_pairs.argtypes = [P(gl_surface), i, f, f, P(gl_filter_params),
                                           P(gl_ghost_pair), P(f), P(f), i, P(i), P(i)]
     lib.gl_trace_rays.argtypes = [P(gl_surface), i, i, i, vp, i, vp, vp]
+    lib.gl_trace_rays_noalloc.argtypes = [P(gl_surface), i, i, i, vp, i, vp, vp]
     render_args = [P(gl_surface), i, P(gl_ghost_pair), P(f), P(C.c_int32), i,
                    P(gl_flare_source), i, P(gl_pupil_sample), P(C.c_int32), i,
                    P(gl_spectral_sample), i, P(gl_ghost_render_params)]

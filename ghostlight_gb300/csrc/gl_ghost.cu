@@ -979,3 +979,91 @@ int gl_trace_rays(const gl_surface* surfaces, int n, int bounce_a, int bounce_b,
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// Allocation-free batched trace
+//
+// Some callers cannot allocate device memory while they run: a plug-in hosted
+// by an application that owns the device heap through its own allocator, code
+// on a real-time thread where an allocation's latency (and the device-wide
+// synchronisation cudaMalloc may imply) is not allowed, or a host that has
+// already reserved the whole device.  For them this entry point keeps the
+// only scratch the trace needs — the packed lens records and dispersion
+// terms — in one fixed array in device memory that is part of this library,
+// sized for the largest lens the path accepts (64 surfaces).  The caller
+// still passes the ray buffer and the result buffer.
+//
+// The array's device address is looked up once per device, with that device
+// current, on the first call made on it; make that first call before any
+// stream capture.  All calls share the array and it keeps whatever the last
+// call wrote: each call overwrites the records it uses before launching, and
+// calls that overlap on the GPU (other threads or streams) race on it.
+// ===========================================================================
+namespace gl {
+
+constexpr int kNoAllocMaxSurfaces = 64;
+
+struct NoAllocTables {
+    SurfRec recs[kNoAllocMaxSurfaces];
+    DispRec disp[kNoAllocMaxSurfaces];
+};
+
+static __device__ __align__(256) unsigned char g_trace_tables[sizeof(NoAllocTables)];
+
+static std::mutex g_trace_tables_mutex;
+static void* g_trace_tables_addr[64] = {};
+
+static int trace_tables_address(int device, void** out)
+{
+    if (device < 0 || device >= 64) return fail(GL_ERR_INVALID, "trace_rays_noalloc: device ordinal out of range");
+    std::lock_guard<std::mutex> lock(g_trace_tables_mutex);
+    if (g_trace_tables_addr[device] == nullptr)
+    {
+        void* ptr = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&ptr, g_trace_tables);
+        if (e != cudaSuccess || ptr == nullptr)
+            return fail(GL_ERR_CUDA, std::string("trace_rays_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+        g_trace_tables_addr[device] = ptr;
+    }
+    *out = g_trace_tables_addr[device];
+    return GL_OK;
+}
+
+}  // namespace gl
+
+extern "C" int gl_trace_rays_noalloc(const gl_surface* surfaces, int n, int bounce_a, int bounce_b,
+                                     const float* d_rays, int n_rays, float* d_out, void* stream)
+{
+    if (!surfaces || n <= 0) return fail(GL_ERR_INVALID, "trace_rays_noalloc: lens has no surfaces");
+    if (n > kNoAllocMaxSurfaces)
+        return fail(GL_ERR_INVALID, "trace_rays_noalloc: lens has more than 64 surfaces, the size of the fixed table");
+    if (bounce_b >= 0 && (bounce_a < 0 || bounce_a >= bounce_b || bounce_b >= n))
+        return fail(GL_ERR_INVALID, "bounce indices must satisfy 0 <= bounce_a < bounce_b < num_surfaces");
+    if (n_rays < 0 || (n_rays > 0 && (!d_rays || !d_out))) return fail(GL_ERR_INVALID, "trace_rays_noalloc: bad ray buffers");
+    if (n_rays == 0) return GL_OK;
+    int device = 0;
+    GL_CUDA_TRY(cudaGetDevice(&device));
+    void* base = nullptr;
+    int rc = trace_tables_address(device, &base);
+    if (rc) return rc;
+    NoAllocTables host;   // staged on the stack: no heap, no device allocation
+    rc = pack_lens(surfaces, n, host.recs);
+    if (rc) return rc;
+    for (int i = 0; i < n; ++i)
+    {
+        host.disp[i].model = surfaces[i].disp_model;
+        host.disp[i].nd = surfaces[i].ior; host.disp[i].vd = surfaces[i].abbe_v; host.disp[i].pad = 0.0f;
+        for (int k = 0; k < 3; ++k) { host.disp[i].B[k] = surfaces[i].sellmeier_B[k]; host.disp[i].C[k] = surfaces[i].sellmeier_C[k]; }
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    NoAllocTables* dev_tables = static_cast<NoAllocTables*>(base);
+    GL_CUDA_TRY(cudaMemcpyAsync(dev_tables->recs, host.recs, sizeof(SurfRec) * n, cudaMemcpyHostToDevice, st));
+    GL_CUDA_TRY(cudaMemcpyAsync(dev_tables->disp, host.disp, sizeof(DispRec) * n, cudaMemcpyHostToDevice, st));
+    trace_rays_kernel<<<(n_rays + 127) / 128, 128, 0, st>>>(dev_tables->recs, dev_tables->disp, n, bounce_a,
+                                                            bounce_b, d_rays, n_rays, d_out);
+    GL_CUDA_TRY(cudaGetLastError());
+    // The staging copy lives on this stack frame until the copies are done.
+    GL_CUDA_TRY(cudaStreamSynchronize(st));
+    g_last_launches = 1;
+    return GL_OK;
+}

@@ -184,6 +184,20 @@ int gl_trace_rays(const gl_surface* surfaces, int n,
                   int bounce_a, int bounce_b,
                   const float* d_rays, int n_rays, float* d_out, void* stream);
 
+/* Allocation-free form of gl_trace_rays, for callers that may not allocate
+ * device memory while they run (a plug-in whose host application owns the
+ * device heap, a real-time thread, a host that reserved the whole device).
+ * No counterpart in the reference.  Same arguments and results as
+ * gl_trace_rays; the packed lens tables go to a fixed array inside the library
+ * (at most 64 surfaces; larger lenses are rejected with GL_ERR_INVALID), so the
+ * call allocates no device memory.  The array's address is looked up on the
+ * first call on each device (make that call before any stream capture).  All
+ * calls share the array; calls that overlap on the GPU race on it.
+ * Synchronous on `stream`. */
+int gl_trace_rays_noalloc(const gl_surface* surfaces, int n,
+                          int bounce_a, int bounce_b,
+                          const float* d_rays, int n_rays, float* d_out, void* stream);
+
 /* Ghost render: the main scatter of launch_ghost_render,
  * ghostlight/src/ghost_render.cu:630-1442 (kernel :209-491, colour
  * correction :610-622).  All pairs x sources are traced by ONE persistent
