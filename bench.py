@@ -212,6 +212,7 @@ def run_gpu(args, rank, world):
               sum(len(g) for g in plan.grids) * 8 + plan.n_items * 16 + len(plan.pairs) * 16 + 32)
     d2h = 3 * W * H * 4
 
+    traced = plan.traced()            # traces of the last (timed) execute: deterministic per frame
     sec = float(sum(t_batched))
     if world > 1:
         t = torch.tensor([sec], device=dev)
@@ -220,7 +221,7 @@ def run_gpu(args, rank, world):
     frames = args.steps * world
     value = frames / sec
     ms_step = 1e3 * sec / args.steps
-    rays_per_s = plan.rays * frames / sec
+    rays_per_s = traced * frames / sec
     plain_fps = len(t_plain) / sum(t_plain)
     res = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -233,7 +234,8 @@ def run_gpu(args, rank, world):
                    "pairs": int(len(plan.pairs)), "grid_sides": plan.grid_sides,
                    "l2": "flushed (512 MB write) between timed steps", "parallelism": "replicas"},
         "rays_per_s": rays_per_s,
-        "ray_lambda_traces_per_frame": plan.rays,
+        "ray_lambda_traces_per_frame": traced,
+        "frame_ray_lambda_before_cull": plan.rays,
         "plain_per_pair": {"value": plain_fps, "unit": UNIT, "ms_per_step": 1e3 / plain_fps,
                            "launches_per_step": len(plan.pairs) + 1},
         "speedup_batched_vs_plain": value / world / plain_fps,
@@ -376,14 +378,18 @@ def roofline(res, plan):
     flops_per_trace = FLOPS_PER_RAY_LAMBDA
     peak = FP32_PEAK_TFLOPS
     sec = res["ms_per_step"] / 1e3
-    achieved = plan.rays * flops_per_trace / sec / 1e12 if flops_per_trace else None
+    achieved = res["ray_lambda_traces_per_frame"] * flops_per_trace / sec / 1e12 if flops_per_trace else None
     return {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
             "frac": (achieved / peak) if (achieved and peak) else None, "traffic": None,
             "kernel": "ghost_render_kernel",
             "peak_note": "GB300 FP32 CUDA-core peak: 152 SMs x 128 lanes x 2 FLOP x max SM clock"}
 
 
-FLOPS_PER_RAY_LAMBDA = None   # set from the ncu instruction counts
+# FP32 operations per traced ray-wavelength (FADD + FMUL + 2 x FFMA, thread
+# level) of the reference-formulation render kernel on this workload, measured
+# once with ncu (smsp__sass_thread_inst_executed_op_{fadd,fmul,ffma}_pred_on:
+# 2.02e11 FLOP over 1.793e8 traces) and frozen as the algorithmic count.
+FLOPS_PER_RAY_LAMBDA = 1126.0
 FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.070e9 / 1e12
 
 

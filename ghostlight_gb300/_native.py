@@ -46,6 +46,7 @@ def _declare(lib):
     lib.gl_ghost_plan_info.argtypes = [vp, P(C.c_longlong), P(i), P(i)]
     lib.gl_ghost_plan_destroy.argtypes = [vp]
     lib.gl_ghost_plan_pair_hits.argtypes = [vp, P(C.c_int32), i]
+    lib.gl_ghost_plan_traced.argtypes = [vp, P(C.c_longlong)]
     return lib
 
 

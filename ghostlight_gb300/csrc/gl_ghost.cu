@@ -65,6 +65,7 @@ struct RenderArgs {
     int* counter;             // persistent queue head; null = static item assignment
     float4* accum;            // RGBA, width x height
     int* pair_hits;           // off-sensor cull: per-pair probe hits (null = no cull)
+    unsigned long long* traced;   // ray-wavelength traces executed (null = not counted)
     int n_surf, n_spec, n_items, item_base;
     int width, height;
     float fmt_w, fmt_h, fmt_x0, fmt_y0;
@@ -321,9 +322,12 @@ __device__ __forceinline__ void trace_warp(const RenderArgs& A, const SurfRec* l
     const int L1 = b + 1, L2 = L1 + (b - a), L = L2 + (n - 1 - a);
     int cx = INT_MIN, cy = INT_MIN;
 
+    const unsigned n_lanes = __popc(__ballot_sync(kFull, active));
+    int n_lambda = 0;
     #pragma unroll 1
     for (int li = 0; li < A.n_spec; ++li)
     {
+        ++n_lambda;
         const float4 sp = spec[li];
         const float kdelta = kdel[li];
         const float* atl = at + li * n;
@@ -366,7 +370,11 @@ __device__ __forceinline__ void trace_warp(const RenderArgs& A, const SurfRec* l
             }
             if (__any_sync(kFull, hit))
             {
-                if ((threadIdx.x & 31) == 0) atomicAdd(A.pair_hits + pair, 1);
+                if ((threadIdx.x & 31) == 0)
+                {
+                    atomicAdd(A.pair_hits + pair, 1);
+                    if (A.traced) atomicAdd(A.traced, (unsigned long long)n_lanes * n_lambda);
+                }
                 return;
             }
         }
@@ -376,6 +384,7 @@ __device__ __forceinline__ void trace_warp(const RenderArgs& A, const SurfRec* l
         }
     }
     if (!PROBE && cx != INT_MIN) flush_taps(A.accum, A.width, A.height, cx, cy, acc);
+    if (A.traced && (threadIdx.x & 31) == 0) atomicAdd(A.traced, (unsigned long long)n_lanes * n_lambda);
 }
 
 template <bool PROBE>
@@ -516,7 +525,9 @@ struct GhostPlan {
     int probe_begin[4] = {0, 0, 0, 0};   // item range of each pass
     int* pair_hits = nullptr;
     int* probe_counters = nullptr;
+    int* pair_hits_init = nullptr;          // 1 = not probed (always rendered), 0 = probed
     long long probe_rays = 0;
+    unsigned long long* traced = nullptr;   // traces executed by the last execute
 };
 
 static void plan_free(GhostPlan* p)
@@ -526,6 +537,7 @@ static void plan_free(GhostPlan* p)
     cudaFree(p->items); cudaFree(p->pairs); cudaFree(p->sources); cudaFree(p->samples);
     cudaFree(p->counter); cudaFree(p->accum);
     cudaFree(p->probe_items); cudaFree(p->probe_samples); cudaFree(p->pair_hits); cudaFree(p->probe_counters);
+    cudaFree(p->traced); cudaFree(p->pair_hits_init);
     delete p;
 }
 
@@ -656,8 +668,25 @@ int plan_create(const gl_surface* surfaces, int n_surf, const gl_ghost_pair* pai
     p->cull = prm->cull_dead_pairs && n_pairs > 1 && n_spec != 3 && !prm->plain_per_pair;
     std::vector<int4> pitems;
     std::vector<gl_pupil_sample> psamples;
+    std::vector<int> hits_init((size_t)n_pairs, 1);
     if (p->cull)
     {
+        // A pair is probed only when its own grid is larger than the three
+        // probe passes: rendering a pair that lands nowhere costs less than
+        // proving it, and never changes the image.
+        int n_probe_samples = 0;
+        for (int pass = 0; pass < 3; ++pass)
+        {
+            gl_sampler_params sp{40, 1, (int)(0x9E3779B9u * (unsigned)(pass + 1)), prm->blades_override, prm->rotation_deg};
+            std::vector<gl_pupil_sample> g;
+            if (build_aperture_samples(surfaces, n_surf, sp, g) == GL_OK) n_probe_samples += (int)g.size();
+        }
+        for (int i = 0; i < n_pairs; ++i)
+        {
+            const int gi = pair_grid ? pair_grid[i] : 0;
+            const int ng = grid_offsets[gi + 1] - grid_offsets[gi];
+            hits_init[i] = (ng > n_probe_samples) ? 0 : 1;
+        }
         for (int pass = 0; pass < 3; ++pass)
         {
             gl_sampler_params sp;
@@ -673,10 +702,13 @@ int plan_create(const gl_surface* surfaces, int n_surf, const gl_ghost_pair* pai
             psamples.insert(psamples.end(), g.begin(), g.end());
             p->probe_begin[pass] = (int)pitems.size();
             for (int i = 0; i < n_pairs; ++i)
+            {
+                if (hits_init[i]) continue;
                 for (int s = 0; s < n_src; ++s)
                     for (int t = 0; t < (int)g.size(); t += kTile)
                         pitems.push_back(make_int4(i, s, base + t, std::min(kTile, (int)g.size() - t)));
-            p->probe_rays += (long long)g.size() * n_src * n_pairs * n_spec;
+                p->probe_rays += (long long)g.size() * n_src * n_spec;
+            }
         }
         p->probe_begin[3] = (int)pitems.size();
     }
@@ -693,11 +725,13 @@ int plan_create(const gl_surface* surfaces, int n_surf, const gl_ghost_pair* pai
     chk(upload(&p->sources, src.data(), src.size()));
     chk(upload(&p->samples, reinterpret_cast<const float2*>(ordered.data()), (size_t)n_samples));
     chk(cudaMalloc(&p->counter, sizeof(int)));
+    chk(cudaMalloc(&p->traced, sizeof(unsigned long long)));
     if (p->cull)
     {
         chk(upload(&p->probe_items, pitems.data(), pitems.size()));
         chk(upload(&p->probe_samples, reinterpret_cast<const float2*>(psamples.data()), psamples.size()));
         chk(cudaMalloc(&p->pair_hits, sizeof(int) * std::max(1, n_pairs)));
+        chk(upload(&p->pair_hits_init, hits_init.data(), hits_init.size()));
         chk(cudaMalloc(&p->probe_counters, sizeof(int) * 4));
     }
     chk(cudaMalloc(&p->accum, (size_t)prm->width * prm->height * sizeof(float4)));
@@ -739,11 +773,14 @@ int plan_execute(GhostPlan* p, float* d_out_r, float* d_out_g, float* d_out_b, c
     A.gain = p->prm.flare_gain;
     A.front_R = p->front_R; A.start_z = p->start_z;
     A.pair_hits = nullptr;
+    A.traced = p->traced;
+    GL_CUDA_TRY(cudaMemsetAsync(p->traced, 0, sizeof(unsigned long long), st));
     if (p->cull && p->n_items > 0)
     {
         // Probe passes: the frame inflated by CULL_MARGIN = 1.25
         // (ghost_render.cu:148), persistent launches over the probe items.
-        GL_CUDA_TRY(cudaMemsetAsync(p->pair_hits, 0, sizeof(int) * p->n_pairs, st));
+        GL_CUDA_TRY(cudaMemcpyAsync(p->pair_hits, p->pair_hits_init, sizeof(int) * p->n_pairs,
+                                    cudaMemcpyDeviceToDevice, st));
         GL_CUDA_TRY(cudaMemsetAsync(p->probe_counters, 0, sizeof(int) * 4, st));
         RenderArgs B = A;
         B.samples = p->probe_samples;
@@ -906,6 +943,15 @@ int gl_ghost_plan_info(const gl_ghost_plan* plan, long long* rays, int* n_items,
     if (rays) *rays = plan->p->rays + plan->p->probe_rays;
     if (n_items) *n_items = plan->p->n_items;
     if (grid) *grid = plan->p->grid_persistent;
+    return GL_OK;
+}
+
+int gl_ghost_plan_traced(const gl_ghost_plan* plan, long long* out)
+{
+    if (!plan || !out) return fail(GL_ERR_INVALID, "ghost_plan_traced: bad arguments");
+    unsigned long long v = 0;
+    GL_CUDA_TRY(cudaMemcpy(&v, plan->p->traced, sizeof(v), cudaMemcpyDeviceToHost));
+    *out = (long long)v;
     return GL_OK;
 }
 

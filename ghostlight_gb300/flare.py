@@ -265,6 +265,12 @@ class GhostRenderPlan:
                                                       out_b.data_ptr(), st), "render_ghosts")
         return _native.last_launch_count()
 
+    def traced(self) -> int:
+        """Ray-wavelength traces the last execute ran (render + probes)."""
+        v = C.c_longlong()
+        _native.check(self._lib.gl_ghost_plan_traced(self._h, C.byref(v)), "traced")
+        return int(v.value)
+
     def pair_hits(self):
         """Probe hits per pair from the last execute (0 = culled)."""
         out = (C.c_int32 * max(1, self.n_pairs))()

@@ -257,6 +257,9 @@ int gl_ghost_plan_execute(gl_ghost_plan* plan, float* d_out_r, float* d_out_g,
  * n_items = 32-sample work items;
  * grid = CTAs of the persistent launch. */
 int gl_ghost_plan_info(const gl_ghost_plan* plan, long long* rays, int* n_items, int* grid);
+/* Ray-wavelength traces the last execute ran (render + cull probes; a probe
+ * warp stops at its first on-sensor hit).  Synchronous. */
+int gl_ghost_plan_traced(const gl_ghost_plan* plan, long long* out);
 /* Per-pair probe hit counts of the last execute (0 = culled); all 1 when the
  * plan does not cull.  Synchronous. */
 int gl_ghost_plan_pair_hits(const gl_ghost_plan* plan, int32_t* out, int n);

@@ -228,8 +228,8 @@ def test_off_sensor_cull_keeps_the_image(pins, meta):
     src = np.array([[np.radians(15.0), 0.0, 1.0, 1.0, 1.0]], np.float32)
     imgs = {}
     for cull in (False, True):
-        cfg = gl.FlareConfig(min_ghost_intensity=1e-6, spectral_samples=16, adaptive_grids=True,
-                             adaptive_grid_max=96, cull_dead_pairs=cull)
+        cfg = gl.FlareConfig(min_ghost_intensity=1e-6, spectral_samples=16, ray_grid=112,
+                             cull_dead_pairs=cull)
         fr = filter_ghosts_device(lens, hw, hh, cfg)
         plan = prepare_ghost_render(lens, src, 384, 384, cfg, hw, hh, filter_result=fr)
         out = [torch.zeros((384, 384), device="cuda") for _ in range(3)]
