@@ -47,6 +47,7 @@ def _declare(lib):
     lib.gl_ghost_plan_destroy.argtypes = [vp]
     lib.gl_ghost_plan_pair_hits.argtypes = [vp, P(C.c_int32), i]
     lib.gl_ghost_plan_traced.argtypes = [vp, P(C.c_longlong)]
+    lib.gl_gemm_bf16_tc.argtypes = [vp, vp, vp, i, i, i, vp]
     return lib
 
 

@@ -265,6 +265,16 @@ int gl_ghost_plan_traced(const gl_ghost_plan* plan, long long* out);
 int gl_ghost_plan_pair_hits(const gl_ghost_plan* plan, int32_t* out, int n);
 int gl_ghost_plan_destroy(gl_ghost_plan* plan);
 
+/* ---- tensor-core building blocks (tcgen05) -------------------------------- */
+
+/* C[M x N] (float32, row-major) = A[M x K] * B[N x K]^T with BF16 operands
+ * (row-major, device) and FP32 accumulation in tensor memory: the TMA +
+ * tcgen05 pipeline the matrix-DFT starburst is built on, exposed so it can
+ * be checked against a library GEMM.  M, N multiples of 128, K of 64.
+ * No counterpart in the reference (its starburst uses SIMT dot products,
+ * mdft_render.cu:137-172).  Synchronous. */
+int gl_gemm_bf16_tc(const void* d_a, const void* d_b, float* d_c, int M, int N, int K, void* stream);
+
 /* Number of kernel launches issued by the last device call on this thread. */
 int gl_last_launch_count(void);
 
