@@ -48,6 +48,11 @@ def _declare(lib):
     lib.gl_ghost_plan_pair_hits.argtypes = [vp, P(C.c_int32), i]
     lib.gl_ghost_plan_traced.argtypes = [vp, P(C.c_longlong)]
     lib.gl_gemm_bf16_tc.argtypes = [vp, vp, vp, i, i, i, vp]
+    d = C.c_double
+    lib.gl_mdft_plan_create.argtypes = [i, i, i, P(d), P(d), d, d, P(f), i, vp, P(vp)]
+    lib.gl_mdft_plan_execute.argtypes = [vp, vp, vp, vp, vp, vp]
+    lib.gl_mdft_plan_status.argtypes = [vp, P(i)]
+    lib.gl_mdft_plan_destroy.argtypes = [vp]
     return lib
 
 

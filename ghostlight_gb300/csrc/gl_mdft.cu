@@ -8,9 +8,11 @@
 #include "gl_tc.cuh"
 
 #include <cuda.h>
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <vector>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -184,5 +186,660 @@ extern "C" int gl_gemm_bf16_tc(const void* d_a, const void* d_b, float* d_c, int
     cudaFreeAsync(d_err, st);
     g_last_launches = 1;
     if (h_err) return fail(GL_ERR_TIMEOUT, "gemm_bf16_tc: a pipeline wait timed out (code " + std::to_string(h_err) + ")");
+    return GL_OK;
+}
+
+// ===========================================================================
+// Matrix-DFT starburst, field form:  E_l = W_y(l) A W_x(l)^T,  I_l = |E_l|^2,
+// out_c = sum_l w_c(l) I_l   (the benchmark spec's form of mdft_render.cu's
+// per-wavelength triple product, evaluated on the tensor cores).
+//
+//   W_x[k][j] = exp(-2 pi i s_x(l) (j - c_j)(k - c_x)),  same for y.
+//
+// Step 1: T'[k][i] = sum_j W_x[k][j] A[i][j]          (K_out x n, complex)
+// Step 2: E[l][k]  = sum_i W_y[l][i] T'[k][i]         (K_out x K_out, complex)
+//
+// FORM 0 (split BF16): every operand X is stored as X_hi = bf16(X) and
+// X_lo = bf16(X - X_hi); the three-term product A_hi B_hi + A_hi B_lo +
+// A_lo B_hi is one GEMM over a tripled reduction axis, A' = [hi | hi | lo],
+// B' = [hi | lo | hi].  FORM 1 (TF32): FP32 operands, kind::tf32 MMAs.
+// Accumulation is FP32 in TMEM throughout.
+//
+// Complex products: step 2 keeps, per 128 output columns, the three row
+// blocks [-Ti | Tr | Ti] of T' next to each other in shared memory, so one
+// N = 256 MMA against [Tr | Ti] (A = Wr) and one against [-Ti | Tr] (A = Wi)
+// accumulate [Re E | Im E] together.
+// ===========================================================================
+namespace gl {
+namespace {
+
+constexpr int kMdftThreads = 192;     // warps 0-3 epilogue, warp 4 TMA, warp 5 MMA
+constexpr int kOpTile = 128 * 128;    // bytes of one 128-row x 128-byte operand tile
+
+struct MdftArgs {
+    int K_out, n, n_lambda, Kp, nkb, NB, NI, n_units;
+    void* tprime;                     // step 1 output / step 2 B operand
+    float* out_r;
+    float* out_g;
+    float* out_b;
+    const float4* weights;            // per wavelength (w_r, w_g, w_b, 0)
+    int* err;
+};
+
+template <int FORM>
+__device__ __forceinline__ void mma_any(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc)
+{
+    if (FORM == 0) tc::mma_f16(d, a, b, idesc, acc);
+    else tc::mma_tf32(d, a, b, idesc, acc);
+}
+
+template <int FORM>
+__host__ __device__ constexpr uint32_t idesc_any(int M, int N)
+{
+    return FORM == 0 ? tc::idesc_bf16(M, N, false) : tc::idesc_tf32(M, N, false);
+}
+
+__device__ __forceinline__ void store_split16(__nv_bfloat16* row, int n, int i0, const float (&v)[16], float sign)
+{
+    // [hi | lo | hi] at columns i0, n + i0, 2n + i0
+    __align__(16) __nv_bfloat16 hi[16], lo[16];
+    #pragma unroll
+    for (int j = 0; j < 16; ++j)
+    {
+        const float x = sign * v[j];
+        hi[j] = __float2bfloat16_rn(x);
+        lo[j] = __float2bfloat16_rn(x - __bfloat162float(hi[j]));
+    }
+    const uint4* h4 = reinterpret_cast<const uint4*>(hi);
+    const uint4* l4 = reinterpret_cast<const uint4*>(lo);
+    uint4* d0 = reinterpret_cast<uint4*>(row + i0);
+    uint4* d1 = reinterpret_cast<uint4*>(row + n + i0);
+    uint4* d2 = reinterpret_cast<uint4*>(row + 2 * n + i0);
+    d0[0] = h4[0]; d0[1] = h4[1];
+    d1[0] = l4[0]; d1[1] = l4[1];
+    d2[0] = h4[0]; d2[1] = h4[1];
+}
+
+template <int FORM, int STEP>
+__global__ void __launch_bounds__(kMdftThreads, 1) mdft_kernel(const __grid_constant__ CUtensorMap tA,
+                                                              const __grid_constant__ CUtensorMap tB, MdftArgs args)
+{
+    constexpr int nB = (STEP == 2) ? 3 : 1;                      // B operand tiles per stage
+    constexpr int kStagesM = (STEP == 2) ? 2 : 4;
+    constexpr int kStageBytes = (2 + nB) * kOpTile;
+    constexpr int kbe = (FORM == 0) ? 64 : 32;                   // reduction elements per 128-byte row
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = align1024(smem_raw);
+    __shared__ uint64_t full[kStagesM], empty[kStagesM], acc_full[2], acc_empty[2], mma_done;
+    __shared__ uint32_t tmem_base;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int* err = args.err;
+
+    if (warp == 5) tc::tmem_alloc(&tmem_base, 512);
+    if (threadIdx.x == 128)
+    {
+        for (int s = 0; s < kStagesM; ++s) { tc::mbar_init(&full[s], 1); tc::mbar_init(&empty[s], 1); }
+        for (int b = 0; b < 2; ++b) { tc::mbar_init(&acc_full[b], 1); tc::mbar_init(&acc_empty[b], 128); }
+        tc::mbar_init(&mma_done, 1);
+        tc::fence_mbar_init();
+        tc::tma_prefetch(&tA);
+        tc::tma_prefetch(&tB);
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    const uint32_t tmem = tmem_base;
+
+    const int G = gridDim.x;
+    const int u0 = (int)(((long long)blockIdx.x * args.n_units) / G);
+    const int u1 = (int)(((long long)(blockIdx.x + 1) * args.n_units) / G);
+
+    auto decode = [&](int u, int& lam, int& mb, int& xb) {
+        if (STEP == 2)
+        {
+            const int tile = u / args.n_lambda;
+            lam = u % args.n_lambda;
+            mb = tile / args.NB;
+            xb = tile % args.NB;
+        }
+        else
+        {
+            lam = u / (args.NB * args.NI);
+            const int r = u % (args.NB * args.NI);
+            mb = r / args.NI;
+            xb = r % args.NI;
+        }
+    };
+
+    if (warp == 4)
+    {
+        if (lane == 0)
+        {
+            int it = 0, issued = 0;
+            bool stop = false;
+            for (int u = u0; u < u1 && !stop; ++u)
+            {
+                int lam, mb, xb;
+                decode(u, lam, mb, xb);
+                const int rowA = (lam * 2) * args.K_out + mb * 128;
+                for (int kb = 0; kb < args.nkb; ++kb, ++it)
+                {
+                    const int s = it % kStagesM, r = it / kStagesM;
+                    if (it >= kStagesM && !tc::mbar_wait(&empty[s], (r - 1) & 1, err, tc::TC_TIMEOUT_EMPTY)) { stop = true; break; }
+                    uint8_t* st = smem + s * kStageBytes;
+                    tc::mbar_expect_tx(&full[s], kStageBytes);
+                    const int x = kb * kbe;
+                    tc::tma_load_2d(st, &tA, x, rowA, &full[s]);
+                    tc::tma_load_2d(st + kOpTile, &tA, x, rowA + args.K_out, &full[s]);
+                    if (STEP == 2)
+                    {
+                        const int rowB = ((lam * args.NB + xb) * 3) * 128;
+                        #pragma unroll
+                        for (int j = 0; j < 3; ++j) tc::tma_load_2d(st + (2 + j) * kOpTile, &tB, x, rowB + j * 128, &full[s]);
+                    }
+                    else
+                    {
+                        tc::tma_load_2d(st + 2 * kOpTile, &tB, x, xb * 128, &full[s]);
+                    }
+                    ++issued;
+                }
+            }
+            for (int q = (issued > kStagesM ? issued - kStagesM : 0); q < issued; ++q)
+                tc::mbar_wait(&full[q % kStagesM], (q / kStagesM) & 1, err, tc::TC_TIMEOUT_FULL);
+        }
+        __syncwarp();
+    }
+    else if (warp == 5)
+    {
+        if (lane == 0)
+        {
+            const uint32_t id256 = idesc_any<FORM>(128, 256);
+            const uint32_t id128 = idesc_any<FORM>(128, 128);
+            int it = 0, ui = 0;
+            bool stop = false;
+            for (int u = u0; u < u1 && !stop; ++u, ++ui)
+            {
+                const int b = ui & 1, ur = ui >> 1;
+                if (ui >= 2 && !tc::mbar_wait(&acc_empty[b], (ur - 1) & 1, err, tc::TC_TIMEOUT_ACC_FREE)) break;
+                tc::tc_fence_after();
+                const uint32_t d = tmem + (uint32_t)(b * 256);
+                for (int kb = 0; kb < args.nkb; ++kb, ++it)
+                {
+                    const int s = it % kStagesM, r = it / kStagesM;
+                    if (!tc::mbar_wait(&full[s], r & 1, err, tc::TC_TIMEOUT_FULL)) { stop = true; break; }
+                    tc::tc_fence_after();
+                    uint8_t* st = smem + s * kStageBytes;
+                    const uint64_t aR = tc::sw128_desc(tc::smem_u32(st));
+                    const uint64_t aI = tc::sw128_desc(tc::smem_u32(st + kOpTile));
+                    if (STEP == 2)
+                    {
+                        const uint64_t bRI = tc::sw128_desc(tc::smem_u32(st + 3 * kOpTile));   // [Tr | Ti]
+                        const uint64_t bNR = tc::sw128_desc(tc::smem_u32(st + 2 * kOpTile));   // [-Ti | Tr]
+                        #pragma unroll
+                        for (int kk = 0; kk < 4; ++kk)
+                        {
+                            mma_any<FORM>(d, aR + 2 * kk, bRI + 2 * kk, id256, (kb | kk) != 0);
+                            mma_any<FORM>(d, aI + 2 * kk, bNR + 2 * kk, id256, 1u);
+                        }
+                    }
+                    else
+                    {
+                        const uint64_t bM = tc::sw128_desc(tc::smem_u32(st + 2 * kOpTile));
+                        #pragma unroll
+                        for (int kk = 0; kk < 4; ++kk)
+                        {
+                            mma_any<FORM>(d, aR + 2 * kk, bM + 2 * kk, id128, (kb | kk) != 0);
+                            mma_any<FORM>(d + 128, aI + 2 * kk, bM + 2 * kk, id128, (kb | kk) != 0);
+                        }
+                    }
+                    tc::mma_commit(&empty[s]);
+                }
+                tc::mma_commit(&acc_full[b]);
+            }
+            // every MMA this thread issued must be complete before TMEM is freed
+            tc::mma_commit(&mma_done);
+            tc::mbar_wait(&mma_done, 0, err, tc::TC_TIMEOUT_ACC);
+        }
+        __syncwarp();
+    }
+    else
+    {
+        // Epilogue warps 0-3: TMEM lane = tile row.
+        int ui = 0;
+        const int row = warp * 32 + lane;
+        for (int u = u0; u < u1; ++u, ++ui)
+        {
+            int lam, mb, xb;
+            decode(u, lam, mb, xb);
+            const int b = ui & 1, ur = ui >> 1;
+            const bool ok = tc::mbar_wait(&acc_full[b], ur & 1, err, tc::TC_TIMEOUT_ACC);
+            tc::tc_fence_after();
+            const uint32_t ta = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(b * 256);
+            if (STEP == 2)
+            {
+                const float4 w = args.weights[lam];
+                const size_t l = (size_t)(mb * 128 + row);
+                #pragma unroll 1
+                for (int c = 0; c < 8; ++c)
+                {
+                    float re[16], im[16];
+                    tc::tmem_ld16(ta + (uint32_t)(c * 16), re);
+                    tc::tmem_ld16(ta + 128u + (uint32_t)(c * 16), im);
+                    if (!ok) continue;
+                    const size_t base = l * (size_t)args.K_out + (size_t)(xb * 128 + c * 16);
+                    #pragma unroll
+                    for (int j = 0; j < 16; j += 4)
+                    {
+                        float I[4];
+                        #pragma unroll
+                        for (int q = 0; q < 4; ++q) I[q] = re[j + q] * re[j + q] + im[j + q] * im[j + q];
+                        atomicAdd(reinterpret_cast<float4*>(args.out_r + base + j), make_float4(w.x * I[0], w.x * I[1], w.x * I[2], w.x * I[3]));
+                        atomicAdd(reinterpret_cast<float4*>(args.out_g + base + j), make_float4(w.y * I[0], w.y * I[1], w.y * I[2], w.y * I[3]));
+                        atomicAdd(reinterpret_cast<float4*>(args.out_b + base + j), make_float4(w.z * I[0], w.z * I[1], w.z * I[2], w.z * I[3]));
+                    }
+                }
+            }
+            else
+            {
+                // T' rows of this k: [-Ti | Tr | Ti] blocks of 128 rows.
+                const int k = row;
+                const size_t blk = ((size_t)(lam * args.NB + mb) * 3) * 128;
+                #pragma unroll 1
+                for (int c = 0; c < 8; ++c)
+                {
+                    float re[16], im[16];
+                    tc::tmem_ld16(ta + (uint32_t)(c * 16), re);
+                    tc::tmem_ld16(ta + 128u + (uint32_t)(c * 16), im);
+                    if (!ok) continue;
+                    const int i0 = xb * 128 + c * 16;
+                    if (FORM == 0)
+                    {
+                        __nv_bfloat16* T = static_cast<__nv_bfloat16*>(args.tprime);
+                        store_split16(T + (blk + 0 * 128 + k) * (size_t)args.Kp, args.n, i0, im, -1.0f);
+                        store_split16(T + (blk + 1 * 128 + k) * (size_t)args.Kp, args.n, i0, re, 1.0f);
+                        store_split16(T + (blk + 2 * 128 + k) * (size_t)args.Kp, args.n, i0, im, 1.0f);
+                    }
+                    else
+                    {
+                        float* T = static_cast<float*>(args.tprime);
+                        float* r0 = T + (blk + 0 * 128 + k) * (size_t)args.Kp + i0;
+                        float* r1 = T + (blk + 1 * 128 + k) * (size_t)args.Kp + i0;
+                        float* r2 = T + (blk + 2 * 128 + k) * (size_t)args.Kp + i0;
+                        #pragma unroll
+                        for (int j = 0; j < 16; j += 4)
+                        {
+                            *reinterpret_cast<float4*>(r0 + j) = make_float4(-im[j], -im[j + 1], -im[j + 2], -im[j + 3]);
+                            *reinterpret_cast<float4*>(r1 + j) = make_float4(re[j], re[j + 1], re[j + 2], re[j + 3]);
+                            *reinterpret_cast<float4*>(r2 + j) = make_float4(im[j], im[j + 1], im[j + 2], im[j + 3]);
+                        }
+                    }
+                }
+            }
+            tc::tc_fence_before();
+            tc::mbar_arrive(&acc_empty[b]);
+        }
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    if (warp == 5) tc::tmem_dealloc(tmem, 512);
+}
+
+// DFT matrices W'[lam][part][k][Kp]: part 0 = Re, 1 = Im of
+// exp(-2 pi i s(lam) (j - cj)(k - ck)).  The phase is reduced in FP64
+// (the index product is exact) and the reduced angle evaluated in FP32.
+// FORM 0 stores [hi | hi | lo] along the reduction axis, FORM 1 the FP32 value.
+template <int FORM>
+__global__ void mdft_dft_kernel(void* out, int n_lambda, int K_out, int n, int Kp, const double* scale, double ck,
+                                double cj)
+{
+    const size_t total = (size_t)n_lambda * K_out * n;
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x)
+    {
+        const int j = (int)(e % n);
+        const int k = (int)((e / n) % K_out);
+        const int lam = (int)(e / ((size_t)n * K_out));
+        const double ph = scale[lam] * (((double)j - cj) * ((double)k - ck));
+        const double fr = ph - rint(ph);            // |fr| <= 1/2 cycles
+        float sv, cv;
+        sincospif((float)(2.0 * fr), &sv, &cv);
+        const float re = cv, im = -sv;
+        const size_t rr = ((size_t)(lam * 2 + 0) * K_out + k) * Kp;
+        const size_t ri = ((size_t)(lam * 2 + 1) * K_out + k) * Kp;
+        if (FORM == 0)
+        {
+            __nv_bfloat16* W = static_cast<__nv_bfloat16*>(out);
+            const __nv_bfloat16 rh = __float2bfloat16_rn(re), ih = __float2bfloat16_rn(im);
+            const __nv_bfloat16 rl = __float2bfloat16_rn(re - __bfloat162float(rh));
+            const __nv_bfloat16 il = __float2bfloat16_rn(im - __bfloat162float(ih));
+            W[rr + j] = rh; W[rr + n + j] = rh; W[rr + 2 * n + j] = rl;
+            W[ri + j] = ih; W[ri + n + j] = ih; W[ri + 2 * n + j] = il;
+        }
+        else
+        {
+            float* W = static_cast<float*>(out);
+            W[rr + j] = re;
+            W[ri + j] = im;
+        }
+    }
+}
+
+// Pupil amplitude A[i][j] (float, n x n) -> B operand [hi | lo | hi] or FP32.
+template <int FORM>
+__global__ void mdft_mask_kernel(const float* __restrict__ a, void* out, int n, int Kp)
+{
+    const size_t total = (size_t)n * n;
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x)
+    {
+        const int j = (int)(e % n), i = (int)(e / n);
+        const float v = a[e];
+        if (FORM == 0)
+        {
+            __nv_bfloat16* M = static_cast<__nv_bfloat16*>(out);
+            const __nv_bfloat16 h = __float2bfloat16_rn(v);
+            const __nv_bfloat16 l = __float2bfloat16_rn(v - __bfloat162float(h));
+            M[(size_t)i * Kp + j] = h; M[(size_t)i * Kp + n + j] = l; M[(size_t)i * Kp + 2 * n + j] = h;
+        }
+        else
+        {
+            static_cast<float*>(out)[(size_t)i * Kp + j] = v;
+        }
+    }
+}
+
+
+// ---- FP32 CUDA-core form -------------------------------------------------------
+// Register-tiled FP32 products on the SIMT pipes over the TF32 form's storage
+// (W' [lam][2][K_out][n], T' [lam][NB][3][128][n]); 256 threads, 128x128
+// tiles, 8x8 outputs per thread, K chunks of 16 staged in shared memory.
+constexpr int kSB = 128, kSK = 16;
+
+__global__ void __launch_bounds__(256) mdft_simt_step1(const float* __restrict__ W, const float* __restrict__ A,
+                                                       float* __restrict__ T, int K_out, int n, int NB)
+{
+    __shared__ float sWr[kSK][kSB + 4], sWi[kSK][kSB + 4], sA[kSK][kSB + 4];
+    const int lam = blockIdx.z, mb = blockIdx.y, ib = blockIdx.x;
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const float* Wr = W + ((size_t)(lam * 2 + 0) * K_out + mb * kSB) * n;
+    const float* Wi = W + ((size_t)(lam * 2 + 1) * K_out + mb * kSB) * n;
+    const float* Ab = A + (size_t)(ib * kSB) * n;
+    float cr[8][8] = {}, ci[8][8] = {};
+    for (int k0 = 0; k0 < n; k0 += kSK)
+    {
+        for (int e = threadIdx.x; e < kSB * kSK; e += 256)
+        {
+            const int r = e / kSK, c = e % kSK;
+            sWr[c][r] = Wr[(size_t)r * n + k0 + c];
+            sWi[c][r] = Wi[(size_t)r * n + k0 + c];
+            sA[c][r] = Ab[(size_t)r * n + k0 + c];
+        }
+        __syncthreads();
+        #pragma unroll
+        for (int kk = 0; kk < kSK; ++kk)
+        {
+            float wr[8], wi[8], a[8];
+            #pragma unroll
+            for (int q = 0; q < 8; ++q) { wr[q] = sWr[kk][ty * 8 + q]; wi[q] = sWi[kk][ty * 8 + q]; a[q] = sA[kk][tx * 8 + q]; }
+            #pragma unroll
+            for (int p = 0; p < 8; ++p)
+                #pragma unroll
+                for (int q = 0; q < 8; ++q) { cr[p][q] += wr[p] * a[q]; ci[p][q] += wi[p] * a[q]; }
+        }
+        __syncthreads();
+    }
+    const size_t blk = ((size_t)(lam * NB + mb) * 3) * 128;
+    #pragma unroll
+    for (int p = 0; p < 8; ++p)
+    {
+        const int k = ty * 8 + p;
+        #pragma unroll
+        for (int q = 0; q < 8; ++q)
+        {
+            const int i = ib * kSB + tx * 8 + q;
+            T[(blk + 0 * 128 + k) * n + i] = -ci[p][q];
+            T[(blk + 1 * 128 + k) * n + i] = cr[p][q];
+            T[(blk + 2 * 128 + k) * n + i] = ci[p][q];
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) mdft_simt_step2(const float* __restrict__ W, const float* __restrict__ T,
+                                                       const float4* __restrict__ weights, float* out_r, float* out_g,
+                                                       float* out_b, int K_out, int n, int NB, int n_lambda)
+{
+    __shared__ float sWr[kSK][kSB + 4], sWi[kSK][kSB + 4], sTr[kSK][kSB + 4], sTi[kSK][kSB + 4];
+    const int mb = blockIdx.y, nb = blockIdx.x;
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    for (int lam = 0; lam < n_lambda; ++lam)
+    {
+        const float* Wr = W + ((size_t)(lam * 2 + 0) * K_out + mb * kSB) * n;
+        const float* Wi = W + ((size_t)(lam * 2 + 1) * K_out + mb * kSB) * n;
+        const size_t blk = ((size_t)(lam * NB + nb) * 3) * 128;
+        const float* Tr = T + (blk + 128) * n;
+        const float* Ti = T + (blk + 256) * n;
+        float er[8][8] = {}, ei[8][8] = {};
+        for (int k0 = 0; k0 < n; k0 += kSK)
+        {
+            for (int e = threadIdx.x; e < kSB * kSK; e += 256)
+            {
+                const int r = e / kSK, c = e % kSK;
+                sWr[c][r] = Wr[(size_t)r * n + k0 + c];
+                sWi[c][r] = Wi[(size_t)r * n + k0 + c];
+                sTr[c][r] = Tr[(size_t)r * n + k0 + c];
+                sTi[c][r] = Ti[(size_t)r * n + k0 + c];
+            }
+            __syncthreads();
+            #pragma unroll 4
+            for (int kk = 0; kk < kSK; ++kk)
+            {
+                float wr[8], wi[8], tr[8], ti[8];
+                #pragma unroll
+                for (int q = 0; q < 8; ++q)
+                {
+                    wr[q] = sWr[kk][ty * 8 + q]; wi[q] = sWi[kk][ty * 8 + q];
+                    tr[q] = sTr[kk][tx * 8 + q]; ti[q] = sTi[kk][tx * 8 + q];
+                }
+                #pragma unroll
+                for (int p = 0; p < 8; ++p)
+                    #pragma unroll
+                    for (int q = 0; q < 8; ++q)
+                    {
+                        er[p][q] += wr[p] * tr[q] - wi[p] * ti[q];
+                        ei[p][q] += wr[p] * ti[q] + wi[p] * tr[q];
+                    }
+            }
+            __syncthreads();
+        }
+        // this block owns the tile across wavelengths: plain read-modify-write
+        const float4 w = weights[lam];
+        #pragma unroll
+        for (int p = 0; p < 8; ++p)
+        {
+            const size_t row = (size_t)(mb * kSB + ty * 8 + p) * K_out + nb * kSB + tx * 8;
+            #pragma unroll
+            for (int q = 0; q < 8; ++q)
+            {
+                const float I = er[p][q] * er[p][q] + ei[p][q] * ei[p][q];
+                out_r[row + q] += w.x * I; out_g[row + q] += w.y * I; out_b[row + q] += w.z * I;
+            }
+        }
+    }
+}
+
+}  // namespace
+
+// ---- MDFT plan ----------------------------------------------------------------
+struct MdftPlan {
+    int n = 0, K_out = 0, n_lambda = 0, form = 0, Kp = 0, elem = 2;
+    void* wx = nullptr;     // W_x' [lam][2][K_out][Kp]
+    void* wy = nullptr;     // W_y'
+    void* mask = nullptr;   // A'   [n][Kp]
+    void* tprime = nullptr; // T'   [lam][NB][3][128][Kp]
+    float4* weights = nullptr;
+    double* scales = nullptr;   // [2][n_lambda] device copy
+    int* err = nullptr;
+    CUtensorMap t_wx, t_wy, t_mask, t_tp;
+    int sms = 0;
+};
+
+static void mdft_free(MdftPlan* p)
+{
+    if (!p) return;
+    cudaFree(p->wx); cudaFree(p->wy); cudaFree(p->mask); cudaFree(p->tprime);
+    cudaFree(p->weights); cudaFree(p->scales); cudaFree(p->err);
+    delete p;
+}
+
+}  // namespace gl
+
+struct gl_mdft_plan { gl::MdftPlan* p; };
+
+extern "C" int gl_mdft_plan_create(int n, int K_out, int n_lambda, const double* scale_x, const double* scale_y,
+                                   double center_x, double center_y, const float* weights_rgb, int form,
+                                   void* stream, gl_mdft_plan** out)
+{
+    using namespace gl;
+    if (!out || !scale_x || !scale_y || !weights_rgb) return fail(GL_ERR_INVALID, "mdft_plan_create: null argument");
+    if (n <= 0 || n % 128 || K_out <= 0 || K_out % 128)
+        return fail(GL_ERR_INVALID, "mdft_plan_create: the pupil side n and output side K_out must be multiples of 128");
+    if (n_lambda < 1 || n_lambda > 1024) return fail(GL_ERR_INVALID, "mdft_plan_create: 1..1024 wavelengths");
+    if (form < 0 || form > 2)
+        return fail(GL_ERR_UNSUPPORTED, "mdft_plan_create: form must be 0 (split BF16), 1 (TF32) or 2 (FP32 CUDA cores)");
+    cudaStream_t st = (cudaStream_t)stream;
+    MdftPlan* p = new MdftPlan();
+    p->n = n; p->K_out = K_out; p->n_lambda = n_lambda; p->form = form;
+    p->Kp = form == 0 ? 3 * n : n;
+    p->elem = form == 0 ? 2 : 4;
+    const int NB = K_out / 128;
+    const int sform = form == 0 ? 0 : 1;   // storage: split BF16, or FP32 for TF32 / FP32 forms
+    (void)sform;
+    const size_t wbytes = (size_t)n_lambda * 2 * K_out * p->Kp * p->elem;
+    const size_t mbytes = (size_t)n * p->Kp * p->elem;
+    const size_t tbytes = (size_t)n_lambda * NB * 3 * 128 * p->Kp * p->elem;
+    cudaError_t e = cudaSuccess;
+    auto chk = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
+    chk(cudaMalloc(&p->wx, wbytes));
+    chk(cudaMalloc(&p->wy, wbytes));
+    chk(cudaMalloc(&p->mask, mbytes));
+    chk(cudaMalloc(&p->tprime, tbytes));
+    chk(cudaMalloc(&p->weights, sizeof(float4) * n_lambda));
+    chk(cudaMalloc(&p->scales, sizeof(double) * 2 * n_lambda));
+    chk(cudaMalloc(&p->err, sizeof(int)));
+    chk(cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, 0));
+    if (e != cudaSuccess)
+    {
+        mdft_free(p);
+        return fail(e == cudaErrorMemoryAllocation ? GL_ERR_OOM : GL_ERR_CUDA, std::string("mdft_plan_create: ") + cudaGetErrorString(e));
+    }
+    std::vector<float4> w((size_t)n_lambda);
+    for (int l = 0; l < n_lambda; ++l) w[l] = make_float4(weights_rgb[3 * l], weights_rgb[3 * l + 1], weights_rgb[3 * l + 2], 0.0f);
+    std::vector<double> sc((size_t)2 * n_lambda);
+    for (int l = 0; l < n_lambda; ++l) { sc[l] = scale_x[l]; sc[n_lambda + l] = scale_y[l]; }
+    chk(cudaMemcpy(p->weights, w.data(), sizeof(float4) * n_lambda, cudaMemcpyHostToDevice));
+    chk(cudaMemcpy(p->scales, sc.data(), sizeof(double) * 2 * n_lambda, cudaMemcpyHostToDevice));
+    const double cj = 0.5 * (n - 1);
+    const int blocks = 4 * p->sms;
+    if (form == 0)
+    {
+        mdft_dft_kernel<0><<<blocks, 256, 0, st>>>(p->wx, n_lambda, K_out, n, p->Kp, p->scales, center_x, cj);
+        mdft_dft_kernel<0><<<blocks, 256, 0, st>>>(p->wy, n_lambda, K_out, n, p->Kp, p->scales + n_lambda, center_y, cj);
+    }
+    else
+    {
+        mdft_dft_kernel<1><<<blocks, 256, 0, st>>>(p->wx, n_lambda, K_out, n, p->Kp, p->scales, center_x, cj);
+        mdft_dft_kernel<1><<<blocks, 256, 0, st>>>(p->wy, n_lambda, K_out, n, p->Kp, p->scales + n_lambda, center_y, cj);
+    }
+    chk(cudaGetLastError());
+    chk(cudaStreamSynchronize(st));
+    const CUtensorMapDataType dt = form == 0 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+    const uint32_t bc = form == 0 ? 64 : 32;
+    int rc = GL_OK;
+    if (e == cudaSuccess && form != 2)
+    {
+        rc = make_tmap_2d(&p->t_wx, p->wx, dt, p->elem, (uint64_t)n_lambda * 2 * K_out, (uint64_t)p->Kp, 128, bc);
+        if (!rc) rc = make_tmap_2d(&p->t_wy, p->wy, dt, p->elem, (uint64_t)n_lambda * 2 * K_out, (uint64_t)p->Kp, 128, bc);
+        if (!rc) rc = make_tmap_2d(&p->t_mask, p->mask, dt, p->elem, (uint64_t)n, (uint64_t)p->Kp, 128, bc);
+        if (!rc) rc = make_tmap_2d(&p->t_tp, p->tprime, dt, p->elem, (uint64_t)n_lambda * NB * 3 * 128, (uint64_t)p->Kp, 128, bc);
+    }
+    if (e != cudaSuccess || rc)
+    {
+        mdft_free(p);
+        if (rc) return rc;
+        return fail(GL_ERR_CUDA, std::string("mdft_plan_create: ") + cudaGetErrorString(e));
+    }
+    *out = new gl_mdft_plan{p};
+    return GL_OK;
+}
+
+extern "C" int gl_mdft_plan_execute(gl_mdft_plan* plan, const float* d_pupil, float* d_out_r, float* d_out_g,
+                                    float* d_out_b, void* stream)
+{
+    using namespace gl;
+    if (!plan || !d_pupil || !d_out_r || !d_out_g || !d_out_b) return fail(GL_ERR_INVALID, "mdft_plan_execute: null argument");
+    MdftPlan* p = plan->p;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int NB = p->K_out / 128, NI = p->n / 128;
+    const size_t npx = (size_t)p->K_out * p->K_out;
+    int launches = 0;
+    GL_CUDA_TRY(cudaMemsetAsync(p->err, 0, sizeof(int), st));
+    if (p->form == 0) mdft_mask_kernel<0><<<2 * p->sms, 256, 0, st>>>(d_pupil, p->mask, p->n, p->Kp);
+    else mdft_mask_kernel<1><<<2 * p->sms, 256, 0, st>>>(d_pupil, p->mask, p->n, p->Kp);
+    ++launches;
+    GL_CUDA_TRY(cudaMemsetAsync(d_out_r, 0, npx * sizeof(float), st));
+    GL_CUDA_TRY(cudaMemsetAsync(d_out_g, 0, npx * sizeof(float), st));
+    GL_CUDA_TRY(cudaMemsetAsync(d_out_b, 0, npx * sizeof(float), st));
+    MdftArgs a;
+    a.K_out = p->K_out; a.n = p->n; a.n_lambda = p->n_lambda; a.Kp = p->Kp;
+    a.nkb = p->Kp / (p->form == 0 ? 64 : 32);
+    a.NB = NB; a.NI = NI;
+    a.tprime = p->tprime; a.out_r = d_out_r; a.out_g = d_out_g; a.out_b = d_out_b;
+    a.weights = p->weights; a.err = p->err;
+    const size_t smem1 = 4 * 3 * (size_t)kOpTile + 1024, smem2 = 2 * 5 * (size_t)kOpTile + 1024;
+    // step 1
+    a.n_units = p->n_lambda * NB * NI;
+    int g1 = std::min(a.n_units, p->sms);
+    // step 2
+    MdftArgs a2 = a;
+    a2.n_units = NB * NB * p->n_lambda;
+    int g2 = std::min(a2.n_units, p->sms);
+    if (p->form == 2)
+    {
+        mdft_simt_step1<<<dim3(NI, NB, p->n_lambda), 256, 0, st>>>(static_cast<const float*>(p->wx),
+                                                                   static_cast<const float*>(p->mask),
+                                                                   static_cast<float*>(p->tprime), p->K_out, p->n, NB);
+        mdft_simt_step2<<<dim3(NB, NB), 256, 0, st>>>(static_cast<const float*>(p->wy), static_cast<const float*>(p->tprime),
+                                                      p->weights, d_out_r, d_out_g, d_out_b, p->K_out, p->n, NB, p->n_lambda);
+    }
+    else if (p->form == 0)
+    {
+        GL_CUDA_TRY(cudaFuncSetAttribute(mdft_kernel<0, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1));
+        GL_CUDA_TRY(cudaFuncSetAttribute(mdft_kernel<0, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2));
+        mdft_kernel<0, 1><<<g1, kMdftThreads, smem1, st>>>(p->t_wx, p->t_mask, a);
+        mdft_kernel<0, 2><<<g2, kMdftThreads, smem2, st>>>(p->t_wy, p->t_tp, a2);
+    }
+    else
+    {
+        GL_CUDA_TRY(cudaFuncSetAttribute(mdft_kernel<1, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1));
+        GL_CUDA_TRY(cudaFuncSetAttribute(mdft_kernel<1, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2));
+        mdft_kernel<1, 1><<<g1, kMdftThreads, smem1, st>>>(p->t_wx, p->t_mask, a);
+        mdft_kernel<1, 2><<<g2, kMdftThreads, smem2, st>>>(p->t_wy, p->t_tp, a2);
+    }
+    GL_CUDA_TRY(cudaGetLastError());
+    launches += 2;
+    g_last_launches = launches;
+    return GL_OK;
+}
+
+extern "C" int gl_mdft_plan_status(gl_mdft_plan* plan, int* err_code)
+{
+    if (!plan || !err_code) return gl::fail(GL_ERR_INVALID, "mdft_plan_status: null argument");
+    GL_CUDA_TRY(cudaMemcpy(err_code, plan->p->err, sizeof(int), cudaMemcpyDeviceToHost));
+    return GL_OK;
+}
+
+extern "C" int gl_mdft_plan_destroy(gl_mdft_plan* plan)
+{
+    if (!plan) return GL_OK;
+    gl::mdft_free(plan->p);
+    delete plan;
     return GL_OK;
 }

@@ -1,0 +1,89 @@
+"""Matrix-DFT starburst on the tensor cores (row d of the flare path).
+
+Field form of the reference's per-wavelength triple product
+(ghostlight/src/mdft_render.cu:137-173): E_l = W_y A W_x^T, I_l = |E_l|^2,
+out_c = sum_l w_c(l) I_l, with
+W[k][j] = exp(-2 pi i s_l (j - (n-1)/2)(k - c)).
+
+Forms: ``"split_bf16"`` (three-term split-BF16 tcgen05 products, FP32
+accumulation in tensor memory), ``"tf32"`` (tcgen05 kind::tf32) and ``"fp32"``
+(FP32 on the CUDA cores).  The DFT matrices are built once per plan and stay
+resident in HBM.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _native
+
+FORMS = {"split_bf16": 0, "tf32": 1, "fp32": 2}
+
+# algorithmic FLOPs of one wavelength (complex W x real A, then complex x
+# complex), K = output side, n = pupil side
+def flops_per_lambda(n: int, K: int) -> float:
+    return 2.0 * (2.0 * n * n * K + 4.0 * n * K * K)
+
+
+class MdftPlan:
+    def __init__(self, n: int, K: int, scale_x, scale_y, weights_rgb, form="split_bf16",
+                 center_x=None, center_y=None, stream=None):
+        import torch
+        self._lib = _native.load()
+        self.n, self.K = int(n), int(K)
+        sx = np.ascontiguousarray(scale_x, np.float64)
+        sy = np.ascontiguousarray(scale_y, np.float64)
+        w = np.ascontiguousarray(weights_rgb, np.float32).reshape(-1, 3)
+        if not (len(sx) == len(sy) == len(w)):
+            raise ValueError("mdft: scale_x, scale_y and weights need one entry per wavelength")
+        self.n_lambda = len(sx)
+        self.form = form
+        cx = self.K / 2.0 if center_x is None else float(center_x)
+        cy = self.K / 2.0 if center_y is None else float(center_y)
+        st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        D = C.c_double * self.n_lambda
+        h = C.c_void_p()
+        _native.check(self._lib.gl_mdft_plan_create(
+            self.n, self.K, self.n_lambda, D(*sx), D(*sy), cx, cy,
+            (C.c_float * w.size)(*w.reshape(-1)), FORMS[form], st, C.byref(h)), "mdft")
+        self._h = h
+
+    def execute(self, pupil, out_r, out_g, out_b, stream=None):
+        import torch
+        if not (pupil.is_cuda and pupil.dtype == torch.float32 and pupil.shape == (self.n, self.n)):
+            raise ValueError("mdft: pupil must be a float32 CUDA (n, n) tensor")
+        st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        _native.check(self._lib.gl_mdft_plan_execute(self._h, pupil.contiguous().data_ptr(), out_r.data_ptr(),
+                                                     out_g.data_ptr(), out_b.data_ptr(), st), "mdft")
+        return _native.last_launch_count()
+
+    def status(self) -> int:
+        v = C.c_int()
+        _native.check(self._lib.gl_mdft_plan_status(self._h, C.byref(v)), "mdft")
+        return int(v.value)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.gl_mdft_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def mdft_starburst_eform(pupil, K, scale_x, scale_y, weights_rgb, form="split_bf16"):
+    """One-shot: returns (3, K, K) float32 CUDA tensor."""
+    import torch
+    plan = MdftPlan(pupil.shape[0], K, scale_x, scale_y, weights_rgb, form)
+    out = torch.empty((3, K, K), dtype=torch.float32, device=pupil.device)
+    plan.execute(pupil, out[0], out[1], out[2])
+    torch.cuda.synchronize()
+    code = plan.status()
+    plan.close()
+    if code:
+        raise _native.GhostlightError("mdft: device pipeline wait timed out (code %d)" % code)
+    return out

@@ -275,6 +275,26 @@ int gl_ghost_plan_destroy(gl_ghost_plan* plan);
  * mdft_render.cu:137-172).  Synchronous. */
 int gl_gemm_bf16_tc(const void* d_a, const void* d_b, float* d_c, int M, int N, int K, void* stream);
 
+/* Matrix-DFT starburst in field form (the benchmark spec's E = W_y A W_x^T of
+ * mdft_render.cu's per-wavelength triple product): for each wavelength l,
+ *   W_x[k][j] = exp(-2 pi i scale_x[l] (j - (n-1)/2)(k - center_x)),
+ *   E_l = W_y A W_x^T  (K_out x K_out),  out_c += weights_rgb[3l+c] |E_l|^2.
+ * form 0: three-term split-BF16 products on tcgen05 with FP32 accumulation;
+ * form 1: TF32 tcgen05.  n and K_out multiples of 128.  The DFT matrices are
+ * built once (phase reduced in FP64) and stay resident in the plan.  The
+ * pupil amplitude is n x n float32 on the device; outputs are K_out x K_out
+ * planar float32, overwritten.  Asynchronous; gl_mdft_plan_status reads the
+ * device error word (non-zero = a bounded pipeline wait gave up). */
+typedef struct gl_mdft_plan gl_mdft_plan;
+int gl_mdft_plan_create(int n, int K_out, int n_lambda, const double* scale_x,
+                        const double* scale_y, double center_x, double center_y,
+                        const float* weights_rgb, int form, void* stream,
+                        gl_mdft_plan** out);
+int gl_mdft_plan_execute(gl_mdft_plan* plan, const float* d_pupil, float* d_out_r,
+                         float* d_out_g, float* d_out_b, void* stream);
+int gl_mdft_plan_status(gl_mdft_plan* plan, int* err_code);
+int gl_mdft_plan_destroy(gl_mdft_plan* plan);
+
 /* Number of kernel launches issued by the last device call on this thread. */
 int gl_last_launch_count(void);
 

@@ -1,0 +1,51 @@
+"""FP64 numpy oracle of the matrix-DFT starburst (TEST INFRASTRUCTURE ONLY).
+
+Field form: E_l = W_y A W_x^T with
+W[k][j] = exp(-2 pi i s_l (j - (n-1)/2)(k - c)), I_l = |E_l|^2,
+out_c = sum_l w_c(l) I_l — the per-wavelength triple product of the
+reference's mdft_render.cu:156-173 in the benchmark spec's field form.  Rows and
+columns can be restricted to a window so full-size outputs are checked on
+sub-windows.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def dft_matrix(n: int, K: int, s: float, c: float, rows=None) -> np.ndarray:
+    k = np.arange(K, dtype=np.float64) if rows is None else np.asarray(rows, np.float64)
+    j = np.arange(n, dtype=np.float64) - 0.5 * (n - 1)
+    ph = s * np.outer(k - c, j)
+    ph = ph - np.rint(ph)
+    return np.exp(-2j * np.pi * ph)
+
+
+def eform(A, K, scale_x, scale_y, cx, cy, weights, rows=None, cols=None):
+    """(3, len(rows), len(cols)) float64."""
+    A = np.asarray(A, np.float64)
+    n = A.shape[0]
+    rows = np.arange(K) if rows is None else np.asarray(rows)
+    cols = np.arange(K) if cols is None else np.asarray(cols)
+    out = np.zeros((3, len(rows), len(cols)))
+    w = np.asarray(weights, np.float64).reshape(-1, 3)
+    for l in range(len(scale_x)):
+        Wx = dft_matrix(n, K, scale_x[l], cx, cols)
+        Wy = dft_matrix(n, K, scale_y[l], cy, rows)
+        E = Wy @ (A @ Wx.T)
+        I = E.real ** 2 + E.imag ** 2
+        for c in range(3):
+            out[c] += w[l, c] * I
+    return out
+
+
+def test_pupil(n: int, seed: int = 3) -> np.ndarray:
+    """A seeded pupil amplitude for tests: a 9-blade disc with a soft edge."""
+    rng = np.random.default_rng(seed)
+    y, x = np.mgrid[0:n, 0:n].astype(np.float64)
+    c = 0.5 * (n - 1)
+    r = np.hypot(x - c, y - c) / (0.4 * n)
+    th = np.arctan2(y - c, x - c)
+    edge = np.cos(np.pi / 9) / np.cos((th % (2 * np.pi / 9)) - np.pi / 9)
+    a = np.clip((edge - r) * 0.4 * n / 2.0 + 0.5, 0.0, 1.0)
+    a *= (rng.random((n, n)) > 0.005)
+    return a.astype(np.float32)

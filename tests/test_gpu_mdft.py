@@ -19,3 +19,54 @@ def test_tcgen05_bf16_gemm_matches_torch(M, N, K):
     ref = a.float() @ b.float().t()
     err = (c - ref).abs().max().item() / ref.abs().max().item()
     assert err < 1e-5, err
+
+
+def _mdft(n, K, n_lambda, form, seed=5):
+    import ctypes as C
+    from ghostlight_gb300 import _native
+    from oracle import mdft_oracle as MO
+    lib = _native.load()
+    lam = np.linspace(420.0, 680.0, n_lambda)
+    s0 = 1.0 / (2.0 * n)
+    sx = (s0 * 550.0 / lam).astype(np.float64)
+    sy = (s0 * 1.1 * 550.0 / lam).astype(np.float64)
+    rng = np.random.default_rng(seed)
+    w = rng.uniform(0.2, 1.0, (n_lambda, 3)).astype(np.float32)
+    cx, cy = K / 2.0 - 0.25, K / 2.0 + 0.5
+    A = MO.test_pupil(n, seed)
+    d = C.c_double
+    h = C.c_void_p()
+    st = torch.cuda.current_stream().cuda_stream
+    _native.check(lib.gl_mdft_plan_create(n, K, n_lambda, (d * n_lambda)(*sx), (d * n_lambda)(*sy), cx, cy,
+                                          (C.c_float * (3 * n_lambda))(*w.reshape(-1)), form, st, C.byref(h)), "mdft")
+    dA = torch.from_numpy(A).cuda()
+    outs = [torch.full((K, K), float("nan"), device="cuda") for _ in range(3)]
+    _native.check(lib.gl_mdft_plan_execute(h, dA.data_ptr(), *[o.data_ptr() for o in outs], st), "mdft")
+    torch.cuda.synchronize()
+    code = C.c_int()
+    lib.gl_mdft_plan_status(h, C.byref(code))
+    lib.gl_mdft_plan_destroy(h)
+    assert code.value == 0
+    got = np.stack([o.cpu().numpy() for o in outs]).astype(np.float64)
+    return got, (A, K, sx, sy, cx, cy, w)
+
+
+@pytest.mark.parametrize("form,tol", [(0, 1e-3), (1, 2e-2), (2, 1e-4)])
+def test_mdft_eform_matches_fp64_oracle(form, tol):
+    from oracle import mdft_oracle as MO
+    got, (A, K, sx, sy, cx, cy, w) = _mdft(128, 256, 3, form)
+    want = MO.eform(A, K, sx, sy, cx, cy, w)
+    err = np.linalg.norm(got - want) / np.linalg.norm(want)
+    assert np.isfinite(got).all() and err < tol, err
+
+
+def test_mdft_config1_size_split_bf16():
+    """Configuration 1: 256^2 pupil to 512^2 at 8 wavelengths."""
+    from oracle import mdft_oracle as MO
+    got, (A, K, sx, sy, cx, cy, w) = _mdft(256, 512, 8, 0)
+    rows = np.arange(0, 512, 7)
+    cols = np.arange(3, 512, 5)
+    want = MO.eform(A, K, sx, sy, cx, cy, w, rows=rows, cols=cols)
+    sub = got[:, rows][:, :, cols]
+    err = np.linalg.norm(sub - want) / np.linalg.norm(want)
+    assert err < 1e-3, err
