@@ -53,6 +53,11 @@ def _declare(lib):
     lib.gl_mdft_plan_execute.argtypes = [vp, vp, vp, vp, vp, vp]
     lib.gl_mdft_plan_status.argtypes = [vp, P(i)]
     lib.gl_mdft_plan_destroy.argtypes = [vp]
+    lib.gl_conv2d_plan_create.argtypes = [i, i, P(f), i, i, vp, P(vp)]
+    lib.gl_conv2d_plan_execute.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp]
+    lib.gl_conv2d_plan_execute2.argtypes = [vp] + [vp] * 9 + [vp]
+    lib.gl_conv2d_plan_info.argtypes = [vp, P(i), P(i)]
+    lib.gl_conv2d_plan_destroy.argtypes = [vp]
     return lib
 
 

@@ -35,6 +35,7 @@ UNITS = {
     "gl_filter.cu": EXACT,
     "gl_ghost.cu": FAST,
     "gl_mdft.cu": FAST,
+    "gl_conv.cu": FAST,
 }
 # Occupancy target of the render kernel (CTAs of 128 threads per SM); an
 # environment override lets a tuning sweep rebuild with another value.

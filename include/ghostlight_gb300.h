@@ -295,6 +295,29 @@ int gl_mdft_plan_execute(gl_mdft_plan* plan, const float* d_pupil, float* d_out_
 int gl_mdft_plan_status(gl_mdft_plan* plan, int* err_code);
 int gl_mdft_plan_destroy(gl_mdft_plan* plan);
 
+/* PSF / veil image convolution: out_c = in_c (*) k ('same' size, kernel
+ * centred, odd kw x kh, float32).  The reference has no such operation on
+ * this path (its veil is an analytic glare-spread sprite splatted per source,
+ * veil_render.cu:94-243); this is the flare path's image-space form.  FFT
+ * route: zero-padded circular convolution of size P x Q = the smallest
+ * 2^a 3^b sizes covering image + kernel - 1, two channels per complex
+ * transform, three HBM passes; the kernel spectrum stays resident in the
+ * plan.  Planes are W x H float32 on the device.  Asynchronous. */
+typedef struct gl_conv_plan gl_conv_plan;
+int gl_conv2d_plan_create(int width, int height, const float* h_kernel, int kw, int kh,
+                          void* stream, gl_conv_plan** out);
+int gl_conv2d_plan_execute(gl_conv_plan* plan, const float* d_in_r, const float* d_in_g,
+                           const float* d_in_b, float* d_out_r, float* d_out_g,
+                           float* d_out_b, void* stream);
+/* The same with a second layer summed into the input on load (the flare
+ * composite, ghosts + starburst, convolved without a separate add pass). */
+int gl_conv2d_plan_execute2(gl_conv_plan* plan, const float* d_in_r, const float* d_in_g,
+                            const float* d_in_b, const float* d_add_r, const float* d_add_g,
+                            const float* d_add_b, float* d_out_r, float* d_out_g,
+                            float* d_out_b, void* stream);
+int gl_conv2d_plan_info(const gl_conv_plan* plan, int* P, int* Q);
+int gl_conv2d_plan_destroy(gl_conv_plan* plan);
+
 /* Number of kernel launches issued by the last device call on this thread. */
 int gl_last_launch_count(void);
 
