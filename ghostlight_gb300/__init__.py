@@ -14,6 +14,9 @@ from .flare import (GhostPair, GhostRenderPlan, enumerate_ghost_pairs, filter_gh
                     render_source_flare, spectral_table, trace_ghost_ray, trace_primary_ray,
                     trace_rays)
 from .calibration import calibrate_lens, solve_source_angle
+from .starburst import MdftPlan, mdft_starburst_eform
+from .psf import ConvPlan, convolve_psf, synthetic_psf_kernel
+from .apertures import curved_blade_mask
 
 __version__ = "0.1.0"
 

@@ -750,6 +750,20 @@ extern "C" int gl_mdft_plan_create(int n, int K_out, int n_lambda, const double*
     }
     chk(cudaGetLastError());
     chk(cudaStreamSynchronize(st));
+    // shared-memory opt-in once here, so execute enqueues kernels only (graph capture)
+    {
+        const int smem1 = 4 * 3 * kOpTile + 1024, smem2 = 2 * 5 * kOpTile + 1024;
+        if (form == 0)
+        {
+            chk(cudaFuncSetAttribute(mdft_kernel<0, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem1));
+            chk(cudaFuncSetAttribute(mdft_kernel<0, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem2));
+        }
+        else if (form == 1)
+        {
+            chk(cudaFuncSetAttribute(mdft_kernel<1, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem1));
+            chk(cudaFuncSetAttribute(mdft_kernel<1, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem2));
+        }
+    }
     const CUtensorMapDataType dt = form == 0 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
     const uint32_t bc = form == 0 ? 64 : 32;
     int rc = GL_OK;
@@ -811,15 +825,11 @@ extern "C" int gl_mdft_plan_execute(gl_mdft_plan* plan, const float* d_pupil, fl
     }
     else if (p->form == 0)
     {
-        GL_CUDA_TRY(cudaFuncSetAttribute(mdft_kernel<0, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1));
-        GL_CUDA_TRY(cudaFuncSetAttribute(mdft_kernel<0, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2));
         mdft_kernel<0, 1><<<g1, kMdftThreads, smem1, st>>>(p->t_wx, p->t_mask, a);
         mdft_kernel<0, 2><<<g2, kMdftThreads, smem2, st>>>(p->t_wy, p->t_tp, a2);
     }
     else
     {
-        GL_CUDA_TRY(cudaFuncSetAttribute(mdft_kernel<1, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1));
-        GL_CUDA_TRY(cudaFuncSetAttribute(mdft_kernel<1, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2));
         mdft_kernel<1, 1><<<g1, kMdftThreads, smem1, st>>>(p->t_wx, p->t_mask, a);
         mdft_kernel<1, 2><<<g2, kMdftThreads, smem2, st>>>(p->t_wy, p->t_tp, a2);
     }

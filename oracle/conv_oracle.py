@@ -33,10 +33,6 @@ def conv_at(img, k, ys, xs):
 
 
 def psf_kernel(size: int, seed: int = 11):
-    """Seeded smooth radial kernel plus noise, normalised to sum 1."""
-    rng = np.random.default_rng(seed)
-    c = size // 2
-    y, x = np.mgrid[0:size, 0:size].astype(np.float64)
-    r = np.hypot(x - c, y - c) / (0.18 * size)
-    k = (1.0 / (1.0 + r * r)) ** 1.5 + 0.02 * rng.random((size, size))
-    return (k / k.sum()).astype(np.float32)
+    """The seeded synthetic veil kernel (input data, not an algorithm under test)."""
+    from ghostlight_gb300.psf import synthetic_psf_kernel
+    return synthetic_psf_kernel(size, seed)

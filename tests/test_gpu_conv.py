@@ -53,3 +53,25 @@ def test_conv_full_size_2048_257_point_checks():
         want = CO.conv_at(i, k, ys, xs)
         assert np.isfinite(g).all()
         assert rel_l2(g[ys, xs], want) < 1e-5
+
+
+def test_conv_plan_composite_add_matches_fp64():
+    """execute(inputs, outputs, add=layer) convolves inputs + layer on load."""
+    import ghostlight_gb300 as gl
+    from oracle import conv_oracle as CO
+    rng = np.random.default_rng(17)
+    H, W = 300, 260
+    a = [rng.random((H, W)).astype(np.float32) ** 3 for _ in range(3)]
+    b = [rng.random((H, W)).astype(np.float32) ** 5 for _ in range(3)]
+    k = CO.psf_kernel(33)
+    plan = gl.ConvPlan(W, H, k)
+    ta = [torch.from_numpy(x).cuda() for x in a]
+    tb = [torch.from_numpy(x).cuda() for x in b]
+    out = [torch.full((H, W), float("nan"), device="cuda") for _ in range(3)]
+    assert plan.execute(ta, out, add=tb) == 3
+    torch.cuda.synchronize()
+    for o, x, y in zip(out, a, b):
+        assert rel_l2(o.cpu().numpy(), CO.conv_same(x.astype(np.float64) + y, k)) < 1e-5
+    with pytest.raises(ValueError):
+        plan.execute(ta, out, add=[tb[0], tb[1], ta[0].t()])
+    plan.close()
