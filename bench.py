@@ -29,6 +29,10 @@ import time
 
 import numpy as np
 
+# every in-flight serving request has its own stream: give each its own
+# hardware work queue (must be set before CUDA starts in this process)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 REPO = pathlib.Path(__file__).resolve().parent
 sys.path.insert(0, str(REPO))
 
@@ -435,6 +439,93 @@ def run_full_frame(args, dev, stream, timed, ghost_plan, plain_plan, sb_inputs, 
                       "of the composite"}
 
 
+# ---- serving (Poisson request mix) -----------------------------------------
+SERVE_RATE = 200.0
+SERVE_LENSES = 24
+SERVE_BUDGET = 120 * 10 ** 9
+
+
+def run_serving(args):
+    """Poisson arrivals at 200 req/s; each request a seeded lens of 8-30
+    surfaces from a resident pool, an output of 512^2..4096^2, 8/16/31
+    wavelengths, a pupil grid of 32^2..256^2 and a source at 0-20 deg;
+    admitted against a 120 GB HBM budget.  Against serial plain renders
+    (per-call plan, per-pair launches, blocking) of a sample of the same
+    requests."""
+    import torch
+    import ghostlight_gb300 as gl
+    from ghostlight_gb300.flare import GhostRenderPlan, pupil_grid
+    from ghostlight_gb300.serve import (FlareServer, _spectral, latency_stats, poisson_requests,
+                                        serving_lens_pool)
+    cfg = gl.FlareConfig(min_ghost_intensity=MIN_INTENSITY)
+    t0 = time.perf_counter()
+    pool = serving_lens_pool(SERVE_LENSES, cfg, seed=100, n_min=8, n_max=30)
+    reqs = poisson_requests(SERVE_RATE, args.serve_seconds, pool.keys(), seed=5)
+    for rl in pool.values():                      # resident tables: grids and IOR slices of the mix
+        for g in sorted({r.ray_grid for r in reqs}):
+            rl.prepare(g)
+        for ns in (8, 16, 31):
+            rl.prepare(0, _spectral(ns, cfg)[0])
+    setup_s = time.perf_counter() - t0
+    # warm: one request per lens
+    from ghostlight_gb300.serve import FlareRequest
+    srv = FlareServer(pool, budget_bytes=SERVE_BUDGET, max_inflight=args.serve_slots, items_per_warp=8)
+    srv.run_trace([FlareRequest(lens_id=i, width=512, height=512, n_spec=8, ray_grid=32, field_deg=5.0, rid=i)
+                   for i in pool])
+    torch.cuda.synchronize()
+    srv = FlareServer(pool, budget_bytes=SERVE_BUDGET, max_inflight=args.serve_slots, items_per_warp=8)
+    srv.exec.prewarm([(w, w) for w in (512, 1024, 2048, 4096)], 8)
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        t1 = time.perf_counter()
+        srv.run_trace(reqs)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t1
+    traced = sum(r.traced for r in reqs)
+    if args.serve_dump:
+        with open(args.serve_dump, "w") as f:
+            f.write("rid,lens,n_surf,n_pairs,width,n_spec,grid,field,priority,est_rays,traced,arrival,start,finish\n")
+            for r in reqs:
+                rl = pool[r.lens_id]
+                f.write("%d,%d,%d,%d,%d,%d,%d,%.3f,%d,%d,%d,%.6f,%.6f,%.6f\n" % (
+                    r.rid, r.lens_id, len(rl.lens.surfaces), rl.n_pairs, r.width, r.n_spec, r.ray_grid, r.field_deg,
+                    r.priority, r.est_rays, r.traced, r.arrival, r.start, r.finish))
+    by_size = {"%dx%d" % (w, w): latency_stats(reqs, lambda r, w=w: r.width == w) for w in (512, 1024, 2048, 4096)}
+    # serial plain renders of a sample of the same requests
+    rng = np.random.default_rng(9)
+    sample = [reqs[i] for i in sorted(rng.choice(len(reqs), size=min(len(reqs), args.serial_sample),
+                                                 replace=False))]
+    ts = []
+    for r in sample:
+        rl = pool[r.lens_id]
+        tt = time.perf_counter()
+        spec, corr = _spectral(r.n_spec, cfg)
+        grid = pupil_grid(rl.lens, r.ray_grid, 0, 0, 0, 0.0)
+        src = np.array([[math.radians(r.field_deg), 0.0, 1.0, 1.0, 1.0]], np.float32)
+        plan = GhostRenderPlan(rl.lens, rl.pairs, rl.boosts, src, [grid], np.zeros(len(rl.pairs), np.int32), spec,
+                               corr, r.width, r.height, rl.sensor_half_w, rl.sensor_half_h, r.gain,
+                               apply_correction=True, plain_per_pair=True)
+        outs = torch.empty((3, r.height, r.width), device="cuda")
+        plan.execute(outs[0], outs[1], outs[2])
+        host = outs.cpu()
+        plan.close()
+        ts.append(time.perf_counter() - tt)
+    serial_req_s = len(ts) / sum(ts)
+    served_req_s = len(reqs) / wall
+    for rl in pool.values():
+        rl.close()
+    return {"workload": "Poisson %.0f req/s for %.0f s (%d requests), %d resident lenses of 8-30 surfaces, "
+                        "outputs 512^2-4096^2, 8/16/31 wavelengths, pupil grids 32^2-256^2, field 0-20 deg, "
+                        "%d slots, %.0f GB HBM budget" % (SERVE_RATE, args.serve_seconds, len(reqs), SERVE_LENSES,
+                                                          args.serve_slots, SERVE_BUDGET / 1e9),
+            "throughput_req_s": served_req_s, "wall_s": wall, "offered_req_s": len(reqs) / args.serve_seconds,
+            "rays_per_s": traced / wall, "ray_lambda_traces": traced,
+            "latency_all": latency_stats(reqs), "latency_by_size": by_size,
+            "peak_inflight": srv.sched.peak_inflight, "peak_budget_bytes": srv.sched.peak_used,
+            "serial_plain": {"sample": len(ts), "req_s": serial_req_s, "mean_ms": 1e3 * sum(ts) / len(ts)},
+            "speedup_served_vs_serial_plain": served_req_s / serial_req_s,
+            "lens_setup_s": setup_s, "clocks": clk.summary()}
+
+
 def cpu_baseline(plan, lens, cal, budget_s=8.0):
     """The oracle port of the reference renderer (FP32, OpenMP over every host
     core) on a bounded sample: a subset of the frame's pairs."""
@@ -534,7 +625,11 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--quick", action="store_true",
                     help="batched timing only (no plain / e2e / CPU legs): for profiler runs")
-    ap.add_argument("--only", default="all", choices=["all", "cfg3"],
+    ap.add_argument("--serve-seconds", type=float, default=30.0)
+    ap.add_argument("--serve-slots", type=int, default=32)
+    ap.add_argument("--serial-sample", type=int, default=40)
+    ap.add_argument("--serve-dump", default="", help="write per-request timings (CSV) here")
+    ap.add_argument("--only", default="all", choices=["all", "cfg3", "serve"],
                     help="with --quick: also run the starburst / convolution section (profiler runs)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
@@ -543,6 +638,12 @@ def main():
     if args.impl == "reference":
         if rank == 0:
             print(json.dumps(run_reference(args)))
+        return
+    if args.only == "serve":
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+        if rank == 0:
+            print(json.dumps({"serving": run_serving(args)}))
         return
     if world > 1:
         import torch

@@ -58,6 +58,21 @@ def _declare(lib):
     lib.gl_conv2d_plan_execute2.argtypes = [vp] + [vp] * 9 + [vp]
     lib.gl_conv2d_plan_info.argtypes = [vp, P(i), P(i)]
     lib.gl_conv2d_plan_destroy.argtypes = [vp]
+    ll = C.c_longlong
+    lib.gl_lens_create.argtypes = [P(gl_surface), i, P(gl_ghost_pair), P(f), i, i, f, P(vp)]
+    lib.gl_lens_prepare.argtypes = [vp, i, P(gl_spectral_sample), i]
+    lib.gl_lens_info.argtypes = [vp, P(i), P(ll)]
+    lib.gl_lens_destroy.argtypes = [vp]
+    lib.gl_request_create.argtypes = [vp, i, P(gl_spectral_sample), i, P(gl_flare_source), i,
+                                      P(gl_ghost_render_params), vp, P(vp)]
+    lib.gl_request_enqueue.argtypes = [vp, vp, vp, vp, i, vp]
+    lib.gl_request_planes.argtypes = [vp, P(vp)]
+    lib.gl_request_copy_out.argtypes = [vp, vp, vp]
+    lib.gl_request_info.argtypes = [vp, P(ll), P(ll), P(i)]
+    lib.gl_request_traced.argtypes = [vp, P(ll), vp]
+    lib.gl_request_destroy.argtypes = [vp, vp]
+    lib.gl_pool_info.argtypes = [P(ll), P(ll)]
+    lib.gl_pool_trim.argtypes = [ll]
     return lib
 
 

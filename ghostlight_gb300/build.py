@@ -36,6 +36,7 @@ UNITS = {
     "gl_ghost.cu": FAST,
     "gl_mdft.cu": FAST,
     "gl_conv.cu": FAST,
+    "gl_serve.cu": FAST,
 }
 # Occupancy target of the render kernel (CTAs of 128 threads per SM); an
 # environment override lets a tuning sweep rebuild with another value.

@@ -22,7 +22,7 @@
 //   * The flush kernel reads the RGBA accumulator once, applies the 3x3
 //     spectral correction (ghost_render.cu:610-622, same rounding order) and
 //     writes the three planar float32 outputs with coalesced vector stores.
-#include "gl_internal.h"
+#include "gl_render.h"
 
 #include <cuda_runtime.h>
 
@@ -34,43 +34,11 @@
 
 namespace gl {
 
-constexpr int kRenderThreads = 128;
 #ifndef GL_RENDER_MIN_BLOCKS
 #define GL_RENDER_MIN_BLOCKS 8
 #endif
 constexpr int kRenderMinBlocks = GL_RENDER_MIN_BLOCKS;
-constexpr int kTile = 32;          // pupil samples per work item = one warp
-constexpr int kMaxSpec = 256;
 constexpr unsigned kFull = 0xffffffffu;
-
-struct PairDev {
-    int a, b;
-    float boost, w_ray;
-};
-
-struct SourceDev {
-    float dx, dy, dz, sdx;
-    float sdy, r, g, b;
-};
-
-struct RenderArgs {
-    const SurfRec* recs;
-    const float* ior_at;
-    const float* ior_bf;
-    const float4* spec;
-    const int4* items;        // (pair, source, sample_start, sample_count)
-    const PairDev* pairs;
-    const SourceDev* sources;
-    const float2* samples;
-    int* counter;             // persistent queue head; null = static item assignment
-    float4* accum;            // RGBA, width x height
-    int* pair_hits;           // off-sensor cull: per-pair probe hits (null = no cull)
-    unsigned long long* traced;   // ray-wavelength traces executed (null = not counted)
-    int n_surf, n_spec, n_items, item_base;
-    int width, height;
-    float fmt_w, fmt_h, fmt_x0, fmt_y0;
-    float hw2, hh2, gain, front_R, start_z;
-};
 
 // Per-lane splat footprint kept in shared memory (12 floats, stride 13 so the
 // lanes of a warp fall in distinct banks) together with its 2x2 origin.
@@ -438,7 +406,15 @@ __global__ void __launch_bounds__(kRenderThreads, kRenderMinBlocks) ghost_render
             next_static += nwarp;
         }
         if (item >= A.n_items) break;
-        const int4 w = A.items[item];
+        int4 w;
+        if (A.items != nullptr) w = A.items[item];
+        else
+        {
+            const int per_pair = A.u_tiles * A.u_n_src;
+            const int pr = item / per_pair, rem = item - pr * per_pair;
+            const int sr = rem / A.u_tiles, t = (rem - sr * A.u_tiles) * kTile;
+            w = make_int4(pr, sr, A.u_grid_base + t, min(kTile, A.u_grid_n - t));
+        }
         if (A.pair_hits != nullptr)
         {
             // render: skip pairs the probe found off-sensor; probe passes
@@ -446,7 +422,8 @@ __global__ void __launch_bounds__(kRenderThreads, kRenderMinBlocks) ghost_render
             const int h = A.pair_hits[w.x];
             if (PROBE ? (h > 0) : (h == 0)) continue;
         }
-        const PairDev P = A.pairs[w.x];
+        PairDev P = A.pairs[w.x];
+        if (A.items == nullptr) P.w_ray = A.w_uniform;
         const SourceDev S = A.sources[w.y];
         const bool active = lane < w.w;
         const float2 uv = active ? A.samples[w.z + lane] : make_float2(0.0f, 0.0f);
@@ -550,10 +527,108 @@ static cudaError_t upload(T** dst, const T* src, size_t count)
     return e;
 }
 
-static size_t render_smem(int n_surf, int n_spec)
+size_t render_smem(int n_surf, int n_spec)
 {
     return (size_t)n_surf * 32 + (size_t)n_spec * 16 + (size_t)n_spec * 4 + 2 * (size_t)n_spec * n_surf * 4 +
            (size_t)n_surf * sizeof(SurfRec) + (size_t)kRenderThreads * kAccStride * 4;
+}
+
+// The opt-in only grows (process-wide, per kernel), so a plan created earlier
+// with a larger table keeps launching after a smaller one was prepared.
+static std::mutex g_smem_mutex;
+static size_t g_smem_optin = 0;
+
+cudaError_t render_prepare(size_t smem, int* per_sm, int* n_sm)
+{
+    cudaError_t e = cudaSuccess;
+    {
+        std::lock_guard<std::mutex> lk(g_smem_mutex);
+        if (smem > g_smem_optin)
+        {
+            e = cudaFuncSetAttribute(ghost_render_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e == cudaSuccess)
+                e = cudaFuncSetAttribute(ghost_render_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e == cudaSuccess) g_smem_optin = smem;
+        }
+    }
+    if (e == cudaSuccess && per_sm) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, ghost_render_kernel<false>, kRenderThreads, smem);
+    int dev = 0;
+    if (e == cudaSuccess && n_sm) e = cudaGetDevice(&dev);
+    if (e == cudaSuccess && n_sm) e = cudaDeviceGetAttribute(n_sm, cudaDevAttrMultiProcessorCount, dev);
+    return e;
+}
+
+cudaError_t render_launch(const RenderArgs& A, bool probe, int grid, size_t smem, cudaStream_t st)
+{
+    if (probe) ghost_render_kernel<true><<<grid, kRenderThreads, smem, st>>>(A);
+    else ghost_render_kernel<false><<<grid, kRenderThreads, smem, st>>>(A);
+    return cudaGetLastError();
+}
+
+cudaError_t flush_launch(const float4* accum, size_t n_px, float* r, float* g, float* b, int apply, const float* C,
+                         cudaStream_t st)
+{
+    const size_t quads = (n_px + 3) / 4;
+    const int fb = 256;
+    ghost_flush_kernel<<<(unsigned)((quads + fb - 1) / fb), fb, 0, st>>>(accum, n_px, r, g, b, apply, C[0], C[1], C[2],
+                                                                         C[3], C[4], C[5], C[6], C[7], C[8]);
+    return cudaGetLastError();
+}
+
+SourceDev make_source(const gl_flare_source& s)
+{
+    const float bx = tanf(s.angle_x), by = tanf(s.angle_y);
+    V3 dir = normalized(v3(bx, by, 1.0f));
+    return {dir.x, dir.y, dir.z, -kSpawnOffset * bx, -kSpawnOffset * by, s.r, s.g, s.b};
+}
+
+// Pupil samples in Morton order over the unit square: 32 consecutive samples
+// (one warp) then cover a compact patch of the pupil, whose rays tend to
+// vignette together, instead of a strip across it.  The set of samples and
+// each one's weight are unchanged.
+void morton_order(const gl_pupil_sample* in, int n, gl_pupil_sample* out)
+{
+    auto spread = [](uint32_t x) {
+        x &= 0x3ffu;
+        x = (x | (x << 16)) & 0x030000ffu;
+        x = (x | (x << 8)) & 0x0300f00fu;
+        x = (x | (x << 4)) & 0x030c30c3u;
+        x = (x | (x << 2)) & 0x09249249u;
+        return x;
+    };
+    std::vector<std::pair<uint32_t, int>> key;
+    key.reserve((size_t)n);
+    for (int i = 0; i < n; ++i)
+    {
+        const float fu = std::min(std::max((in[i].u + 1.0f) * 512.0f, 0.0f), 1023.0f);
+        const float fv = std::min(std::max((in[i].v + 1.0f) * 512.0f, 0.0f), 1023.0f);
+        key.push_back({(spread((uint32_t)fu) << 1) | spread((uint32_t)fv), i});
+    }
+    std::stable_sort(key.begin(), key.end(),
+                     [](const std::pair<uint32_t, int>& x, const std::pair<uint32_t, int>& y) { return x.first < y.first; });
+    for (int i = 0; i < n; ++i) out[i] = in[key[i].second];
+}
+
+int probe_grids(const gl_surface* surfaces, int n_surf, int blades_override, float rotation_deg,
+                std::vector<gl_pupil_sample>& out, int begin[4])
+{
+    out.clear();
+    for (int pass = 0; pass < 3; ++pass)
+    {
+        gl_sampler_params sp;
+        sp.ray_grid = 40;
+        sp.pupil_jitter = 1;
+        sp.jitter_seed = (int)(0x9E3779B9u * (unsigned)(pass + 1));
+        sp.blades_override = blades_override;
+        sp.rotation_deg = rotation_deg;
+        std::vector<gl_pupil_sample> g;
+        const int rc = build_aperture_samples(surfaces, n_surf, sp, g);
+        if (rc) return rc;
+        begin[pass] = (int)out.size();
+        out.insert(out.end(), g.begin(), g.end());
+    }
+    begin[3] = (int)out.size();
+    return GL_OK;
 }
 
 int plan_create(const gl_surface* surfaces, int n_surf, const gl_ghost_pair* pairs, const float* boosts,
@@ -606,45 +681,12 @@ int plan_create(const gl_surface* surfaces, int n_surf, const gl_ghost_pair* pai
     // Per-source beam (ghost_render.cu:349-358): tanf slopes, the normalised
     // direction and the spawn-plane shift that follows the beam.
     std::vector<SourceDev> src((size_t)n_src);
-    for (int i = 0; i < n_src; ++i)
-    {
-        const float bx = tanf(sources[i].angle_x), by = tanf(sources[i].angle_y);
-        V3 dir = normalized(v3(bx, by, 1.0f));
-        src[i] = {dir.x, dir.y, dir.z, -kSpawnOffset * bx, -kSpawnOffset * by, sources[i].r, sources[i].g, sources[i].b};
-    }
+    for (int i = 0; i < n_src; ++i) src[i] = make_source(sources[i]);
 
-    // Pupil samples of each grid in Morton order over the unit square: 32
-    // consecutive samples (one warp) then cover a compact patch of the pupil,
-    // whose rays tend to vignette together, instead of a strip across it.
-    // The set of samples and each one's weight are unchanged.
     const int n_samples_all = n_grids > 0 ? grid_offsets[n_grids] : 0;
     std::vector<gl_pupil_sample> ordered((size_t)n_samples_all);
-    {
-        auto spread = [](uint32_t x) {
-            x &= 0x3ffu;
-            x = (x | (x << 16)) & 0x030000ffu;
-            x = (x | (x << 8)) & 0x0300f00fu;
-            x = (x | (x << 4)) & 0x030c30c3u;
-            x = (x | (x << 2)) & 0x09249249u;
-            return x;
-        };
-        std::vector<std::pair<uint32_t, int>> key;
-        for (int g = 0; g < n_grids; ++g)
-        {
-            const int g0 = grid_offsets[g], g1 = grid_offsets[g + 1];
-            key.clear();
-            for (int i = g0; i < g1; ++i)
-            {
-                const float fu = std::min(std::max((samples[i].u + 1.0f) * 512.0f, 0.0f), 1023.0f);
-                const float fv = std::min(std::max((samples[i].v + 1.0f) * 512.0f, 0.0f), 1023.0f);
-                const uint32_t m = (spread((uint32_t)fu) << 1) | spread((uint32_t)fv);
-                key.push_back({m, i});
-            }
-            std::stable_sort(key.begin(), key.end(),
-                             [](const std::pair<uint32_t, int>& x, const std::pair<uint32_t, int>& y) { return x.first < y.first; });
-            for (int i = g0; i < g1; ++i) ordered[i] = samples[key[i - g0].second];
-        }
-    }
+    for (int g = 0; g < n_grids; ++g)
+        morton_order(samples + grid_offsets[g], grid_offsets[g + 1] - grid_offsets[g], ordered.data() + grid_offsets[g]);
 
     std::vector<PairDev> pd((size_t)n_pairs);
     std::vector<int4> items;
@@ -674,13 +716,12 @@ int plan_create(const gl_surface* surfaces, int n_surf, const gl_ghost_pair* pai
         // A pair is probed only when its own grid is larger than the three
         // probe passes: rendering a pair that lands nowhere costs less than
         // proving it, and never changes the image.
-        int n_probe_samples = 0;
-        for (int pass = 0; pass < 3; ++pass)
+        int pbeg[4];
         {
-            gl_sampler_params sp{40, 1, (int)(0x9E3779B9u * (unsigned)(pass + 1)), prm->blades_override, prm->rotation_deg};
-            std::vector<gl_pupil_sample> g;
-            if (build_aperture_samples(surfaces, n_surf, sp, g) == GL_OK) n_probe_samples += (int)g.size();
+            const int rcs = probe_grids(surfaces, n_surf, prm->blades_override, prm->rotation_deg, psamples, pbeg);
+            if (rcs) { plan_free(p); return rcs; }
         }
+        const int n_probe_samples = pbeg[3];
         for (int i = 0; i < n_pairs; ++i)
         {
             const int gi = pair_grid ? pair_grid[i] : 0;
@@ -689,25 +730,15 @@ int plan_create(const gl_surface* surfaces, int n_surf, const gl_ghost_pair* pai
         }
         for (int pass = 0; pass < 3; ++pass)
         {
-            gl_sampler_params sp;
-            sp.ray_grid = 40;
-            sp.pupil_jitter = 1;
-            sp.jitter_seed = (int)(0x9E3779B9u * (unsigned)(pass + 1));
-            sp.blades_override = prm->blades_override;
-            sp.rotation_deg = prm->rotation_deg;
-            std::vector<gl_pupil_sample> g;
-            int rcs = build_aperture_samples(surfaces, n_surf, sp, g);
-            if (rcs) { plan_free(p); return rcs; }
-            const int base = (int)psamples.size();
-            psamples.insert(psamples.end(), g.begin(), g.end());
+            const int base = pbeg[pass], cnt = pbeg[pass + 1] - pbeg[pass];
             p->probe_begin[pass] = (int)pitems.size();
             for (int i = 0; i < n_pairs; ++i)
             {
                 if (hits_init[i]) continue;
                 for (int s = 0; s < n_src; ++s)
-                    for (int t = 0; t < (int)g.size(); t += kTile)
-                        pitems.push_back(make_int4(i, s, base + t, std::min(kTile, (int)g.size() - t)));
-                p->probe_rays += (long long)g.size() * n_src * n_spec;
+                    for (int t = 0; t < cnt; t += kTile)
+                        pitems.push_back(make_int4(i, s, base + t, std::min(kTile, cnt - t)));
+                p->probe_rays += (long long)cnt * n_src * n_spec;
             }
         }
         p->probe_begin[3] = (int)pitems.size();
@@ -737,11 +768,8 @@ int plan_create(const gl_surface* surfaces, int n_surf, const gl_ghost_pair* pai
     chk(cudaMalloc(&p->accum, (size_t)prm->width * prm->height * sizeof(float4)));
     if (e == cudaSuccess) chk(cudaMemset(p->accum, 0, (size_t)prm->width * prm->height * sizeof(float4)));
     p->smem = render_smem(n_surf, n_spec);
-    if (e == cudaSuccess) chk(cudaFuncSetAttribute(ghost_render_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem));
-    if (e == cudaSuccess) chk(cudaFuncSetAttribute(ghost_render_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem));
     int per_sm = 0, n_sm = 0;
-    if (e == cudaSuccess) chk(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ghost_render_kernel<false>, kRenderThreads, p->smem));
-    if (e == cudaSuccess) chk(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, p->device));
+    if (e == cudaSuccess) chk(render_prepare(p->smem, &per_sm, &n_sm));
     if (e != cudaSuccess)
     {
         plan_free(p);
@@ -761,7 +789,7 @@ int plan_execute(GhostPlan* p, float* d_out_r, float* d_out_g, float* d_out_b, c
     const size_t n_px = (size_t)p->width * p->height;
     int launches = 0;
     GL_CUDA_TRY(cudaMemsetAsync(p->accum, 0, n_px * sizeof(float4), st));
-    RenderArgs A;
+    RenderArgs A{};
     A.recs = p->recs; A.ior_at = p->ior_at; A.ior_bf = p->ior_bf; A.spec = p->spec;
     A.items = p->items; A.pairs = p->pairs; A.sources = p->sources; A.samples = p->samples;
     A.counter = nullptr; A.accum = p->accum;

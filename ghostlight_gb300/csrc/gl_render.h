@@ -1,0 +1,69 @@
+// gl_render.h — the render kernel's device-side argument block and the
+// launch helpers shared by the plan path (gl_ghost.cu) and the serving path
+// (gl_serve.cu).
+#pragma once
+
+#include "gl_internal.h"
+
+#include <cuda_runtime.h>
+
+#include <vector>
+
+namespace gl {
+
+constexpr int kRenderThreads = 128;
+constexpr int kTile = 32;          // pupil samples per work item = one warp
+constexpr int kMaxSpec = 256;
+
+struct PairDev {
+    int a, b;
+    float boost, w_ray;
+};
+
+struct SourceDev {
+    float dx, dy, dz, sdx;
+    float sdy, r, g, b;
+};
+
+struct RenderArgs {
+    const SurfRec* recs;
+    const float* ior_at;
+    const float* ior_bf;
+    const float4* spec;
+    const int4* items;        // (pair, source, sample_start, sample_count)
+    const PairDev* pairs;
+    const SourceDev* sources;
+    const float2* samples;
+    int* counter;             // persistent queue head; null = static item assignment
+    float4* accum;            // RGBA, width x height
+    int* pair_hits;           // off-sensor cull: per-pair probe hits (null = no cull)
+    unsigned long long* traced;   // ray-wavelength traces executed (null = not counted)
+    int n_surf, n_spec, n_items, item_base;
+    // Uniform-grid items (items == null): every pair x source traces the same
+    // grid, item i = (pair, source, 32-sample tile) in pair-major order,
+    // computed from the index; w_uniform replaces the pairs' per-ray weight.
+    int u_tiles, u_n_src, u_grid_base, u_grid_n;
+    float w_uniform;
+    int width, height;
+    float fmt_w, fmt_h, fmt_x0, fmt_y0;
+    float hw2, hh2, gain, front_R, start_z;
+};
+
+// Shared memory of one render CTA for a lens of n_surf surfaces and n_spec wavelengths.
+size_t render_smem(int n_surf, int n_spec);
+// Opt the render kernels in to `smem` bytes of dynamic shared memory and
+// report resident CTAs per SM and the SM count.
+cudaError_t render_prepare(size_t smem, int* per_sm, int* n_sm);
+cudaError_t render_launch(const RenderArgs& A, bool probe, int grid, size_t smem, cudaStream_t st);
+cudaError_t flush_launch(const float4* accum, size_t n_px, float* r, float* g, float* b, int apply, const float* C,
+                         cudaStream_t st);
+// Beam of one source (direction, spawn-plane shift, colour), ghost_render.cu:349-358.
+SourceDev make_source(const gl_flare_source& s);
+// Samples of [begin, end) reordered along a Morton curve over the pupil square.
+void morton_order(const gl_pupil_sample* in, int n, gl_pupil_sample* out);
+// Pupil samples of the three off-sensor probe passes (40x40, wang jitter,
+// fixed seeds; ghost_render.cu:1022-1027), concatenated; pass p starts at begin[p].
+int probe_grids(const gl_surface* surfaces, int n_surf, int blades_override, float rotation_deg,
+                std::vector<gl_pupil_sample>& out, int begin[4]);
+
+}  // namespace gl

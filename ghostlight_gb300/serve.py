@@ -1,0 +1,455 @@
+"""Flare request serving on one GPU: resident lenses, continuous batching.
+
+A request (lens, output size, wavelength count, pupil grid, source field)
+renders the ghost layer of one point source.  The server keeps every
+registered lens resident in HBM (gl_lens: packed surfaces, filtered pairs,
+probe grids, cached IOR slices and pupil grids) and admits requests as they
+arrive whenever a slot and enough of the HBM budget are free — not in
+batches: a request that arrives while others are on the GPU starts at once on
+its own CUDA stream, and its kernels share the SMs with theirs.  Requests run
+as short CTAs (``items_per_warp`` items of 32 pupil samples per warp), so the
+CTA scheduler interleaves them at CTA boundaries, preferring streams of higher
+priority; the priority is the request's estimated trace count (shortest job
+first).  Every request's device memory comes from a stream-ordered pool, and
+nothing on the request path synchronises the device.
+
+The reference has no serving layer: it renders one flare per blocking call
+(bind_renderers.cpp:85-134 -> ghost_render.cu:630) under process-wide mutexes
+(ghost_render.cu:504-511).
+
+``Scheduler`` holds the admission policy and is pure Python (tested on the
+CPU with a fake executor); ``CudaExecutor`` runs requests through the C-ABI.
+"""
+from __future__ import annotations
+
+import collections
+import ctypes as C
+import dataclasses
+import math
+import time
+from typing import Callable, Dict, List, Optional
+
+import numpy as np
+
+from . import _native
+from ._abi import gl_flare_source, gl_ghost_pair, gl_ghost_render_params, gl_spectral_sample
+
+
+@dataclasses.dataclass
+class FlareRequest:
+    lens_id: int
+    width: int
+    height: int
+    n_spec: int
+    ray_grid: int
+    field_deg: float
+    gain: float = 1000.0
+    rid: int = 0
+    arrival: float = 0.0            # seconds on the serving clock
+    # filled by the server
+    est_rays: int = 0
+    device_bytes: int = 0
+    priority: int = 0
+    start: float = 0.0
+    finish: float = 0.0
+    traced: int = 0                 # ray-wavelength traces the device ran
+
+    @property
+    def latency(self) -> float:
+        return self.finish - self.arrival
+
+
+# ---------------------------------------------------------------------------
+# admission policy (no CUDA)
+# ---------------------------------------------------------------------------
+class Scheduler:
+    """Admit pending requests oldest first, skipping ahead past a request that
+    does not fit the remaining HBM budget (so one large request cannot block
+    small ones behind it while memory is short), never more than
+    ``max_inflight`` at once."""
+
+    def __init__(self, budget_bytes: int, max_inflight: int):
+        if budget_bytes <= 0 or max_inflight <= 0:
+            raise ValueError("scheduler: budget and slot count must be positive")
+        self.budget = int(budget_bytes)
+        self.max_inflight = int(max_inflight)
+        self.used = 0
+        self.inflight = 0
+        self.pending: collections.deque = collections.deque()
+        self.peak_used = 0
+        self.peak_inflight = 0
+
+    def submit(self, req: FlareRequest):
+        if req.device_bytes > self.budget:
+            raise ValueError("request %d needs %d bytes, above the %d-byte budget"
+                             % (req.rid, req.device_bytes, self.budget))
+        self.pending.append(req)
+
+    def admit(self) -> List[FlareRequest]:
+        out = []
+        if not self.pending or self.inflight >= self.max_inflight:
+            return out
+        keep = collections.deque()
+        while self.pending:
+            r = self.pending.popleft()
+            if self.inflight < self.max_inflight and self.used + r.device_bytes <= self.budget:
+                self.used += r.device_bytes
+                self.inflight += 1
+                out.append(r)
+            else:
+                keep.append(r)
+        self.pending = keep
+        self.peak_used = max(self.peak_used, self.used)
+        self.peak_inflight = max(self.peak_inflight, self.inflight)
+        return out
+
+    def release(self, req: FlareRequest):
+        self.used -= req.device_bytes
+        self.inflight -= 1
+        assert self.used >= 0 and self.inflight >= 0
+
+
+def priority_class(est_rays: int, rays_per_s: float = 7e9) -> int:
+    """Stream priority from the estimated service time (lower = sooner):
+    < 1 ms -> -3, < 4 ms -> -2, < 16 ms -> -1, else 0."""
+    t = est_rays / rays_per_s
+    if t < 1e-3:
+        return -3
+    if t < 4e-3:
+        return -2
+    if t < 16e-3:
+        return -1
+    return 0
+
+
+def request_bytes(width: int, height: int, n_pairs: int, host_copy: bool = True) -> int:
+    """HBM a request holds: RGBA accumulator + three output planes + tables."""
+    px = int(width) * int(height)
+    return px * 16 + px * 12 + 4 * max(1, n_pairs) + 16384
+
+
+# ---------------------------------------------------------------------------
+# resident lens
+# ---------------------------------------------------------------------------
+class ResidentLens:
+    """gl_lens: a lens with its filtered ghost pairs kept on the device."""
+
+    def __init__(self, lens, sensor_half_w: float, sensor_half_h: float, config, pairs=None, boosts=None):
+        from .flare import filter_ghosts_device
+        self._lib = _native.load()
+        self.lens = lens
+        self.sensor_half_w, self.sensor_half_h = float(sensor_half_w), float(sensor_half_h)
+        self.config = config
+        if pairs is None:
+            fr = filter_ghosts_device(lens, sensor_half_w, sensor_half_h, config)
+            pairs, boosts = fr.pairs, fr.boosts
+        self.pairs = np.ascontiguousarray(pairs, np.int32).reshape(-1, 2)
+        self.boosts = np.ascontiguousarray(boosts, np.float32).reshape(-1)
+        arr = lens.to_array()
+        P = C.POINTER
+        h = C.c_void_p()
+        _native.check(self._lib.gl_lens_create(arr, len(arr), self.pairs.ctypes.data_as(P(gl_ghost_pair)),
+                                               self.boosts.ctypes.data_as(P(C.c_float)), len(self.pairs),
+                                               int(config.aperture_blades), float(config.aperture_rotation),
+                                               C.byref(h)), "lens_create")
+        self._h = h
+
+    @property
+    def n_pairs(self) -> int:
+        return len(self.pairs)
+
+    def prepare(self, ray_grid: int, spec: Optional[np.ndarray] = None):
+        P = C.POINTER
+        sp = None if spec is None else np.ascontiguousarray(spec, np.float32).reshape(-1, 4)
+        _native.check(self._lib.gl_lens_prepare(self._h, int(ray_grid),
+                                                None if sp is None else sp.ctypes.data_as(P(gl_spectral_sample)),
+                                                0 if sp is None else len(sp)), "lens_prepare")
+
+    def device_bytes(self) -> int:
+        n, b = C.c_int(), C.c_longlong()
+        _native.check(self._lib.gl_lens_info(self._h, C.byref(n), C.byref(b)), "lens_info")
+        return int(b.value)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.gl_lens_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_spec_cache: Dict[int, tuple] = {}
+
+
+def _spectral(n_spec: int, config):
+    from .flare import spectral_table
+    key = (int(n_spec), int(config.output_cs))
+    v = _spec_cache.get(key)
+    if v is None:
+        v = spectral_table(n_spec, int(config.output_cs), config.custom_xyz_to_output)
+        _spec_cache[key] = v
+    return v
+
+
+def render_params(rl: ResidentLens, req: FlareRequest, correction, apply_correction: bool):
+    prm = gl_ghost_render_params()
+    prm.width, prm.height = int(req.width), int(req.height)
+    prm.fmt_w, prm.fmt_h, prm.fmt_x0, prm.fmt_y0 = int(req.width), int(req.height), 0, 0
+    prm.sensor_half_w, prm.sensor_half_h = rl.sensor_half_w, rl.sensor_half_h
+    prm.flare_gain = float(req.gain)
+    prm.apply_correction = int(bool(apply_correction))
+    for k, v in enumerate(np.asarray(correction, np.float32).reshape(-1)):
+        prm.correction[k] = float(v)
+    prm.plain_per_pair = 0
+    prm.cull_dead_pairs = int(bool(rl.config.cull_dead_pairs))
+    prm.blades_override = int(rl.config.aperture_blades)
+    prm.rotation_deg = float(rl.config.aperture_rotation)
+    return prm
+
+
+# ---------------------------------------------------------------------------
+# CUDA executor
+# ---------------------------------------------------------------------------
+class _Running:
+    __slots__ = ("req", "handle", "stream", "outs", "host", "event")
+
+
+class CudaExecutor:
+    """Creates, enqueues and completes requests through gl_request_*.  Each
+    in-flight request owns a stream (one pool of streams per priority level);
+    its result is copied into pinned host memory on that stream."""
+
+    LEVELS = (0, -1, -2, -3)
+
+    def __init__(self, lenses: Dict[int, ResidentLens], max_inflight: int, items_per_warp: int = 8,
+                 host_output: bool = True, device=None):
+        import torch
+        self.torch = torch
+        self._lib = _native.load()
+        self.lenses = lenses
+        self.items_per_warp = int(items_per_warp)
+        self.host_output = bool(host_output)
+        self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else device
+        self.streams = {lv: [torch.cuda.Stream(device=self.device, priority=lv) for _ in range(max_inflight)]
+                        for lv in self.LEVELS}
+        self.free_streams = {lv: list(v) for lv, v in self.streams.items()}
+        self._pinned: Dict[tuple, list] = collections.defaultdict(list)
+
+    def cta_items(self, req: FlareRequest) -> int:
+        """Items per warp for this request's CTAs: about the same CTA lifetime
+        for every request (an item costs ~ wavelengths x surfaces), so the
+        CTA scheduler can hand SMs to a higher-priority stream often."""
+        if self.items_per_warp <= 0:
+            return 0
+        n_surf = len(self.lenses[req.lens_id].lens.surfaces)
+        cost = max(1.0, req.n_spec * n_surf / 80.0)
+        return max(1, int(round(self.items_per_warp / cost)))
+
+    def estimate(self, req: FlareRequest) -> None:
+        rl = self.lenses[req.lens_id]
+        masked = 0.8 * req.ray_grid * req.ray_grid
+        req.est_rays = int(rl.n_pairs * masked * req.n_spec)
+        req.priority = priority_class(req.est_rays)
+        req.device_bytes = request_bytes(req.width, req.height, rl.n_pairs)
+
+    def _pinned_buf(self, shape):
+        lst = self._pinned[shape]
+        if lst:
+            return lst.pop()
+        return self.torch.empty(shape, dtype=self.torch.float32, pin_memory=True)
+
+    def recycle(self, host):
+        if host is not None:
+            self._pinned[tuple(host.shape)].append(host)
+
+    def start(self, req: FlareRequest) -> _Running:
+        torch = self.torch
+        rl = self.lenses[req.lens_id]
+        lv = req.priority if req.priority in self.free_streams else 0
+        pool = self.free_streams[lv]
+        stream = pool.pop() if pool else torch.cuda.Stream(device=self.device, priority=lv)
+        spec, corr = _spectral(req.n_spec, rl.config)
+        apply_corr = bool(rl.config.spectral_correction) and req.n_spec != 3
+        prm = render_params(rl, req, corr, apply_corr)
+        src = np.array([[math.radians(req.field_deg), 0.0, 1.0, 1.0, 1.0]], np.float32)
+        P = C.POINTER
+        st = stream.cuda_stream
+        h = C.c_void_p()
+        sp = np.ascontiguousarray(spec, np.float32)
+        _native.check(self._lib.gl_request_create(rl._h, int(req.ray_grid), sp.ctypes.data_as(P(gl_spectral_sample)),
+                                                  len(sp), src.ctypes.data_as(P(gl_flare_source)), 1, C.byref(prm),
+                                                  st, C.byref(h)), "request_create")
+        run = _Running()
+        run.req, run.handle, run.stream = req, h, (lv, stream)
+        # the request renders into its own pool-allocated planes
+        _native.check(self._lib.gl_request_enqueue(h, None, None, None, self.cta_items(req), st), "request_enqueue")
+        run.host = None
+        run.outs = None
+        if self.host_output:
+            run.host = self._pinned_buf((3, req.height, req.width))
+            _native.check(self._lib.gl_request_copy_out(h, run.host.data_ptr(), st), "request_copy_out")
+        else:
+            # device result: copied out of the pool block into a torch tensor on the same stream
+            with torch.cuda.stream(stream):
+                run.outs = torch.empty((3, req.height, req.width), dtype=torch.float32, device=self.device)
+                _native.check(self._lib.gl_request_copy_out(h, run.outs.data_ptr(), st), "request_copy_out")
+        run.event = torch.cuda.Event()
+        run.event.record(stream)
+        return run
+
+    def prewarm(self, shapes, count: int):
+        """Pinned host buffers for `count` results of each (width, height)."""
+        for (w, h) in shapes:
+            bufs = [self._pinned_buf((3, h, w)) for _ in range(count)]
+            for b in bufs:
+                self.recycle(b)
+
+    def done(self, run: _Running) -> bool:
+        return run.event.query()
+
+    def finish(self, run: _Running):
+        """Release the request's device memory (stream-ordered) and stream;
+        returns the host planes (or the device tensor)."""
+        lv, stream = run.stream
+        v = C.c_longlong()
+        if self._lib.gl_request_traced(run.handle, C.byref(v), None) == 0:
+            run.req.traced = int(v.value)          # the stream is idle: no wait
+        self._lib.gl_request_destroy(run.handle, stream.cuda_stream)
+        run.handle = None
+        self.free_streams[lv].append(stream)
+        out = run.host if run.host is not None else run.outs
+        run.outs = None
+        return out
+
+
+class FlareServer:
+    """Continuous-batching request loop over one GPU.
+
+    Streams beyond the device's hardware work queues share queues and
+    serialise; run the process with CUDA_DEVICE_MAX_CONNECTIONS=32 (set before
+    CUDA starts) and at most 32 requests in flight."""
+
+    def __init__(self, lenses: Dict[int, ResidentLens], budget_bytes: int = 120 * 10 ** 9,
+                 max_inflight: int = 16, items_per_warp: int = 8, host_output: bool = True,
+                 executor=None, clock: Callable[[], float] = time.perf_counter):
+        self.lenses = lenses
+        self.sched = Scheduler(budget_bytes, max_inflight)
+        self.exec = executor if executor is not None else CudaExecutor(lenses, max_inflight, items_per_warp,
+                                                                       host_output)
+        self.clock = clock
+        self.t0 = clock()
+        self.running: list = []             # (request, executor handle)
+        self.completed: List[FlareRequest] = []
+        self.on_result: Optional[Callable] = None
+
+    def now(self) -> float:
+        return self.clock() - self.t0
+
+    def submit(self, req: FlareRequest):
+        self.exec.estimate(req)
+        self.sched.submit(req)
+
+    def step(self) -> int:
+        """Complete finished requests, then admit and start new ones.
+        Returns the number of state changes."""
+        changes = 0
+        still = []
+        for req, run in self.running:
+            if self.exec.done(run):
+                out = self.exec.finish(run)
+                req.finish = self.now()
+                self.sched.release(req)
+                self.completed.append(req)
+                if self.on_result is not None:
+                    self.on_result(req, out)      # the host buffer is reused after this returns
+                if hasattr(self.exec, "recycle"):
+                    self.exec.recycle(out if getattr(self.exec, "host_output", False) else None)
+                changes += 1
+            else:
+                still.append((req, run))
+        self.running = still
+        for req in self.sched.admit():
+            req.start = self.now()
+            self.running.append((req, self.exec.start(req)))
+            changes += 1
+        return changes
+
+    def idle(self) -> bool:
+        return not self.running and not self.sched.pending
+
+    def run_trace(self, requests: List[FlareRequest], poll_s: float = 2e-4) -> List[FlareRequest]:
+        """Replay requests at their arrival times (seconds from now) and
+        serve them; returns them with start/finish times filled."""
+        reqs = sorted(requests, key=lambda r: r.arrival)
+        self.t0 = self.clock()
+        i = 0
+        while i < len(reqs) or not self.idle():
+            now = self.now()
+            while i < len(reqs) and reqs[i].arrival <= now:
+                self.submit(reqs[i])
+                i += 1
+            if self.step() == 0:
+                nxt = reqs[i].arrival - self.now() if i < len(reqs) else poll_s
+                time.sleep(max(0.0, min(poll_s, nxt)))
+        return reqs
+
+
+def latency_stats(reqs: List[FlareRequest], where: Optional[Callable] = None) -> dict:
+    sel = [r for r in reqs if where is None or where(r)]
+    if not sel:
+        return {"n": 0}
+    lat = np.array([r.latency for r in sel]) * 1e3
+    return {"n": len(sel), "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "mean_ms": float(lat.mean()), "max_ms": float(lat.max())}
+
+
+def poisson_requests(rate_hz: float, duration_s: float, lens_ids, seed: int = 5,
+                     sizes=((512, 512), (1024, 1024), (2048, 2048), (4096, 4096)),
+                     n_specs=(8, 16, 31), grid_min: int = 32, grid_max: int = 256,
+                     field_max_deg: float = 20.0) -> List[FlareRequest]:
+    """The serving mix: Poisson arrivals; per request a lens from the pool,
+    an output size, a wavelength count, a pupil grid side (multiple of 16 in
+    [grid_min, grid_max]) and a source field angle, all seeded."""
+    rng = np.random.default_rng(seed)
+    t, out = 0.0, []
+    lens_ids = list(lens_ids)
+    grids = list(range(grid_min, grid_max + 1, 16))
+    while True:
+        t += rng.exponential(1.0 / rate_hz)
+        if t >= duration_s:
+            break
+        w, h = sizes[int(rng.integers(len(sizes)))]
+        out.append(FlareRequest(lens_id=lens_ids[int(rng.integers(len(lens_ids)))], width=w, height=h,
+                                n_spec=int(n_specs[int(rng.integers(len(n_specs)))]),
+                                ray_grid=int(grids[int(rng.integers(len(grids)))]),
+                                field_deg=float(rng.uniform(0.0, field_max_deg)), rid=len(out), arrival=t))
+    return out
+
+
+def serving_lens(seed: int, n_surfaces: int, field_deg: float = 20.0):
+    """(OpticalSystem, sensor_half_w, sensor_half_h) of one seeded serving
+    lens: the random prescription with n_surfaces entries, and a square
+    sensor whose half diagonal images the lens's full field (half side =
+    EFL tan(field) / sqrt 2, paraxial, FP64)."""
+    from .optics import OpticalSystem
+    from .prescriptions import paraxial_efl_bfd, random_lens
+    surfs = random_lens(seed, n_surfaces, field_deg=field_deg)
+    efl, _ = paraxial_efl_bfd(surfs)
+    half = abs(efl) * math.tan(math.radians(field_deg)) / math.sqrt(2.0)
+    return OpticalSystem.from_records(surfs, name="serve_%d_%d" % (seed, n_surfaces)), half, half
+
+
+def serving_lens_pool(n_lenses: int, config, seed: int = 100, n_min: int = 8, n_max: int = 30):
+    """Register n_lenses seeded lenses with n_min..n_max surfaces as resident
+    lenses; returns {lens_id: ResidentLens}."""
+    rng = np.random.default_rng(seed)
+    pool = {}
+    for i in range(n_lenses):
+        n = int(rng.integers(n_min, n_max + 1))
+        lens, hw, hh = serving_lens(seed + i, n)
+        pool[i] = ResidentLens(lens, hw, hh, config)
+    return pool

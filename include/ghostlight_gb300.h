@@ -318,6 +318,59 @@ int gl_conv2d_plan_execute2(gl_conv_plan* plan, const float* d_in_r, const float
 int gl_conv2d_plan_info(const gl_conv_plan* plan, int* P, int* Q);
 int gl_conv2d_plan_destroy(gl_conv_plan* plan);
 
+/* ---- Serving: resident lenses and stream-ordered requests -----------------
+ * The reference renders one flare per blocking call under process-wide
+ * mutexes (ghost_render.cu:504-511, entered from bind_renderers.cpp:85-134)
+ * and has no serving layer; these calls are what a request loop over the
+ * flare path binds instead.
+ *
+ * gl_lens: one lens kept in HBM across requests — packed surfaces, the
+ * filtered ghost pairs (gl_filter_ghost_pairs output, order kept), the
+ * off-sensor probe grids, and caches of IOR slices per wavelength set and of
+ * pupil grids per ray_grid (filled on first use, or ahead by
+ * gl_lens_prepare).  A lens must outlive every request created on it. */
+typedef struct gl_lens gl_lens;
+int gl_lens_create(const gl_surface* surfaces, int n_surfaces, const gl_ghost_pair* pairs,
+                   const float* area_boosts, int n_pairs, int blades_override,
+                   float rotation_deg, gl_lens** out);
+int gl_lens_prepare(gl_lens* lens, int ray_grid, const gl_spectral_sample* spec, int n_spec);
+int gl_lens_info(const gl_lens* lens, int* n_pairs, long long* device_bytes);
+int gl_lens_destroy(gl_lens* lens);
+
+/* gl_request: one ghost-layer render on a resident lens with one uniform
+ * pupil grid (ray_grid^2, masked) for every pair — the computation of
+ * launch_ghost_render (ghost_render.cu:630) for those inputs.  Its device
+ * memory (accumulator, spectral table, counters) is one allocation from a
+ * stream-ordered pool on `stream`; create / enqueue / destroy never
+ * synchronise the device, so requests on different streams overlap.
+ * items_per_warp = 0: persistent work queue over the whole GPU;
+ * > 0: short CTAs of that many 32-sample items per warp, which the CTA
+ * scheduler interleaves with other streams' work by stream priority.
+ * destroy frees the memory in stream order after the enqueued work. */
+typedef struct gl_request gl_request;
+int gl_request_create(gl_lens* lens, int ray_grid, const gl_spectral_sample* spec, int n_spec,
+                      const gl_flare_source* sources, int n_sources,
+                      const gl_ghost_render_params* params, void* stream, gl_request** out);
+/* Null outputs render into the request's own planes (r | g | b, contiguous,
+ * W x H float32 each): gl_request_planes gives their device address and
+ * gl_request_copy_out enqueues one copy of all three to host memory (pinned
+ * for an asynchronous copy) or to device memory. */
+int gl_request_enqueue(gl_request* req, float* d_out_r, float* d_out_g, float* d_out_b,
+                       int items_per_warp, void* stream);
+int gl_request_planes(const gl_request* req, float** d_rgb);
+int gl_request_copy_out(const gl_request* req, void* host_rgb, void* stream);
+int gl_request_info(const gl_request* req, long long* rays, long long* device_bytes,
+                    int* grid_samples);
+/* Ray-wavelength traces of the last enqueue.  stream == NULL: the caller has
+ * seen that work complete, and the count is read from a pinned host word the
+ * enqueue filled (no CUDA call); otherwise a synchronous read on `stream`. */
+int gl_request_traced(const gl_request* req, long long* out, void* stream);
+int gl_request_destroy(gl_request* req, void* stream);
+/* The request pool of the current device: bytes reserved / in use; trim
+ * releases reserved bytes above keep_bytes back to the driver. */
+int gl_pool_info(long long* reserved, long long* used);
+int gl_pool_trim(long long keep_bytes);
+
 /* Number of kernel launches issued by the last device call on this thread. */
 int gl_last_launch_count(void);
 

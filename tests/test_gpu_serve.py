@@ -1,0 +1,93 @@
+"""Serving path on the GPU: a request equals the plan render of the same
+inputs, the two work modes agree, and every result is the same alone and in
+a concurrent mix."""
+import math
+
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def pool():
+    import ghostlight_gb300 as gl
+    from ghostlight_gb300.serve import serving_lens_pool
+    cfg = gl.FlareConfig(min_ghost_intensity=1e-6)
+    p = serving_lens_pool(3, cfg, seed=200, n_min=8, n_max=16)
+    yield p, cfg
+    for rl in p.values():
+        rl.close()
+
+
+def _run_server(pool, reqs, **kw):
+    from ghostlight_gb300.serve import FlareServer
+    results = {}
+    srv = FlareServer(pool, max_inflight=kw.pop("max_inflight", 8), **kw)
+    srv.on_result = lambda r, out: results.__setitem__(r.rid, out.clone())
+    srv.run_trace(reqs)
+    torch.cuda.synchronize()
+    return results
+
+
+def _reqs():
+    from ghostlight_gb300.serve import FlareRequest
+    shapes = [(256, 256, 8, 48, 3.0), (512, 512, 16, 64, 12.0), (384, 256, 8, 96, 18.0),
+              (512, 512, 31, 48, 7.0), (256, 256, 16, 80, 0.0), (512, 384, 8, 64, 15.0)]
+    out = []
+    for i, (w, h, ns, g, f) in enumerate(shapes):
+        out.append(FlareRequest(lens_id=i % 3, width=w, height=h, n_spec=ns, ray_grid=g, field_deg=f, rid=i))
+    return out
+
+
+def test_request_matches_plan_render(pool):
+    from ghostlight_gb300.flare import GhostRenderPlan, pupil_grid
+    from ghostlight_gb300.serve import _spectral
+    p, cfg = pool
+    for req in _reqs()[:3]:
+        rl = p[req.lens_id]
+        got = _run_server(p, [req])[req.rid]
+        spec, corr = _spectral(req.n_spec, cfg)
+        grid = pupil_grid(rl.lens, req.ray_grid, 0, 0, 0, 0.0)
+        src = np.array([[math.radians(req.field_deg), 0.0, 1.0, 1.0, 1.0]], np.float32)
+        plan = GhostRenderPlan(rl.lens, rl.pairs, rl.boosts, src, [grid], np.zeros(len(rl.pairs), np.int32), spec,
+                               corr, req.width, req.height, rl.sensor_half_w, rl.sensor_half_h, req.gain,
+                               apply_correction=True, cull_dead_pairs=True)
+        outs = [torch.zeros((req.height, req.width), device="cuda") for _ in range(3)]
+        plan.execute(*outs)
+        torch.cuda.synchronize()
+        want = torch.stack(outs).cpu().numpy()
+        plan.close()
+        assert np.abs(want).sum() > 0
+        assert rel_l2(got.numpy(), want) < 1e-5
+
+
+@pytest.mark.parametrize("ipw", [0, 2])
+def test_work_modes_agree(pool, ipw):
+    p, _ = pool
+    reqs = _reqs()[3:5]
+    a = _run_server(p, [r for r in reqs], items_per_warp=8)
+    for r in reqs:
+        r.start = r.finish = 0.0
+    b = _run_server(p, reqs, items_per_warp=ipw)
+    for r in reqs:
+        assert rel_l2(b[r.rid].numpy(), a[r.rid].numpy()) < 1e-5
+
+
+def test_alone_and_in_the_mix_agree(pool):
+    p, _ = pool
+    reqs = _reqs()
+    alone = {}
+    for r in reqs:
+        alone.update(_run_server(p, [r]))
+    for r in reqs:
+        r.arrival = 0.0
+    mix = _run_server(p, reqs, max_inflight=6)
+    assert set(mix) == set(alone)
+    for r in reqs:
+        a, m = alone[r.rid].numpy(), mix[r.rid].numpy()
+        assert np.isfinite(m).all()
+        assert rel_l2(m, a) < 1e-5, r
