@@ -653,6 +653,8 @@ def main():
         lens, cal = _workload()
         if not (args.no_cpu_baseline or args.quick):
             res["cpu_baseline"] = cpu_baseline(plan, lens, cal)
+        if not args.quick and args.serve_seconds > 0:
+            res["serving"] = run_serving(args)
         res["roofline"] = roofline(res, plan)
         print(json.dumps(res))
     if world > 1:
