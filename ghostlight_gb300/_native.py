@@ -53,6 +53,10 @@ def _declare(lib):
     lib.gl_mdft_plan_execute.argtypes = [vp, vp, vp, vp, vp, vp]
     lib.gl_mdft_plan_status.argtypes = [vp, P(i)]
     lib.gl_mdft_plan_destroy.argtypes = [vp]
+    lib.gl_mdft_plan_create2.argtypes = [i, i, i, i, P(d), P(d), d, d, P(f), i, vp, P(vp)]
+    lib.gl_mdft_plan_set_center.argtypes = [vp, d, d, vp]
+    lib.gl_mdft_plan_execute2.argtypes = [vp, vp, vp, vp, vp, i, vp]
+    lib.gl_build_pupil.argtypes = [P(gl_surface), i, i, f, i, f, vp, vp]
     lib.gl_conv2d_plan_create.argtypes = [i, i, P(f), i, i, vp, P(vp)]
     lib.gl_conv2d_plan_execute.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp]
     lib.gl_conv2d_plan_execute2.argtypes = [vp] + [vp] * 9 + [vp]

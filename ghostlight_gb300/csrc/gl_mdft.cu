@@ -217,7 +217,10 @@ constexpr int kMdftThreads = 192;     // warps 0-3 epilogue, warp 4 TMA, warp 5 
 constexpr int kOpTile = 128 * 128;    // bytes of one 128-row x 128-byte operand tile
 
 struct MdftArgs {
-    int K_out, n, n_lambda, Kp, nkb, NB, NI, n_units;
+    int KA;       // rows of the A operand per (wavelength, re/im part): Kx in step 1, Ky in step 2
+    int Kx;       // output width = T' k range; row stride of the output planes
+    int NBm;      // 128-row blocks of the A operand (step 1: Kx / 128, step 2: Ky / 128)
+    int n, n_lambda, Kp, nkb, NB, NI, n_units;   // NB = Kx / 128 (T' blocks per wavelength)
     void* tprime;                     // step 1 output / step 2 B operand
     float* out_r;
     float* out_g;
@@ -304,8 +307,8 @@ __global__ void __launch_bounds__(kMdftThreads, 1) mdft_kernel(const __grid_cons
         }
         else
         {
-            lam = u / (args.NB * args.NI);
-            const int r = u % (args.NB * args.NI);
+            lam = u / (args.NBm * args.NI);
+            const int r = u % (args.NBm * args.NI);
             mb = r / args.NI;
             xb = r % args.NI;
         }
@@ -321,7 +324,7 @@ __global__ void __launch_bounds__(kMdftThreads, 1) mdft_kernel(const __grid_cons
             {
                 int lam, mb, xb;
                 decode(u, lam, mb, xb);
-                const int rowA = (lam * 2) * args.K_out + mb * 128;
+                const int rowA = (lam * 2) * args.KA + mb * 128;
                 for (int kb = 0; kb < args.nkb; ++kb, ++it)
                 {
                     const int s = it % kStagesM, r = it / kStagesM;
@@ -330,7 +333,7 @@ __global__ void __launch_bounds__(kMdftThreads, 1) mdft_kernel(const __grid_cons
                     tc::mbar_expect_tx(&full[s], kStageBytes);
                     const int x = kb * kbe;
                     tc::tma_load_2d(st, &tA, x, rowA, &full[s]);
-                    tc::tma_load_2d(st + kOpTile, &tA, x, rowA + args.K_out, &full[s]);
+                    tc::tma_load_2d(st + kOpTile, &tA, x, rowA + args.KA, &full[s]);
                     if (STEP == 2)
                     {
                         const int rowB = ((lam * args.NB + xb) * 3) * 128;
@@ -426,7 +429,7 @@ __global__ void __launch_bounds__(kMdftThreads, 1) mdft_kernel(const __grid_cons
                     tc::tmem_ld16(ta + (uint32_t)(c * 16), re);
                     tc::tmem_ld16(ta + 128u + (uint32_t)(c * 16), im);
                     if (!ok) continue;
-                    const size_t base = l * (size_t)args.K_out + (size_t)(xb * 128 + c * 16);
+                    const size_t base = l * (size_t)args.Kx + (size_t)(xb * 128 + c * 16);
                     #pragma unroll
                     for (int j = 0; j < 16; j += 4)
                     {
@@ -485,26 +488,44 @@ __global__ void __launch_bounds__(kMdftThreads, 1) mdft_kernel(const __grid_cons
 }
 
 // DFT matrices W'[lam][part][k][Kp]: part 0 = Re, 1 = Im of
-// exp(-2 pi i s(lam) (j - cj)(k - ck)).  The phase is reduced in FP64
-// (the index product is exact) and the reduced angle evaluated in FP32.
+// exp(-2 pi i s(lam) (j - cj)(k - ck)).  The phase is formed in FP32
+// double-float arithmetic (Dekker / Ogita-Rump-Oishi error-free products
+// with FMA): s = s_hi + s_lo and ck = ck_hi + ck_lo are split on the host,
+// a = j - cj is exact (cj a half-integer), b = k - ck is carried as a
+// two-float sum, and the product's integer cycles are removed from
+// the leading term exactly; the reduced phase is accurate to ~1e-9 cycles,
+// then evaluated with sincospif.  (The FP64 units of this part are slow.)
 // FORM 0 stores [hi | hi | lo] along the reduction axis, FORM 1 the FP32 value.
 template <int FORM>
-__global__ void mdft_dft_kernel(void* out, int n_lambda, int K_out, int n, int Kp, const double* scale, double ck,
-                                double cj)
+__global__ void mdft_dft_kernel(void* out, int n_lambda, int K_rows, int n, int Kp, const float2* __restrict__ scale,
+                                float ck_hi, float ck_lo, float cj)
 {
-    const size_t total = (size_t)n_lambda * K_out * n;
+    const size_t total = (size_t)n_lambda * K_rows * n;
     for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x)
     {
         const int j = (int)(e % n);
-        const int k = (int)((e / n) % K_out);
-        const int lam = (int)(e / ((size_t)n * K_out));
-        const double ph = scale[lam] * (((double)j - cj) * ((double)k - ck));
-        const double fr = ph - rint(ph);            // |fr| <= 1/2 cycles
+        const int k = (int)((e / n) % K_rows);
+        const int lam = (int)(e / ((size_t)n * K_rows));
+        const float2 sc = scale[lam];                  // (s_hi, s_lo)
+        const float a = (float)j - cj;                 // exact
+        // b = k - ck as bh + bl: Knuth's two-sum of k and -ck_hi, then -ck_lo
+        const float kf = (float)k;
+        const float bh = kf - ck_hi;
+        const float bb = bh - kf;
+        const float bl = ((kf - (bh - bb)) + (-ck_hi - bb)) - ck_lo;
+        const float p1 = a * bh;
+        const float e1 = fmaf(a, bh, -p1);             // a*bh = p1 + e1 exactly
+        const float m_lo = e1 + a * bl;
+        const float q = sc.x * p1;
+        const float eq = fmaf(sc.x, p1, -q);           // s_hi*p1 = q + eq exactly
+        const float rest = eq + sc.x * m_lo + sc.y * p1;
+        float fr = (q - rintf(q)) + rest;              // q - rint(q) is exact
+        fr -= rintf(fr);
         float sv, cv;
-        sincospif((float)(2.0 * fr), &sv, &cv);
+        sincospif(2.0f * fr, &sv, &cv);
         const float re = cv, im = -sv;
-        const size_t rr = ((size_t)(lam * 2 + 0) * K_out + k) * Kp;
-        const size_t ri = ((size_t)(lam * 2 + 1) * K_out + k) * Kp;
+        const size_t rr = ((size_t)(lam * 2 + 0) * K_rows + k) * Kp;
+        const size_t ri = ((size_t)(lam * 2 + 1) * K_rows + k) * Kp;
         if (FORM == 0)
         {
             __nv_bfloat16* W = static_cast<__nv_bfloat16*>(out);
@@ -521,6 +542,49 @@ __global__ void mdft_dft_kernel(void* out, int n_lambda, int K_out, int n, int K
             W[ri + j] = im;
         }
     }
+}
+
+// Pupil amplitude of the lens's stop (build_pupil_kernel,
+// starburst_render.cu:155-191, stop term): grid coordinate g in [-1, 1) maps
+// to pupil coordinate g / pupil_fill; 4 x 4 supersamples per texel tested
+// against the stop silhouette (PupilMask::contains, aperture_sampler.h:63-82:
+// ellipse of the stop's aspect, then the regular n-gon).
+struct PupilDev {
+    float aspect, rot_rad, apothem, sector;
+    int n_blades;
+};
+
+__device__ __forceinline__ bool pupil_in(const PupilDev& m, float u, float v)
+{
+    const float ux = u / m.aspect;
+    const float r2 = ux * ux + v * v;
+    if (r2 > 1.0f) return false;
+    if (m.n_blades >= 3)
+    {
+        const float angle = atan2f(v, ux) - m.rot_rad;
+        float sector = fmodf(angle, m.sector);
+        if (sector < 0.0f) sector += m.sector;
+        if (sqrtf(r2) * cosf(sector - m.sector * 0.5f) > m.apothem) return false;
+    }
+    return true;
+}
+
+__global__ void pupil_build_kernel(float* __restrict__ out, int N, float fill, PupilDev m)
+{
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= N * N) return;
+    const int i = idx % N, j = idx / N;
+    int cnt = 0;
+    #pragma unroll
+    for (int sy = 0; sy < 4; ++sy)
+        #pragma unroll
+        for (int sx = 0; sx < 4; ++sx)
+        {
+            const float u = (((float)i + ((float)sx + 0.5f) * 0.25f) / (float)N * 2.0f - 1.0f) / fill;
+            const float v = (((float)j + ((float)sy + 0.5f) * 0.25f) / (float)N * 2.0f - 1.0f) / fill;
+            cnt += pupil_in(m, u, v) ? 1 : 0;
+        }
+    out[idx] = (float)cnt * (1.0f / 16.0f);
 }
 
 // Pupil amplitude A[i][j] (float, n x n) -> B operand [hi | lo | hi] or FP32.
@@ -556,6 +620,7 @@ constexpr int kSB = 128, kSK = 16;
 __global__ void __launch_bounds__(256) mdft_simt_step1(const float* __restrict__ W, const float* __restrict__ A,
                                                        float* __restrict__ T, int K_out, int n, int NB)
 {
+    // K_out = rows of W_x per (wavelength, part) = Kx
     __shared__ float sWr[kSK][kSB + 4], sWi[kSK][kSB + 4], sA[kSK][kSB + 4];
     const int lam = blockIdx.z, mb = blockIdx.y, ib = blockIdx.x;
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
@@ -604,15 +669,16 @@ __global__ void __launch_bounds__(256) mdft_simt_step1(const float* __restrict__
 
 __global__ void __launch_bounds__(256) mdft_simt_step2(const float* __restrict__ W, const float* __restrict__ T,
                                                        const float4* __restrict__ weights, float* out_r, float* out_g,
-                                                       float* out_b, int K_out, int n, int NB, int n_lambda)
+                                                       float* out_b, int K_rows, int K_out, int n, int NB, int n_lambda)
 {
+    // K_rows = rows of W_y per (wavelength, part) = Ky; K_out = output width Kx
     __shared__ float sWr[kSK][kSB + 4], sWi[kSK][kSB + 4], sTr[kSK][kSB + 4], sTi[kSK][kSB + 4];
     const int mb = blockIdx.y, nb = blockIdx.x;
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     for (int lam = 0; lam < n_lambda; ++lam)
     {
-        const float* Wr = W + ((size_t)(lam * 2 + 0) * K_out + mb * kSB) * n;
-        const float* Wi = W + ((size_t)(lam * 2 + 1) * K_out + mb * kSB) * n;
+        const float* Wr = W + ((size_t)(lam * 2 + 0) * K_rows + mb * kSB) * n;
+        const float* Wi = W + ((size_t)(lam * 2 + 1) * K_rows + mb * kSB) * n;
         const size_t blk = ((size_t)(lam * NB + nb) * 3) * 128;
         const float* Tr = T + (blk + 128) * n;
         const float* Ti = T + (blk + 256) * n;
@@ -669,13 +735,14 @@ __global__ void __launch_bounds__(256) mdft_simt_step2(const float* __restrict__
 
 // ---- MDFT plan ----------------------------------------------------------------
 struct MdftPlan {
-    int n = 0, K_out = 0, n_lambda = 0, form = 0, Kp = 0, elem = 2;
-    void* wx = nullptr;     // W_x' [lam][2][K_out][Kp]
-    void* wy = nullptr;     // W_y'
+    int n = 0, Kx = 0, Ky = 0, n_lambda = 0, form = 0, Kp = 0, elem = 2;
+    void* wx = nullptr;     // W_x' [lam][2][Kx][Kp]
+    void* wy = nullptr;     // W_y' [lam][2][Ky][Kp]
     void* mask = nullptr;   // A'   [n][Kp]
-    void* tprime = nullptr; // T'   [lam][NB][3][128][Kp]
+    void* tprime = nullptr; // T'   [lam][Kx/128][3][128][Kp]
     float4* weights = nullptr;
-    double* scales = nullptr;   // [2][n_lambda] device copy
+    float2* scales = nullptr;   // [2][n_lambda] (s_hi, s_lo) device copy
+    double cx = 0.0, cy = 0.0;
     int* err = nullptr;
     CUtensorMap t_wx, t_wy, t_mask, t_tp;
     int sms = 0;
@@ -693,38 +760,69 @@ static void mdft_free(MdftPlan* p)
 
 struct gl_mdft_plan { gl::MdftPlan* p; };
 
-extern "C" int gl_mdft_plan_create(int n, int K_out, int n_lambda, const double* scale_x, const double* scale_y,
-                                   double center_x, double center_y, const float* weights_rgb, int form,
-                                   void* stream, gl_mdft_plan** out)
+namespace gl {
+
+// Enqueue the DFT matrices of the plan's current centre.
+static cudaError_t mdft_build_matrices(MdftPlan* p, cudaStream_t st)
+{
+    const int blocks = 4 * p->sms;
+    const float cj = 0.5f * (float)(p->n - 1);
+    const float cxh = (float)p->cx, cxl = (float)(p->cx - (double)cxh);
+    const float cyh = (float)p->cy, cyl = (float)(p->cy - (double)cyh);
+    if (p->form == 0)
+    {
+        mdft_dft_kernel<0><<<blocks, 256, 0, st>>>(p->wx, p->n_lambda, p->Kx, p->n, p->Kp, p->scales, cxh, cxl, cj);
+        mdft_dft_kernel<0><<<blocks, 256, 0, st>>>(p->wy, p->n_lambda, p->Ky, p->n, p->Kp, p->scales + p->n_lambda, cyh,
+                                                   cyl, cj);
+    }
+    else
+    {
+        mdft_dft_kernel<1><<<blocks, 256, 0, st>>>(p->wx, p->n_lambda, p->Kx, p->n, p->Kp, p->scales, cxh, cxl, cj);
+        mdft_dft_kernel<1><<<blocks, 256, 0, st>>>(p->wy, p->n_lambda, p->Ky, p->n, p->Kp, p->scales + p->n_lambda, cyh,
+                                                   cyl, cj);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace gl
+
+extern "C" int gl_mdft_plan_create2(int n, int Kx, int Ky, int n_lambda, const double* scale_x, const double* scale_y,
+                                    double center_x, double center_y, const float* weights_rgb, int form, void* stream,
+                                    gl_mdft_plan** out)
 {
     using namespace gl;
     if (!out || !scale_x || !scale_y || !weights_rgb) return fail(GL_ERR_INVALID, "mdft_plan_create: null argument");
-    if (n <= 0 || n % 128 || K_out <= 0 || K_out % 128)
-        return fail(GL_ERR_INVALID, "mdft_plan_create: the pupil side n and output side K_out must be multiples of 128");
+    if (n <= 0 || n % 128 || Kx <= 0 || Kx % 128 || Ky <= 0 || Ky % 128)
+        return fail(GL_ERR_INVALID, "mdft_plan_create: the pupil side n and output sides Kx, Ky must be multiples of 128");
+    if (Kx > 8192 || Ky > 8192 || n > 4096) return fail(GL_ERR_INVALID, "mdft_plan_create: sides above 8192 (4096 for n)");
     if (n_lambda < 1 || n_lambda > 1024) return fail(GL_ERR_INVALID, "mdft_plan_create: 1..1024 wavelengths");
     if (form < 0 || form > 2)
         return fail(GL_ERR_UNSUPPORTED, "mdft_plan_create: form must be 0 (split BF16), 1 (TF32) or 2 (FP32 CUDA cores)");
+    if (!(std::fabs(center_x) < 4096.0) || !(std::fabs(center_y) < 4096.0))
+        return fail(GL_ERR_INVALID, "mdft_plan_create: centre coordinates must lie within +-4096 pixels");
     cudaStream_t st = (cudaStream_t)stream;
     MdftPlan* p = new MdftPlan();
-    p->n = n; p->K_out = K_out; p->n_lambda = n_lambda; p->form = form;
+    p->n = n; p->Kx = Kx; p->Ky = Ky; p->n_lambda = n_lambda; p->form = form;
+    p->cx = center_x; p->cy = center_y;
     p->Kp = form == 0 ? 3 * n : n;
     p->elem = form == 0 ? 2 : 4;
-    const int NB = K_out / 128;
-    const int sform = form == 0 ? 0 : 1;   // storage: split BF16, or FP32 for TF32 / FP32 forms
-    (void)sform;
-    const size_t wbytes = (size_t)n_lambda * 2 * K_out * p->Kp * p->elem;
+    const int NBx = Kx / 128;
+    const size_t wxbytes = (size_t)n_lambda * 2 * Kx * p->Kp * p->elem;
+    const size_t wybytes = (size_t)n_lambda * 2 * Ky * p->Kp * p->elem;
     const size_t mbytes = (size_t)n * p->Kp * p->elem;
-    const size_t tbytes = (size_t)n_lambda * NB * 3 * 128 * p->Kp * p->elem;
+    const size_t tbytes = (size_t)n_lambda * NBx * 3 * 128 * p->Kp * p->elem;
     cudaError_t e = cudaSuccess;
     auto chk = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
-    chk(cudaMalloc(&p->wx, wbytes));
-    chk(cudaMalloc(&p->wy, wbytes));
+    chk(cudaMalloc(&p->wx, wxbytes));
+    chk(cudaMalloc(&p->wy, wybytes));
     chk(cudaMalloc(&p->mask, mbytes));
     chk(cudaMalloc(&p->tprime, tbytes));
     chk(cudaMalloc(&p->weights, sizeof(float4) * n_lambda));
-    chk(cudaMalloc(&p->scales, sizeof(double) * 2 * n_lambda));
+    chk(cudaMalloc(&p->scales, sizeof(float2) * 2 * n_lambda));
     chk(cudaMalloc(&p->err, sizeof(int)));
-    chk(cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, 0));
+    int dev = 0;
+    chk(cudaGetDevice(&dev));
+    chk(cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, dev));
     if (e != cudaSuccess)
     {
         mdft_free(p);
@@ -732,23 +830,16 @@ extern "C" int gl_mdft_plan_create(int n, int K_out, int n_lambda, const double*
     }
     std::vector<float4> w((size_t)n_lambda);
     for (int l = 0; l < n_lambda; ++l) w[l] = make_float4(weights_rgb[3 * l], weights_rgb[3 * l + 1], weights_rgb[3 * l + 2], 0.0f);
-    std::vector<double> sc((size_t)2 * n_lambda);
-    for (int l = 0; l < n_lambda; ++l) { sc[l] = scale_x[l]; sc[n_lambda + l] = scale_y[l]; }
+    std::vector<float2> sc((size_t)2 * n_lambda);
+    for (int l = 0; l < n_lambda; ++l)
+    {
+        const float xh = (float)scale_x[l], yh = (float)scale_y[l];
+        sc[l] = make_float2(xh, (float)(scale_x[l] - (double)xh));
+        sc[n_lambda + l] = make_float2(yh, (float)(scale_y[l] - (double)yh));
+    }
     chk(cudaMemcpy(p->weights, w.data(), sizeof(float4) * n_lambda, cudaMemcpyHostToDevice));
-    chk(cudaMemcpy(p->scales, sc.data(), sizeof(double) * 2 * n_lambda, cudaMemcpyHostToDevice));
-    const double cj = 0.5 * (n - 1);
-    const int blocks = 4 * p->sms;
-    if (form == 0)
-    {
-        mdft_dft_kernel<0><<<blocks, 256, 0, st>>>(p->wx, n_lambda, K_out, n, p->Kp, p->scales, center_x, cj);
-        mdft_dft_kernel<0><<<blocks, 256, 0, st>>>(p->wy, n_lambda, K_out, n, p->Kp, p->scales + n_lambda, center_y, cj);
-    }
-    else
-    {
-        mdft_dft_kernel<1><<<blocks, 256, 0, st>>>(p->wx, n_lambda, K_out, n, p->Kp, p->scales, center_x, cj);
-        mdft_dft_kernel<1><<<blocks, 256, 0, st>>>(p->wy, n_lambda, K_out, n, p->Kp, p->scales + n_lambda, center_y, cj);
-    }
-    chk(cudaGetLastError());
+    chk(cudaMemcpy(p->scales, sc.data(), sizeof(float2) * 2 * n_lambda, cudaMemcpyHostToDevice));
+    if (e == cudaSuccess) chk(mdft_build_matrices(p, st));
     chk(cudaStreamSynchronize(st));
     // shared-memory opt-in once here, so execute enqueues kernels only (graph capture)
     {
@@ -769,10 +860,10 @@ extern "C" int gl_mdft_plan_create(int n, int K_out, int n_lambda, const double*
     int rc = GL_OK;
     if (e == cudaSuccess && form != 2)
     {
-        rc = make_tmap_2d(&p->t_wx, p->wx, dt, p->elem, (uint64_t)n_lambda * 2 * K_out, (uint64_t)p->Kp, 128, bc);
-        if (!rc) rc = make_tmap_2d(&p->t_wy, p->wy, dt, p->elem, (uint64_t)n_lambda * 2 * K_out, (uint64_t)p->Kp, 128, bc);
+        rc = make_tmap_2d(&p->t_wx, p->wx, dt, p->elem, (uint64_t)n_lambda * 2 * Kx, (uint64_t)p->Kp, 128, bc);
+        if (!rc) rc = make_tmap_2d(&p->t_wy, p->wy, dt, p->elem, (uint64_t)n_lambda * 2 * Ky, (uint64_t)p->Kp, 128, bc);
         if (!rc) rc = make_tmap_2d(&p->t_mask, p->mask, dt, p->elem, (uint64_t)n, (uint64_t)p->Kp, 128, bc);
-        if (!rc) rc = make_tmap_2d(&p->t_tp, p->tprime, dt, p->elem, (uint64_t)n_lambda * NB * 3 * 128, (uint64_t)p->Kp, 128, bc);
+        if (!rc) rc = make_tmap_2d(&p->t_tp, p->tprime, dt, p->elem, (uint64_t)n_lambda * NBx * 3 * 128, (uint64_t)p->Kp, 128, bc);
     }
     if (e != cudaSuccess || rc)
     {
@@ -784,44 +875,69 @@ extern "C" int gl_mdft_plan_create(int n, int K_out, int n_lambda, const double*
     return GL_OK;
 }
 
-extern "C" int gl_mdft_plan_execute(gl_mdft_plan* plan, const float* d_pupil, float* d_out_r, float* d_out_g,
-                                    float* d_out_b, void* stream)
+extern "C" int gl_mdft_plan_create(int n, int K_out, int n_lambda, const double* scale_x, const double* scale_y,
+                                   double center_x, double center_y, const float* weights_rgb, int form,
+                                   void* stream, gl_mdft_plan** out)
+{
+    return gl_mdft_plan_create2(n, K_out, K_out, n_lambda, scale_x, scale_y, center_x, center_y, weights_rgb, form,
+                                stream, out);
+}
+
+extern "C" int gl_mdft_plan_set_center(gl_mdft_plan* plan, double center_x, double center_y, void* stream)
+{
+    using namespace gl;
+    if (!plan) return fail(GL_ERR_INVALID, "mdft_plan_set_center: null plan");
+    if (!(std::fabs(center_x) < 4096.0) || !(std::fabs(center_y) < 4096.0))
+        return fail(GL_ERR_INVALID, "mdft_plan_set_center: centre coordinates must lie within +-4096 pixels");
+    plan->p->cx = center_x;
+    plan->p->cy = center_y;
+    GL_CUDA_TRY(mdft_build_matrices(plan->p, (cudaStream_t)stream));
+    g_last_launches = 2;
+    return GL_OK;
+}
+
+extern "C" int gl_mdft_plan_execute2(gl_mdft_plan* plan, const float* d_pupil, float* d_out_r, float* d_out_g,
+                                     float* d_out_b, int accumulate, void* stream)
 {
     using namespace gl;
     if (!plan || !d_pupil || !d_out_r || !d_out_g || !d_out_b) return fail(GL_ERR_INVALID, "mdft_plan_execute: null argument");
     MdftPlan* p = plan->p;
     cudaStream_t st = (cudaStream_t)stream;
-    const int NB = p->K_out / 128, NI = p->n / 128;
-    const size_t npx = (size_t)p->K_out * p->K_out;
+    const int NBx = p->Kx / 128, NBy = p->Ky / 128, NI = p->n / 128;
+    const size_t npx = (size_t)p->Kx * p->Ky;
     int launches = 0;
     GL_CUDA_TRY(cudaMemsetAsync(p->err, 0, sizeof(int), st));
     if (p->form == 0) mdft_mask_kernel<0><<<2 * p->sms, 256, 0, st>>>(d_pupil, p->mask, p->n, p->Kp);
     else mdft_mask_kernel<1><<<2 * p->sms, 256, 0, st>>>(d_pupil, p->mask, p->n, p->Kp);
     ++launches;
-    GL_CUDA_TRY(cudaMemsetAsync(d_out_r, 0, npx * sizeof(float), st));
-    GL_CUDA_TRY(cudaMemsetAsync(d_out_g, 0, npx * sizeof(float), st));
-    GL_CUDA_TRY(cudaMemsetAsync(d_out_b, 0, npx * sizeof(float), st));
+    if (!accumulate)
+    {
+        GL_CUDA_TRY(cudaMemsetAsync(d_out_r, 0, npx * sizeof(float), st));
+        GL_CUDA_TRY(cudaMemsetAsync(d_out_g, 0, npx * sizeof(float), st));
+        GL_CUDA_TRY(cudaMemsetAsync(d_out_b, 0, npx * sizeof(float), st));
+    }
     MdftArgs a;
-    a.K_out = p->K_out; a.n = p->n; a.n_lambda = p->n_lambda; a.Kp = p->Kp;
+    a.KA = p->Kx; a.Kx = p->Kx; a.NBm = NBx;
+    a.n = p->n; a.n_lambda = p->n_lambda; a.Kp = p->Kp;
     a.nkb = p->Kp / (p->form == 0 ? 64 : 32);
-    a.NB = NB; a.NI = NI;
+    a.NB = NBx; a.NI = NI;
     a.tprime = p->tprime; a.out_r = d_out_r; a.out_g = d_out_g; a.out_b = d_out_b;
     a.weights = p->weights; a.err = p->err;
     const size_t smem1 = 4 * 3 * (size_t)kOpTile + 1024, smem2 = 2 * 5 * (size_t)kOpTile + 1024;
-    // step 1
-    a.n_units = p->n_lambda * NB * NI;
-    int g1 = std::min(a.n_units, p->sms);
-    // step 2
+    a.n_units = p->n_lambda * NBx * NI;                 // step 1: (lambda, k block, pupil-row block)
+    const int g1 = std::min(a.n_units, p->sms);
     MdftArgs a2 = a;
-    a2.n_units = NB * NB * p->n_lambda;
-    int g2 = std::min(a2.n_units, p->sms);
+    a2.KA = p->Ky; a2.NBm = NBy;
+    a2.n_units = NBy * NBx * p->n_lambda;               // step 2: (output tile, lambda)
+    const int g2 = std::min(a2.n_units, p->sms);
     if (p->form == 2)
     {
-        mdft_simt_step1<<<dim3(NI, NB, p->n_lambda), 256, 0, st>>>(static_cast<const float*>(p->wx),
-                                                                   static_cast<const float*>(p->mask),
-                                                                   static_cast<float*>(p->tprime), p->K_out, p->n, NB);
-        mdft_simt_step2<<<dim3(NB, NB), 256, 0, st>>>(static_cast<const float*>(p->wy), static_cast<const float*>(p->tprime),
-                                                      p->weights, d_out_r, d_out_g, d_out_b, p->K_out, p->n, NB, p->n_lambda);
+        mdft_simt_step1<<<dim3(NI, NBx, p->n_lambda), 256, 0, st>>>(static_cast<const float*>(p->wx),
+                                                                    static_cast<const float*>(p->mask),
+                                                                    static_cast<float*>(p->tprime), p->Kx, p->n, NBx);
+        mdft_simt_step2<<<dim3(NBx, NBy), 256, 0, st>>>(static_cast<const float*>(p->wy), static_cast<const float*>(p->tprime),
+                                                       p->weights, d_out_r, d_out_g, d_out_b, p->Ky, p->Kx, p->n, NBx,
+                                                       p->n_lambda);
     }
     else if (p->form == 0)
     {
@@ -836,6 +952,28 @@ extern "C" int gl_mdft_plan_execute(gl_mdft_plan* plan, const float* d_pupil, fl
     GL_CUDA_TRY(cudaGetLastError());
     launches += 2;
     g_last_launches = launches;
+    return GL_OK;
+}
+
+extern "C" int gl_mdft_plan_execute(gl_mdft_plan* plan, const float* d_pupil, float* d_out_r, float* d_out_g,
+                                    float* d_out_b, void* stream)
+{
+    return gl_mdft_plan_execute2(plan, d_pupil, d_out_r, d_out_g, d_out_b, 0, stream);
+}
+
+extern "C" int gl_build_pupil(const gl_surface* surfaces, int n_surfaces, int N, float pupil_fill,
+                              int blades_override, float rotation_deg, float* d_out, void* stream)
+{
+    using namespace gl;
+    if (!surfaces || n_surfaces <= 0 || !d_out) return fail(GL_ERR_INVALID, "build_pupil: bad arguments");
+    if (N <= 0 || N > 8192) return fail(GL_ERR_INVALID, "build_pupil: N must be 1..8192");
+    if (!(pupil_fill > 0.0f) || pupil_fill > 1.0f) return fail(GL_ERR_INVALID, "build_pupil: pupil_fill must lie in (0, 1]");
+    const PupilMask m = resolve_pupil_mask(surfaces, n_surfaces, blades_override, rotation_deg);
+    PupilDev d{m.aspect, m.rot_rad, m.apothem, m.sector, m.n_blades};
+    const int total = N * N;
+    pupil_build_kernel<<<(total + 255) / 256, 256, 0, (cudaStream_t)stream>>>(d_out, N, pupil_fill, d);
+    GL_CUDA_TRY(cudaGetLastError());
+    g_last_launches = 1;
     return GL_OK;
 }
 

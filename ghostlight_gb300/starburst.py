@@ -27,11 +27,15 @@ def flops_per_lambda(n: int, K: int) -> float:
 
 
 class MdftPlan:
-    def __init__(self, n: int, K: int, scale_x, scale_y, weights_rgb, form="split_bf16",
+    """K: output side, or (Kx, Ky) for a Kx-wide, Ky-high output."""
+
+    def __init__(self, n: int, K, scale_x, scale_y, weights_rgb, form="split_bf16",
                  center_x=None, center_y=None, stream=None):
         import torch
         self._lib = _native.load()
-        self.n, self.K = int(n), int(K)
+        Kx, Ky = (int(K), int(K)) if np.isscalar(K) else (int(K[0]), int(K[1]))
+        self.n, self.Kx, self.Ky = int(n), Kx, Ky
+        self.K = Kx
         sx = np.ascontiguousarray(scale_x, np.float64)
         sy = np.ascontiguousarray(scale_y, np.float64)
         w = np.ascontiguousarray(weights_rgb, np.float32).reshape(-1, 3)
@@ -39,23 +43,34 @@ class MdftPlan:
             raise ValueError("mdft: scale_x, scale_y and weights need one entry per wavelength")
         self.n_lambda = len(sx)
         self.form = form
-        cx = self.K / 2.0 if center_x is None else float(center_x)
-        cy = self.K / 2.0 if center_y is None else float(center_y)
+        cx = self.Kx / 2.0 if center_x is None else float(center_x)
+        cy = self.Ky / 2.0 if center_y is None else float(center_y)
         st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
         D = C.c_double * self.n_lambda
         h = C.c_void_p()
-        _native.check(self._lib.gl_mdft_plan_create(
-            self.n, self.K, self.n_lambda, D(*sx), D(*sy), cx, cy,
+        _native.check(self._lib.gl_mdft_plan_create2(
+            self.n, self.Kx, self.Ky, self.n_lambda, D(*sx), D(*sy), cx, cy,
             (C.c_float * w.size)(*w.reshape(-1)), FORMS[form], st, C.byref(h)), "mdft")
         self._h = h
 
-    def execute(self, pupil, out_r, out_g, out_b, stream=None):
+    def set_center(self, center_x: float, center_y: float, stream=None):
+        """Enqueue the DFT-matrix rebuild for a new pattern centre."""
+        import torch
+        st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        _native.check(self._lib.gl_mdft_plan_set_center(self._h, float(center_x), float(center_y), st), "mdft")
+        return _native.last_launch_count()
+
+    def execute(self, pupil, out_r, out_g, out_b, stream=None, accumulate=False):
         import torch
         if not (pupil.is_cuda and pupil.dtype == torch.float32 and pupil.shape == (self.n, self.n)):
             raise ValueError("mdft: pupil must be a float32 CUDA (n, n) tensor")
+        for t in (out_r, out_g, out_b):
+            if not (t.is_cuda and t.dtype == torch.float32 and t.is_contiguous() and t.numel() == self.Kx * self.Ky):
+                raise ValueError("mdft: outputs must be contiguous float32 CUDA (Ky, Kx) tensors")
         st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
-        _native.check(self._lib.gl_mdft_plan_execute(self._h, pupil.contiguous().data_ptr(), out_r.data_ptr(),
-                                                     out_g.data_ptr(), out_b.data_ptr(), st), "mdft")
+        _native.check(self._lib.gl_mdft_plan_execute2(self._h, pupil.contiguous().data_ptr(), out_r.data_ptr(),
+                                                      out_g.data_ptr(), out_b.data_ptr(), int(bool(accumulate)), st),
+                      "mdft")
         return _native.last_launch_count()
 
     def status(self) -> int:
@@ -75,11 +90,25 @@ class MdftPlan:
             pass
 
 
+def build_pupil(lens, N: int, pupil_fill: float = 0.45, blades_override: int = 0, rotation_deg: float = 0.0,
+                stream=None):
+    """Stop-silhouette pupil amplitude (N, N) float32 CUDA tensor, 4 x 4
+    supersampled on the device (build_pupil_kernel, starburst_render.cu:155)."""
+    import torch
+    lib = _native.load()
+    arr = lens.to_array()
+    out = torch.empty((N, N), dtype=torch.float32, device="cuda")
+    st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+    _native.check(lib.gl_build_pupil(arr, len(arr), int(N), float(pupil_fill), int(blades_override),
+                                     float(rotation_deg), out.data_ptr(), st), "build_pupil")
+    return out
+
+
 def mdft_starburst_eform(pupil, K, scale_x, scale_y, weights_rgb, form="split_bf16"):
     """One-shot: returns (3, K, K) float32 CUDA tensor."""
     import torch
     plan = MdftPlan(pupil.shape[0], K, scale_x, scale_y, weights_rgb, form)
-    out = torch.empty((3, K, K), dtype=torch.float32, device=pupil.device)
+    out = torch.empty((3, plan.Ky, plan.Kx), dtype=torch.float32, device=pupil.device)
     plan.execute(pupil, out[0], out[1], out[2])
     torch.cuda.synchronize()
     code = plan.status()

@@ -294,6 +294,28 @@ int gl_mdft_plan_execute(gl_mdft_plan* plan, const float* d_pupil, float* d_out_
                          float* d_out_g, float* d_out_b, void* stream);
 int gl_mdft_plan_status(gl_mdft_plan* plan, int* err_code);
 int gl_mdft_plan_destroy(gl_mdft_plan* plan);
+/* Rectangular output (Kx columns x Ky rows, multiples of 128); the square
+ * create above is Kx = Ky = K_out. */
+int gl_mdft_plan_create2(int n, int Kx, int Ky, int n_lambda, const double* scale_x,
+                         const double* scale_y, double center_x, double center_y,
+                         const float* weights_rgb, int form, void* stream, gl_mdft_plan** out);
+/* Move the pattern's centre (output pixels, |c| < 4096): enqueues the
+ * rebuild of the plan's DFT matrices on `stream` (graph-capturable), as the
+ * reference rebuilds its phase matrices per source (mdft_render.cu:109-135). */
+int gl_mdft_plan_set_center(gl_mdft_plan* plan, double center_x, double center_y, void* stream);
+/* execute with accumulate != 0 adds into the output planes instead of
+ * overwriting them (a starburst layered onto a ghost image). */
+int gl_mdft_plan_execute2(gl_mdft_plan* plan, const float* d_pupil, float* d_out_r,
+                          float* d_out_g, float* d_out_b, int accumulate, void* stream);
+
+/* Pupil amplitude of the lens's stop on an N x N grid, 4 x 4 supersampled
+ * (build_pupil_kernel, starburst_render.cu:155-191, stop term only): grid
+ * coordinate g in [-1, 1) maps to pupil coordinate g / pupil_fill; a
+ * supersample counts when it lies inside the stop silhouette
+ * (PupilMask::contains, aperture_sampler.h:63-82).  float N x N on the
+ * device, asynchronous. */
+int gl_build_pupil(const gl_surface* surfaces, int n_surfaces, int N, float pupil_fill,
+                   int blades_override, float rotation_deg, float* d_out, void* stream);
 
 /* PSF / veil image convolution: out_c = in_c (*) k ('same' size, kernel
  * centred, odd kw x kh, float32).  The reference has no such operation on

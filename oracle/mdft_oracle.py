@@ -21,11 +21,12 @@ def dft_matrix(n: int, K: int, s: float, c: float, rows=None) -> np.ndarray:
 
 
 def eform(A, K, scale_x, scale_y, cx, cy, weights, rows=None, cols=None):
-    """(3, len(rows), len(cols)) float64."""
+    """(3, len(rows), len(cols)) float64; K = side or (Kx, Ky)."""
     A = np.asarray(A, np.float64)
     n = A.shape[0]
-    rows = np.arange(K) if rows is None else np.asarray(rows)
-    cols = np.arange(K) if cols is None else np.asarray(cols)
+    Kx, Ky = (K, K) if np.isscalar(K) else K
+    rows = np.arange(Ky) if rows is None else np.asarray(rows)
+    cols = np.arange(Kx) if cols is None else np.asarray(cols)
     out = np.zeros((3, len(rows), len(cols)))
     w = np.asarray(weights, np.float64).reshape(-1, 3)
     for l in range(len(scale_x)):
@@ -49,3 +50,28 @@ def test_pupil(n: int, seed: int = 3) -> np.ndarray:
     a = np.clip((edge - r) * 0.4 * n / 2.0 + 0.5, 0.0, 1.0)
     a *= (rng.random((n, n)) > 0.005)
     return a.astype(np.float32)
+
+
+def stop_pupil(aspect: float, n_blades: int, rot_rad: float, N: int, fill: float) -> np.ndarray:
+    """4 x 4 supersampled stop silhouette in float32 arithmetic, the stop term
+    of build_pupil_kernel (starburst_render.cu:155-191) with
+    PupilMask::contains (aperture_sampler.h:63-82)."""
+    f = np.float32
+    apothem = f(np.cos(f(np.pi) / f(n_blades))) if n_blades >= 3 else f(1)
+    sector = f(f(2) * f(np.pi) / f(n_blades)) if n_blades >= 3 else f(1)
+    j, i = np.mgrid[0:N, 0:N]
+    cnt = np.zeros((N, N), np.int32)
+    for sy in range(4):
+        for sx in range(4):
+            u = ((i.astype(f) + (f(sx) + f(0.5)) * f(0.25)) / f(N) * f(2) - f(1)) / f(fill)
+            v = ((j.astype(f) + (f(sy) + f(0.5)) * f(0.25)) / f(N) * f(2) - f(1)) / f(fill)
+            ux = (u / f(aspect)).astype(f)
+            r2 = (ux * ux + v * v).astype(f)
+            inside = r2 <= f(1)
+            if n_blades >= 3:
+                ang = (np.arctan2(v, ux).astype(f) - f(rot_rad)).astype(f)
+                sec = np.fmod(ang, sector).astype(f)
+                sec = np.where(sec < 0, sec + sector, sec).astype(f)
+                inside &= ~((np.sqrt(r2).astype(f) * np.cos(sec - sector * f(0.5)).astype(f)) > apothem)
+            cnt += inside
+    return (cnt.astype(f) * f(1.0 / 16.0))

@@ -70,3 +70,78 @@ def test_mdft_config1_size_split_bf16():
     sub = got[:, rows][:, :, cols]
     err = np.linalg.norm(sub - want) / np.linalg.norm(want)
     assert err < 1e-3, err
+
+
+def _inputs(n, n_lambda, seed=5):
+    from oracle import mdft_oracle as MO
+    lam = np.linspace(420.0, 680.0, n_lambda)
+    s0 = 1.0 / (2.0 * n)
+    sx = (s0 * 550.0 / lam).astype(np.float64)
+    sy = (s0 * 1.1 * 550.0 / lam).astype(np.float64)
+    w = np.random.default_rng(seed).uniform(0.2, 1.0, (n_lambda, 3)).astype(np.float32)
+    return MO.test_pupil(n, seed), sx, sy, w
+
+
+@pytest.mark.parametrize("form,tol", [("split_bf16", 1e-3), ("fp32", 1e-4)])
+def test_rectangular_recentred_and_accumulated(form, tol):
+    """Kx != Ky, a fractional off-frame centre set after creation, and the
+    accumulate mode, against the FP64 oracle."""
+    import ghostlight_gb300 as gl
+    from oracle import mdft_oracle as MO
+    n, Kx, Ky, L = 128, 384, 256, 3
+    A, sx, sy, w = _inputs(n, L)
+    plan = gl.MdftPlan(n, (Kx, Ky), sx, sy, w, form, center_x=10.0, center_y=20.0)
+    cx, cy = 421.3771, -17.618                      # beyond the frame edge, sub-pixel
+    assert plan.set_center(cx, cy) == 2
+    base = [torch.full((Ky, Kx), 0.25, device="cuda") for _ in range(3)]
+    dA = torch.from_numpy(A).cuda()
+    plan.execute(dA, *base, accumulate=True)
+    torch.cuda.synchronize()
+    assert plan.status() == 0
+    plan.close()
+    got = np.stack([b.cpu().numpy() for b in base]).astype(np.float64) - 0.25
+    want = MO.eform(A, (Kx, Ky), sx, sy, cx, cy, w)
+    err = np.linalg.norm(got - want) / np.linalg.norm(want)
+    assert got.shape == (3, Ky, Kx) and err < tol, err
+
+
+def test_set_center_matches_fresh_plan():
+    import ghostlight_gb300 as gl
+    n, K, L = 128, 256, 2
+    A, sx, sy, w = _inputs(n, L, seed=8)
+    dA = torch.from_numpy(A).cuda()
+    a = gl.MdftPlan(n, K, sx, sy, w, "split_bf16", center_x=77.5, center_y=140.25)
+    b = gl.MdftPlan(n, K, sx, sy, w, "split_bf16", center_x=3.0, center_y=3.0)
+    b.set_center(77.5, 140.25)
+    oa = [torch.empty((K, K), device="cuda") for _ in range(3)]
+    ob = [torch.empty((K, K), device="cuda") for _ in range(3)]
+    a.execute(dA, *oa)
+    b.execute(dA, *ob)
+    torch.cuda.synchronize()
+    for x, y in zip(oa, ob):
+        assert torch.allclose(x, y, rtol=1e-6, atol=1e-6 * float(x.abs().max()))
+    a.close(); b.close()
+
+
+@pytest.mark.parametrize("blades,rot,aspect", [(6, 0.3, 1.0), (9, 0.0, 1.0), (0, 0.0, 1.5), (5, 1.1, 0.8)])
+def test_stop_pupil_matches_oracle(blades, rot, aspect):
+    """Device pupil builder vs the float32 restatement: supersample decisions
+    may differ only where the float edge test is within rounding."""
+    from ghostlight_gb300.prescriptions import double_gauss_12
+    from ghostlight_gb300.optics import OpticalSystem
+    from ghostlight_gb300.starburst import build_pupil
+    from oracle import mdft_oracle as MO
+    surfs = double_gauss_12()
+    for s in surfs:
+        if s.is_stop:
+            s.aperture_aspect = aspect
+            s.aperture_shape = 1 if blades >= 3 else 0
+            s.aperture_blades = blades
+            s.aperture_rotation_rad = rot
+    lens = OpticalSystem.from_records(surfs)
+    N, fill = 256, 0.45
+    got = build_pupil(lens, N, fill).cpu().numpy()
+    want = MO.stop_pupil(aspect, blades, rot, N, fill)
+    diff = np.abs(got - want)
+    assert got.sum() > 0.2 * N * N * 0.45 ** 2
+    assert diff.max() <= 2.0 / 16.0 and (diff > 0).mean() < 2e-3
