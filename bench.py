@@ -265,7 +265,7 @@ def run_gpu(args, rank, world):
 
 # ---- starburst precision sweep + PSF/veil convolution (cfg3) -----------------
 SB_N, SB_K = 512, 2048          # pupil side -> output side
-SB_S0 = 1.0 / 1024.0            # DFT scale at 550 nm (output pixels per pupil cycle)
+SB_S0 = 400.0 / 550.0 / 2048.0  # DFT scale at 550 nm: the 400 nm pattern period spans the 2048 frame
 CONV_K = 257
 
 
@@ -526,6 +526,120 @@ def run_serving(args):
             "lens_setup_s": setup_s, "clocks": clk.summary()}
 
 
+# ---- anamorphic source sweep (120 frames, one graph) ---------------------------
+SWEEP_N, SWEEP_W, SWEEP_H, SWEEP_GRID, SWEEP_DEG = 120, 2048, 1024, 128, 20.0
+SWEEP_PUPIL, SWEEP_FILL = 256, 0.30
+
+
+def run_sweep(args):
+    """Seeded 18-surface 1.5x anamorphic (4 cylinders, per-element decenter
+    and tilt): 120 sources along the frame diagonal from on-axis to 20 deg,
+    31 wavelengths, 128^2 pupil grids, 2048x1024 frames (a 4:3 sensor inscribed
+    in the lens's image circle, shown desqueezed); each frame = ghost layer +
+    split-BF16 starburst at the source's paraxial image point; all 120 frames
+    one CUDA graph.  Against the plain form: per-pair ghost launches and the
+    same starburst, frame by frame, no graph."""
+    import torch
+    import ghostlight_gb300 as gl
+    from ghostlight_gb300._abi import gl_surface
+    from ghostlight_gb300.flare import GhostRenderPlan, pupil_grid
+    from ghostlight_gb300.optics import OpticalSystem
+    from ghostlight_gb300.serve import ResidentLens, _spectral
+    from ghostlight_gb300.starburst import build_pupil
+    from ghostlight_gb300.sweep import SourceSweep, diagonal_sources, paraxial_centers
+    pins = np.load(GOLDEN / "ref_pins.npz")
+    raw = pins["cfg4_anamorphic_18/lens"]
+    lens = OpticalSystem.from_records(list((gl_surface * raw.shape[0]).from_buffer_copy(raw.tobytes())),
+                                      name="cfg4_anamorphic_18")
+    cal = json.loads((GOLDEN / "ref_meta.json").read_text())["cfg4_anamorphic_18"]["calibration"]
+    a, b = cal["image_circle_semi_w"], cal["image_circle_semi_h"]
+    hh = 1.0 / math.sqrt((4.0 / 3.0 / a) ** 2 + (1.0 / b) ** 2)
+    hw = 4.0 / 3.0 * hh
+    fx, fy = cal["focal_length_x"], cal["focal_length_y"]
+    cfg = gl.FlareConfig(spectral_samples=N_SPEC, min_ghost_intensity=MIN_INTENSITY)
+    rl = ResidentLens(lens, hw, hh, cfg)
+    src = diagonal_sources(SWEEP_N, SWEEP_DEG, hw, hh, fx, fy)
+    W_, H_ = SWEEP_W, SWEEP_H
+    pupil = build_pupil(lens, SWEEP_PUPIL, SWEEP_FILL)
+    spec, _ = _spectral(N_SPEC, cfg)
+    lam = spec[:, 0].astype(np.float64)
+    # physically proportioned pattern (pupil sample pitch 2 EP / (fill n), pixel pitch, focal
+    # length per axis), trimmed so that the 400 nm period spans the frame width
+    dxp = 2 * cal["entrance_pupil_semi_x"] / (SWEEP_FILL * SWEEP_PUPIL)
+    dyp = 2 * cal["entrance_pupil_semi_y"] / (SWEEP_FILL * SWEEP_PUPIL)
+    sx_phys = dxp * (2 * hw / W_) / (lam * 1e-6 * fx)
+    sy_phys = dyp * (2 * hh / H_) / (lam * 1e-6 * fy)
+    trim = float(sx_phys[np.argmin(lam)] * W_)
+    sx, sy = sx_phys / trim, sy_phys / trim
+    amp = float(pupil.double().sum())
+    w = (spec[:, 1:4].astype(np.float64) / amp ** 2).astype(np.float32)
+    centers = paraxial_centers(src, fx, fy, hw, hh, W_, H_)
+    stream = torch.cuda.Stream()
+    plan = gl.MdftPlan(SWEEP_PUPIL, (W_, H_), sx, sy, w, "split_bf16", stream=stream.cuda_stream)
+    sb = dict(plan=plan, pupil=pupil, centers=centers)
+    sweep = SourceSweep(rl, src, W_, H_, N_SPEC, SWEEP_GRID, starburst=sb, stream=stream)
+    sweep.capture()
+    flush = torch.empty(128 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    steps = max(1, min(args.steps, 3))
+    with torch.cuda.stream(stream):
+        sweep.replay()
+        stream.synchronize()
+        ts = []
+        for _ in range(steps):
+            flush.add_(1.0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            sweep.replay()
+            e1.record(stream)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1) / 1e3)
+    if plan.status() != 0:
+        raise RuntimeError("sweep starburst: device wait timed out")
+    traced = sweep.traced()
+    t = sum(ts) / len(ts)
+    # e2e: replay + every frame to pinned host memory
+    host = torch.empty((SWEEP_N, 3, H_, W_), dtype=torch.float32).pin_memory()
+    with torch.cuda.stream(stream):
+        t0 = time.perf_counter()
+        sweep.replay()
+        for k in range(SWEEP_N):
+            sweep.copy_out(host[k], k)
+        stream.synchronize()
+        te = time.perf_counter() - t0
+    # plain form on a sample of frames
+    spec31, corr = _spectral(N_SPEC, cfg)
+    grid = pupil_grid(lens, SWEEP_GRID, 0, 0, 0, 0.0)
+    sample = [0, SWEEP_N // 3, 2 * SWEEP_N // 3, SWEEP_N - 1]
+    outs = [torch.zeros((H_, W_), device="cuda") for _ in range(3)]
+    tp = []
+    for k in sample:
+        s1 = np.array([[src[k, 0], src[k, 1], 1.0, 1.0, 1.0]], np.float32)
+        gp = GhostRenderPlan(lens, rl.pairs, rl.boosts, s1, [grid], np.zeros(len(rl.pairs), np.int32), spec31,
+                             corr, W_, H_, hw, hh, 1000.0, apply_correction=True, plain_per_pair=True)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        gp.execute(*outs)
+        plan.set_center(*centers[k])
+        plan.execute(pupil, *outs, accumulate=True)
+        e1.record()
+        e1.synchronize()
+        tp.append(e0.elapsed_time(e1) / 1e3)
+        gp.close()
+    plain_fps = len(tp) / sum(tp)
+    res = {"workload": "18-surface 1.5x anamorphic (4 cylinders, decentred/tilted elements), %d pairs, %d sources "
+                       "on the diagonal 0-%.0f deg, %d wavelengths, %d^2 pupil grids, %dx%d frames, starburst %d^2 "
+                       "pupil split-BF16 per frame; one CUDA graph" % (rl.n_pairs, SWEEP_N, SWEEP_DEG, N_SPEC,
+                                                                       SWEEP_GRID, W_, H_, SWEEP_PUPIL),
+           "frames_per_s": SWEEP_N / t, "ms_per_sweep": 1e3 * t, "graph_launches": sweep.launches,
+           "ray_lambda_traces_per_sweep": traced, "rays_per_s": traced / t,
+           "plain_frames_per_s": plain_fps, "plain_sample_frames": len(tp),
+           "speedup_batched_vs_plain": (SWEEP_N / t) / plain_fps,
+           "e2e_frames_per_s": SWEEP_N / te, "e2e_d2h_bytes": int(host.numel() * 4)}
+    sweep.close(); plan.close(); rl.close()
+    return res
+
+
 def cpu_baseline(plan, lens, cal, budget_s=8.0):
     """The oracle port of the reference renderer (FP32, OpenMP over every host
     core) on a bounded sample: a subset of the frame's pairs."""
@@ -629,7 +743,7 @@ def main():
     ap.add_argument("--serve-slots", type=int, default=32)
     ap.add_argument("--serial-sample", type=int, default=40)
     ap.add_argument("--serve-dump", default="", help="write per-request timings (CSV) here")
-    ap.add_argument("--only", default="all", choices=["all", "cfg3", "serve"],
+    ap.add_argument("--only", default="all", choices=["all", "cfg3", "serve", "sweep"],
                     help="with --quick: also run the starburst / convolution section (profiler runs)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
@@ -638,6 +752,12 @@ def main():
     if args.impl == "reference":
         if rank == 0:
             print(json.dumps(run_reference(args)))
+        return
+    if args.only == "sweep":
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+        if rank == 0:
+            print(json.dumps({"anamorphic_sweep": run_sweep(args)}))
         return
     if args.only == "serve":
         import torch
@@ -653,6 +773,8 @@ def main():
         lens, cal = _workload()
         if not (args.no_cpu_baseline or args.quick):
             res["cpu_baseline"] = cpu_baseline(plan, lens, cal)
+        if not args.quick:
+            res["anamorphic_sweep"] = run_sweep(args)
         if not args.quick and args.serve_seconds > 0:
             res["serving"] = run_serving(args)
         res["roofline"] = roofline(res, plan)

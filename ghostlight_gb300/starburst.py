@@ -73,6 +73,15 @@ class MdftPlan:
                       "mdft")
         return _native.last_launch_count()
 
+    def execute_raw(self, pupil_ptr: int, r_ptr: int, g_ptr: int, b_ptr: int, stream=None, accumulate=False):
+        """execute on raw device addresses (planes owned by another component,
+        e.g. a serving request); the caller guarantees the sizes."""
+        import torch
+        st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        _native.check(self._lib.gl_mdft_plan_execute2(self._h, int(pupil_ptr), int(r_ptr), int(g_ptr), int(b_ptr),
+                                                      int(bool(accumulate)), st), "mdft")
+        return _native.last_launch_count()
+
     def status(self) -> int:
         v = C.c_int()
         _native.check(self._lib.gl_mdft_plan_status(self._h, C.byref(v)), "mdft")
