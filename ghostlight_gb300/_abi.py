@@ -83,6 +83,24 @@ class gl_ghost_render_params(C.Structure):
                 ("blades_override", C.c_int32), ("rotation_deg", C.c_float)]
 
 
+CALIBRATION_FIELDS = ["sensor_half_w", "sensor_half_h", "max_half_angle_h", "max_half_angle_v",
+                      "image_circle_semi_w", "image_circle_semi_h", "focal_length_x", "focal_length_y",
+                      "entrance_pupil_semi_x", "entrance_pupil_semi_y", "f_number_x", "f_number_y",
+                      "pupil_area_frac"]
+
+
+class gl_lens_calibration(C.Structure):
+    _fields_ = [(n, C.c_float) for n in CALIBRATION_FIELDS] + [("field_crossed", C.c_int32)]
+
+
+class gl_source_solve(C.Structure):
+    _fields_ = [("angle_x", C.c_float), ("angle_y", C.c_float), ("status", C.c_int32),
+                ("residual_mm", C.c_float), ("anchor_ax", C.c_float), ("anchor_ay", C.c_float),
+                ("anchor_x", C.c_float), ("anchor_y", C.c_float), ("J", C.c_float * 4),
+                ("eff_half_w", C.c_float), ("eff_half_h", C.c_float), ("inv_tan_w", C.c_float),
+                ("inv_tan_h", C.c_float), ("probe_evals", C.c_int32)]
+
+
 SURFACE_DTYPE = np.dtype([(name, np.float32 if t in (C.c_float,) else np.int32)
                           if not hasattr(t, "_length_") else
                           (name, np.float32, (t._length_,))

@@ -11,7 +11,8 @@ import threading
 
 from . import _abi
 from ._abi import (gl_filter_params, gl_flare_source, gl_ghost_pair, gl_ghost_render_params,
-                   gl_pupil_sample, gl_sampler_params, gl_spectral_sample, gl_surface)
+                   gl_lens_calibration, gl_pupil_sample, gl_sampler_params, gl_source_solve,
+                   gl_spectral_sample, gl_surface)
 
 _lock = threading.Lock()
 _lib = None
@@ -77,6 +78,10 @@ def _declare(lib):
     lib.gl_request_destroy.argtypes = [vp, vp]
     lib.gl_pool_info.argtypes = [P(ll), P(ll)]
     lib.gl_pool_trim.argtypes = [ll]
+    lib.gl_calibrate_lens.argtypes = [P(gl_surface), i, f, f, P(gl_lens_calibration)]
+    lib.gl_solve_source_angle.argtypes = [P(gl_surface), i, P(gl_lens_calibration), f, f, f, f,
+                                          P(gl_source_solve)]
+    lib.gl_source_map_screen.argtypes = [P(gl_source_solve), f, f, P(f), P(f)]
     return lib
 
 

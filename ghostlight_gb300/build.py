@@ -32,6 +32,7 @@ EXACT = ["-fmad=false", "-ftz=false", "-prec-div=true", "-prec-sqrt=true"]
 
 UNITS = {
     "gl_host.cpp": [],
+    "gl_calib.cpp": [],
     "gl_filter.cu": EXACT,
     "gl_ghost.cu": FAST,
     "gl_mdft.cu": FAST,
@@ -40,8 +41,10 @@ UNITS = {
 }
 # Occupancy target of the render kernel (CTAs of 128 threads per SM); an
 # environment override lets a tuning sweep rebuild with another value.
-if os.environ.get("GL_RENDER_MIN_BLOCKS"):
-    UNITS["gl_ghost.cu"] = FAST + ["-DGL_RENDER_MIN_BLOCKS=%d" % int(os.environ["GL_RENDER_MIN_BLOCKS"])]
+# Render occupancy target (CTAs of 128 threads per SM) for tuning sweeps.
+for _var in ("GL_RENDER_MIN_BLOCKS",):
+    if os.environ.get(_var):
+        UNITS["gl_ghost.cu"] = UNITS["gl_ghost.cu"] + ["-D%s=%d" % (_var, int(os.environ[_var]))]
 
 
 def nvcc() -> str:

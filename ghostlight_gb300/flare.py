@@ -373,11 +373,15 @@ def render_source_flare(offsets, width: int, height: int, lens: OpticalSystem,
                          "[d_angle_x, d_angle_y, weight] rows with N >= 1")
     if not np.isfinite(off).all():
         raise ValueError("render_source_flare: source offsets must be finite")
+    if lens.num_surfaces() <= 0:
+        raise ValueError("render_source_flare: lens has no surfaces")
     hw, hh = _eff_half(config, calibration)
     if source_angle is None:
         from .calibration import solve_source_angle
-        ax0, ay0 = solve_source_angle(lens, calibration, (config.source_x - 0.5) * 2.0,
-                                      (config.source_y - 0.5) * 2.0, hw, hh)
+        f = np.float32
+        smap = solve_source_angle(lens, calibration, float((f(config.source_x) - f(0.5)) * f(2.0)),
+                                  float((f(config.source_y) - f(0.5)) * f(2.0)), hw, hh)
+        ax0, ay0 = smap.angle_x, smap.angle_y
     else:
         ax0, ay0 = source_angle
     r, g, b = source_rgb(config, config.source_r, config.source_g, config.source_b)

@@ -393,6 +393,47 @@ int gl_request_destroy(gl_request* req, void* stream);
 int gl_pool_info(long long* reserved, long long* used);
 int gl_pool_trim(long long keep_bytes);
 
+/* ---- First-order calibration and the source-position solve (host) ---------
+ * calibrate_lens (lens_calibration.cpp:344) — covered field, image circle,
+ * per-axis EFL, entrance pupil and f-number by tracing the spawn disc — and
+ * solve_source_angle / source_map_screen (source_map.cpp:182, :456), in the
+ * reference's float32 arithmetic so the values equal the reference's. */
+typedef struct gl_lens_calibration {
+    float sensor_half_w, sensor_half_h;        /* covered field landing (mm)    */
+    float max_half_angle_h, max_half_angle_v;  /* covered field (rad)           */
+    float image_circle_semi_w, image_circle_semi_h;
+    float focal_length_x, focal_length_y;
+    float entrance_pupil_semi_x, entrance_pupil_semi_y;
+    float f_number_x, f_number_y;
+    float pupil_area_frac;
+    int32_t field_crossed;                     /* 0: field probe hit the 60 deg ceiling */
+} gl_lens_calibration;
+
+#define GL_SOURCE_SOLVED    0
+#define GL_SOURCE_CONTINUED 1
+#define GL_SOURCE_FALLBACK  2
+
+typedef struct gl_source_solve {
+    float angle_x, angle_y;                    /* radians: the answer           */
+    int32_t status;                            /* GL_SOURCE_*                   */
+    float residual_mm;
+    float anchor_ax, anchor_ay, anchor_x, anchor_y;
+    float J[4];                                /* d(landing mm)/d(angle), row-major */
+    float eff_half_w, eff_half_h;
+    float inv_tan_w, inv_tan_h;
+    int32_t probe_evals;
+} gl_source_solve;
+
+int gl_calibrate_lens(const gl_surface* surfaces, int n_surfaces, float lens_focal_length,
+                      float d_line_nm, gl_lens_calibration* out);
+/* ndc in [-1, 1] (0 on the axis); eff_half_w/h: the rendered frame's half
+ * extents in mm.  A lens with no surfaces gives the FALLBACK solve. */
+int gl_solve_source_angle(const gl_surface* surfaces, int n_surfaces,
+                          const gl_lens_calibration* calib, float ndc_x, float ndc_y,
+                          float eff_half_w, float eff_half_h, gl_source_solve* out);
+int gl_source_map_screen(const gl_source_solve* base, float angle_x, float angle_y,
+                         float* out_sx, float* out_sy);
+
 /* Number of kernel launches issued by the last device call on this thread. */
 int gl_last_launch_count(void);
 

@@ -150,6 +150,28 @@ def test_render_matches_reference_gpu_golden(pins, meta, ref_images, golden):
     assert rel_l2(got, want) < IMG_TOL
 
 
+@pytest.mark.parametrize("golden", ["refgpu_pfs_dg_axial_c1", "refgpu_ab_hex_axial"])
+def test_drop_in_point_flare_calibrates_and_solves(pins, meta, ref_images, golden):
+    """The reference call shape with nothing precomputed: the lens calibrates
+    itself (calibrate_lens) and the source position is solved to a field
+    angle (solve_source_angle) before the render."""
+    import ghostlight_gb300 as gl
+    m = meta[golden]
+    lens = gl.OpticalSystem.from_records(lens_from_pins(pins, m["lens"]),
+                                         focal_length=meta[m["lens"]]["focal_length"])
+    cfg = gl.PointFlareConfig(ray_grid=m["ray_grid"], spectral_samples=m["spectral_samples"],
+                              pupil_jitter=m["pupil_jitter"], jitter_seed=m["jitter_seed"],
+                              flare_gain=m["flare_gain"], min_ghost_intensity=m["min_ghost_intensity"],
+                              source_r=m["source_rgb"], source_g=m["source_rgb"], source_b=m["source_rgb"],
+                              source_x=m["source_xy"][0], source_y=m["source_xy"][1],
+                              cull_dead_pairs=bool(m.get("cull", False)))
+    if m["sensor_half"] != "calib":
+        cfg.sensor_half_w = cfg.sensor_half_h = float(m["sensor_half"])
+    out = lens.render_point_flare(m["W"], m["H"], cfg)
+    got = np.stack([out[k].cpu().numpy() for k in ("ghost_r", "ghost_g", "ghost_b")], -1)
+    assert rel_l2(got, ref_images[golden + "/image"]) < IMG_TOL
+
+
 def test_graph_capture_replays_plan(pins, meta, ref_images):
     from ghostlight_gb300.flare import GhostRenderPlan
     lens = _lens(pins, "cfg1_double_gauss_12")
