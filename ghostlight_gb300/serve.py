@@ -432,15 +432,15 @@ def poisson_requests(rate_hz: float, duration_s: float, lens_ids, seed: int = 5,
 
 def serving_lens(seed: int, n_surfaces: int, field_deg: float = 20.0):
     """(OpticalSystem, sensor_half_w, sensor_half_h) of one seeded serving
-    lens: the random prescription with n_surfaces entries, and a square
-    sensor whose half diagonal images the lens's full field (half side =
-    EFL tan(field) / sqrt 2, paraxial, FP64)."""
+    lens: the random prescription with n_surfaces entries, and the sensor of
+    its calibration (calibrate_lens: the covered field's landing per axis)."""
+    from .calibration import calibrate_lens
     from .optics import OpticalSystem
-    from .prescriptions import paraxial_efl_bfd, random_lens
+    from .prescriptions import random_lens
     surfs = random_lens(seed, n_surfaces, field_deg=field_deg)
-    efl, _ = paraxial_efl_bfd(surfs)
-    half = abs(efl) * math.tan(math.radians(field_deg)) / math.sqrt(2.0)
-    return OpticalSystem.from_records(surfs, name="serve_%d_%d" % (seed, n_surfaces)), half, half
+    lens = OpticalSystem.from_records(surfs, name="serve_%d_%d" % (seed, n_surfaces))
+    cal = calibrate_lens(lens)
+    return lens, cal.sensor_half_w, cal.sensor_half_h
 
 
 def serving_lens_pool(n_lenses: int, config, seed: int = 100, n_min: int = 8, n_max: int = 30):
