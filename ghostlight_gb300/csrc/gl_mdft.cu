@@ -293,15 +293,19 @@ __global__ void __launch_bounds__(kMdftThreads, 1) mdft_kernel(const __grid_cons
     tc::tc_fence_after();
     const uint32_t tmem = tmem_base;
 
+    // Units are dealt round-robin (unit u to CTA u mod G), so the units in
+    // flight at any moment are consecutive: with wavelength-major unit order
+    // they share one wavelength's operands, which then stay in L2.
     const int G = gridDim.x;
-    const int u0 = (int)(((long long)blockIdx.x * args.n_units) / G);
-    const int u1 = (int)(((long long)(blockIdx.x + 1) * args.n_units) / G);
+    const int u0 = blockIdx.x, u1 = args.n_units;
 
     auto decode = [&](int u, int& lam, int& mb, int& xb) {
         if (STEP == 2)
         {
-            const int tile = u / args.n_lambda;
-            lam = u % args.n_lambda;
+            // wavelength-major: all output tiles of one wavelength, then the next
+            const int tiles = args.NBm * args.NB;
+            lam = u / tiles;
+            const int tile = u - lam * tiles;
             mb = tile / args.NB;
             xb = tile % args.NB;
         }
@@ -320,7 +324,7 @@ __global__ void __launch_bounds__(kMdftThreads, 1) mdft_kernel(const __grid_cons
         {
             int it = 0, issued = 0;
             bool stop = false;
-            for (int u = u0; u < u1 && !stop; ++u)
+            for (int u = u0; u < u1 && !stop; u += G)
             {
                 int lam, mb, xb;
                 decode(u, lam, mb, xb);
@@ -360,7 +364,7 @@ __global__ void __launch_bounds__(kMdftThreads, 1) mdft_kernel(const __grid_cons
             const uint32_t id128 = idesc_any<FORM>(128, 128);
             int it = 0, ui = 0;
             bool stop = false;
-            for (int u = u0; u < u1 && !stop; ++u, ++ui)
+            for (int u = u0; u < u1 && !stop; u += G, ++ui)
             {
                 const int b = ui & 1, ur = ui >> 1;
                 if (ui >= 2 && !tc::mbar_wait(&acc_empty[b], (ur - 1) & 1, err, tc::TC_TIMEOUT_ACC_FREE)) break;
@@ -410,7 +414,7 @@ __global__ void __launch_bounds__(kMdftThreads, 1) mdft_kernel(const __grid_cons
         // Epilogue warps 0-3: TMEM lane = tile row.
         int ui = 0;
         const int row = warp * 32 + lane;
-        for (int u = u0; u < u1; ++u, ++ui)
+        for (int u = u0; u < u1; u += G, ++ui)
         {
             int lam, mb, xb;
             decode(u, lam, mb, xb);
@@ -928,7 +932,7 @@ extern "C" int gl_mdft_plan_execute2(gl_mdft_plan* plan, const float* d_pupil, f
     const int g1 = std::min(a.n_units, p->sms);
     MdftArgs a2 = a;
     a2.KA = p->Ky; a2.NBm = NBy;
-    a2.n_units = NBy * NBx * p->n_lambda;               // step 2: (output tile, lambda)
+    a2.n_units = NBy * NBx * p->n_lambda;               // step 2: (lambda, output tile)
     const int g2 = std::min(a2.n_units, p->sms);
     if (p->form == 2)
     {
