@@ -155,7 +155,12 @@ def run_gpu(args, rank, world):
     flush = torch.empty(128 * 1024 * 1024, dtype=torch.float32, device=dev)
     stream = torch.cuda.Stream(device=dev)
 
-    # ---- batched form: graph-captured persistent launch ----
+    # ---- launch shape picked by the autotuner on this workload ----
+    from ghostlight_gb300.autotune import Tuner, tune_ghost_plan
+    tuner = Tuner(reps=3)
+    tune_ghost_plan(plan, outs, stream=stream, tuner=tuner)
+
+    # ---- batched form: graph-captured launch ----
     with torch.cuda.stream(stream):
         for _ in range(2):
             plan.execute(*outs, stream=stream.cuda_stream)
@@ -255,6 +260,7 @@ def run_gpu(args, rank, world):
                 "uploads) + execute + pinned D2H of the 3 planes"},
         "gpu_launches": int(launches_per_step) * args.steps,
         "clocks": clk.summary(),
+        "autotune": tuner.log,
     }
     if cfg3 is not None:
         res["starburst_psf"] = cfg3
@@ -352,8 +358,12 @@ def run_cfg3(args, dev, stream, flush, timed):
     forms = {}
     peak_tc = {"split_bf16": peaks["bf16_tflops"] / 3.0, "tf32": peaks["bf16_tflops"] / 2.0,
                "fp32": FP32_PEAK_TFLOPS}
+    from ghostlight_gb300.autotune import Tuner, tune_mdft_plan
+    tuner = Tuner(reps=3)
     for form in ("split_bf16", "tf32", "fp32"):
         plan = gl.MdftPlan(SB_N, SB_K, sx, sy, w, form, cx, cy, stream=stream.cuda_stream)
+        if form != "fp32":
+            tune_mdft_plan(plan, A, sb, stream=stream, tuner=tuner)
         steps = args.steps if form != "fp32" else max(2, min(args.steps, 5))
         ts = timed(lambda: plan.execute(A, *sb, stream=stream.cuda_stream), steps, args.warmup)
         stream.synchronize()
@@ -361,7 +371,8 @@ def run_cfg3(args, dev, stream, flush, timed):
             raise RuntimeError("mdft %s: device wait timed out" % form)
         sec = sum(ts) / len(ts)
         ach = flops / sec / 1e12
-        forms[form] = dict(ms=1e3 * sec, tflops_algorithmic=ach, **_errs(sb, ref),
+        forms[form] = dict(ms=1e3 * sec, tflops_algorithmic=ach, launch=getattr(plan, "launch", None),
+                           **_errs(sb, ref),
                            roofline={"bound": "tensor" if form != "fp32" else "fp32", "achieved": ach,
                                      "peak": peak_tc[form], "unit": "TFLOP/s", "frac": ach / peak_tc[form],
                                      "peak_note": {"split_bf16": "measured cuBLAS bf16 burst / 3 (three "
@@ -388,7 +399,7 @@ def run_cfg3(args, dev, stream, flush, timed):
                 "direct_equivalent_tflops": 2.0 * W * H * CONV_K * CONV_K * 3 / csec / 1e12,
                 "roofline": {"bound": "hbm", "achieved": gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                              "frac": gbs / peaks["hbm_gbs"], "algorithmic_bytes": cbytes}}
-    return {"workload": "512^2 9-blade curved-blade pupil (2 px AA, 0.5%% dust r 1-4 px) -> %d^2, %d wavelengths; "
+    return {"autotune": tuner.log, "workload": "512^2 9-blade curved-blade pupil (2 px AA, 0.5%% dust r 1-4 px) -> %d^2, %d wavelengths; "
                         "conv %dx%d x3 (*) %d^2 FP32" % (SB_K, N_SPEC, W, H, CONV_K),
             "gflop_algorithmic": flops / 1e9, "mdft": forms, "conv": conv_res}, (A, sx, sy, w, conv, kern)
 

@@ -48,6 +48,7 @@ def _declare(lib):
     lib.gl_ghost_plan_destroy.argtypes = [vp]
     lib.gl_ghost_plan_pair_hits.argtypes = [vp, P(C.c_int32), i]
     lib.gl_ghost_plan_traced.argtypes = [vp, P(C.c_longlong)]
+    lib.gl_ghost_plan_set_launch.argtypes = [vp, i, i]
     lib.gl_gemm_bf16_tc.argtypes = [vp, vp, vp, i, i, i, vp]
     d = C.c_double
     lib.gl_mdft_plan_create.argtypes = [i, i, i, P(d), P(d), d, d, P(f), i, vp, P(vp)]
@@ -56,6 +57,7 @@ def _declare(lib):
     lib.gl_mdft_plan_destroy.argtypes = [vp]
     lib.gl_mdft_plan_create2.argtypes = [i, i, i, i, P(d), P(d), d, d, P(f), i, vp, P(vp)]
     lib.gl_mdft_plan_set_center.argtypes = [vp, d, d, vp]
+    lib.gl_mdft_plan_set_launch.argtypes = [vp, i]
     lib.gl_mdft_plan_execute2.argtypes = [vp, vp, vp, vp, vp, i, vp]
     lib.gl_build_pupil.argtypes = [P(gl_surface), i, i, f, i, f, vp, vp]
     lib.gl_conv2d_plan_create.argtypes = [i, i, P(f), i, i, vp, P(vp)]

@@ -493,6 +493,8 @@ struct GhostPlan {
     float4* accum = nullptr;            // RGBA scratch, width x height
     size_t smem = 0;
     int grid_persistent = 0;
+    int per_sm = 0, n_sm = 0;           // resident render CTAs per SM, SM count
+    int launch_ipw = 0;                 // 0: persistent queue; > 0: static chunks of this many items per warp
     long long rays = 0;                 // ray-wavelength traces per execute
     float front_R = 0.0f, start_z = 0.0f;
     // off-sensor cull (probe passes)
@@ -777,9 +779,24 @@ int plan_create(const gl_surface* surfaces, int n_surf, const gl_ghost_pair* pai
                     std::string("render_ghosts: ") + cudaGetErrorString(e));
     }
     const int warps_per_block = kRenderThreads / 32;
+    p->per_sm = std::max(1, per_sm);
+    p->n_sm = n_sm;
     p->grid_persistent = std::max(1, std::min((p->n_items + warps_per_block - 1) / warps_per_block,
-                                              std::max(1, per_sm) * n_sm));
+                                              p->per_sm * n_sm));
     *out = p;
+    return GL_OK;
+}
+
+// Launch shape of the batched render (the autotuner's knob): items_per_warp
+// 0 = persistent work queue over ctas_per_sm CTAs per SM (0 = every resident
+// slot); > 0 = one-shot CTAs of that many 32-sample items per warp.
+int plan_set_launch(GhostPlan* p, int items_per_warp, int ctas_per_sm)
+{
+    if (items_per_warp < 0 || ctas_per_sm < 0) return fail(GL_ERR_INVALID, "ghost_plan_set_launch: negative value");
+    const int cps = ctas_per_sm == 0 ? p->per_sm : std::min(ctas_per_sm, p->per_sm);
+    const int warps_per_block = kRenderThreads / 32;
+    p->launch_ipw = items_per_warp;
+    p->grid_persistent = std::max(1, std::min((p->n_items + warps_per_block - 1) / warps_per_block, cps * p->n_sm));
     return GL_OK;
 }
 
@@ -847,6 +864,14 @@ int plan_execute(GhostPlan* p, float* d_out_r, float* d_out_g, float* d_out_b, c
                 ++launches;
             }
             GL_CUDA_TRY(cudaGetLastError());
+        }
+        else if (p->launch_ipw > 0)
+        {
+            const int per_cta = (kRenderThreads / 32) * p->launch_ipw;
+            const int grid = std::max(1, (p->n_items + per_cta - 1) / per_cta);
+            ghost_render_kernel<false><<<grid, kRenderThreads, p->smem, st>>>(A);
+            GL_CUDA_TRY(cudaGetLastError());
+            ++launches;
         }
         else
         {
@@ -963,6 +988,12 @@ int gl_ghost_plan_execute(gl_ghost_plan* plan, float* d_out_r, float* d_out_g, f
 {
     if (!plan) return fail(GL_ERR_INVALID, "ghost_plan_execute: null plan");
     return plan_execute(plan->p, d_out_r, d_out_g, d_out_b, (cudaStream_t)stream);
+}
+
+int gl_ghost_plan_set_launch(gl_ghost_plan* plan, int items_per_warp, int ctas_per_sm)
+{
+    if (!plan) return fail(GL_ERR_INVALID, "ghost_plan_set_launch: null plan");
+    return plan_set_launch(plan->p, items_per_warp, ctas_per_sm);
 }
 
 int gl_ghost_plan_info(const gl_ghost_plan* plan, long long* rays, int* n_items, int* grid)

@@ -747,6 +747,7 @@ struct MdftPlan {
     float4* weights = nullptr;
     float2* scales = nullptr;   // [2][n_lambda] (s_hi, s_lo) device copy
     double cx = 0.0, cy = 0.0;
+    int ctas = 0;               // GEMM grid (0 = one CTA per SM)
     int* err = nullptr;
     CUtensorMap t_wx, t_wy, t_mask, t_tp;
     int sms = 0;
@@ -929,11 +930,12 @@ extern "C" int gl_mdft_plan_execute2(gl_mdft_plan* plan, const float* d_pupil, f
     a.weights = p->weights; a.err = p->err;
     const size_t smem1 = 4 * 3 * (size_t)kOpTile + 1024, smem2 = 2 * 5 * (size_t)kOpTile + 1024;
     a.n_units = p->n_lambda * NBx * NI;                 // step 1: (lambda, k block, pupil-row block)
-    const int g1 = std::min(a.n_units, p->sms);
+    const int gmax = p->ctas > 0 ? p->ctas : p->sms;
+    const int g1 = std::min(a.n_units, gmax);
     MdftArgs a2 = a;
     a2.KA = p->Ky; a2.NBm = NBy;
     a2.n_units = NBy * NBx * p->n_lambda;               // step 2: (lambda, output tile)
-    const int g2 = std::min(a2.n_units, p->sms);
+    const int g2 = std::min(a2.n_units, gmax);
     if (p->form == 2)
     {
         mdft_simt_step1<<<dim3(NI, NBx, p->n_lambda), 256, 0, st>>>(static_cast<const float*>(p->wx),
@@ -956,6 +958,15 @@ extern "C" int gl_mdft_plan_execute2(gl_mdft_plan* plan, const float* d_pupil, f
     GL_CUDA_TRY(cudaGetLastError());
     launches += 2;
     g_last_launches = launches;
+    return GL_OK;
+}
+
+extern "C" int gl_mdft_plan_set_launch(gl_mdft_plan* plan, int ctas)
+{
+    using namespace gl;
+    if (!plan || ctas < 0) return fail(GL_ERR_INVALID, "mdft_plan_set_launch: bad arguments");
+    // one 192-thread CTA with ~161 KB of shared memory fits per SM
+    plan->p->ctas = ctas == 0 ? 0 : std::min(ctas, plan->p->sms);
     return GL_OK;
 }
 

@@ -265,6 +265,14 @@ class GhostRenderPlan:
                                                       out_b.data_ptr(), st), "render_ghosts")
         return _native.last_launch_count()
 
+    def set_launch(self, items_per_warp: int = 0, ctas_per_sm: int = 0):
+        """Launch shape of the batched render: 0 = persistent work queue over
+        ctas_per_sm CTAs per SM (0 = all resident), > 0 = one-shot CTAs of that
+        many 32-sample items per warp."""
+        _native.check(self._lib.gl_ghost_plan_set_launch(self._h, int(items_per_warp), int(ctas_per_sm)),
+                      "set_launch")
+        self.launch = (int(items_per_warp), int(ctas_per_sm))
+
     def traced(self) -> int:
         """Ray-wavelength traces the last execute ran (render + probes)."""
         v = C.c_longlong()

@@ -73,6 +73,11 @@ class MdftPlan:
                       "mdft")
         return _native.last_launch_count()
 
+    def set_launch(self, ctas: int = 0):
+        """GEMM grid of the tensor-core forms (0 = one CTA per SM)."""
+        _native.check(self._lib.gl_mdft_plan_set_launch(self._h, int(ctas)), "mdft")
+        self.launch = int(ctas)
+
     def execute_raw(self, pupil_ptr: int, r_ptr: int, g_ptr: int, b_ptr: int, stream=None, accumulate=False):
         """execute on raw device addresses (planes owned by another component,
         e.g. a serving request); the caller guarantees the sizes."""

@@ -257,6 +257,11 @@ int gl_ghost_plan_execute(gl_ghost_plan* plan, float* d_out_r, float* d_out_g,
  * n_items = 32-sample work items;
  * grid = CTAs of the persistent launch. */
 int gl_ghost_plan_info(const gl_ghost_plan* plan, long long* rays, int* n_items, int* grid);
+/* Launch shape of the batched render (the autotuner's knob; no counterpart in
+ * the reference, whose launch shape is fixed at ghost_render.cu:1544):
+ * items_per_warp = 0 -> persistent work queue over ctas_per_sm CTAs per SM
+ * (0 = all resident); > 0 -> one-shot CTAs of that many 32-sample items per warp. */
+int gl_ghost_plan_set_launch(gl_ghost_plan* plan, int items_per_warp, int ctas_per_sm);
 /* Ray-wavelength traces the last execute ran (render + cull probes; a probe
  * warp stops at its first on-sensor hit).  Synchronous. */
 int gl_ghost_plan_traced(const gl_ghost_plan* plan, long long* out);
@@ -303,6 +308,8 @@ int gl_mdft_plan_create2(int n, int Kx, int Ky, int n_lambda, const double* scal
  * rebuild of the plan's DFT matrices on `stream` (graph-capturable), as the
  * reference rebuilds its phase matrices per source (mdft_render.cu:109-135). */
 int gl_mdft_plan_set_center(gl_mdft_plan* plan, double center_x, double center_y, void* stream);
+/* GEMM grid of the tcgen05 forms (0 = one CTA per SM); autotuner knob. */
+int gl_mdft_plan_set_launch(gl_mdft_plan* plan, int ctas);
 /* execute with accumulate != 0 adds into the output planes instead of
  * overwriting them (a starburst layered onto a ghost image). */
 int gl_mdft_plan_execute2(gl_mdft_plan* plan, const float* d_pupil, float* d_out_r,

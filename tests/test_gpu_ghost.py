@@ -264,3 +264,29 @@ def test_off_sensor_cull_keeps_the_image(pins, meta):
         plan.close()
     assert imgs[False].sum() > 0
     assert rel_l2(imgs[True], imgs[False]) < 1e-4
+
+
+def test_autotuned_launch_shapes_give_the_same_image(pins, meta, ref_images, tmp_path):
+    from ghostlight_gb300.autotune import Tuner, tune_ghost_plan
+    from ghostlight_gb300.flare import GhostRenderPlan
+    lens = _lens(pins, "cfg1_double_gauss_12")
+    cal = meta["cfg1_double_gauss_12"]["calibration"]
+    pairs, boosts = ref_images["cfg1_small/pairs"], ref_images["cfg1_small/boosts"]
+    spec, corr = ref_images["cfg1_small/spec"], ref_images["cfg1_small/corr"]
+    grid = O.aperture_samples(lens.records(), 96, 0)
+    plan = GhostRenderPlan(lens, pairs, boosts, ref_images["cfg1_small/source"], [grid], None, spec, corr,
+                           256, 256, cal["sensor_half_w"], cal["sensor_half_h"], 1000.0)
+    ref = [torch.zeros((256, 256), device="cuda") for _ in range(3)]
+    plan.execute(*ref)
+    torch.cuda.synchronize()
+    want = torch.stack(ref).cpu().numpy()
+    for shape in ((0, 4), (1, 0), (8, 0)):
+        plan.set_launch(*shape)
+        outs = [torch.zeros((256, 256), device="cuda") for _ in range(3)]
+        plan.execute(*outs)
+        torch.cuda.synchronize()
+        assert rel_l2(torch.stack(outs).cpu().numpy(), want) < 1e-6
+    t = Tuner(cache_path=str(tmp_path / "t.json"), reps=2)
+    choice = tune_ghost_plan(plan, ref, tuner=t)
+    assert tuple(choice) in [tuple(c) for c in __import__("ghostlight_gb300.autotune").autotune.GHOST_CANDIDATES]
+    plan.close()
