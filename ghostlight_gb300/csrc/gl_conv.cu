@@ -8,15 +8,18 @@
 // GB300 route: the transform is memory-bound, so it is laid out for HBM.
 //   * linear convolution by zero-padded circular convolution of size P x Q,
 //     P, Q = the smallest 2^a 3^b >= image + kernel - 1 (2048 + 257 - 1 = 2304
-//     = 4^4 * 3^2: no power-of-two padding waste);
+//     = 16 * 16 * 9: no power-of-two padding waste);
 //   * two real channels per complex transform (the kernel is real, so the
 //     real and imaginary parts of the result are the two channels);
-//   * mixed-radix (4, 3, 2) Stockham FFTs in shared memory, twiddles from
-//     sincospif;
-//   * three HBM passes: (1) forward row FFTs of the H image rows; (2) per
-//     group of four columns: forward column FFT, multiply by the kernel
-//     spectrum, inverse column FFT, all in one shared-memory residency;
-//     (3) inverse row FFTs writing the cropped W x H planes.
+//   * Stockham FFTs in shared memory with large radices held in registers
+//     (16, 8, 4, 2 and 9, 3: three passes over shared memory for 2304
+//     points), twiddles from a per-plan table computed in FP64; the shared
+//     arrays carry one pad word per 16 so the strided radix writes do not
+//     collide in banks;
+//   * three HBM passes: (1) forward row FFTs, two rows per CTA; (2) per group
+//     of four columns: forward column FFT, multiply by the kernel spectrum,
+//     inverse column FFT, all in one shared-memory residency; (3) inverse row
+//     FFTs writing the cropped W x H planes.
 // The kernel spectrum (normalisation 1/(PQ) folded in) is built once per plan
 // and stays resident.
 #include "gl_internal.h"
@@ -47,77 +50,169 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 b)
 {
     return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+// (sign i) * a
+__device__ __forceinline__ float2 cis(float2 a, float sign) { return make_float2(-sign * a.y, sign * a.x); }
 
-// One Stockham stage over NB interleaved sequences (element i of sequence s
-// at x[i * NB + s]).  tw[t] = exp(-2 pi i t / n); the inverse uses conj.
-template <int NB>
-__device__ __forceinline__ void stockham_stage(const float2* __restrict__ x, float2* __restrict__ y, int n, int r,
-                                               int Ls, uint32_t lmag, int twstep, const float2* __restrict__ tw,
-                                               bool inv)
+// Padded shared-memory index: one spare word per 16 elements, so a warp
+// writing 16-element runs at a stride of 16 hits 16 different banks.
+__device__ __forceinline__ int pad(int i) { return i + (i >> 4); }
+__host__ __device__ inline size_t padded(size_t n) { return n + (n >> 4) + 1; }
+
+// ---- small DFTs in registers: X[p] = sum_q v[q] w^(pq), w = exp(sign 2 pi i / R) ----
+__device__ __forceinline__ void dft2(float2& a, float2& b)
 {
-    const int m = n / r;
+    const float2 t = a;
+    a = cadd(t, b);
+    b = csub(t, b);
+}
+
+__device__ __forceinline__ void dft4(float2& v0, float2& v1, float2& v2, float2& v3, float sign)
+{
+    const float2 t0 = cadd(v0, v2), t1 = csub(v0, v2), t2 = cadd(v1, v3), t3 = cis(csub(v1, v3), sign);
+    v0 = cadd(t0, t2);
+    v2 = csub(t0, t2);
+    v1 = cadd(t1, t3);
+    v3 = csub(t1, t3);
+}
+
+__device__ __forceinline__ void dft3(float2& v0, float2& v1, float2& v2, float sign)
+{
+    const float c = 0.86602540378443864676f;   // sqrt(3)/2
+    const float2 t1 = cadd(v1, v2);
+    const float2 t2 = csub(v1, v2);
+    const float2 base = make_float2(v0.x - 0.5f * t1.x, v0.y - 0.5f * t1.y);
+    const float2 rot = cis(make_float2(c * t2.x, c * t2.y), sign);
+    v0 = cadd(v0, t1);
+    v1 = cadd(base, rot);
+    v2 = csub(base, rot);
+}
+
+// w_N^k = (cos 2 pi k / N, sign sin 2 pi k / N) for the in-register twiddles
+__device__ __forceinline__ float2 wk(float c, float s, float sign) { return make_float2(c, sign * s); }
+
+template <int R>
+__device__ __forceinline__ void dft(float2 (&v)[R], float sign);
+
+template <>
+__device__ __forceinline__ void dft<2>(float2 (&v)[2], float) { dft2(v[0], v[1]); }
+
+template <>
+__device__ __forceinline__ void dft<3>(float2 (&v)[3], float sign) { dft3(v[0], v[1], v[2], sign); }
+
+template <>
+__device__ __forceinline__ void dft<4>(float2 (&v)[4], float sign) { dft4(v[0], v[1], v[2], v[3], sign); }
+
+// 8 = 2 x 4: q = q1 + 2 q2; inner DFT4 over q2, twiddle w8^(q1 p1), outer DFT2.
+template <>
+__device__ __forceinline__ void dft<8>(float2 (&v)[8], float sign)
+{
+    const float h = 0.70710678118654752440f;
+    dft4(v[0], v[2], v[4], v[6], sign);   // q1 = 0 -> A0[p1] at v[0], v[2], v[4], v[6]
+    dft4(v[1], v[3], v[5], v[7], sign);   // q1 = 1 -> A1[p1]
+    v[3] = cmul(v[3], wk(h, h, sign));
+    v[5] = cis(v[5], sign);
+    v[7] = cmul(v[7], wk(-h, h, sign));
+    float2 x[8];
+    #pragma unroll
+    for (int p1 = 0; p1 < 4; ++p1)
+    {
+        x[p1] = cadd(v[2 * p1], v[2 * p1 + 1]);
+        x[p1 + 4] = csub(v[2 * p1], v[2 * p1 + 1]);
+    }
+    #pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = x[i];
+}
+
+// 16 = 4 x 4: q = q1 + 4 q2; inner DFT4 over q2, twiddle w16^(q1 p1), outer DFT4 over q1.
+template <>
+__device__ __forceinline__ void dft<16>(float2 (&v)[16], float sign)
+{
+    const float c1 = 0.92387953251128675613f, s1 = 0.38268343236508977173f, h = 0.70710678118654752440f;
+    #pragma unroll
+    for (int q1 = 0; q1 < 4; ++q1) dft4(v[q1], v[q1 + 4], v[q1 + 8], v[q1 + 12], sign);
+    // v[q1 + 4 p1] = A[q1][p1]; multiply by w16^(q1 p1)
+    v[5] = cmul(v[5], wk(c1, s1, sign));     // q1 1, p1 1: k 1
+    v[9] = cmul(v[9], wk(h, h, sign));       // 1,2: k 2
+    v[13] = cmul(v[13], wk(s1, c1, sign));   // 1,3: k 3
+    v[6] = cmul(v[6], wk(h, h, sign));       // 2,1: k 2
+    v[10] = cis(v[10], sign);                // 2,2: k 4
+    v[14] = cmul(v[14], wk(-h, h, sign));    // 2,3: k 6
+    v[7] = cmul(v[7], wk(s1, c1, sign));     // 3,1: k 3
+    v[11] = cmul(v[11], wk(-h, h, sign));    // 3,2: k 6
+    v[15] = cmul(v[15], wk(-c1, -s1, sign)); // 3,3: k 9
+    #pragma unroll
+    for (int p1 = 0; p1 < 4; ++p1) dft4(v[4 * p1], v[4 * p1 + 1], v[4 * p1 + 2], v[4 * p1 + 3], sign);
+    // now v[4 p1 + p2] = X[p1 + 4 p2]: transpose the 4 x 4 index
+    float2 x[16];
+    #pragma unroll
+    for (int p1 = 0; p1 < 4; ++p1)
+        #pragma unroll
+        for (int p2 = 0; p2 < 4; ++p2) x[p1 + 4 * p2] = v[4 * p1 + p2];
+    #pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = x[i];
+}
+
+// 9 = 3 x 3: q = q1 + 3 q2; inner DFT3 over q2, twiddle w9^(q1 p1), outer DFT3 over q1.
+template <>
+__device__ __forceinline__ void dft<9>(float2 (&v)[9], float sign)
+{
+    const float c1 = 0.76604444311897803520f, s1 = 0.64278760968653932632f;   // 2 pi / 9
+    const float c2 = 0.17364817766693034885f, s2 = 0.98480775301220805936f;   // 4 pi / 9
+    const float c4 = -0.93969262078590838405f, s4 = 0.34202014332566873304f; // 8 pi / 9
+    #pragma unroll
+    for (int q1 = 0; q1 < 3; ++q1) dft3(v[q1], v[q1 + 3], v[q1 + 6], sign);
+    v[4] = cmul(v[4], wk(c1, s1, sign));   // q1 1, p1 1: k 1
+    v[7] = cmul(v[7], wk(c2, s2, sign));   // 1,2: k 2
+    v[5] = cmul(v[5], wk(c2, s2, sign));   // 2,1: k 2
+    v[8] = cmul(v[8], wk(c4, s4, sign));   // 2,2: k 4
+    #pragma unroll
+    for (int p1 = 0; p1 < 3; ++p1) dft3(v[3 * p1], v[3 * p1 + 1], v[3 * p1 + 2], sign);
+    float2 x[9];
+    #pragma unroll
+    for (int p1 = 0; p1 < 3; ++p1)
+        #pragma unroll
+        for (int p2 = 0; p2 < 3; ++p2) x[p1 + 3 * p2] = v[3 * p1 + p2];
+    #pragma unroll
+    for (int i = 0; i < 9; ++i) v[i] = x[i];
+}
+
+// One Stockham stage of radix R over NB interleaved sequences (element i of
+// sequence s at logical index i * NB + s, stored at pad()), x -> y.
+template <int R, int NB>
+__device__ __forceinline__ void radix_stage(const float2* __restrict__ x, float2* __restrict__ y, int n, int Ls,
+                                            uint32_t lmag, int twstep, const float2* __restrict__ tw, bool inv)
+{
+    const int m = n / R;
     const int items = m * NB;
     const float sign = inv ? 1.0f : -1.0f;
     for (int it = threadIdx.x; it < items; it += blockDim.x)
     {
         const int s = it % NB, j = it / NB;
-        int g, k;
-        if (Ls == 1) { g = j; k = 0; }
-        else
+        int g = j, k = 0;
+        if (Ls > 1)
         {
             g = (int)__umulhi((uint32_t)j, lmag);
             k = j - g * Ls;
         }
-        float2 v[4];
+        float2 v[R];
         #pragma unroll
-        for (int q = 0; q < 4; ++q)
+        for (int q = 0; q < R; ++q) v[q] = x[pad((j + q * m) * NB + s)];
+        if (k > 0)
         {
-            if (q >= r) break;
-            float2 a = x[(j + q * m) * NB + s];
-            if (q > 0 && k > 0)
+            #pragma unroll
+            for (int q = 1; q < R; ++q)
             {
-                float2 w = __ldg(&tw[q * k * twstep]);   // q k < r Ls, so the index is < n
+                float2 w = __ldg(&tw[q * k * twstep]);   // q k < R Ls: index < n
                 if (inv) w.y = -w.y;
-                a = cmul(a, w);
+                v[q] = cmul(v[q], w);
             }
-            v[q] = a;
         }
-        float2 z[4];
-        if (r == 4)
-        {
-            const float2 t0 = make_float2(v[0].x + v[2].x, v[0].y + v[2].y);
-            const float2 t1 = make_float2(v[0].x - v[2].x, v[0].y - v[2].y);
-            const float2 t2 = make_float2(v[1].x + v[3].x, v[1].y + v[3].y);
-            const float2 t3 = make_float2(v[1].x - v[3].x, v[1].y - v[3].y);
-            const float2 it3 = make_float2(-sign * t3.y, sign * t3.x);   // (sign i) t3
-            z[0] = make_float2(t0.x + t2.x, t0.y + t2.y);
-            z[1] = make_float2(t1.x + it3.x, t1.y + it3.y);
-            z[2] = make_float2(t0.x - t2.x, t0.y - t2.y);
-            z[3] = make_float2(t1.x - it3.x, t1.y - it3.y);
-        }
-        else if (r == 3)
-        {
-            const float c = 0.86602540378443864676f;   // sqrt(3)/2
-            const float2 t1 = make_float2(v[1].x + v[2].x, v[1].y + v[2].y);
-            const float2 t2 = make_float2(v[1].x - v[2].x, v[1].y - v[2].y);
-            const float2 base = make_float2(v[0].x - 0.5f * t1.x, v[0].y - 0.5f * t1.y);
-            const float2 rot = make_float2(-sign * c * t2.y, sign * c * t2.x);   // (sign i) (sqrt3/2) t2
-            z[0] = make_float2(v[0].x + t1.x, v[0].y + t1.y);
-            z[1] = make_float2(base.x + rot.x, base.y + rot.y);
-            z[2] = make_float2(base.x - rot.x, base.y - rot.y);
-        }
-        else
-        {
-            z[0] = make_float2(v[0].x + v[1].x, v[0].y + v[1].y);
-            z[1] = make_float2(v[0].x - v[1].x, v[0].y - v[1].y);
-        }
-        const int ob = g * Ls * r + k;
+        dft<R>(v, sign);
+        const int ob = g * Ls * R + k;
         #pragma unroll
-        for (int p = 0; p < 4; ++p)
-        {
-            if (p >= r) break;
-            y[(ob + p * Ls) * NB + s] = z[p];
-        }
+        for (int p = 0; p < R; ++p) y[pad((ob + p * Ls) * NB + s)] = v[p];
     }
 }
 
@@ -127,7 +222,17 @@ __device__ float2* stockham(float2* x, float2* y, const FftDims& d, const float2
 {
     for (int st = 0; st < d.nrad; ++st)
     {
-        stockham_stage<NB>(x, y, d.n, d.rad[st], d.ls[st], d.lmag[st], d.twstep[st], tw, inv);
+        const int n = d.n, L = d.ls[st], ts = d.twstep[st];
+        const uint32_t lm = d.lmag[st];
+        switch (d.rad[st])
+        {
+        case 16: radix_stage<16, NB>(x, y, n, L, lm, ts, tw, inv); break;
+        case 9: radix_stage<9, NB>(x, y, n, L, lm, ts, tw, inv); break;
+        case 8: radix_stage<8, NB>(x, y, n, L, lm, ts, tw, inv); break;
+        case 4: radix_stage<4, NB>(x, y, n, L, lm, ts, tw, inv); break;
+        case 3: radix_stage<3, NB>(x, y, n, L, lm, ts, tw, inv); break;
+        default: radix_stage<2, NB>(x, y, n, L, lm, ts, tw, inv); break;
+        }
         __syncthreads();
         float2* t = x; x = y; y = t;
     }
@@ -144,179 +249,196 @@ __device__ __forceinline__ size_t tile_index(int pair, int G, int rows, int r, i
     return (((size_t)pair * G + (q >> 2)) * rows + r) * 4 + (q & 3);
 }
 
-constexpr int kRowThreads = 256;
-constexpr int kRowLoads = 12;   // per-thread loads issued before use (covers rows of up to 3072)
+constexpr int kRowsPerCta = 2;
+constexpr int kRowLoads = 8;   // per-thread loads in flight per row pass
 
-// Pass 1: forward row FFTs.  blockIdx.y selects the packed pair:
-// pair 0 = in0 + i in1, pair 1 = in2 (+ i 0); an optional second layer is
-// summed in on load (flare composite = ghosts + starburst).  Rows [0, H) of
-// width W, zero-padded to Q, written as column-group tiles of `rows` rows.
-__global__ void __launch_bounds__(kRowThreads) conv_rows_fwd(const float* __restrict__ in0,
-                                                             const float* __restrict__ in1,
-                                                             const float* __restrict__ in2,
-                                                             const float* __restrict__ add0,
-                                                             const float* __restrict__ add1,
-                                                             const float* __restrict__ add2, int W, int rows,
-                                                             float2* __restrict__ buf, FftDims dq,
-                                                             const float2* __restrict__ tw)
+// Pass 1: forward row FFTs, two rows per CTA (rows 2b, 2b+1; blockIdx.y =
+// packed pair: 0 = in0 + i in1, 1 = in2).  An optional second layer is summed
+// in on load (flare composite = ghosts + starburst).  Rows of width W,
+// zero-padded to Q, written as column-group tiles of `rows` rows.
+__global__ void __launch_bounds__(1024) conv_rows_fwd(const float* __restrict__ in0, const float* __restrict__ in1,
+                              const float* __restrict__ in2, const float* __restrict__ add0,
+                              const float* __restrict__ add1, const float* __restrict__ add2, int W, int rows,
+                              float2* __restrict__ buf, FftDims dq, const float2* __restrict__ tw)
 {
     extern __shared__ float2 sm[];
-    float2* x = sm;
-    float2* y = sm + dq.n;
-    const int row = blockIdx.x, pair = blockIdx.y;
     const int Q = dq.n, G = (Q + 3) >> 2;
+    float2* x = sm;
+    float2* y = sm + padded((size_t)Q * kRowsPerCta);
+    const int pair = blockIdx.y;
+    const int row0 = blockIdx.x * kRowsPerCta;
     const float* re = pair == 0 ? in0 : in2;
     const float* im = pair == 0 ? in1 : nullptr;
     const float* are = pair == 0 ? add0 : add2;
     const float* aim = pair == 0 ? add1 : nullptr;
-    const size_t ro = (size_t)row * W;
-    // issue every load of this thread first (bytes in flight), then stage
-    for (int i0 = 0; i0 < Q; i0 += kRowThreads * kRowLoads)
+    const int total = Q * kRowsPerCta;
+    for (int e0 = 0; e0 < total; e0 += blockDim.x * kRowLoads)
     {
         float a[kRowLoads], b[kRowLoads];
         #pragma unroll
         for (int u = 0; u < kRowLoads; ++u)
         {
-            const int i = i0 + u * kRowThreads + threadIdx.x;
+            const int e = e0 + u * blockDim.x + threadIdx.x;
+            const int rr = e / Q, i = e - rr * Q;
+            const int row = row0 + rr;
             a[u] = 0.0f; b[u] = 0.0f;
-            if (i < W)
+            if (e < total && i < W && row < rows)
             {
-                a[u] = re[ro + i];
-                if (are) a[u] += are[ro + i];
-                if (im) b[u] = im[ro + i];
-                if (aim) b[u] += aim[ro + i];
+                const size_t o = (size_t)row * W + i;
+                a[u] = re[o];
+                if (are) a[u] += are[o];
+                if (im) b[u] = im[o];
+                if (aim) b[u] += aim[o];
             }
         }
         #pragma unroll
         for (int u = 0; u < kRowLoads; ++u)
         {
-            const int i = i0 + u * kRowThreads + threadIdx.x;
-            if (i < Q) x[i] = make_float2(a[u], b[u]);
+            const int e = e0 + u * blockDim.x + threadIdx.x;
+            if (e < total)
+            {
+                const int rr = e / Q, i = e - rr * Q;
+                x[pad(i * kRowsPerCta + rr)] = make_float2(a[u], b[u]);
+            }
         }
     }
     __syncthreads();
-    const float2* r = stockham<1>(x, y, dq, tw, false);
-    // two complex per thread -> one 16-byte store into the tile
-    for (int h = threadIdx.x; 2 * h < Q; h += kRowThreads)
+    const float2* r = stockham<kRowsPerCta>(x, y, dq, tw, false);
+    // two complex of one row per thread -> one 16-byte store into the tile
+    const int half = (Q + 1) / 2;
+    for (int h = threadIdx.x; h < half * kRowsPerCta; h += blockDim.x)
     {
-        const int q = 2 * h;
-        const float2 v0 = r[q];
-        const float2 v1 = (q + 1 < Q) ? r[q + 1] : make_float2(0.0f, 0.0f);
+        const int rr = h / half, q = 2 * (h - rr * half);
+        const int row = row0 + rr;
+        if (row >= rows) continue;
+        const float2 v0 = r[pad(q * kRowsPerCta + rr)];
+        const float2 v1 = (q + 1 < Q) ? r[pad((q + 1) * kRowsPerCta + rr)] : make_float2(0.0f, 0.0f);
         *reinterpret_cast<float4*>(buf + tile_index(pair, G, rows, row, q)) = make_float4(v0.x, v0.y, v1.x, v1.y);
     }
 }
 
-constexpr int kColGroup = 4;
-constexpr int kColThreads = 512;
+constexpr int kColGroup = 4;      // columns per tile group in the HBM layout
+constexpr int kColsPerCta = 2;    // columns per CTA: half a group, so two CTAs fit an SM
 
-// Pass 2: one column group (4 columns) per CTA: forward column FFT over P rows
-// (rows >= rows_in are zero), times the kernel spectrum, inverse column FFT;
-// rows [0, rows_out) back in place.  mode 1 (kernel-spectrum setup): forward
-// only, result for all P rows.
-__global__ void __launch_bounds__(kColThreads) conv_cols(float2* __restrict__ buf, const float2* __restrict__ khat,
-                                                         int rows_in, int rows_out, FftDims dp, int Q, int mode,
-                                                         const float2* __restrict__ tw)
+// Pass 2: two columns (half a tile group) per CTA: forward column FFT over P
+// rows (rows >= rows_in are zero), times the kernel spectrum, inverse column
+// FFT; rows [0, rows_out) back in place.  mode 1 (kernel-spectrum setup):
+// forward only, result for all P rows.  The two halves of a group are
+// neighbouring CTAs, so each 32-byte sector they share is read from DRAM once.
+__global__ void __launch_bounds__(1024) conv_cols(float2* __restrict__ buf, const float2* __restrict__ khat,
+                                                  int rows_in, int rows_out, FftDims dp, int Q, int mode,
+                                                  const float2* __restrict__ tw)
 {
     extern __shared__ float2 sm[];
-    float2* x = sm;
-    float2* y = sm + (size_t)dp.n * kColGroup;
     const int P = dp.n, G = (Q + 3) >> 2;
-    const int g = blockIdx.x;
+    float2* x = sm;
+    float2* y = sm + padded((size_t)P * kColsPerCta);
+    const int g = blockIdx.x >> 1, hcol = (blockIdx.x & 1) * kColsPerCta;
     float2* base = buf + ((size_t)blockIdx.y * G + g) * rows_in * kColGroup;
-    const int valid = min(kColGroup, Q - g * kColGroup);
+    const int valid = max(0, min(kColsPerCta, Q - g * kColGroup - hcol));
+    if (valid == 0) return;
     {
-        const float4* src = reinterpret_cast<const float4*>(base);
-        float4* xs = reinterpret_cast<float4*>(x);
-        const int n4 = rows_in * 2, p4 = P * 2;
         constexpr int U = 8;
-        for (int e0 = 0; e0 < p4; e0 += kColThreads * U)
+        for (int r0 = 0; r0 < P; r0 += blockDim.x * U)
         {
             float4 v[U];
             #pragma unroll
             for (int u = 0; u < U; ++u)
             {
-                const int e = e0 + u * kColThreads + threadIdx.x;
-                v[u] = e < n4 ? src[e] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                const int r = r0 + u * blockDim.x + threadIdx.x;
+                v[u] = r < rows_in ? *reinterpret_cast<const float4*>(base + (size_t)r * kColGroup + hcol)
+                                   : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             }
             #pragma unroll
             for (int u = 0; u < U; ++u)
             {
-                const int e = e0 + u * kColThreads + threadIdx.x;
-                if (e < p4) xs[e] = v[u];
+                const int r = r0 + u * blockDim.x + threadIdx.x;
+                if (r < P)
+                {
+                    x[pad(2 * r)] = make_float2(v[u].x, v[u].y);
+                    x[pad(2 * r + 1)] = valid > 1 ? make_float2(v[u].z, v[u].w) : make_float2(0.0f, 0.0f);
+                }
             }
         }
     }
-    if (valid < kColGroup)
-    {
-        __syncthreads();
-        for (int e = threadIdx.x; e < P * kColGroup; e += kColThreads)
-            if ((e & 3) >= valid) x[e] = make_float2(0.0f, 0.0f);
-    }
     __syncthreads();
-    float2* f = stockham<kColGroup>(x, y, dp, tw, false);
+    float2* f = stockham<kColsPerCta>(x, y, dp, tw, false);
     float2* other = (f == x) ? y : x;
-    float4* f4 = reinterpret_cast<float4*>(f);
-    float4* dst = reinterpret_cast<float4*>(base);
     if (mode == 1)
     {
-        for (int e = threadIdx.x; e < P * 2; e += kColThreads) dst[e] = f4[e];
+        for (int r = threadIdx.x; r < P; r += blockDim.x)
+        {
+            const float2 a = f[pad(2 * r)], b = f[pad(2 * r + 1)];
+            *reinterpret_cast<float4*>(base + (size_t)r * kColGroup + hcol) = make_float4(a.x, a.y, b.x, b.y);
+        }
         return;
     }
-    const float4* k4 = reinterpret_cast<const float4*>(khat + (size_t)g * P * kColGroup);
-    for (int e = threadIdx.x; e < P * 2; e += kColThreads)
+    const float2* kb = khat + (size_t)g * P * kColGroup + hcol;
+    for (int r = threadIdx.x; r < P; r += blockDim.x)
     {
-        const float4 a = f4[e], k = __ldg(&k4[e]);
-        const float2 lo = cmul(make_float2(a.x, a.y), make_float2(k.x, k.y));
-        const float2 hi = cmul(make_float2(a.z, a.w), make_float2(k.z, k.w));
-        f4[e] = make_float4(lo.x, lo.y, hi.x, hi.y);
+        const float4 k = __ldg(reinterpret_cast<const float4*>(kb + (size_t)r * kColGroup));
+        f[pad(2 * r)] = cmul(f[pad(2 * r)], make_float2(k.x, k.y));
+        f[pad(2 * r + 1)] = cmul(f[pad(2 * r + 1)], make_float2(k.z, k.w));
     }
     __syncthreads();
-    const float4* r4 = reinterpret_cast<const float4*>(stockham<kColGroup>(f, other, dp, tw, true));
-    for (int e = threadIdx.x; e < rows_out * 2; e += kColThreads) dst[e] = r4[e];
+    const float2* res = stockham<kColsPerCta>(f, other, dp, tw, true);
+    for (int r = threadIdx.x; r < rows_out; r += blockDim.x)
+    {
+        const float2 a = res[pad(2 * r)], b = res[pad(2 * r + 1)];
+        *reinterpret_cast<float4*>(base + (size_t)r * kColGroup + hcol) = make_float4(a.x, a.y, b.x, b.y);
+    }
 }
 
-// Pass 3: inverse row FFTs from the tiles; real part -> out0 (pair 0) / out2
-// (pair 1), imaginary part -> out1 (pair 0).  Crop to W.
-__global__ void __launch_bounds__(kRowThreads) conv_rows_inv(const float2* __restrict__ buf, int W, int H,
-                                                             float* __restrict__ out0, float* __restrict__ out1,
-                                                             float* __restrict__ out2, FftDims dq,
-                                                             const float2* __restrict__ tw)
+// Pass 3: inverse row FFTs from the tiles, two rows per CTA; real part ->
+// out0 (pair 0) / out2 (pair 1), imaginary part -> out1 (pair 0).  Crop to W.
+__global__ void __launch_bounds__(1024) conv_rows_inv(const float2* __restrict__ buf, int W, int H, float* __restrict__ out0,
+                              float* __restrict__ out1, float* __restrict__ out2, FftDims dq,
+                              const float2* __restrict__ tw)
 {
     extern __shared__ float2 sm[];
-    float2* x = sm;
-    float2* y = sm + dq.n;
-    const int row = blockIdx.x, pair = blockIdx.y;
     const int Q = dq.n, G = (Q + 3) >> 2;
-    const int nh = (Q + 1) / 2;
-    for (int h0 = 0; h0 < nh; h0 += kRowThreads * 6)
+    float2* x = sm;
+    float2* y = sm + padded((size_t)Q * kRowsPerCta);
+    const int pair = blockIdx.y;
+    const int row0 = blockIdx.x * kRowsPerCta;
+    const int half = (Q + 1) / 2;
+    const int total = half * kRowsPerCta;
+    constexpr int U = 6;
+    for (int h0 = 0; h0 < total; h0 += blockDim.x * U)
     {
-        float4 v[6];
+        float4 v[U];
         #pragma unroll
-        for (int u = 0; u < 6; ++u)
+        for (int u = 0; u < U; ++u)
         {
-            const int h = h0 + u * kRowThreads + threadIdx.x;
-            v[u] = h < nh ? __ldg(reinterpret_cast<const float4*>(buf + tile_index(pair, G, H, row, 2 * h)))
-                          : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            const int h = h0 + u * blockDim.x + threadIdx.x;
+            const int rr = h / half, q = 2 * (h - rr * half);
+            const int row = row0 + rr;
+            v[u] = (h < total && row < H) ? __ldg(reinterpret_cast<const float4*>(buf + tile_index(pair, G, H, row, q)))
+                                          : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         }
         #pragma unroll
-        for (int u = 0; u < 6; ++u)
+        for (int u = 0; u < U; ++u)
         {
-            const int h = h0 + u * kRowThreads + threadIdx.x;
-            if (h < nh)
+            const int h = h0 + u * blockDim.x + threadIdx.x;
+            if (h < total)
             {
-                x[2 * h] = make_float2(v[u].x, v[u].y);
-                if (2 * h + 1 < Q) x[2 * h + 1] = make_float2(v[u].z, v[u].w);
+                const int rr = h / half, q = 2 * (h - rr * half);
+                x[pad(q * kRowsPerCta + rr)] = make_float2(v[u].x, v[u].y);
+                if (q + 1 < Q) x[pad((q + 1) * kRowsPerCta + rr)] = make_float2(v[u].z, v[u].w);
             }
         }
     }
     __syncthreads();
-    const float2* r = stockham<1>(x, y, dq, tw, true);
-    float* o_re = pair == 0 ? out0 : out2;
-    float* o_im = pair == 0 ? out1 : nullptr;
-    for (int i = threadIdx.x; i < W; i += kRowThreads)
+    const float2* r = stockham<kRowsPerCta>(x, y, dq, tw, true);
+    for (int e = threadIdx.x; e < W * kRowsPerCta; e += blockDim.x)
     {
-        o_re[(size_t)row * W + i] = r[i].x;
-        if (o_im) o_im[(size_t)row * W + i] = r[i].y;
+        const int rr = e / W, i = e - rr * W;
+        const int row = row0 + rr;
+        if (row >= H) continue;
+        const float2 v = r[pad(i * kRowsPerCta + rr)];
+        const size_t o = (size_t)row * W + i;
+        if (pair == 0) { out0[o] = v.x; out1[o] = v.y; }
+        else out2[o] = v.x;
     }
 }
 
@@ -325,9 +447,12 @@ FftDims make_dims(int n)
     FftDims d{};
     d.n = n;
     int m = n;
-    while (m % 4 == 0) { d.rad[d.nrad++] = 4; m /= 4; }
-    while (m % 2 == 0) { d.rad[d.nrad++] = 2; m /= 2; }
-    while (m % 3 == 0) { d.rad[d.nrad++] = 3; m /= 3; }
+    while (m % 16 == 0) { d.rad[d.nrad++] = 16; m /= 16; }
+    if (m % 8 == 0) { d.rad[d.nrad++] = 8; m /= 8; }
+    if (m % 4 == 0) { d.rad[d.nrad++] = 4; m /= 4; }
+    if (m % 2 == 0) { d.rad[d.nrad++] = 2; m /= 2; }
+    while (m % 9 == 0) { d.rad[d.nrad++] = 9; m /= 9; }
+    if (m % 3 == 0) { d.rad[d.nrad++] = 3; m /= 3; }
     int Ls = 1;
     for (int s = 0; s < d.nrad; ++s)
     {
@@ -373,6 +498,7 @@ struct ConvPlan {
     float2* tw_p = nullptr;   // twiddles for P (== tw_q when P == Q)
     float2* tw_q = nullptr;
     size_t smem_row = 0, smem_col = 0;
+    int thr_row = 0, thr_col = 0;
 };
 
 }  // namespace gl
@@ -401,13 +527,25 @@ extern "C" int gl_conv2d_plan_create(int width, int height, const float* h_kerne
     p->Q = good_size(width + kw - 1);
     p->P = good_size(height + kh - 1);
     p->G = (p->Q + 3) / 4;
-    if (p->P > 8192 || p->Q > 3072)
+    if (p->P > 3072 || p->Q > 3072)
     {
         delete p;
-        return fail(GL_ERR_INVALID, "conv2d_plan_create: padded transform above 8192 rows or 3072 columns");
+        return fail(GL_ERR_INVALID, "conv2d_plan_create: padded transform above 3072 points per axis");
     }
-    p->smem_row = 2 * (size_t)p->Q * sizeof(float2);
-    p->smem_col = 2 * (size_t)p->P * kColGroup * sizeof(float2);
+    p->smem_row = 2 * padded((size_t)p->Q * kRowsPerCta) * sizeof(float2);
+    p->smem_col = 2 * padded((size_t)p->P * kColsPerCta) * sizeof(float2);
+    {
+        // one thread per butterfly of the largest-radix stage
+        const FftDims dq = make_dims(p->Q), dp = make_dims(p->P);
+        auto threads = [](const FftDims& d, int nb) {
+            int rmax = 2;
+            for (int i = 0; i < d.nrad; ++i) rmax = std::max(rmax, d.rad[i]);
+            const int t = (d.n * nb / rmax + 31) / 32 * 32;
+            return std::min(1024, std::max(64, t));
+        };
+        p->thr_row = threads(dq, kRowsPerCta);
+        p->thr_col = threads(dp, kColsPerCta);
+    }
     if (p->smem_col > 227 * 1024 || p->smem_row > 227 * 1024)
     {
         delete p;
@@ -449,10 +587,10 @@ extern "C" int gl_conv2d_plan_create(int width, int height, const float* h_kerne
         if (e == cudaSuccess)
         {
             // kernel spectrum: row FFTs of the real plane into tiles, then forward column FFTs in place
-            conv_rows_fwd<<<dim3(p->P, 1), kRowThreads, p->smem_row, st>>>(kdev, nullptr, nullptr, nullptr, nullptr,
+            conv_rows_fwd<<<dim3((p->P + kRowsPerCta - 1) / kRowsPerCta, 1), p->thr_row, p->smem_row, st>>>(kdev, nullptr, nullptr, nullptr, nullptr,
                                                                             nullptr, p->Q, p->P, p->khat, dq,
                                                                             p->tw_q);
-            conv_cols<<<dim3(p->G, 1), kColThreads, p->smem_col, st>>>(p->khat, nullptr, p->P, p->P, dp, p->Q, 1,
+            conv_cols<<<dim3(2 * p->G, 1), p->thr_col, p->smem_col, st>>>(p->khat, nullptr, p->P, p->P, dp, p->Q, 1,
                                                                        p->tw_p);
             chk(cudaGetLastError());
         }
@@ -480,10 +618,11 @@ extern "C" int gl_conv2d_plan_execute2(gl_conv_plan* plan, const float* d_in_r, 
     ConvPlan* p = plan->p;
     cudaStream_t st = (cudaStream_t)stream;
     const FftDims dq = make_dims(p->Q), dp = make_dims(p->P);
-    conv_rows_fwd<<<dim3(p->H, 2), kRowThreads, p->smem_row, st>>>(d_in_r, d_in_g, d_in_b, d_add_r, d_add_g, d_add_b,
+    const unsigned rb = (unsigned)((p->H + kRowsPerCta - 1) / kRowsPerCta);
+    conv_rows_fwd<<<dim3(rb, 2), p->thr_row, p->smem_row, st>>>(d_in_r, d_in_g, d_in_b, d_add_r, d_add_g, d_add_b,
                                                                     p->W, p->H, p->buf, dq, p->tw_q);
-    conv_cols<<<dim3(p->G, 2), kColThreads, p->smem_col, st>>>(p->buf, p->khat, p->H, p->H, dp, p->Q, 0, p->tw_p);
-    conv_rows_inv<<<dim3(p->H, 2), kRowThreads, p->smem_row, st>>>(p->buf, p->W, p->H, d_out_r, d_out_g, d_out_b, dq,
+    conv_cols<<<dim3(2 * p->G, 2), p->thr_col, p->smem_col, st>>>(p->buf, p->khat, p->H, p->H, dp, p->Q, 0, p->tw_p);
+    conv_rows_inv<<<dim3(rb, 2), p->thr_row, p->smem_row, st>>>(p->buf, p->W, p->H, d_out_r, d_out_g, d_out_b, dq,
                                                                     p->tw_q);
     GL_CUDA_TRY(cudaGetLastError());
     g_last_launches = 3;
