@@ -101,6 +101,12 @@ class gl_source_solve(C.Structure):
                 ("inv_tan_h", C.c_float), ("probe_evals", C.c_int32)]
 
 
+class gl_veil_params(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("fmt_w", C.c_int32), ("fmt_h", C.c_int32),
+                ("sensor_half_w", C.c_float), ("sensor_half_h", C.c_float), ("spread", C.c_float),
+                ("gain", C.c_float), ("accumulate", C.c_int32)]
+
+
 SURFACE_DTYPE = np.dtype([(name, np.float32 if t in (C.c_float,) else np.int32)
                           if not hasattr(t, "_length_") else
                           (name, np.float32, (t._length_,))

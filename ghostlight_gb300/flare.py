@@ -384,6 +384,7 @@ def render_source_flare(offsets, width: int, height: int, lens: OpticalSystem,
     if lens.num_surfaces() <= 0:
         raise ValueError("render_source_flare: lens has no surfaces")
     hw, hh = _eff_half(config, calibration)
+    smap = None
     if source_angle is None:
         from .calibration import solve_source_angle
         f = np.float32
@@ -397,7 +398,25 @@ def render_source_flare(offsets, width: int, height: int, lens: OpticalSystem,
     src = np.zeros((off.shape[0], 5), np.float32)
     for i, (dx, dy, w) in enumerate(off):
         src[i] = (f(ax0) + dx, f(ay0) + dy, f(r) * w, f(g) * w, f(b) * w)
-    return render_ghosts(lens, src, width, height, config, hw, hh)
+    out = render_ghosts(lens, src, width, height, config, hw, hh)
+    dc = getattr(config, "diffraction", None)
+    if dc is not None and getattr(dc, "veil", False):
+        # veil layer around each source's image point, from the solve's forward
+        # map (SourceFlareRenderer.cpp:105-118) or the paraxial map when the
+        # angle was given directly
+        from .veil import render_veil
+        pos = np.zeros((len(src), 5), np.float32)
+        for i in range(len(src)):
+            if smap is not None:
+                sx, sy = smap.screen(float(src[i, 0]), float(src[i, 1]))
+            else:
+                sx = 0.5 + 0.5 * math.tan(float(src[i, 0])) / math.tan(calibration.max_half_angle_h) \
+                    * calibration.sensor_half_w / hw
+                sy = 0.5 + 0.5 * math.tan(float(src[i, 1])) / math.tan(calibration.max_half_angle_v) \
+                    * calibration.sensor_half_h / hh
+            pos[i] = (sx * width, sy * height, src[i, 2], src[i, 3], src[i, 4])
+        out.update(render_veil(pos, width, height, hw, hh, dc.veil_spread, dc.veil_falloff, dc.veil_gain))
+    return out
 
 
 def render_point_flare(width: int, height: int, lens: OpticalSystem, calibration: LensCalibration,

@@ -441,6 +441,28 @@ int gl_solve_source_angle(const gl_surface* surfaces, int n_surfaces,
 int gl_source_map_screen(const gl_source_solve* base, float angle_x, float angle_y,
                          float* out_sx, float* out_sy);
 
+/* ---- Veiling glare (render_veil, veil_render.cu:243-414) -------------------
+ * The analytic glare-spread function g(r) = (a^2 / (r^2 + a^2))^p, a =
+ * spread * sensor half-height, baked once per falloff p (clamped to [1, 3])
+ * into a resident 1024^2 sprite normalised to unit sum; each execute box-
+ * downsamples it toward the output pitch and area-resamples it onto the frame
+ * around every source, tinted by the source colour times gain.  Sources are
+ * a device array (buffer-pixel position, output-space colour). */
+typedef struct gl_veil_source { float px, py, r, g, b; } gl_veil_source;
+typedef struct gl_veil_params {
+    int32_t width, height, fmt_w, fmt_h;
+    float sensor_half_w, sensor_half_h;
+    float spread;                              /* core radius / sensor half-height */
+    float gain;                                /* fraction of the source flux      */
+    int32_t accumulate;                        /* add into the planes              */
+} gl_veil_params;
+typedef struct gl_veil_plan gl_veil_plan;
+int gl_veil_plan_create(float falloff, void* stream, gl_veil_plan** out);
+int gl_veil_plan_execute(gl_veil_plan* plan, const gl_veil_source* d_sources, int n_sources,
+                         const gl_veil_params* params, float* d_out_r, float* d_out_g,
+                         float* d_out_b, void* stream);
+int gl_veil_plan_destroy(gl_veil_plan* plan);
+
 /* Number of kernel launches issued by the last device call on this thread. */
 int gl_last_launch_count(void);
 
