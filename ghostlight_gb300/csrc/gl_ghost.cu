@@ -825,7 +825,11 @@ int plan_execute(GhostPlan* p, float* d_out_r, float* d_out_g, float* d_out_b, c
     if (p->cull && p->n_items > 0)
     {
         // Probe passes: the frame inflated by CULL_MARGIN = 1.25
-        // (ghost_render.cu:148), persistent launches over the probe items.
+        // (ghost_render.cu:148).  The three passes are one persistent launch
+        // over their items in pass order: a pair is culled only when no item
+        // of any pass hits, and an item whose pair already has a hit is
+        // skipped, so a later pass re-probes only the pairs still without one
+        // (the reference's candidate rule) without a launch boundary per pass.
         GL_CUDA_TRY(cudaMemcpyAsync(p->pair_hits, p->pair_hits_init, sizeof(int) * p->n_pairs,
                                     cudaMemcpyDeviceToDevice, st));
         GL_CUDA_TRY(cudaMemsetAsync(p->probe_counters, 0, sizeof(int) * 4, st));
@@ -836,13 +840,12 @@ int plan_execute(GhostPlan* p, float* d_out_r, float* d_out_g, float* d_out_b, c
         B.hw2 = 2.0f * (p->prm.sensor_half_w * 1.25f);
         B.hh2 = 2.0f * (p->prm.sensor_half_h * 1.25f);
         const int warps_per_block = kRenderThreads / 32;
-        for (int pass = 0; pass < 3; ++pass)
+        const int n_it = p->probe_begin[3];
+        if (n_it > 0)
         {
-            const int n_it = p->probe_begin[pass + 1] - p->probe_begin[pass];
-            if (n_it <= 0) continue;
-            B.items = p->probe_items + p->probe_begin[pass];
+            B.items = p->probe_items;
             B.n_items = n_it;
-            B.counter = p->probe_counters + pass;
+            B.counter = p->probe_counters;
             const int grid = std::max(1, std::min((n_it + warps_per_block - 1) / warps_per_block, p->grid_persistent));
             ghost_render_kernel<true><<<grid, kRenderThreads, p->smem, st>>>(B);
             ++launches;
