@@ -412,10 +412,16 @@ __global__ void __launch_bounds__(kRenderThreads, kRenderMinBlocks) ghost_render
         if (A.items != nullptr) w = A.items[item];
         else
         {
-            const int per_pair = A.u_tiles * A.u_n_src;
-            const int pr = item / per_pair, rem = item - pr * per_pair;
-            const int sr = rem / A.u_tiles, t = (rem - sr * A.u_tiles) * kTile;
-            w = make_int4(pr, sr, A.u_grid_base + t, min(kTile, A.u_grid_n - t));
+            int tiles = A.u_tiles, base = A.u_grid_base, gn = A.u_grid_n, local = item;
+            if (A.u_npass > 0)
+            {
+                const int q = (item >= A.u_start[2]) ? 2 : (item >= A.u_start[1] ? 1 : 0);
+                tiles = A.u_tl[q]; base = A.u_base[q]; gn = A.u_n[q]; local = item - A.u_start[q];
+            }
+            const int per_pair = tiles * A.u_n_src;
+            const int pr = local / per_pair, rem = local - pr * per_pair;
+            const int sr = rem / tiles, t = (rem - sr * tiles) * kTile;
+            w = make_int4(pr, sr, base + t, min(kTile, gn - t));
         }
         if (A.pair_hits != nullptr)
         {

@@ -44,6 +44,11 @@ struct RenderArgs {
     // computed from the index; w_uniform replaces the pairs' per-ray weight.
     int u_tiles, u_n_src, u_grid_base, u_grid_n;
     float w_uniform;
+    // Up to three uniform item ranges in one queue (the off-sensor probe
+    // passes): items [u_start[q], u_start[q + 1]) trace grid u_base[q] ..
+    // + u_n[q] in u_tl[q] tiles.  u_npass = 0: the single range above.
+    int u_npass;
+    int u_start[4], u_base[3], u_n[3], u_tl[3];
     int width, height;
     float fmt_w, fmt_h, fmt_x0, fmt_y0;
     float hw2, hh2, gain, front_R, start_z;

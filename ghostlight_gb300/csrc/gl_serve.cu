@@ -413,15 +413,25 @@ int gl_request_enqueue(gl_request* req, float* d_out_r, float* d_out_g, float* d
         B.pair_hits = r->pair_hits;
         B.hw2 = 2.0f * (r->prm.sensor_half_w * 1.25f);
         B.hh2 = 2.0f * (r->prm.sensor_half_h * 1.25f);
+        // the three passes as one launch over consecutive item ranges, in pass
+        // order: an item whose pair already has a hit is skipped, so a later
+        // pass re-probes only the pairs still without one
+        int start = 0;
+        B.u_npass = 3;
         for (int pass = 0; pass < 3; ++pass)
         {
             const int cnt = L->probe_begin[pass + 1] - L->probe_begin[pass];
-            if (cnt <= 0) continue;
-            B.u_grid_base = L->probe_begin[pass];
-            B.u_grid_n = cnt;
-            B.u_tiles = (cnt + kTile - 1) / kTile;
-            B.n_items = L->n_pairs * r->n_src * B.u_tiles;
-            B.counter = items_per_warp == 0 ? r->counters + pass : nullptr;
+            B.u_start[pass] = start;
+            B.u_base[pass] = L->probe_begin[pass];
+            B.u_n[pass] = cnt;
+            B.u_tl[pass] = (cnt + kTile - 1) / kTile;
+            start += L->n_pairs * r->n_src * B.u_tl[pass];
+        }
+        B.u_start[3] = start;
+        B.n_items = start;
+        B.counter = items_per_warp == 0 ? r->counters : nullptr;
+        if (start > 0)
+        {
             GL_CUDA_TRY(render_launch(B, true, grid_for(B.n_items), r->smem, st));
             ++launches;
         }
