@@ -26,7 +26,8 @@ from .serve import ResidentLens, _spectral, render_params, FlareRequest
 
 class SourceSweep:
     def __init__(self, resident: ResidentLens, sources_rad, width: int, height: int, n_spec: int, ray_grid: int,
-                 gain: float = 1000.0, starburst=None, stream=None, items_per_warp: int = 0):
+                 gain: float = 1000.0, starburst=None, stream=None, items_per_warp: int = 0,
+                 side_streams: int = 3):
         """sources_rad: (N, 2) field angles (x, y) in radians, one frame each.
         starburst: None, or dict(plan=MdftPlan over (width, height), pupil=(n, n) tensor,
         centers=(N, 2) pixel centres)."""
@@ -38,6 +39,7 @@ class SourceSweep:
         self.n_spec, self.ray_grid = int(n_spec), int(ray_grid)
         self.items_per_warp = int(items_per_warp)
         self.stream = stream if stream is not None else torch.cuda.Stream()
+        self.side = [torch.cuda.Stream() for _ in range(max(1, int(side_streams)))]
         self.starburst = starburst
         src = np.asarray(sources_rad, np.float64).reshape(-1, 2)
         self.n_frames = len(src)
@@ -68,19 +70,38 @@ class SourceSweep:
         self.launches = 0
 
     def _enqueue_all(self) -> int:
-        st = self.stream.cuda_stream
+        """Ghost frames round-robin over the side streams (a frame's probe and
+        render launches overlap the previous frame's tail); the starburst of
+        frame k runs on the main stream once frame k's ghost layer is written
+        (one plan, one centre at a time); the main stream joins every side
+        stream at the end."""
+        torch = self.torch
+        main = self.stream
         n = 0
         npx = self.width * self.height
         sb = self.starburst
+        fork = torch.cuda.Event()
+        fork.record(main)
+        for s in self.side:
+            s.wait_event(fork)
         for k, h in enumerate(self.requests):
-            _native.check(self._lib.gl_request_enqueue(h, None, None, None, self.items_per_warp, st), "request_enqueue")
+            side = self.side[k % len(self.side)]
+            _native.check(self._lib.gl_request_enqueue(h, None, None, None, self.items_per_warp, side.cuda_stream),
+                          "request_enqueue")
             n += _native.last_launch_count()
             if sb is not None:
+                ev = torch.cuda.Event()
+                ev.record(side)
+                main.wait_event(ev)
                 cx, cy = sb["centers"][k]
-                n += sb["plan"].set_center(cx, cy, stream=st)
+                n += sb["plan"].set_center(cx, cy, stream=main.cuda_stream)
                 base = self.planes[k]
-                n += sb["plan"].execute_raw(sb["pupil"].data_ptr(), base, base + 4 * npx, base + 8 * npx, stream=st,
-                                            accumulate=True)
+                n += sb["plan"].execute_raw(sb["pupil"].data_ptr(), base, base + 4 * npx, base + 8 * npx,
+                                            stream=main.cuda_stream, accumulate=True)
+        for s in self.side:
+            ev = torch.cuda.Event()
+            ev.record(s)
+            main.wait_event(ev)
         return n
 
     def run(self) -> int:
