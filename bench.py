@@ -423,9 +423,19 @@ def run_full_frame(args, dev, stream, timed, ghost_plan, plain_plan, sb_inputs, 
     star = [torch.zeros((H, W), dtype=torch.float32, device=dev) for _ in range(3)]
     final = [torch.zeros((H, W), dtype=torch.float32, device=dev) for _ in range(3)]
 
+    side = torch.cuda.Stream()
+
     def frame(gp):
-        n = gp.execute(*ghost, stream=stream.cuda_stream)
-        n += sbp.execute(A, *star, stream=stream.cuda_stream)
+        # the starburst does not depend on the ghost layer: it runs on a side
+        # stream beside the ghost launches, and the convolution joins both
+        fork = torch.cuda.Event()
+        fork.record(stream)
+        side.wait_event(fork)
+        n = sbp.execute(A, *star, stream=side.cuda_stream)
+        n += gp.execute(*ghost, stream=stream.cuda_stream)
+        join = torch.cuda.Event()
+        join.record(side)
+        stream.wait_event(join)
         n += conv.execute(ghost, final, add=star, stream=stream.cuda_stream)
         return n
 
