@@ -400,11 +400,13 @@ def render_source_flare(offsets, width: int, height: int, lens: OpticalSystem,
         src[i] = (f(ax0) + dx, f(ay0) + dy, f(r) * w, f(g) * w, f(b) * w)
     out = render_ghosts(lens, src, width, height, config, hw, hh)
     dc = getattr(config, "diffraction", None)
-    if dc is not None and getattr(dc, "veil", False):
-        # veil layer around each source's image point, from the solve's forward
-        # map (SourceFlareRenderer.cpp:105-118) or the paraxial map when the
-        # angle was given directly
-        from .veil import render_veil
+    want_sb = dc is not None and getattr(dc, "starburst", False)
+    want_veil = dc is not None and getattr(dc, "veil", False)
+    pos = None
+    if want_sb or want_veil:
+        # each source's image point, from the solve's forward map
+        # (SourceFlareRenderer.cpp:105-118) or the paraxial map when the angle
+        # was given directly
         pos = np.zeros((len(src), 5), np.float32)
         for i in range(len(src)):
             if smap is not None:
@@ -415,6 +417,11 @@ def render_source_flare(offsets, width: int, height: int, lens: OpticalSystem,
                 sy = 0.5 + 0.5 * math.tan(float(src[i, 1])) / math.tan(calibration.max_half_angle_v) \
                     * calibration.sensor_half_h / hh
             pos[i] = (sx * width, sy * height, src[i, 2], src[i, 3], src[i, 4])
+    if want_sb:
+        from .starburst import starburst_layer
+        out.update(starburst_layer(lens, calibration, config, pos, width, height, hw, hh))
+    if want_veil:
+        from .veil import render_veil
         out.update(render_veil(pos, width, height, hw, hh, dc.veil_spread, dc.veil_falloff, dc.veil_gain))
     return out
 

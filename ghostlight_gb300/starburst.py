@@ -130,3 +130,65 @@ def mdft_starburst_eform(pupil, K, scale_x, scale_y, weights_rgb, form="split_bf
     if code:
         raise _native.GhostlightError("mdft: device pipeline wait timed out (code %d)" % code)
     return out
+
+
+def _round128(x: int) -> int:
+    return max(128, (int(x) + 127) // 128 * 128)
+
+
+def starburst_layer(lens, calibration, config, sources_px, width: int, height: int, sensor_half_w: float,
+                    sensor_half_h: float, form: str = "split_bf16"):
+    """The starburst layer of a flare render: the Fraunhofer pattern |E|^2 of
+    the stop pupil (built on the device) around each source's image point,
+    summed over the config's wavelengths.
+
+    Scale per axis (the reference sizes its pattern by first-order optics,
+    render_config.h:128-150): pupil sample pitch 2 EP / (fill n), output
+    pixel pitch 2 half / size, focal length f -> s = pitch_pupil pitch_px /
+    (lambda f) cycles per sample per pixel, divided by scale_trim.  Brightness:
+    starburst_gain x the source flux per wavelength (cmf-weighted) over one
+    period of the pattern.  sources_px: (N, 5) [px, py, r, g, b].
+    Returns {"starburst_r", "starburst_g", "starburst_b"} (H, W) tensors.
+    """
+    import torch
+    from .flare import spectral_table
+    dc = config.diffraction
+    n = 256 if int(dc.starburst_grid) <= 1024 else 512
+    fill = float(dc.pupil_fill) if 0.02 < float(dc.pupil_fill) < 0.9 else 0.30
+    ns = int(dc.spectral_samples) if int(dc.spectral_samples) > 0 else int(config.spectral_samples)
+    ns = max(3, ns)
+    spec, _ = spectral_table(ns, int(config.output_cs), config.custom_xyz_to_output)
+    lam_mm = spec[:, 0].astype(np.float64) * 1e-6
+    trim = float(dc.scale_trim) if float(dc.scale_trim) > 0 else 1.0
+    fx = float(calibration.focal_length_x) or 1.0
+    fy = float(calibration.focal_length_y) or 1.0
+    dxp = 2.0 * float(calibration.entrance_pupil_semi_x) / (fill * n)
+    dyp = 2.0 * float(calibration.entrance_pupil_semi_y) / (fill * n)
+    sx = dxp * (2.0 * sensor_half_w / width) / (lam_mm * fx) / trim
+    sy = dyp * (2.0 * sensor_half_h / height) / (lam_mm * fy) / trim
+    pupil = build_pupil(lens, n, fill, int(config.aperture_blades), float(config.aperture_rotation))
+    amp2 = float((pupil.double() ** 2).sum())
+    Kx, Ky = _round128(width), _round128(height)
+    src = np.asarray(sources_px, np.float64).reshape(-1, 5)
+    out = torch.zeros((3, Ky, Kx), dtype=torch.float32, device="cuda")
+    if amp2 <= 0.0 or len(src) == 0:
+        return {k: torch.zeros((height, width), dtype=torch.float32, device="cuda")
+                for k in ("starburst_r", "starburst_g", "starburst_b")}
+    plan = None
+    for (px, py, r, g, b) in src:
+        # one period of |E|^2 sums to (1 / (sx sy)) sum |A|^2: normalise it to gain x flux per wavelength
+        w = spec[:, 1:4].astype(np.float64) * np.array([r, g, b])[None, :] * (sx * sy)[:, None] / amp2
+        w *= float(dc.starburst_gain)
+        if plan is None:
+            plan = MdftPlan(n, (Kx, Ky), sx, sy, w.astype(np.float32), form, center_x=px, center_y=py)
+        else:
+            plan.close()
+            plan = MdftPlan(n, (Kx, Ky), sx, sy, w.astype(np.float32), form, center_x=px, center_y=py)
+        plan.execute(pupil, out[0], out[1], out[2], accumulate=True)
+    torch.cuda.synchronize()
+    code = plan.status()
+    plan.close()
+    if code:
+        raise _native.GhostlightError("starburst: device pipeline wait timed out (code %d)" % code)
+    return {"starburst_r": out[0, :height, :width].contiguous(), "starburst_g": out[1, :height, :width].contiguous(),
+            "starburst_b": out[2, :height, :width].contiguous()}

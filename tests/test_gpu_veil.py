@@ -49,3 +49,22 @@ def test_point_flare_with_veil_layer(pins, meta):
     v = out["veil_g"].cpu().numpy()
     y, x = np.unravel_index(np.argmax(v), v.shape)
     assert abs(x - 0.7 * 256) <= 3 and abs(y - 0.4 * 256) <= 3
+
+
+def test_point_flare_with_starburst_layer(pins, meta):
+    """render_point_flare with the starburst switched on returns starburst_r/g/b:
+    the pattern peaks on the source's image point and carries at most
+    starburst_gain x the source flux (one period of the pattern)."""
+    import ghostlight_gb300 as gl
+    from conftest import lens_from_pins
+    lens = gl.OpticalSystem.from_records(lens_from_pins(pins, "cfg1_double_gauss_12"))
+    cal = gl.LensCalibration.from_dict(meta["cfg1_double_gauss_12"]["calibration"])
+    cfg = gl.PointFlareConfig(ray_grid=32, spectral_samples=8, source_x=0.6, source_y=0.45)
+    cfg.diffraction.starburst = True
+    cfg.diffraction.scale_trim = 200.0         # enlarge: one period of the pattern spans the frame
+    out = gl.render_point_flare(250, 200, lens, cal, cfg)
+    assert {"ghost_r", "starburst_r", "starburst_g", "starburst_b"} <= set(out)
+    g = out["starburst_g"].cpu().numpy()
+    assert g.shape == (200, 250) and np.isfinite(g).all() and g.max() > 0
+    y, x = np.unravel_index(np.argmax(g), g.shape)
+    assert abs(x - 0.6 * 250) <= 2 and abs(y - 0.45 * 200) <= 2
