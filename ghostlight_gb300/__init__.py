@@ -17,6 +17,8 @@ from .calibration import calibrate_lens, solve_source_angle
 from .starburst import MdftPlan, mdft_starburst_eform
 from .psf import ConvPlan, convolve_psf, synthetic_psf_kernel
 from .apertures import curved_blade_mask
+from .psf_grid import render_psf
+from .veil import render_veil
 
 __version__ = "0.1.0"
 

@@ -107,6 +107,18 @@ class gl_veil_params(C.Structure):
                 ("gain", C.c_float), ("accumulate", C.c_int32)]
 
 
+class gl_psf_cell(C.Structure):
+    _fields_ = [("beam_ax", C.c_float), ("beam_ay", C.c_float), ("chief_x_mm", C.c_float),
+                ("chief_y_mm", C.c_float), ("status", C.c_int32), ("pupil_fraction", C.c_float),
+                ("aim_residual_mm", C.c_float)]
+
+
+class gl_psf_source(C.Structure):
+    _fields_ = [("angle_x", C.c_float), ("angle_y", C.c_float), ("r", C.c_float), ("g", C.c_float),
+                ("b", C.c_float), ("chief_x_mm", C.c_float), ("chief_y_mm", C.c_float),
+                ("tile_x0", C.c_int32), ("tile_y0", C.c_int32)]
+
+
 SURFACE_DTYPE = np.dtype([(name, np.float32 if t in (C.c_float,) else np.int32)
                           if not hasattr(t, "_length_") else
                           (name, np.float32, (t._length_,))

@@ -12,7 +12,7 @@ import threading
 from . import _abi
 from ._abi import (gl_filter_params, gl_flare_source, gl_ghost_pair, gl_ghost_render_params,
                    gl_lens_calibration, gl_pupil_sample, gl_sampler_params, gl_source_solve,
-                   gl_spectral_sample, gl_surface, gl_veil_params)
+                   gl_spectral_sample, gl_surface, gl_veil_params, gl_psf_cell, gl_psf_source)
 
 _lock = threading.Lock()
 _lib = None
@@ -80,6 +80,9 @@ def _declare(lib):
     lib.gl_request_destroy.argtypes = [vp, vp]
     lib.gl_pool_info.argtypes = [P(ll), P(ll)]
     lib.gl_pool_trim.argtypes = [ll]
+    lib.gl_psf_prepass.argtypes = [P(gl_surface), i, P(f), i, i, P(gl_psf_cell)]
+    lib.gl_psf_render.argtypes = [P(gl_surface), i, P(gl_psf_source), i, P(gl_pupil_sample), i,
+                                  P(gl_spectral_sample), i, i, i, i, i, f, i, f, i, vp, vp, vp, vp]
     lib.gl_veil_plan_create.argtypes = [f, vp, P(vp)]
     lib.gl_veil_plan_execute.argtypes = [vp, vp, i, P(gl_veil_params), vp, vp, vp, vp]
     lib.gl_veil_plan_destroy.argtypes = [vp]

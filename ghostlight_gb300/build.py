@@ -39,6 +39,7 @@ UNITS = {
     "gl_conv.cu": FAST,
     "gl_serve.cu": FAST,
     "gl_veil.cu": FAST,
+    "gl_psf.cu": FAST,
 }
 # Occupancy target of the render kernel (CTAs of 128 threads per SM); an
 # environment override lets a tuning sweep rebuild with another value.

@@ -522,10 +522,222 @@ bool measure_jacobian(SolveProbe& P, float ax, float ay, float* land, float* J)
     return true;
 }
 
+// ---- PSF grid: chief-ray pre-pass (PSFRenderer.cpp:28-243) -------------------
+constexpr float kChiefLambda = 587.56f;
+
+// One pupil sample of the beam at (ax, ay), spawn-shifted, at the d line.
+bool chief_candidate(ProbeLens& L, float start_z, float front_R, float ax, float ay, float u, float v, float& x,
+                     float& y)
+{
+    const float bx = tanf(ax), by = tanf(ay);
+    const float sdx = -kSpawnOffset * bx, sdy = -kSpawnOffset * by;
+    L.set_lambda(kChiefLambda);
+    const V3 o = v3(u * front_R + sdx, v * front_R + sdy, start_z);
+    const V3 d = normalized(v3(bx, by, 1.0f));
+    const TraceOut r = trace_primary(L.recs.data(), L.n, L.at.data(), o, d, kChiefLambda);
+    if (r.status != GL_TRACE_OK || !std::isfinite(r.x) || !std::isfinite(r.y)) return false;
+    x = r.x;
+    y = r.y;
+    return true;
+}
+
+struct PupilProbe {
+    int hits = 0;
+    float frac = 0.0f, mean_x = 0.0f, mean_y = 0.0f;
+};
+
+// N x N unit-disc pupil probe: transmitting fraction and survivor-mean landing.
+PupilProbe pupil_probe(ProbeLens& L, float start_z, float front_R, float ax, float ay, int N)
+{
+    float sx = 0.0f, sy = 0.0f;
+    int hits = 0, total = 0;
+    for (int iy = 0; iy < N; ++iy)
+    {
+        const float v = -1.0f + ((float)iy + 0.5f) * (2.0f / (float)N);
+        for (int ix = 0; ix < N; ++ix)
+        {
+            const float u = -1.0f + ((float)ix + 0.5f) * (2.0f / (float)N);
+            if (u * u + v * v > 1.0f) continue;
+            ++total;
+            float x, y;
+            if (chief_candidate(L, start_z, front_R, ax, ay, u, v, x, y)) { sx += x; sy += y; ++hits; }
+        }
+    }
+    PupilProbe p;
+    p.hits = hits;
+    p.frac = total > 0 ? (float)hits / (float)total : 0.0f;
+    p.mean_x = hits > 0 ? sx / (float)hits : 0.0f;
+    p.mean_y = hits > 0 ? sy / (float)hits : 0.0f;
+    return p;
+}
+
+struct AxialPupil {
+    Window win;
+    bool usable = false;
+};
+
+AxialPupil axial_pupil(ProbeLens& L)
+{
+    AxialPupil a;
+    Window full;
+    const DiscArea d = probe_window(L, 0.0f, 0.0f, kChiefLambda, full);
+    if (d.area > 0.0f) { a.win = d.fit; a.usable = true; }
+    return a;
+}
+
+// Aim the chief ray of one cell at its sensor target: the clean u = v = 0 ray
+// first, then the survivor mean of a 9 x 9 probe, then the tracked window of a
+// deep pupil; a cell with no light keeps its seed and is DARK.
+void aim_chief(ProbeLens& L, float start_z, float front_R, const AxialPupil& axial, float seed_ax, float seed_ay,
+               float tx, float ty, gl_psf_cell& c)
+{
+    constexpr int kIter = 8;
+    constexpr float kFd = 1e-4f, kTol = 1e-4f, kTolSoft = 5e-3f;
+    constexpr int kAimN = 9, kFracN = 17, kMinHits = 4;
+    constexpr float kDeepFd = 1e-3f, kDeepWarm = 0.10f;
+    const float seed_mag = sqrtf(seed_ax * seed_ax + seed_ay * seed_ay);
+    const float cap = std::max(0.02f, 0.5f * seed_mag);
+    {
+        auto landing = [&](float ax, float ay, float& x, float& y) {
+            return chief_candidate(L, start_z, front_R, ax, ay, 0.0f, 0.0f, x, y);
+        };
+        float ax = seed_ax, ay = seed_ay, tx0, ty0;
+        if (landing(ax, ay, tx0, ty0))
+        {
+            float res = 0.0f;
+            newton_aim(landing, tx, ty, ax, ay, res, kIter, kFd, cap, kTol);
+            landing(ax, ay, c.chief_x_mm, c.chief_y_mm);
+            c.beam_ax = ax; c.beam_ay = ay;
+            c.status = GL_PSF_CELL_OK;
+            c.aim_residual_mm = res;
+            c.pupil_fraction = pupil_probe(L, start_z, front_R, ax, ay, kFracN).frac;
+            return;
+        }
+    }
+    {
+        auto landing = [&](float ax, float ay, float& x, float& y) {
+            const PupilProbe p = pupil_probe(L, start_z, front_R, ax, ay, kAimN);
+            if (p.hits < kMinHits) return false;
+            x = p.mean_x; y = p.mean_y;
+            return true;
+        };
+        float ax = seed_ax, ay = seed_ay, tx0, ty0;
+        if (landing(ax, ay, tx0, ty0))
+        {
+            float res = 0.0f;
+            newton_aim(landing, tx, ty, ax, ay, res, kIter, kFd, cap, kTolSoft);
+            landing(ax, ay, c.chief_x_mm, c.chief_y_mm);
+            c.beam_ax = ax; c.beam_ay = ay;
+            c.status = GL_PSF_CELL_CHIEF_VIGNETTED;
+            c.aim_residual_mm = res;
+            c.pupil_fraction = pupil_probe(L, start_z, front_R, ax, ay, kFracN).frac;
+            return;
+        }
+    }
+    if (axial.usable)
+    {
+        Window track = axial.win;
+        auto landing = [&](float ax, float ay, float& x, float& y) {
+            Window w = track;
+            const DiscArea d = probe_disc(L, ax, ay, kChiefLambda, &w);
+            if (!(d.area > 0.0f) || !std::isfinite(d.mean_x) || !std::isfinite(d.mean_y)) return false;
+            track = w;
+            x = d.mean_x; y = d.mean_y;
+            return true;
+        };
+        if (track.r < 1.0f && seed_mag > 0.0f)
+        {
+            const int steps = std::max(3, std::min(16, (int)std::ceil(seed_mag / kDeepWarm)));
+            float a, b;
+            for (int k = 1; k <= steps; ++k)
+            {
+                const float f = (float)k / (float)steps;
+                landing(seed_ax * f, seed_ay * f, a, b);
+            }
+        }
+        float ax = seed_ax, ay = seed_ay, tx0, ty0;
+        if (landing(ax, ay, tx0, ty0))
+        {
+            float res = 0.0f;
+            newton_aim(landing, tx, ty, ax, ay, res, kIter, kDeepFd, cap, kTolSoft);
+            if (landing(ax, ay, c.chief_x_mm, c.chief_y_mm))
+            {
+                c.beam_ax = ax; c.beam_ay = ay;
+                c.status = GL_PSF_CELL_CHIEF_VIGNETTED;
+                c.aim_residual_mm = res;
+                c.pupil_fraction = pupil_probe(L, start_z, front_R, ax, ay, kFracN).frac;
+                return;
+            }
+        }
+    }
+    c.beam_ax = seed_ax; c.beam_ay = seed_ay;
+    c.chief_x_mm = tx; c.chief_y_mm = ty;
+    c.status = GL_PSF_CELL_DARK;
+    c.aim_residual_mm = 1e30f;
+    c.pupil_fraction = 0.0f;
+}
+
 }  // namespace
 }  // namespace gl
 
 using namespace gl;
+
+extern "C" int gl_psf_prepass(const gl_surface* surfaces, int n, const float* sources7, int n_src, int center_mode,
+                              gl_psf_cell* out)
+{
+    if (!surfaces || n <= 0 || (n_src > 0 && (!sources7 || !out)) || n_src < 0)
+        return fail(GL_ERR_INVALID, "psf_prepass: bad arguments");
+    ProbeLens L;
+    int rc = open_lens(surfaces, n, L);
+    if (rc) return rc;
+    const float start_z = surfaces[0].z - kSpawnOffset;
+    const float front_R = L.front_R;
+    const AxialPupil axial = axial_pupil(L);
+    const bool target = center_mode == GL_PSF_CENTER_FIXED_TARGET;
+    for (int i = 0; i < n_src; ++i)
+    {
+        const float* s = sources7 + 7 * (size_t)i;
+        gl_psf_cell c{};
+        c.beam_ax = s[0]; c.beam_ay = s[1];
+        c.status = GL_PSF_CELL_OK;
+        if (target)
+        {
+            aim_chief(L, start_z, front_R, axial, s[0], s[1], s[5], s[6], c);
+        }
+        else
+        {
+            // unweighted 7 x 7 pupil-mean landing; a deep pupil the full-disc
+            // probe misses is found through the tracked axial window
+            const PupilProbe p = pupil_probe(L, start_z, front_R, s[0], s[1], 7);
+            c.chief_x_mm = p.mean_x; c.chief_y_mm = p.mean_y;
+            c.status = p.hits > 0 ? GL_PSF_CELL_OK : GL_PSF_CELL_DARK;
+            c.pupil_fraction = p.frac;
+            if (p.hits == 0 && axial.usable)
+            {
+                Window w = axial.win;
+                const float mag = sqrtf(s[0] * s[0] + s[1] * s[1]);
+                if (w.r < 1.0f && mag > 0.0f)
+                {
+                    const int steps = std::max(3, std::min(16, (int)std::ceil(mag / 0.10f)));
+                    for (int k = 1; k <= steps; ++k)
+                    {
+                        const float f = (float)k / (float)steps;
+                        probe_disc(L, s[0] * f, s[1] * f, kChiefLambda, &w);
+                    }
+                }
+                const DiscArea d = probe_disc(L, s[0], s[1], kChiefLambda, &w);
+                if (d.area > 0.0f && std::isfinite(d.mean_x) && std::isfinite(d.mean_y))
+                {
+                    c.chief_x_mm = d.mean_x; c.chief_y_mm = d.mean_y;
+                    c.status = GL_PSF_CELL_OK;
+                }
+            }
+        }
+        if (!std::isfinite(c.aim_residual_mm)) c.aim_residual_mm = 0.0f;
+        out[i] = c;
+    }
+    return GL_OK;
+}
 
 extern "C" int gl_calibrate_lens(const gl_surface* surfaces, int n, float lens_focal_length, float d_line_nm,
                                  gl_lens_calibration* out)

@@ -1,0 +1,209 @@
+// gl_psf.cu — PSF grid renderer: per source, the lens's primary-ray spot
+// (every pupil sample at every wavelength) splatted into its own tile of a
+// composite atlas (psf_kernel, psf_render.cu:30-232).
+//
+// GB300 layout: the packed lens records and the per-wavelength IOR slices are
+// staged in shared memory once per CTA; one thread per (source, pupil sample)
+// walks the wavelengths with the reference-formulation primary trace; the
+// splat is bilinear, or a normalised Gaussian of the configured physical
+// width, clipped to the source's tile.
+#include "gl_internal.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <string>
+#include <vector>
+
+namespace gl {
+namespace {
+
+constexpr int kPsfThreads = 256;
+
+struct PsfArgs {
+    const SurfRec* recs;
+    const float* ior_at;         // [spec][surf]
+    const float4* spec;          // lambda, cmf r g b
+    const gl_psf_source* src;
+    const float2* grid;
+    int n_surf, n_spec, n_src, n_grid;
+    float front_R, start_z, mm_per_pixel, ray_weight;
+    int tile_w, tile_h, comp_w, comp_h, mono;
+    float sigma_px;
+    int radius_px;
+    float* out_r;
+    float* out_g;
+    float* out_b;
+};
+
+__device__ __forceinline__ void deposit(const PsfArgs& A, int pix, float lum, float cr, float cg, float cb, float wt)
+{
+    if (A.mono)
+    {
+        if (fabsf(lum) > 1e-14f) atomicAdd(A.out_r + pix, lum * wt);
+    }
+    else
+    {
+        if (fabsf(cr) > 1e-14f) atomicAdd(A.out_r + pix, cr * wt);
+        if (fabsf(cg) > 1e-14f) atomicAdd(A.out_g + pix, cg * wt);
+        if (fabsf(cb) > 1e-14f) atomicAdd(A.out_b + pix, cb * wt);
+    }
+}
+
+__global__ void __launch_bounds__(kPsfThreads) psf_kernel(PsfArgs A)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    SurfRec* lens = reinterpret_cast<SurfRec*>(smem_raw);
+    float* at = reinterpret_cast<float*>(lens + A.n_surf);
+    {
+        const int words = A.n_surf * (int)(sizeof(SurfRec) / 4);
+        const int* s = reinterpret_cast<const int*>(A.recs);
+        int* d = reinterpret_cast<int*>(lens);
+        for (int i = threadIdx.x; i < words; i += blockDim.x) d[i] = s[i];
+        for (int i = threadIdx.x; i < A.n_spec * A.n_surf; i += blockDim.x) at[i] = A.ior_at[i];
+    }
+    __syncthreads();
+    const int si = blockIdx.x;
+    const int gi = blockIdx.y * kPsfThreads + threadIdx.x;
+    if (si >= A.n_src || gi >= A.n_grid) return;
+    const gl_psf_source S = A.src[si];
+    const float2 uv = A.grid[gi];
+    const float bx = tanf(S.angle_x), by = tanf(S.angle_y);
+    const V3 dir = normalized(v3(bx, by, 1.0f));
+    const V3 org = v3(uv.x * A.front_R - kSpawnOffset * bx, uv.y * A.front_R - kSpawnOffset * by, A.start_z);
+    const int tx_min = S.tile_x0, ty_min = S.tile_y0, tx_max = S.tile_x0 + A.tile_w, ty_max = S.tile_y0 + A.tile_h;
+    for (int l = 0; l < A.n_spec; ++l)
+    {
+        const float4 sp = A.spec[l];
+        const TraceOut r = trace_primary(lens, A.n_surf, at + l * A.n_surf, org, dir, sp.x);
+        if (r.status != GL_TRACE_OK || !isfinite(r.x) || !isfinite(r.y)) continue;
+        const float tx = (r.x - S.chief_x_mm) / A.mm_per_pixel + (float)A.tile_w * 0.5f;
+        const float ty = (r.y - S.chief_y_mm) / A.mm_per_pixel + (float)A.tile_h * 0.5f;
+        const float margin = (float)(A.radius_px > 0 ? A.radius_px + 1 : 1);
+        if (tx < -margin || tx > (float)A.tile_w + margin || ty < -margin || ty > (float)A.tile_h + margin) continue;
+        const float px = tx + (float)S.tile_x0, py = ty + (float)S.tile_y0;
+        const float w = r.w * A.ray_weight;
+        const float lum = (S.r + S.g + S.b) * (1.0f / 3.0f) * sp.z * w;
+        const float cr = S.r * sp.y * w, cg = S.g * sp.z * w, cb = S.b * sp.w * w;
+        if (A.sigma_px <= 0.0f)
+        {
+            const int x0 = (int)floorf(px - 0.5f), y0 = (int)floorf(py - 0.5f);
+            const float fx = (px - 0.5f) - (float)x0, fy = (py - 0.5f) - (float)y0;
+            const float bw[4] = {(1.0f - fx) * (1.0f - fy), fx * (1.0f - fy), (1.0f - fx) * fy, fx * fy};
+            #pragma unroll
+            for (int k = 0; k < 4; ++k)
+            {
+                const int xi = x0 + (k & 1), yi = y0 + (k >> 1);
+                if (xi < tx_min || xi >= tx_max || yi < ty_min || yi >= ty_max || xi < 0 || xi >= A.comp_w ||
+                    yi < 0 || yi >= A.comp_h)
+                    continue;
+                deposit(A, yi * A.comp_w + xi, lum, cr, cg, cb, bw[k]);
+            }
+        }
+        else
+        {
+            const float inv2 = 1.0f / (2.0f * A.sigma_px * A.sigma_px);
+            const int cx = (int)floorf(px), cy = (int)floorf(py);
+            const float ox = px - ((float)cx + 0.5f), oy = py - ((float)cy + 0.5f);
+            const int R = A.radius_px;
+            float wsum = 0.0f;
+            for (int dy = -R; dy <= R; ++dy)
+            {
+                const float dyr = (float)dy - oy;
+                for (int dx = -R; dx <= R; ++dx)
+                {
+                    const float dxr = (float)dx - ox;
+                    wsum += expf(-(dxr * dxr + dyr * dyr) * inv2);
+                }
+            }
+            const float inv_wsum = wsum > 1e-20f ? 1.0f / wsum : 0.0f;
+            for (int dy = -R; dy <= R; ++dy)
+            {
+                const int yi = cy + dy;
+                if (yi < ty_min || yi >= ty_max || yi < 0 || yi >= A.comp_h) continue;
+                const float dyr = (float)dy - oy;
+                for (int dx = -R; dx <= R; ++dx)
+                {
+                    const int xi = cx + dx;
+                    if (xi < tx_min || xi >= tx_max || xi < 0 || xi >= A.comp_w) continue;
+                    const float dxr = (float)dx - ox;
+                    const float wt = expf(-(dxr * dxr + dyr * dyr) * inv2) * inv_wsum;
+                    if (wt < 1e-6f) continue;
+                    deposit(A, yi * A.comp_w + xi, lum, cr, cg, cb, wt);
+                }
+            }
+        }
+    }
+}
+
+}  // namespace
+}  // namespace gl
+
+using namespace gl;
+
+extern "C" int gl_psf_render(const gl_surface* surfaces, int n_surfaces, const gl_psf_source* sources, int n_sources,
+                             const gl_pupil_sample* grid, int n_grid, const gl_spectral_sample* spec, int n_spec,
+                             int tile_w, int tile_h, int composite_w, int composite_h, float mm_per_pixel,
+                             int monochromatic, float splat_sigma_px, int splat_radius_px, float* d_out_r,
+                             float* d_out_g, float* d_out_b, void* stream)
+{
+    if (!surfaces || n_surfaces <= 0) return fail(GL_ERR_INVALID, "psf_render: lens has no surfaces");
+    if (n_sources < 0 || n_grid < 0 || n_spec < 1 || (n_sources > 0 && !sources) || (n_grid > 0 && !grid) || !spec)
+        return fail(GL_ERR_INVALID, "psf_render: bad arguments");
+    if (tile_w <= 0 || tile_h <= 0 || composite_w <= 0 || composite_h <= 0 || !(mm_per_pixel > 0.0f))
+        return fail(GL_ERR_INVALID, "psf_render: grid and tile dimensions must be positive");
+    if ((long long)composite_w * composite_h > (1LL << 31)) return fail(GL_ERR_INVALID, "psf_render: too many pixels");
+    if (!d_out_r || (!monochromatic && (!d_out_g || !d_out_b))) return fail(GL_ERR_INVALID, "psf_render: null output");
+    if (splat_radius_px < 0 || splat_radius_px > 16) return fail(GL_ERR_INVALID, "psf_render: splat radius must be 0..16");
+    if (n_sources == 0 || n_grid == 0) return GL_OK;
+    std::vector<SurfRec> recs((size_t)n_surfaces);
+    int rc = pack_lens(surfaces, n_surfaces, recs.data());
+    if (rc) return rc;
+    std::vector<float> lams((size_t)n_spec), at((size_t)n_spec * n_surfaces), bf((size_t)n_spec * n_surfaces);
+    std::vector<float4> sp((size_t)n_spec);
+    for (int i = 0; i < n_spec; ++i)
+    {
+        lams[i] = spec[i].lambda;
+        sp[i] = make_float4(spec[i].lambda, spec[i].cmf_r, spec[i].cmf_g, spec[i].cmf_b);
+    }
+    build_ior_tables(surfaces, n_surfaces, lams.data(), n_spec, at.data(), bf.data());
+    cudaStream_t st = (cudaStream_t)stream;
+    SurfRec* d_recs = nullptr; float* d_at = nullptr; float4* d_spec = nullptr;
+    gl_psf_source* d_src = nullptr; float2* d_grid = nullptr;
+    cudaError_t e = cudaMalloc(&d_recs, recs.size() * sizeof(SurfRec));
+    if (e == cudaSuccess) e = cudaMalloc(&d_at, at.size() * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&d_spec, sp.size() * sizeof(float4));
+    if (e == cudaSuccess) e = cudaMalloc(&d_src, (size_t)n_sources * sizeof(gl_psf_source));
+    if (e == cudaSuccess) e = cudaMalloc(&d_grid, (size_t)n_grid * sizeof(float2));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_recs, recs.data(), recs.size() * sizeof(SurfRec), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_at, at.data(), at.size() * sizeof(float), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_spec, sp.data(), sp.size() * sizeof(float4), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_src, sources, (size_t)n_sources * sizeof(gl_psf_source), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_grid, grid, (size_t)n_grid * sizeof(float2), cudaMemcpyHostToDevice, st);
+    const size_t smem = recs.size() * sizeof(SurfRec) + at.size() * sizeof(float);
+    if (e == cudaSuccess && smem > 48 * 1024)
+        e = cudaFuncSetAttribute(psf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+    {
+        PsfArgs A;
+        A.recs = d_recs; A.ior_at = d_at; A.spec = d_spec; A.src = d_src; A.grid = d_grid;
+        A.n_surf = n_surfaces; A.n_spec = n_spec; A.n_src = n_sources; A.n_grid = n_grid;
+        A.front_R = surfaces[0].semi_aperture; A.start_z = surfaces[0].z - kSpawnOffset;
+        A.mm_per_pixel = mm_per_pixel; A.ray_weight = 1.0f / (float)n_grid;
+        A.tile_w = tile_w; A.tile_h = tile_h; A.comp_w = composite_w; A.comp_h = composite_h;
+        A.mono = monochromatic ? 1 : 0;
+        A.sigma_px = splat_sigma_px; A.radius_px = splat_radius_px;
+        A.out_r = d_out_r; A.out_g = d_out_g; A.out_b = d_out_b;
+        const dim3 g((unsigned)n_sources, (unsigned)((n_grid + kPsfThreads - 1) / kPsfThreads));
+        psf_kernel<<<g, kPsfThreads, smem, st>>>(A);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(d_recs); cudaFree(d_at); cudaFree(d_spec); cudaFree(d_src); cudaFree(d_grid);
+    if (e != cudaSuccess)
+        return fail(e == cudaErrorMemoryAllocation ? GL_ERR_OOM : GL_ERR_CUDA, std::string("psf_render: ") + cudaGetErrorString(e));
+    g_last_launches = 1;
+    return GL_OK;
+}

@@ -463,6 +463,41 @@ int gl_veil_plan_execute(gl_veil_plan* plan, const gl_veil_source* d_sources, in
                          float* d_out_b, void* stream);
 int gl_veil_plan_destroy(gl_veil_plan* plan);
 
+/* ---- PSF grid (render_psf: PSFRenderer.cpp:243-465, psf_render.cu) --------
+ * Per source, the lens's primary-ray spot in its own tile of a composite
+ * atlas.  gl_psf_prepass centres each tile (host, float32, the reference's
+ * arithmetic): CHIEF_CENTROID = the unweighted 7 x 7 pupil-mean landing;
+ * FIXED_TARGET = the chief ray aimed at (target_x, target_y) mm by 2x2
+ * Newton, with the survivor-mean and tracked-window fallbacks.
+ * sources7: per source [angle_x, angle_y, r, g, b, target_x_mm, target_y_mm]. */
+#define GL_PSF_CENTER_CHIEF_CENTROID 0
+#define GL_PSF_CENTER_FIXED_TARGET   1
+#define GL_PSF_CELL_OK               0
+#define GL_PSF_CELL_CHIEF_VIGNETTED  1
+#define GL_PSF_CELL_DARK             2
+typedef struct gl_psf_cell {
+    float beam_ax, beam_ay;          /* field direction the tile's rays are traced at */
+    float chief_x_mm, chief_y_mm;    /* tile centre on the sensor                     */
+    int32_t status;                  /* GL_PSF_CELL_*                                 */
+    float pupil_fraction;
+    float aim_residual_mm;
+} gl_psf_cell;
+int gl_psf_prepass(const gl_surface* surfaces, int n_surfaces, const float* sources7, int n_sources,
+                   int center_mode, gl_psf_cell* out);
+typedef struct gl_psf_source {
+    float angle_x, angle_y, r, g, b, chief_x_mm, chief_y_mm;
+    int32_t tile_x0, tile_y0;
+} gl_psf_source;
+/* Accumulates into caller-zeroed planes (d_out_g/b unused when monochromatic);
+ * splat_sigma_px <= 0: bilinear; else a normalised Gaussian of radius
+ * splat_radius_px (<= 16).  Synchronous. */
+int gl_psf_render(const gl_surface* surfaces, int n_surfaces, const gl_psf_source* sources,
+                  int n_sources, const gl_pupil_sample* grid, int n_grid,
+                  const gl_spectral_sample* spec, int n_spec, int tile_w, int tile_h,
+                  int composite_w, int composite_h, float mm_per_pixel, int monochromatic,
+                  float splat_sigma_px, int splat_radius_px, float* d_out_r, float* d_out_g,
+                  float* d_out_b, void* stream);
+
 /* Number of kernel launches issued by the last device call on this thread. */
 int gl_last_launch_count(void);
 
