@@ -161,6 +161,11 @@ def run_gpu(args, rank, world):
     tune_ghost_plan(plan, outs, stream=stream, tuner=tuner)
 
     # ---- batched form: graph-captured launch ----
+    # Events around the render launch are captured into the graph (external
+    # event-record nodes), so every timed replay also times the render kernel
+    # alone on its own stream.
+    kev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    plan.set_timing(*kev)
     with torch.cuda.stream(stream):
         for _ in range(2):
             plan.execute(*outs, stream=stream.cuda_stream)
@@ -169,7 +174,7 @@ def run_gpu(args, rank, world):
         with torch.cuda.graph(graph, stream=stream):
             launches_per_step = plan.execute(*outs, stream=stream.cuda_stream)
 
-    def timed(fn, steps, warm):
+    def timed(fn, steps, warm, after=None):
         with torch.cuda.stream(stream):
             for _ in range(warm):
                 fn()
@@ -184,14 +189,24 @@ def run_gpu(args, rank, world):
                 e1.record(stream)
                 e1.synchronize()
                 ts.append(e0.elapsed_time(e1) / 1e3)
+                if after is not None:
+                    after()
         return ts
+
+    kernel_ms = {"probe": [], "render": []}
+
+    def read_kernel_events():
+        kernel_ms["probe"].append(kev[0].elapsed_time(kev[1]))
+        kernel_ms["render"].append(kev[1].elapsed_time(kev[2]))
 
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
     with ClockSampler(dev.index) as clk:
-        t_batched = timed(graph.replay, args.steps, args.warmup)
+        t_batched = timed(graph.replay, args.steps, args.warmup, after=read_kernel_events)
     torch.cuda.synchronize()
+    plan.set_timing()
+    traced_render, traced_probe = plan.traced_split()
     if args.quick:
         t_plain = [float("nan")]
     else:
@@ -250,6 +265,9 @@ def run_gpu(args, rank, world):
                    "pairs": int(len(plan.pairs)), "grid_sides": plan.grid_sides,
                    "l2": "flushed (512 MB write) between timed steps", "parallelism": "replicas"},
         "rays_per_s": rays_per_s,
+        "kernel_ms": {"render": float(np.mean(kernel_ms["render"])), "probe": float(np.mean(kernel_ms["probe"])),
+                      "how": "CUDA events captured into the replayed graph around each launch, every timed step"},
+        "traces_render": traced_render, "traces_probe": traced_probe,
         "ray_lambda_traces_per_frame": traced,
         "frame_ray_lambda_before_cull": plan.rays,
         "plain_per_pair": {"value": plain_fps, "unit": UNIT, "ms_per_step": 1e3 / plain_fps,
@@ -494,7 +512,8 @@ def run_serving(args):
     srv.run_trace([FlareRequest(lens_id=i, width=512, height=512, n_spec=8, ray_grid=32, field_deg=5.0, rid=i)
                    for i in pool])
     torch.cuda.synchronize()
-    srv = FlareServer(pool, budget_bytes=SERVE_BUDGET, max_inflight=args.serve_slots, items_per_warp=8)
+    srv = FlareServer(pool, budget_bytes=SERVE_BUDGET, max_inflight=args.serve_slots, items_per_warp=8,
+                      policy=args.serve_policy)
     srv.exec.prewarm([(w, w) for w in (512, 1024, 2048, 4096)], 8)
     with ClockSampler(torch.cuda.current_device()) as clk:
         t1 = time.perf_counter()
@@ -536,8 +555,9 @@ def run_serving(args):
         rl.close()
     return {"workload": "Poisson %.0f req/s for %.0f s (%d requests), %d resident lenses of 8-30 surfaces, "
                         "outputs 512^2-4096^2, 8/16/31 wavelengths, pupil grids 32^2-256^2, field 0-20 deg, "
-                        "%d slots, %.0f GB HBM budget" % (SERVE_RATE, args.serve_seconds, len(reqs), SERVE_LENSES,
-                                                          args.serve_slots, SERVE_BUDGET / 1e9),
+                        "%d slots, %.0f GB HBM budget, %s priorities" % (
+                            SERVE_RATE, args.serve_seconds, len(reqs), SERVE_LENSES, args.serve_slots,
+                            SERVE_BUDGET / 1e9, args.serve_policy),
             "throughput_req_s": served_req_s, "wall_s": wall, "offered_req_s": len(reqs) / args.serve_seconds,
             "rays_per_s": traced / wall, "ray_lambda_traces": traced,
             "latency_all": latency_stats(reqs), "latency_by_size": by_size,
@@ -762,6 +782,8 @@ def main():
                     help="batched timing only (no plain / e2e / CPU legs): for profiler runs")
     ap.add_argument("--serve-seconds", type=float, default=30.0)
     ap.add_argument("--serve-slots", type=int, default=32)
+    ap.add_argument("--serve-policy", default="sjf", choices=("sjf", "lsf"),
+                    help="stream priority of a request: shortest first, or longest (least slack) first")
     ap.add_argument("--serial-sample", type=int, default=40)
     ap.add_argument("--serve-dump", default="", help="write per-request timings (CSV) here")
     ap.add_argument("--only", default="all", choices=["all", "cfg3", "serve", "sweep"],
@@ -806,18 +828,23 @@ def main():
 
 
 def roofline(res, plan):
-    """Dominant kernel: ghost_render_kernel, bound by FP32 issue on the CUDA
-    cores (the trace is sequential FP32 arithmetic; the splat is a small
-    share).  Algorithmic FLOPs = traced ray-wavelengths x the per-trace FP32
-    operation count measured once with ncu on this workload."""
+    """Dominant kernel: ghost_render_kernel (render launch), bound by FP32
+    issue on the CUDA cores (the trace is sequential FP32 arithmetic; the
+    splat is a small share).  Algorithmic FLOPs per launch = the launch's
+    traced ray-wavelengths x the per-trace FP32 operation count measured once
+    with ncu on this workload; duration = the launch's CUDA-event time in the
+    timed replays."""
     flops_per_trace = FLOPS_PER_RAY_LAMBDA
     peak = FP32_PEAK_TFLOPS
-    sec = res["ms_per_step"] / 1e3
-    achieved = res["ray_lambda_traces_per_frame"] * flops_per_trace / sec / 1e12 if flops_per_trace else None
+    sec = res["kernel_ms"]["render"] / 1e3
+    achieved = res["traces_render"] * flops_per_trace / sec / 1e12 if (flops_per_trace and sec > 0) else None
     return {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-            "frac": (achieved / peak) if (achieved and peak) else None, "traffic": None,
-            "kernel": "ghost_render_kernel",
-            "peak_note": "GB300 FP32 CUDA-core peak: 152 SMs x 128 lanes x 2 FLOP x max SM clock"}
+            "frac": (achieved / peak) if (achieved and peak) else None, "traffic": RENDER_DRAM_BYTES,
+            "kernel": "ghost_render_kernel", "kernel_ms": res["kernel_ms"]["render"],
+            "flop_per_launch": res["traces_render"] * flops_per_trace,
+            "peak_note": "GB300 FP32 CUDA-core peak: 152 SMs x 128 lanes x 2 FLOP x max SM clock",
+            "traffic_note": "DRAM bytes of one render launch from ncu (dram__bytes.sum.per_second x "
+                            "gpu__time_duration on this frame): the image accumulator stays in L2"}
 
 
 # FP32 operations per traced ray-wavelength (FADD + FMUL + 2 x FFMA, thread
@@ -825,6 +852,9 @@ def roofline(res, plan):
 # once with ncu (smsp__sass_thread_inst_executed_op_{fadd,fmul,ffma}_pred_on:
 # 2.02e11 FLOP over 1.793e8 traces) and frozen as the algorithmic count.
 FLOPS_PER_RAY_LAMBDA = 1126.0
+# DRAM bytes (read + write) of one render launch on this frame, from one ncu
+# capture: 7.285 GB/s x 5.936 ms.
+RENDER_DRAM_BYTES = 43.2e6
 FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.070e9 / 1e12
 
 

@@ -190,6 +190,10 @@ __device__ __forceinline__ float mgf2_reflectance(float cos_i, float n1, float n
 }
 
 // One surface interaction on the lane's ray; false when the ray died.
+// WEIGHT = false skips the energy weight: whether a ray dies (missed,
+// clipped, TIR) is geometry only (trace_cuda.h sets the status from geometry
+// alone), so the off-sensor probe needs none of it.
+template <bool WEIGHT>
 __device__ __forceinline__ bool surface_step(V3& o, V3& d, const HotRec& h, const SurfRec& s, float lam,
                                              float kdelta, float n2, bool reflecting, float reflect_ior,
                                              float& cur, float& w)
@@ -219,9 +223,12 @@ __device__ __forceinline__ bool surface_step(V3& o, V3& d, const HotRec& h, cons
     const bool simple = (h.bits & HB_SIMPLE) != 0;
     if (reflecting)
     {
-        w *= simple ? mgf2_reflectance(fabsf(dot(nrm, d)), n1, n2, h.ar_layers, kdelta)
-                    : weight_general(d, nrm, n1, n2, s, lam, true);
-        if (h.bits & HB_ATTEN) w *= attenuator_general(hit, s);
+        if (WEIGHT)
+        {
+            w *= simple ? mgf2_reflectance(fabsf(dot(nrm, d)), n1, n2, h.ar_layers, kdelta)
+                        : weight_general(d, nrm, n1, n2, s, lam, true);
+            if (h.bits & HB_ATTEN) w *= attenuator_general(hit, s);
+        }
         d = reflect(d, nrm);
         cur = reflect_ior;
     }
@@ -229,9 +236,12 @@ __device__ __forceinline__ bool surface_step(V3& o, V3& d, const HotRec& h, cons
     {
         V3 nd;
         if (!refract(d, nrm, n1, n2, nd)) return false;
-        w *= simple ? 1.0f - mgf2_reflectance(fabsf(dot(nrm, d)), n1, n2, h.ar_layers, kdelta)
-                    : weight_general(d, nrm, n1, n2, s, lam, false);
-        if (h.bits & HB_ATTEN) w *= attenuator_general(hit, s);
+        if (WEIGHT)
+        {
+            w *= simple ? 1.0f - mgf2_reflectance(fabsf(dot(nrm, d)), n1, n2, h.ar_layers, kdelta)
+                        : weight_general(d, nrm, n1, n2, s, lam, false);
+            if (h.bits & HB_ATTEN) w *= attenuator_general(hit, s);
+        }
         d = nd;
         cur = n2;
     }
@@ -297,6 +307,9 @@ __device__ __forceinline__ void trace_warp(const RenderArgs& A, const SurfRec* l
     #pragma unroll 1
     for (int li = 0; li < A.n_spec; ++li)
     {
+        // probe: stop once any warp has found the pair on the sensor (read
+        // through L2, where the other warps' atomics land)
+        if (PROBE && li > 0 && A.pair_hits != nullptr && __ldcg(A.pair_hits + pair) > 0) break;
         ++n_lambda;
         const float4 sp = spec[li];
         const float kdelta = kdel[li];
@@ -318,7 +331,7 @@ __device__ __forceinline__ void trace_warp(const RenderArgs& A, const SurfRec* l
             if (!(hr.bits & HB_ACTIVE)) continue;
             n2 = back ? bfl[s] : atl[s];
             const float rior = (back && refl) ? atl[a] : cur;
-            if (alive) alive = surface_step(o, d, hr, lens[s], sp.x, kdelta, n2, refl, rior, cur, w);
+            if (alive) alive = surface_step<!PROBE>(o, d, hr, lens[s], sp.x, kdelta, n2, refl, rior, cur, w);
         }
         if (PROBE)
         {
@@ -427,7 +440,7 @@ __global__ void __launch_bounds__(kRenderThreads, kRenderMinBlocks) ghost_render
         {
             // render: skip pairs the probe found off-sensor; probe passes
             // after the first: skip pairs already known to be on-sensor
-            const int h = A.pair_hits[w.x];
+            const int h = PROBE ? __ldcg(A.pair_hits + w.x) : A.pair_hits[w.x];
             if (PROBE ? (h > 0) : (h == 0)) continue;
         }
         PairDev P = A.pairs[w.x];
@@ -514,7 +527,9 @@ struct GhostPlan {
     int* probe_counters = nullptr;
     int* pair_hits_init = nullptr;          // 1 = not probed (always rendered), 0 = probed
     long long probe_rays = 0;
-    unsigned long long* traced = nullptr;   // traces executed by the last execute
+    unsigned long long* traced = nullptr;   // [render, probe] traces executed by the last execute
+    // optional timing events recorded around the probe and render launches
+    cudaEvent_t ev_probe = nullptr, ev_render = nullptr, ev_end = nullptr;
 };
 
 static void plan_free(GhostPlan* p)
@@ -766,7 +781,7 @@ int plan_create(const gl_surface* surfaces, int n_surf, const gl_ghost_pair* pai
     chk(upload(&p->sources, src.data(), src.size()));
     chk(upload(&p->samples, reinterpret_cast<const float2*>(ordered.data()), (size_t)n_samples));
     chk(cudaMalloc(&p->counter, sizeof(int)));
-    chk(cudaMalloc(&p->traced, sizeof(unsigned long long)));
+    chk(cudaMalloc(&p->traced, 2 * sizeof(unsigned long long)));
     if (p->cull)
     {
         chk(upload(&p->probe_items, pitems.data(), pitems.size()));
@@ -808,6 +823,17 @@ int plan_set_launch(GhostPlan* p, int items_per_warp, int ctas_per_sm)
     return GL_OK;
 }
 
+// An event recorded inside a stream capture becomes an event-record node
+// (external), so a replayed graph records it too.
+static cudaError_t record_event(cudaEvent_t ev, cudaStream_t st)
+{
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaError_t e = cudaStreamIsCapturing(st, &cs);
+    if (e != cudaSuccess) return e;
+    return cs == cudaStreamCaptureStatusActive ? cudaEventRecordWithFlags(ev, st, cudaEventRecordExternal)
+                                               : cudaEventRecord(ev, st);
+}
+
 int plan_execute(GhostPlan* p, float* d_out_r, float* d_out_g, float* d_out_b, cudaStream_t st)
 {
     if (!p || !d_out_r || !d_out_g || !d_out_b) return fail(GL_ERR_INVALID, "render_ghosts: null output");
@@ -827,7 +853,8 @@ int plan_execute(GhostPlan* p, float* d_out_r, float* d_out_g, float* d_out_b, c
     A.front_R = p->front_R; A.start_z = p->start_z;
     A.pair_hits = nullptr;
     A.traced = p->traced;
-    GL_CUDA_TRY(cudaMemsetAsync(p->traced, 0, sizeof(unsigned long long), st));
+    GL_CUDA_TRY(cudaMemsetAsync(p->traced, 0, 2 * sizeof(unsigned long long), st));
+    if (p->ev_probe) GL_CUDA_TRY(record_event(p->ev_probe, st));
     if (p->cull && p->n_items > 0)
     {
         // Probe passes: the frame inflated by CULL_MARGIN = 1.25
@@ -843,6 +870,7 @@ int plan_execute(GhostPlan* p, float* d_out_r, float* d_out_g, float* d_out_b, c
         B.samples = p->probe_samples;
         B.items = p->probe_items;
         B.pair_hits = p->pair_hits;
+        B.traced = p->traced + 1;
         B.hw2 = 2.0f * (p->prm.sensor_half_w * 1.25f);
         B.hh2 = 2.0f * (p->prm.sensor_half_h * 1.25f);
         const int warps_per_block = kRenderThreads / 32;
@@ -859,6 +887,7 @@ int plan_execute(GhostPlan* p, float* d_out_r, float* d_out_g, float* d_out_b, c
         GL_CUDA_TRY(cudaGetLastError());
         A.pair_hits = p->pair_hits;
     }
+    if (p->ev_render) GL_CUDA_TRY(record_event(p->ev_render, st));
     if (p->n_items > 0)
     {
         if (p->prm.plain_per_pair)
@@ -893,6 +922,7 @@ int plan_execute(GhostPlan* p, float* d_out_r, float* d_out_g, float* d_out_b, c
             ++launches;
         }
     }
+    if (p->ev_end) GL_CUDA_TRY(record_event(p->ev_end, st));
     const float* C = p->prm.correction;
     const size_t quads = (n_px + 3) / 4;
     const int fb = 256;
@@ -1019,9 +1049,28 @@ int gl_ghost_plan_info(const gl_ghost_plan* plan, long long* rays, int* n_items,
 int gl_ghost_plan_traced(const gl_ghost_plan* plan, long long* out)
 {
     if (!plan || !out) return fail(GL_ERR_INVALID, "ghost_plan_traced: bad arguments");
-    unsigned long long v = 0;
-    GL_CUDA_TRY(cudaMemcpy(&v, plan->p->traced, sizeof(v), cudaMemcpyDeviceToHost));
-    *out = (long long)v;
+    unsigned long long v[2] = {0, 0};
+    GL_CUDA_TRY(cudaMemcpy(v, plan->p->traced, sizeof(v), cudaMemcpyDeviceToHost));
+    *out = (long long)(v[0] + v[1]);
+    return GL_OK;
+}
+
+int gl_ghost_plan_traced_split(const gl_ghost_plan* plan, long long* render, long long* probe)
+{
+    if (!plan) return fail(GL_ERR_INVALID, "ghost_plan_traced_split: null plan");
+    unsigned long long v[2] = {0, 0};
+    GL_CUDA_TRY(cudaMemcpy(v, plan->p->traced, sizeof(v), cudaMemcpyDeviceToHost));
+    if (render) *render = (long long)v[0];
+    if (probe) *probe = (long long)v[1];
+    return GL_OK;
+}
+
+int gl_ghost_plan_set_timing(gl_ghost_plan* plan, void* ev_probe, void* ev_render, void* ev_end)
+{
+    if (!plan) return fail(GL_ERR_INVALID, "ghost_plan_set_timing: null plan");
+    plan->p->ev_probe = (cudaEvent_t)ev_probe;
+    plan->p->ev_render = (cudaEvent_t)ev_render;
+    plan->p->ev_end = (cudaEvent_t)ev_end;
     return GL_OK;
 }
 

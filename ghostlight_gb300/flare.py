@@ -279,6 +279,24 @@ class GhostRenderPlan:
         _native.check(self._lib.gl_ghost_plan_traced(self._h, C.byref(v)), "traced")
         return int(v.value)
 
+    def traced_split(self):
+        """(render, probe) ray-wavelength traces of the last execute."""
+        r, q = C.c_longlong(), C.c_longlong()
+        _native.check(self._lib.gl_ghost_plan_traced_split(self._h, C.byref(r), C.byref(q)), "traced_split")
+        return int(r.value), int(q.value)
+
+    def set_timing(self, ev_probe=None, ev_render=None, ev_end=None):
+        """torch.cuda.Event objects (enable_timing=True; None = none) that every
+        later execute records before the probe launch, before the render launch
+        and after it: ev_render.elapsed_time(ev_end) is the render kernel alone."""
+        h = []
+        for e in (ev_probe, ev_render, ev_end):
+            if e is not None and not e.cuda_event:
+                e.record()                       # torch creates its event on first record
+            h.append(None if e is None else e.cuda_event)
+        _native.check(self._lib.gl_ghost_plan_set_timing(self._h, *h), "set_timing")
+        self._timing = (ev_probe, ev_render, ev_end)     # keep the events alive
+
     def pair_hits(self):
         """Probe hits per pair from the last execute (0 = culled)."""
         out = (C.c_int32 * max(1, self.n_pairs))()

@@ -10,7 +10,7 @@ its own CUDA stream, and its kernels share the SMs with theirs.  Requests run
 as short CTAs (``items_per_warp`` items of 32 pupil samples per warp), so the
 CTA scheduler interleaves them at CTA boundaries, preferring streams of higher
 priority; the priority is the request's estimated trace count (shortest job
-first).  Every request's device memory comes from a stream-ordered pool, and
+first by default; ``policy="lsf"`` reverses it).  Every request's device memory comes from a stream-ordered pool, and
 nothing on the request path synchronises the device.
 
 The reference has no serving layer: it renders one flare per blocking call
@@ -109,17 +109,24 @@ class Scheduler:
         assert self.used >= 0 and self.inflight >= 0
 
 
-def priority_class(est_rays: int, rays_per_s: float = 7e9) -> int:
-    """Stream priority from the estimated service time (lower = sooner):
-    < 1 ms -> -3, < 4 ms -> -2, < 16 ms -> -1, else 0."""
+POLICIES = ("sjf", "lsf")
+
+
+def priority_class(est_rays: int, rays_per_s: float = 7e9, policy: str = "sjf") -> int:
+    """Stream priority (lower = sooner) from the estimated service time class
+    c: < 1 ms -> 0, < 4 ms -> 1, < 16 ms -> 2, else 3.
+
+    sjf (shortest job first): priority c - 3, so short requests overtake long
+    ones; the tail is the long requests, starved while short ones keep coming.
+    lsf (least slack first, for a common latency target): priority -c, so a
+    long request, whose service time alone is closest to the target, takes the
+    SMs first and short ones fill the CTA slots it leaves; the tail is the
+    short requests that arrive behind a long one."""
+    if policy not in POLICIES:
+        raise ValueError("priority policy must be one of %s" % (POLICIES,))
     t = est_rays / rays_per_s
-    if t < 1e-3:
-        return -3
-    if t < 4e-3:
-        return -2
-    if t < 16e-3:
-        return -1
-    return 0
+    c = 0 if t < 1e-3 else 1 if t < 4e-3 else 2 if t < 16e-3 else 3
+    return c - 3 if policy == "sjf" else -c
 
 
 def request_bytes(width: int, height: int, n_pairs: int, host_copy: bool = True) -> int:
@@ -226,8 +233,11 @@ class CudaExecutor:
     LEVELS = (0, -1, -2, -3)
 
     def __init__(self, lenses: Dict[int, ResidentLens], max_inflight: int, items_per_warp: int = 8,
-                 host_output: bool = True, device=None):
+                 host_output: bool = True, device=None, policy: str = "sjf"):
         import torch
+        if policy not in POLICIES:
+            raise ValueError("priority policy must be one of %s" % (POLICIES,))
+        self.policy = policy
         self.torch = torch
         self._lib = _native.load()
         self.lenses = lenses
@@ -253,7 +263,7 @@ class CudaExecutor:
         rl = self.lenses[req.lens_id]
         masked = 0.8 * req.ray_grid * req.ray_grid
         req.est_rays = int(rl.n_pairs * masked * req.n_spec)
-        req.priority = priority_class(req.est_rays)
+        req.priority = priority_class(req.est_rays, policy=self.policy)
         req.device_bytes = request_bytes(req.width, req.height, rl.n_pairs)
 
     def _pinned_buf(self, shape):
@@ -335,11 +345,11 @@ class FlareServer:
 
     def __init__(self, lenses: Dict[int, ResidentLens], budget_bytes: int = 120 * 10 ** 9,
                  max_inflight: int = 16, items_per_warp: int = 8, host_output: bool = True,
-                 executor=None, clock: Callable[[], float] = time.perf_counter):
+                 executor=None, clock: Callable[[], float] = time.perf_counter, policy: str = "sjf"):
         self.lenses = lenses
         self.sched = Scheduler(budget_bytes, max_inflight)
         self.exec = executor if executor is not None else CudaExecutor(lenses, max_inflight, items_per_warp,
-                                                                       host_output)
+                                                                       host_output, policy=policy)
         self.clock = clock
         self.t0 = clock()
         self.running: list = []             # (request, executor handle)

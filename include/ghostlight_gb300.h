@@ -265,6 +265,15 @@ int gl_ghost_plan_set_launch(gl_ghost_plan* plan, int items_per_warp, int ctas_p
 /* Ray-wavelength traces the last execute ran (render + cull probes; a probe
  * warp stops at its first on-sensor hit).  Synchronous. */
 int gl_ghost_plan_traced(const gl_ghost_plan* plan, long long* out);
+/* The same count split into the render launch and the off-sensor probe
+ * launch.  Synchronous.  (No counterpart in the reference.) */
+int gl_ghost_plan_traced_split(const gl_ghost_plan* plan, long long* render, long long* probe);
+/* Optional cudaEvent_t handles (NULL = none) that every later execute records
+ * on its stream before the probe launch, before the render launch and after
+ * the render launch, so a caller can time the render kernel alone with
+ * cudaEventElapsedTime.  Inside a stream capture they become external
+ * event-record nodes.  (No counterpart in the reference.) */
+int gl_ghost_plan_set_timing(gl_ghost_plan* plan, void* ev_probe, void* ev_render, void* ev_end);
 /* Per-pair probe hit counts of the last execute (0 = culled); all 1 when the
  * plan does not cull.  Synchronous. */
 int gl_ghost_plan_pair_hits(const gl_ghost_plan* plan, int32_t* out, int n);

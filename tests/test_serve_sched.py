@@ -106,6 +106,17 @@ def test_priority_is_shortest_job_first():
     assert priority_class(1e5) < priority_class(1e7) < priority_class(1e8) <= priority_class(1e10)
 
 
+def test_priority_least_slack_first_reverses():
+    ests = (1e5, 1e7, 1e8, 1e10)
+    sjf = [priority_class(e, policy="sjf") for e in ests]
+    lsf = [priority_class(e, policy="lsf") for e in ests]
+    assert lsf[0] > lsf[1] > lsf[2] > lsf[3]
+    assert all(-3 <= p <= 0 for p in sjf + lsf)
+    assert [a + b for a, b in zip(sjf, lsf)] == [-3] * 4
+    with pytest.raises(ValueError):
+        priority_class(1e5, policy="fifo")
+
+
 def test_latency_stats():
     rs = []
     for i in range(100):
