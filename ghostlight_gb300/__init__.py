@@ -19,6 +19,7 @@ from .psf import ConvPlan, convolve_psf, synthetic_psf_kernel
 from .apertures import curved_blade_mask
 from .psf_grid import render_psf
 from .veil import render_veil
+from .lensfile import lens_format_version, load_lens, save_lens
 
 __version__ = "0.1.0"
 

@@ -43,7 +43,6 @@ UNITS = {
 }
 # Occupancy target of the render kernel (CTAs of 128 threads per SM); an
 # environment override lets a tuning sweep rebuild with another value.
-# Render occupancy target (CTAs of 128 threads per SM) for tuning sweeps.
 for _var in ("GL_RENDER_MIN_BLOCKS",):
     if os.environ.get(_var):
         UNITS["gl_ghost.cu"] = UNITS["gl_ghost.cu"] + ["-D%s=%d" % (_var, int(os.environ[_var]))]

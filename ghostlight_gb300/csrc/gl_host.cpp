@@ -457,6 +457,25 @@ int gl_finalize_z(gl_surface* s, int n)
     return GL_OK;
 }
 
+// Element rotation of the lens-file loader (make_rotation,
+// optical_system.cpp:185-199): R = Ry(tilt_y) Rx(tilt_x) Rz(roll), row-major,
+// float arithmetic with the C library's float cosine and sine.
+int gl_euler_rotation(float tilt_x_deg, float tilt_y_deg, float roll_deg, float* out)
+{
+    if (!out) return fail(GL_ERR_INVALID, "euler_rotation: null output");
+    const float kPi = 3.14159265358979323846f;
+    const float tx = tilt_x_deg * (kPi / 180.0f);
+    const float ty = tilt_y_deg * (kPi / 180.0f);
+    const float rz = roll_deg * (kPi / 180.0f);
+    const float cx = std::cos(tx), sx = std::sin(tx);
+    const float cy = std::cos(ty), sy = std::sin(ty);
+    const float cz = std::cos(rz), sz = std::sin(rz);
+    out[0] = cy * cz + sy * sx * sz;  out[1] = -cy * sz + sy * sx * cz;  out[2] = sy * cx;
+    out[3] = cx * sz;                 out[4] = cx * cz;                  out[5] = -sx;
+    out[6] = -sy * cz + cy * sx * sz; out[7] = sy * sz + cy * sx * cz;   out[8] = cy * cx;
+    return GL_OK;
+}
+
 int gl_enumerate_ghost_pairs(const gl_surface* s, int n, gl_ghost_pair* out, int cap, int* n_out)
 {
     if (!s || n <= 0 || !n_out) return fail(GL_ERR_INVALID, "enumerate_ghost_pairs: bad arguments");

@@ -191,6 +191,20 @@ class OpticalSystem:
             self.surfaces.append(s if isinstance(s, Surface) else Surface(s))
         self._calib = None
         self._calib_key = None
+        self.unsupported = []           # (surface index, feature) a lens file used that this build lacks
+        self.source_path = None
+
+    @classmethod
+    def load(cls, path) -> "OpticalSystem":
+        """Load a ``ghostlight-optical`` lens file (optical_system.py:90,
+        OpticalSystem::load at optical_system.cpp:1342)."""
+        from .lensfile import load_lens
+        return load_lens(path)
+
+    def save(self, path) -> None:
+        """Write this lens as a ``ghostlight-optical`` file (optical_system.py:252)."""
+        from .lensfile import save_lens
+        save_lens(self, path, self.name)
 
     @classmethod
     def from_records(cls, recs, name: str = "", focal_length: float = 0.0):

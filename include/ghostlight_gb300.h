@@ -142,6 +142,11 @@ int         gl_version(void);
  * lays z so the chain ends at the sensor (z = 0). */
 int gl_finalize_z(gl_surface* surfaces, int n);
 
+/* make_rotation, ghostlight/src/optical_system.cpp:185-199 — the element
+ * rotation R = Ry(tilt_y) Rx(tilt_x) Rz(roll) of the lens-file loader
+ * (row-major 3x3 into out[9]; float arithmetic, C library cosf/sinf). */
+int gl_euler_rotation(float tilt_x_deg, float tilt_y_deg, float roll_deg, float* out);
+
 /* enumerate_ghost_pairs, ghostlight/src/ghost.cpp:17-31 */
 int gl_enumerate_ghost_pairs(const gl_surface* surfaces, int n,
                              gl_ghost_pair* out, int cap, int* n_out);
