@@ -51,6 +51,7 @@ def _declare(lib):
     lib.gl_ghost_plan_traced.argtypes = [vp, P(C.c_longlong)]
     lib.gl_ghost_plan_traced_split.argtypes = [vp, P(C.c_longlong), P(C.c_longlong)]
     lib.gl_ghost_plan_set_timing.argtypes = [vp, vp, vp, vp]
+    lib.gl_morton_order.argtypes = [P(gl_pupil_sample), i, P(gl_pupil_sample)]
     lib.gl_ghost_plan_set_launch.argtypes = [vp, i, i]
     lib.gl_gemm_bf16_tc.argtypes = [vp, vp, vp, i, i, i, vp]
     d = C.c_double

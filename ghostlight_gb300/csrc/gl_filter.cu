@@ -19,6 +19,7 @@
 
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 namespace gl {
@@ -97,6 +98,20 @@ filter_probe_kernel(const SurfRec* __restrict__ recs, int n, const float* __rest
 
 using namespace gl;
 
+// Device scratch of the filter, kept per device and grown on demand (never
+// shrunk): a per-call cudaMalloc/cudaFree pair would cost a device-wide
+// synchronisation each call, stalling whatever other streams have in flight
+// (the reference keeps its ghost buffers in a leaked cache for the same
+// reason, ghost_render.cu:505-510).  The mutex serialises callers; each call
+// finishes its copies before it returns.
+namespace {
+std::mutex g_scratch_mu;
+struct Scratch { void* ptr = nullptr; size_t bytes = 0; };
+Scratch g_scratch[64];
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+}  // namespace
+
 extern "C" int gl_filter_ghost_pairs(const gl_surface* surfaces, int n, float hw, float hh,
                                      const gl_filter_params* prm, gl_ghost_pair* out_pairs,
                                      float* out_boosts, float* out_fp, int cap, int* n_out,
@@ -130,16 +145,32 @@ extern "C" int gl_filter_ghost_pairs(const gl_surface* surfaces, int n, float hw
         std::vector<float> at(3 * (size_t)n), bf(3 * (size_t)n);
         build_ior_tables(surfaces, n, lams, 3, at.data(), bf.data());
         const int np = (int)cand.size();
-        SurfRec* d_recs = nullptr; float* d_at = nullptr; float* d_bf = nullptr;
-        int2* d_pairs = nullptr; ProbeOut* d_out = nullptr;
         std::vector<ProbeOut> res((size_t)np);
         cudaError_t e = cudaSuccess;
         auto chk = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
-        chk(cudaMalloc(&d_recs, sizeof(SurfRec) * n));
-        chk(cudaMalloc(&d_at, sizeof(float) * 3 * n));
-        chk(cudaMalloc(&d_bf, sizeof(float) * 3 * n));
-        chk(cudaMalloc(&d_pairs, sizeof(int2) * np));
-        chk(cudaMalloc(&d_out, sizeof(ProbeOut) * np));
+        const size_t o_at = align256(sizeof(SurfRec) * n), o_bf = o_at + align256(sizeof(float) * 3 * n);
+        const size_t o_pairs = o_bf + align256(sizeof(float) * 3 * n);
+        const size_t o_out = o_pairs + align256(sizeof(int2) * np);
+        const size_t need = o_out + align256(sizeof(ProbeOut) * np);
+        int dev = 0;
+        chk(cudaGetDevice(&dev));
+        if (e == cudaSuccess && (dev < 0 || dev >= 64)) e = cudaErrorInvalidDevice;
+        std::unique_lock<std::mutex> lock(g_scratch_mu);
+        Scratch& sc = g_scratch[e == cudaSuccess ? dev : 0];
+        if (e == cudaSuccess && sc.bytes < need)
+        {
+            if (sc.ptr) cudaFree(sc.ptr);
+            sc.ptr = nullptr;
+            sc.bytes = 0;
+            chk(cudaMalloc(&sc.ptr, need));
+            if (e == cudaSuccess) sc.bytes = need;
+        }
+        char* base = static_cast<char*>(sc.ptr);
+        SurfRec* d_recs = reinterpret_cast<SurfRec*>(base);
+        float* d_at = reinterpret_cast<float*>(base + o_at);
+        float* d_bf = reinterpret_cast<float*>(base + o_bf);
+        int2* d_pairs = reinterpret_cast<int2*>(base + o_pairs);
+        ProbeOut* d_out = reinterpret_cast<ProbeOut*>(base + o_out);
         if (e == cudaSuccess)
         {
             chk(cudaMemcpy(d_recs, recs.data(), sizeof(SurfRec) * n, cudaMemcpyHostToDevice));
@@ -155,7 +186,7 @@ extern "C" int gl_filter_ghost_pairs(const gl_surface* surfaces, int n, float hw
             chk(cudaGetLastError());
             chk(cudaMemcpy(res.data(), d_out, sizeof(ProbeOut) * np, cudaMemcpyDeviceToHost));
         }
-        cudaFree(d_recs); cudaFree(d_at); cudaFree(d_bf); cudaFree(d_pairs); cudaFree(d_out);
+        lock.unlock();
         if (e != cudaSuccess)
             return fail(e == cudaErrorMemoryAllocation ? GL_ERR_OOM : GL_ERR_CUDA,
                         std::string("filter_ghost_pairs: ") + cudaGetErrorString(e));

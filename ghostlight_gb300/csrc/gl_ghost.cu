@@ -611,7 +611,7 @@ SourceDev make_source(const gl_flare_source& s)
 // (one warp) then cover a compact patch of the pupil, whose rays tend to
 // vignette together, instead of a strip across it.  The set of samples and
 // each one's weight are unchanged.
-void morton_order(const gl_pupil_sample* in, int n, gl_pupil_sample* out)
+static inline uint32_t morton_code(const gl_pupil_sample& p)
 {
     auto spread = [](uint32_t x) {
         x &= 0x3ffu;
@@ -621,14 +621,32 @@ void morton_order(const gl_pupil_sample* in, int n, gl_pupil_sample* out)
         x = (x | (x << 2)) & 0x09249249u;
         return x;
     };
+    const float fu = std::min(std::max((p.u + 1.0f) * 512.0f, 0.0f), 1023.0f);
+    const float fv = std::min(std::max((p.v + 1.0f) * 512.0f, 0.0f), 1023.0f);
+    return (spread((uint32_t)fu) << 1) | spread((uint32_t)fv);
+}
+
+// A stable sort on the code: ordering an ordered grid again changes nothing,
+// so a caller may hand in grids it has ordered (and cached) once, and the
+// plan build then only checks them (one linear pass instead of a sort).
+void morton_order(const gl_pupil_sample* in, int n, gl_pupil_sample* out)
+{
+    bool sorted = true;
+    uint32_t prev = 0;
+    for (int i = 0; i < n && sorted; ++i)
+    {
+        const uint32_t c = morton_code(in[i]);
+        sorted = (i == 0) || c >= prev;
+        prev = c;
+    }
+    if (sorted)
+    {
+        std::copy(in, in + n, out);
+        return;
+    }
     std::vector<std::pair<uint32_t, int>> key;
     key.reserve((size_t)n);
-    for (int i = 0; i < n; ++i)
-    {
-        const float fu = std::min(std::max((in[i].u + 1.0f) * 512.0f, 0.0f), 1023.0f);
-        const float fv = std::min(std::max((in[i].v + 1.0f) * 512.0f, 0.0f), 1023.0f);
-        key.push_back({(spread((uint32_t)fu) << 1) | spread((uint32_t)fv), i});
-    }
+    for (int i = 0; i < n; ++i) key.push_back({morton_code(in[i]), i});
     std::stable_sort(key.begin(), key.end(),
                      [](const std::pair<uint32_t, int>& x, const std::pair<uint32_t, int>& y) { return x.first < y.first; });
     for (int i = 0; i < n; ++i) out[i] = in[key[i].second];
@@ -1029,6 +1047,13 @@ int gl_ghost_plan_execute(gl_ghost_plan* plan, float* d_out_r, float* d_out_g, f
 {
     if (!plan) return fail(GL_ERR_INVALID, "ghost_plan_execute: null plan");
     return plan_execute(plan->p, d_out_r, d_out_g, d_out_b, (cudaStream_t)stream);
+}
+
+int gl_morton_order(const gl_pupil_sample* in, int n, gl_pupil_sample* out)
+{
+    if (n < 0 || (n > 0 && (!in || !out))) return fail(GL_ERR_INVALID, "morton_order: bad arguments");
+    morton_order(in, n, out);
+    return GL_OK;
 }
 
 int gl_ghost_plan_set_launch(gl_ghost_plan* plan, int items_per_warp, int ctas_per_sm)

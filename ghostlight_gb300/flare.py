@@ -169,6 +169,27 @@ def pupil_grid(lens: OpticalSystem, ray_grid: int, jitter: int = 0, seed: int = 
     return g
 
 
+def render_order_grid(lens: OpticalSystem, ray_grid: int, jitter: int = 0, seed: int = 0,
+                      blades_override: int = 0, rotation_deg: float = 0.0) -> np.ndarray:
+    """The same samples as ``pupil_grid`` in the order the batched render
+    traces them (gl_morton_order), cached like the grid itself, so a plan
+    build only checks the order instead of sorting again."""
+    key = ("morton", lens.state_key(), ray_grid, jitter, seed, blades_override, float(rotation_deg))
+    g = _grid_cache.get(key)
+    if g is not None:
+        return g
+    base = pupil_grid(lens, ray_grid, jitter, seed, blades_override, rotation_deg)
+    src = np.ascontiguousarray(base, np.float32)
+    out = np.empty_like(src)
+    P = C.POINTER(gl_pupil_sample)
+    _native.check(_native.load().gl_morton_order(src.ctypes.data_as(P), len(src), out.ctypes.data_as(P)),
+                  "morton_order")
+    if len(_grid_cache) > 256:
+        _grid_cache.clear()
+    _grid_cache[key] = out
+    return out
+
+
 def color_matrices(config):
     lib = _native.load()
     mi, mo = (C.c_float * 9)(), (C.c_float * 9)()
@@ -342,11 +363,11 @@ def prepare_ghost_render(lens: OpticalSystem, sources, width: int, height: int, 
         sizes = [adaptive_grid_size(fp, sensor_half_w, sensor_half_h, width, height,
                                     config.adaptive_grid_min, config.adaptive_grid_max) for fp in fps]
         uniq = sorted(set(sizes))
-        grids = [pupil_grid(lens, g, jitter, seed, bo, rot) for g in uniq]
+        grids = [render_order_grid(lens, g, jitter, seed, bo, rot) for g in uniq]
         pair_grid = np.asarray([uniq.index(s) for s in sizes], np.int32)
     else:
         uniq = [int(config.ray_grid)]
-        grids = [pupil_grid(lens, int(config.ray_grid), jitter, seed, bo, rot)]
+        grids = [render_order_grid(lens, int(config.ray_grid), jitter, seed, bo, rot)]
         pair_grid = np.zeros(len(pairs), np.int32)
     plan = GhostRenderPlan(lens, pairs, boosts, sources, grids, pair_grid, spec, corr, width, height,
                            sensor_half_w, sensor_half_h, config.flare_gain, apply_corr, plain_per_pair,

@@ -270,6 +270,12 @@ int gl_ghost_plan_set_launch(gl_ghost_plan* plan, int items_per_warp, int ctas_p
 /* Ray-wavelength traces the last execute ran (render + cull probes; a probe
  * warp stops at its first on-sensor hit).  Synchronous. */
 int gl_ghost_plan_traced(const gl_ghost_plan* plan, long long* out);
+/* The pupil-sample order the batched render traces in: a stable sort along a
+ * Morton curve over the pupil square, so the 32 samples of a warp are
+ * neighbours.  Plans order their grids themselves; a grid ordered once by
+ * this call (and cached by the caller) is only checked, not re-sorted.
+ * (No counterpart in the reference, which traces in mask order.) */
+int gl_morton_order(const gl_pupil_sample* in, int n, gl_pupil_sample* out);
 /* The same count split into the render launch and the off-sensor probe
  * launch.  Synchronous.  (No counterpart in the reference.) */
 int gl_ghost_plan_traced_split(const gl_ghost_plan* plan, long long* render, long long* probe);

@@ -35,7 +35,8 @@ def test_lens_file_flare_matches_oracle(name):
     spec, corr = spectral_table(8)
     src = np.array([[np.radians(8.0), np.radians(3.0), 1.0, 1.0, 1.0]], np.float32)
     W = H = 128
-    plan = GhostRenderPlan(lens, fr.pairs, fr.boosts, src, grids, pair_grid, spec, corr, W, H, hw, hh, 1000.0)
+    plan = GhostRenderPlan(lens, fr.pairs, fr.boosts, src, grids, pair_grid, spec, corr, W, H, hw, hh, 1000.0,
+                           apply_correction=False)
     out = [torch.zeros((H, W), dtype=torch.float32, device="cuda") for _ in range(3)]
     plan.execute(*out)
     torch.cuda.synchronize()
