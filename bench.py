@@ -516,7 +516,7 @@ def run_serving(args):
     cfg = gl.FlareConfig(min_ghost_intensity=MIN_INTENSITY)
     t0 = time.perf_counter()
     pool = serving_lens_pool(SERVE_LENSES, cfg, seed=100, n_min=8, n_max=30)
-    reqs = poisson_requests(SERVE_RATE, args.serve_seconds, pool.keys(), seed=5)
+    reqs = poisson_requests(args.serve_rate, args.serve_seconds, pool.keys(), seed=5)
     for rl in pool.values():                      # resident tables: grids and IOR slices of the mix
         for g in sorted({r.ray_grid for r in reqs}):
             rl.prepare(g)
@@ -573,7 +573,7 @@ def run_serving(args):
     return {"workload": "Poisson %.0f req/s for %.0f s (%d requests), %d resident lenses of 8-30 surfaces, "
                         "outputs 512^2-4096^2, 8/16/31 wavelengths, pupil grids 32^2-256^2, field 0-20 deg, "
                         "%d slots, %.0f GB HBM budget, %s priorities" % (
-                            SERVE_RATE, args.serve_seconds, len(reqs), SERVE_LENSES, args.serve_slots,
+                            args.serve_rate, args.serve_seconds, len(reqs), SERVE_LENSES, args.serve_slots,
                             SERVE_BUDGET / 1e9, args.serve_policy),
             "throughput_req_s": served_req_s, "wall_s": wall, "offered_req_s": len(reqs) / args.serve_seconds,
             "rays_per_s": traced / wall, "ray_lambda_traces": traced,
@@ -799,8 +799,10 @@ def main():
                     help="batched timing only (no plain / e2e / CPU legs): for profiler runs")
     ap.add_argument("--serve-seconds", type=float, default=30.0)
     ap.add_argument("--serve-slots", type=int, default=32)
-    ap.add_argument("--serve-policy", default="sjf", choices=("sjf", "lsf"),
-                    help="stream priority of a request: shortest first, or longest (least slack) first")
+    ap.add_argument("--serve-rate", type=float, default=SERVE_RATE, help="Poisson arrival rate (requests/s)")
+    ap.add_argument("--serve-policy", default="sjf", choices=("sjf", "lsf", "sjf_fifo"),
+                    help="stream priority of a request: shortest first; longest (least slack) first; or "
+                         "shortest first with the long requests ranked by arrival")
     ap.add_argument("--serial-sample", type=int, default=40)
     ap.add_argument("--serve-dump", default="", help="write per-request timings (CSV) here")
     ap.add_argument("--only", default="all", choices=["all", "cfg3", "serve", "sweep"],

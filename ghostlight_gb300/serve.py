@@ -109,7 +109,41 @@ class Scheduler:
         assert self.used >= 0 and self.inflight >= 0
 
 
-POLICIES = ("sjf", "lsf")
+POLICIES = ("sjf", "lsf", "sjf_fifo")
+
+
+def size_class(est_rays: int, rays_per_s: float = 7e9) -> int:
+    """Estimated service time class: < 1 ms -> 0, < 4 ms -> 1, < 16 ms -> 2, else 3."""
+    t = est_rays / rays_per_s
+    return 0 if t < 1e-3 else 1 if t < 4e-3 else 2 if t < 16e-3 else 3
+
+
+def _light_levels(greatest: int, least: int) -> int:
+    """How many of the device's stream priority levels the three short
+    classes take under ``sjf_fifo`` (the rest rank the long requests): three
+    when there are six or more levels, two with four or five (the two
+    shortest classes share the top level), one otherwise."""
+    n = least - greatest + 1
+    return 3 if n >= 6 else (2 if n >= 4 else 1)
+
+
+def fifo_light_level(cls: int, greatest: int, least: int) -> int:
+    """Stream priority of a short request (size class 0..2) under ``sjf_fifo``."""
+    k = _light_levels(greatest, least)
+    return greatest + max(0, cls - (3 - k))
+
+
+def fifo_heavy_level(heavy_inflight_levels, greatest: int, least: int) -> int:
+    """Stream priority of a new long request under ``sjf_fifo``: the levels
+    below the short classes rank the long requests in flight by arrival — a
+    new one takes the level after the youngest one running (the lowest level
+    once they run out), so the oldest long request keeps the SMs the short
+    ones leave, instead of every long request sharing them equally and all
+    finishing late."""
+    first = min(least, greatest + _light_levels(greatest, least))
+    if not heavy_inflight_levels:
+        return first
+    return min(least, max(heavy_inflight_levels) + 1)
 
 
 def priority_class(est_rays: int, rays_per_s: float = 7e9, policy: str = "sjf") -> int:
@@ -124,9 +158,8 @@ def priority_class(est_rays: int, rays_per_s: float = 7e9, policy: str = "sjf") 
     short requests that arrive behind a long one."""
     if policy not in POLICIES:
         raise ValueError("priority policy must be one of %s" % (POLICIES,))
-    t = est_rays / rays_per_s
-    c = 0 if t < 1e-3 else 1 if t < 4e-3 else 2 if t < 16e-3 else 3
-    return c - 3 if policy == "sjf" else -c
+    c = size_class(est_rays, rays_per_s)
+    return -c if policy == "lsf" else c - 3
 
 
 def request_bytes(width: int, height: int, n_pairs: int, host_copy: bool = True) -> int:
@@ -230,8 +263,6 @@ class CudaExecutor:
     in-flight request owns a stream (one pool of streams per priority level);
     its result is copied into pinned host memory on that stream."""
 
-    LEVELS = (0, -1, -2, -3)
-
     def __init__(self, lenses: Dict[int, ResidentLens], max_inflight: int, items_per_warp: int = 8,
                  host_output: bool = True, device=None, policy: str = "sjf"):
         import torch
@@ -239,6 +270,13 @@ class CudaExecutor:
             raise ValueError("priority policy must be one of %s" % (POLICIES,))
         self.policy = policy
         self.torch = torch
+        lo, hi = torch.cuda.Stream.priority_range()
+        self.least, self.greatest = max(lo, hi), min(lo, hi)      # e.g. 0 and -5
+        if policy == "sjf_fifo":
+            self.LEVELS = tuple(range(self.least, self.greatest - 1, -1))
+        else:
+            self.LEVELS = tuple(lv for lv in (0, -1, -2, -3) if lv >= self.greatest)
+        self._heavy: Dict[int, int] = {}         # id(run) -> level of a long request in flight
         self._lib = _native.load()
         self.lenses = lenses
         self.items_per_warp = int(items_per_warp)
@@ -263,7 +301,12 @@ class CudaExecutor:
         rl = self.lenses[req.lens_id]
         masked = 0.8 * req.ray_grid * req.ray_grid
         req.est_rays = int(rl.n_pairs * masked * req.n_spec)
-        req.priority = priority_class(req.est_rays, policy=self.policy)
+        if self.policy == "sjf_fifo":
+            c = size_class(req.est_rays)
+            req.priority = (fifo_light_level(c, self.greatest, self.least) if c < 3
+                            else self.least)                                  # long: ranked at start()
+        else:
+            req.priority = max(self.greatest, priority_class(req.est_rays, policy=self.policy))
         req.device_bytes = request_bytes(req.width, req.height, rl.n_pairs)
 
     def _pinned_buf(self, shape):
@@ -279,7 +322,10 @@ class CudaExecutor:
     def start(self, req: FlareRequest) -> _Running:
         torch = self.torch
         rl = self.lenses[req.lens_id]
-        lv = req.priority if req.priority in self.free_streams else 0
+        heavy = self.policy == "sjf_fifo" and size_class(req.est_rays) == 3
+        if heavy:
+            req.priority = fifo_heavy_level(list(self._heavy.values()), self.greatest, self.least)
+        lv = req.priority if req.priority in self.free_streams else self.least
         pool = self.free_streams[lv]
         stream = pool.pop() if pool else torch.cuda.Stream(device=self.device, priority=lv)
         spec, corr = _spectral(req.n_spec, rl.config)
@@ -309,6 +355,8 @@ class CudaExecutor:
                 _native.check(self._lib.gl_request_copy_out(h, run.outs.data_ptr(), st), "request_copy_out")
         run.event = torch.cuda.Event()
         run.event.record(stream)
+        if heavy:
+            self._heavy[id(run)] = lv
         return run
 
     def prewarm(self, shapes, count: int):
@@ -325,6 +373,7 @@ class CudaExecutor:
         """Release the request's device memory (stream-ordered) and stream;
         returns the host planes (or the device tensor)."""
         lv, stream = run.stream
+        self._heavy.pop(id(run), None)
         v = C.c_longlong()
         if self._lib.gl_request_traced(run.handle, C.byref(v), None) == 0:
             run.req.traced = int(v.value)          # the stream is idle: no wait

@@ -117,6 +117,21 @@ def test_priority_least_slack_first_reverses():
         priority_class(1e5, policy="fifo")
 
 
+def test_fifo_levels_for_long_requests():
+    from ghostlight_gb300.serve import fifo_heavy_level, fifo_light_level, size_class
+    assert [size_class(e) for e in (1e5, 1e7, 1e8, 1e10)] == [0, 1, 2, 3]
+    g, l = -5, 0
+    assert fifo_heavy_level([], g, l) == -2                 # first long request: right below the short classes
+    assert fifo_heavy_level([-2], g, l) == -1               # the next one ranks behind it
+    assert fifo_heavy_level([-2, -1], g, l) == 0
+    assert fifo_heavy_level([-2, -1, 0], g, l) == 0         # out of levels: the lowest
+    assert fifo_heavy_level([-1], g, l) == 0                # never ahead of an older one still running
+    # a device with four levels (0 .. -3): the two shortest classes share the top
+    assert [fifo_light_level(c, -3, 0) for c in (0, 1, 2)] == [-3, -3, -2]
+    assert fifo_heavy_level([], -3, 0) == -1 and fifo_heavy_level([-1], -3, 0) == 0
+    assert [fifo_light_level(c, -5, 0) for c in (0, 1, 2)] == [-5, -4, -3]
+
+
 def test_latency_stats():
     rs = []
     for i in range(100):
