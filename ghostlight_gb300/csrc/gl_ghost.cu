@@ -142,7 +142,9 @@ __device__ __noinline__ float attenuator_general(V3 hit, const SurfRec& s)
 // vector shared-memory loads per step instead of a dozen scalar ones).
 struct __align__(16) HotRec {
     float z, c, sa2, inv_aspect;
-    int bits, ar_layers, pad0, pad1;
+    int bits, ar_layers;
+    float ar_scale;                 // 0.25^(ar_layers - 1): the extra AR layers of the SIMPLE model
+    int pad;
 };
 enum HotBits { HB_ACTIVE = 1, HB_GENERAL = 2, HB_POLYGON = 4, HB_SIMPLE = 8, HB_ATTEN = 16 };
 
@@ -158,7 +160,9 @@ __device__ __forceinline__ HotRec make_hot(const SurfRec& s)
              ((s.shape == 1) ? HB_POLYGON : 0) | ((s.coating == 0) ? HB_SIMPLE : 0) |
              ((s.coating == 4) ? HB_ATTEN : 0);
     h.ar_layers = s.ar_layers;
-    h.pad0 = h.pad1 = 0;
+    h.ar_scale = 1.0f;
+    for (int i = 1; i < s.ar_layers; ++i) h.ar_scale *= 0.25f;
+    h.pad = 0;
     return h;
 }
 
@@ -166,7 +170,15 @@ __device__ __forceinline__ HotRec make_hot(const SurfRec& s)
 // fresnel.h:92-178) with the film phase factor 2*pi*n_c*d/lambda supplied per
 // wavelength (kdelta) and cos(2 delta) formed as 2 cos^2(delta) - 1: delta is
 // below pi here, where the SFU cosine is accurate.
-__device__ __forceinline__ float mgf2_reflectance(float cos_i, float n1, float n2, int layers, float kdelta)
+//
+// The Airy sum R = (r01^2 + r12^2 + 2 r01 r12 c) / (1 + r01^2 r12^2 + 2 r01 r12 c)
+// with r01 = A/B, r12 = C/D is evaluated as one quotient of the numerators
+// and denominators scaled by (B D)^2 — one division where the textbook form
+// has three.  cos_2 >= 0 is the substrate-side cosine when the caller already
+// has it (a refraction's transmitted cosine: the film keeps n sin(theta), so
+// it is the same angle); cos_2 < 0 computes it here.
+__device__ __forceinline__ float mgf2_reflectance(float cos_i, float n1, float n2, int layers, float ar_scale,
+                                                  float kdelta, float cos_2)
 {
     if (layers <= 0) return fresnel_reflectance(cos_i, n1, n2);
     const float cn = 1.38f;
@@ -174,19 +186,37 @@ __device__ __forceinline__ float mgf2_reflectance(float cos_i, float n1, float n
     const float sin2_c = a1 * a1 * (1.0f - cos_i * cos_i);
     if (sin2_c >= 1.0f) return fresnel_reflectance(cos_i, n1, n2);
     const float cos_c = sqrtf(1.0f - sin2_c);
-    const float a2 = cn / n2;
-    const float sin2_2 = a2 * a2 * (1.0f - cos_c * cos_c);
-    if (sin2_2 >= 1.0f) return fresnel_reflectance(cos_i, n1, n2);
-    const float cos_2 = sqrtf(1.0f - sin2_2);
-    const float r01 = (n1 * cos_i - cn * cos_c) / (n1 * cos_i + cn * cos_c);
-    const float r12 = (cn * cos_c - n2 * cos_2) / (cn * cos_c + n2 * cos_2);
+    if (cos_2 < 0.0f)
+    {
+        const float a2 = cn / n2;
+        const float sin2_2 = a2 * a2 * (1.0f - cos_c * cos_c);
+        if (sin2_2 >= 1.0f) return fresnel_reflectance(cos_i, n1, n2);
+        cos_2 = sqrtf(1.0f - sin2_2);
+    }
+    const float p1 = n1 * cos_i, pc = cn * cos_c, p2 = n2 * cos_2;
+    const float A = p1 - pc, B = p1 + pc, Cn = pc - p2, D = pc + p2;
+    const float AD = A * D, CB = Cn * B, BD = B * D, AC = A * Cn;
     const float cd = __cosf(kdelta * cos_c);
     const float c2d = 2.0f * cd * cd - 1.0f;
-    const float x = 2.0f * r01 * r12 * c2d;
-    float R = (r01 * r01 + r12 * r12 + x) / (1.0f + r01 * r01 * r12 * r12 + x);
+    const float x = 2.0f * AC * BD * c2d;
+    float R = (AD * AD + CB * CB + x) / (BD * BD + AC * AC + x);
     R = fminf(fmaxf(R, 0.0f), 1.0f);
-    for (int i = 1; i < layers; ++i) R *= 0.25f;
-    return R;
+    return R * ar_scale;
+}
+
+// Refraction for the walk's unit vectors (the source direction is
+// normalised, sphere normals are unit by construction, and a refraction of
+// unit vectors is unit): Snell's law as refract_ray (trace_core.h:533-552)
+// without its renormalisation.  ci = -dot(nrm, d) >= 0; returns the
+// transmitted cosine (for the coating), or -1 on total internal reflection.
+__device__ __forceinline__ float refract_unit(V3& d, V3 nrm, float ci, float n1, float n2)
+{
+    const float nr = n1 / n2;
+    const float s2t = nr * nr * (1.0f - ci * ci);
+    if (s2t >= 1.0f) return -1.0f;
+    const float ct = sqrtf(1.0f - s2t);
+    d = d * nr + nrm * (nr * ci - ct);
+    return ct;
 }
 
 // One surface interaction on the lane's ray; false when the ray died.
@@ -198,11 +228,12 @@ __device__ __forceinline__ bool surface_step(V3& o, V3& d, const HotRec& h, cons
                                              float kdelta, float n2, bool reflecting, float reflect_ior,
                                              float& cur, float& w)
 {
-    float t; V3 nrm;
+    V3 nrm, hit;
     if (!(h.bits & HB_GENERAL))
     {
         const float c = h.c;
         V3 q;
+        float t;
         if (!sphere_hit(o, d, h.z, c, t, q)) return false;
         const float hx = q.x * h.inv_aspect, hy = q.y;
         const float h2 = hx * hx + hy * hy;
@@ -211,13 +242,16 @@ __device__ __forceinline__ bool surface_step(V3& o, V3& d, const HotRec& h, cons
         // outward normal (c q_x, c q_y, c q_z - 1), turned to oppose the ray
         nrm = v3(c * q.x, c * q.y, c * q.z - 1.0f);
         if (c == 0.0f) nrm = v3(0.0f, 0.0f, -1.0f);
-        if (dot(nrm, d) > 0.0f) nrm = -nrm;
+        hit = v3(q.x, q.y, q.z + h.z);
     }
-    else if (!intersect_general(o, d, s, t, nrm))
+    else
     {
-        return false;
+        float t;
+        if (!intersect_general(o, d, s, t, nrm)) return false;
+        hit = o + d * t;
     }
-    const V3 hit = o + d * t;
+    float ci = -dot(nrm, d);
+    if (ci < 0.0f) { nrm = -nrm; ci = -ci; }
     o = hit;
     const float n1 = cur;
     const bool simple = (h.bits & HB_SIMPLE) != 0;
@@ -225,24 +259,24 @@ __device__ __forceinline__ bool surface_step(V3& o, V3& d, const HotRec& h, cons
     {
         if (WEIGHT)
         {
-            w *= simple ? mgf2_reflectance(fabsf(dot(nrm, d)), n1, n2, h.ar_layers, kdelta)
+            w *= simple ? mgf2_reflectance(ci, n1, n2, h.ar_layers, h.ar_scale, kdelta, -1.0f)
                         : weight_general(d, nrm, n1, n2, s, lam, true);
             if (h.bits & HB_ATTEN) w *= attenuator_general(hit, s);
         }
-        d = reflect(d, nrm);
+        d = d + nrm * (2.0f * ci);
         cur = reflect_ior;
     }
     else
     {
-        V3 nd;
-        if (!refract(d, nrm, n1, n2, nd)) return false;
+        const V3 d_in = d;
+        const float ct = refract_unit(d, nrm, ci, n1, n2);
+        if (ct < 0.0f) return false;
         if (WEIGHT)
         {
-            w *= simple ? 1.0f - mgf2_reflectance(fabsf(dot(nrm, d)), n1, n2, h.ar_layers, kdelta)
-                        : weight_general(d, nrm, n1, n2, s, lam, false);
+            w *= simple ? 1.0f - mgf2_reflectance(ci, n1, n2, h.ar_layers, h.ar_scale, kdelta, ct)
+                        : weight_general(d_in, nrm, n1, n2, s, lam, false);
             if (h.bits & HB_ATTEN) w *= attenuator_general(hit, s);
         }
-        d = nd;
         cur = n2;
     }
     return true;
