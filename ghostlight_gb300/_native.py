@@ -30,6 +30,8 @@ def _declare(lib):
     lib.gl_last_launch_count.restype = i
     lib.gl_finalize_z.argtypes = [P(gl_surface), i]
     lib.gl_euler_rotation.argtypes = [C.c_float, C.c_float, C.c_float, P(C.c_float)]
+    lib.gl_blade_radius.argtypes = [i, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, P(C.c_float), i,
+                                    P(C.c_float)]
     lib.gl_enumerate_ghost_pairs.argtypes = [P(gl_surface), i, P(gl_ghost_pair), i, P(i)]
     lib.gl_build_aperture_samples.argtypes = [P(gl_surface), i, P(gl_sampler_params),
                                               P(gl_pupil_sample), i, P(i)]

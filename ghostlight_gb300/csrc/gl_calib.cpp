@@ -10,8 +10,8 @@
 // reference host build).  The traces are the reference-formulation
 // trace_primary of gl_trace.cuh with per-wavelength IOR slices.
 //
-// Only plain-polygon and round stops are calibrated; authored blade shapes
-// are rejected by the trace tables already (pack_lens).
+// Bladed stops carry their authored shape (gl_blade.h): the traces test it and
+// the pupil area fraction is its enclosed area (lens_calibration.cpp:363).
 #include "gl_internal.h"
 
 #include <algorithm>
@@ -251,35 +251,6 @@ void marginal_support(ProbeLens& L, const gl_surface& stop, float lam, float* sx
     consider((float)(3.14159265358979323846 / 2.0));
     *sx = bx;
     *sy = by;
-}
-
-// Enclosed area of a regular n-gon stop as a fraction of the unit disc,
-// Simpson's rule over one sector (512 panels, FP64 sum) of r(phi)^2 with the
-// edge in the conic form u = u_w - (u_w - 1) sin^2(phi/2) / sin^2(half/2)
-// (aperture_profile.h:108-130, 268-281 with no deformation authored).
-float polygon_area_frac(int blades)
-{
-    if (blades < 3) return 1.0f;
-    const float sigma = 2.0f * (float)3.14159265358979323846 / (float)blades;
-    const float half = 0.5f * sigma;
-    const float a = cosf(half);
-    const float u_w = 1.0f / a;
-    const float u_rise = u_w - 1.0f;
-    const float sh = sinf(0.5f * half);
-    const float q = 1.0f / (sh * sh);
-    const int n = 512;
-    const double h = (double)sigma / n;
-    double total = 0.0;
-    for (int i = 0; i <= n; ++i)
-    {
-        const float phi = (float)(-(double)half + i * h);
-        const float sp = sinf(0.5f * phi);
-        const float u = u_w - u_rise * (sp * sp) * q;
-        const double r = 1.0 / (double)u;
-        const double w = (i == 0 || i == n) ? 1.0 : ((i % 2) ? 4.0 : 2.0);
-        total += w * r * r;
-    }
-    return (float)(blades * (total * h / 3.0) / (2.0 * 3.14159265358979323846));
 }
 
 // ---- covered field ----------------------------------------------------------------
@@ -757,7 +728,10 @@ extern "C" int gl_calibrate_lens(const gl_surface* surfaces, int n, float lens_f
     if (stop && stop->aperture_shape == GL_APERTURE_POLYGON && stop->aperture_blades >= 3)
     {
         marginal_support(L, *stop, lam, &out->entrance_pupil_semi_x, &out->entrance_pupil_semi_y);
-        out->pupil_area_frac = polygon_area_frac(stop->aperture_blades);
+        out->pupil_area_frac = make_blade_profile(stop->aperture_blades, stop->aperture_rotation_rad,
+                                                  stop->aperture_curvature, stop->aperture_twist,
+                                                  stop->aperture_notch_rad,
+                                                  stop->aperture_notch_angle_rad).area_frac;
     }
     else
     {

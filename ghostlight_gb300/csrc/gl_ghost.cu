@@ -105,6 +105,7 @@ __device__ __forceinline__ bool check_polygon(float hx, float hy, float h2, cons
 {
     float r = sqrtf(h2);
     if (r < 1e-9f) return true;
+    if (s.blade.deformed) return r <= s.semi_ap * blade_radius_at(s.blade, atan2f(hy, hx));
     const float angle = atan2f(hy, hx) - s.rot_rad;
     float off = fmodf(angle, s.sector);
     if (off < 0.0f) off += s.sector;

@@ -35,12 +35,6 @@ static bool rot_identity(const float* m)
             fabsf(m[6]) < eps && fabsf(m[7]) < eps && fabsf(m[8] - 1.f) < eps);
 }
 
-static bool blade_shape_authored(const gl_surface& s)
-{
-    return s.aperture_curvature != 0.0f || s.aperture_twist != 0.0f ||
-           s.aperture_notch_rad != 0.0f || s.aperture_notch_angle_rad != 0.0f;
-}
-
 int pack_lens(const gl_surface* in, int n, SurfRec* out)
 {
     if (in == nullptr || n <= 0) return fail(GL_ERR_INVALID, "lens has no surfaces");
@@ -52,8 +46,6 @@ int pack_lens(const gl_surface* in, int n, SurfRec* out)
         std::memset(&r, 0, sizeof(r));
         if (g.aperture_shape == GL_APERTURE_IMAGE)
             return fail(GL_ERR_UNSUPPORTED, "image apertures are outside the flare path");
-        if (g.aperture_shape == GL_APERTURE_POLYGON && g.aperture_blades >= 3 && blade_shape_authored(g))
-            return fail(GL_ERR_UNSUPPORTED, "authored blade shapes are not traced (plain polygon only)");
         if (g.coating_model != GL_COATING_SIMPLE && g.coating_model != GL_COATING_ARTIST &&
             g.coating_model != GL_COATING_ATTENUATOR)
             return fail(GL_ERR_UNSUPPORTED, "table-backed coatings are outside the flare path");
@@ -72,6 +64,8 @@ int pack_lens(const gl_surface* in, int n, SurfRec* out)
             // the same float operations once here give the same values.
             r.sector = 2.0f * kPi / (float)g.aperture_blades;
             r.apothem = g.semi_aperture * cosf(0.5f * r.sector);
+            r.blade = make_blade_profile(g.aperture_blades, g.aperture_rotation_rad, g.aperture_curvature,
+                                         g.aperture_twist, g.aperture_notch_rad, g.aperture_notch_angle_rad);
         }
         r.conic = g.conic_k;
         r.dec_x = g.decenter_x;
@@ -147,6 +141,7 @@ PupilMask resolve_pupil_mask(const gl_surface* surfs, int n, int blades_override
 {
     int n_blades = 0;
     float rot_rad = 0.0f, aspect = 1.0f;
+    BladeProfile blade = make_blade_profile(0, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f);
     for (int i = 0; i < n; ++i)
     {
         if (!surfs[i].is_stop) continue;
@@ -155,15 +150,20 @@ PupilMask resolve_pupil_mask(const gl_surface* surfs, int n, int blades_override
         {
             n_blades = surfs[i].aperture_blades;
             rot_rad = surfs[i].aperture_rotation_rad;
+            blade = make_blade_profile(n_blades, rot_rad, surfs[i].aperture_curvature, surfs[i].aperture_twist,
+                                       surfs[i].aperture_notch_rad, surfs[i].aperture_notch_angle_rad);
         }
         break;
     }
     if (blades_override > 0)
     {
+        // a plain n-gon by definition: the stop's blade shape is dropped
         n_blades = blades_override;
         rot_rad = rotation_deg * (kPi / 180.0f);
+        blade = make_blade_profile(0, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f);
     }
     PupilMask m;
+    m.blade = blade;
     m.aspect = aspect;
     m.n_blades = n_blades;
     m.rot_rad = rot_rad;
@@ -180,6 +180,7 @@ bool pupil_contains(const PupilMask& m, float u, float v)
     if (r2 > 1.0f) return false;
     if (m.n_blades >= 3)
     {
+        if (m.blade.deformed) return sqrtf(r2) <= blade_radius_at(m.blade, atan2f(v, ux));
         float angle = atan2f(v, ux) - m.rot_rad;
         float sector = fmodf(angle, m.sector);
         if (sector < 0.0f) sector += m.sector;
@@ -454,6 +455,33 @@ int gl_finalize_z(gl_surface* s, int n)
     for (int i = 0; i < n; ++i) total += s[i].thickness;
     float z = -total;
     for (int i = 0; i < n; ++i) { s[i].z = z; z += s[i].thickness; }
+    return GL_OK;
+}
+
+// Boundary radius (normalised; 1 = blade tip) of a bladed stop's silhouette
+// at angles theta: ApertureProfile::radius_at of make_aperture_profile
+// (aperture_profile.h:192-196, 285-358), host float arithmetic.
+int gl_blade_radius(int blades, float rotation_rad, float curvature, float twist, float notch_rad,
+                    float notch_angle_rad, const float* theta, int n, float* out)
+{
+    if (blades < 3 || n < 0 || (n > 0 && (!theta || !out)))
+        return fail(GL_ERR_INVALID, "blade_radius: needs >= 3 blades and n angles");
+    const BladeProfile b = make_blade_profile(blades, rotation_rad, curvature, twist, notch_rad, notch_angle_rad);
+    for (int i = 0; i < n; ++i)
+    {
+        if (b.deformed)
+        {
+            out[i] = blade_radius_at(b, theta[i]);
+        }
+        else
+        {
+            // the regular polygon, as check_aperture evaluates it (trace_core.h:159-166)
+            float off = fmodf(theta[i] - rotation_rad, b.sigma);
+            if (off < 0.0f) off += b.sigma;
+            off -= 0.5f * b.sigma;
+            out[i] = cosf(0.5f * b.sigma) / cosf(off);
+        }
+    }
     return GL_OK;
 }
 

@@ -21,6 +21,7 @@ struct PupilMask {
     float rot_rad = 0.0f;
     float apothem = 1.0f;
     float sector = 1.0f;
+    BladeProfile blade{};       // the stop's authored blade shape (blade.deformed), dropped under an override
 };
 
 int pack_lens(const gl_surface* in, int n, SurfRec* out);

@@ -552,10 +552,12 @@ __global__ void mdft_dft_kernel(void* out, int n_lambda, int K_rows, int n, int 
 // starburst_render.cu:155-191, stop term): grid coordinate g in [-1, 1) maps
 // to pupil coordinate g / pupil_fill; 4 x 4 supersamples per texel tested
 // against the stop silhouette (PupilMask::contains, aperture_sampler.h:63-82:
-// ellipse of the stop's aspect, then the regular n-gon).
+// ellipse of the stop's aspect, then the regular n-gon or the authored blade
+// profile).
 struct PupilDev {
     float aspect, rot_rad, apothem, sector;
     int n_blades;
+    BladeProfile blade;
 };
 
 __device__ __forceinline__ bool pupil_in(const PupilDev& m, float u, float v)
@@ -565,6 +567,7 @@ __device__ __forceinline__ bool pupil_in(const PupilDev& m, float u, float v)
     if (r2 > 1.0f) return false;
     if (m.n_blades >= 3)
     {
+        if (m.blade.deformed) return sqrtf(r2) <= blade_radius_at(m.blade, atan2f(v, ux));
         const float angle = atan2f(v, ux) - m.rot_rad;
         float sector = fmodf(angle, m.sector);
         if (sector < 0.0f) sector += m.sector;
@@ -984,7 +987,7 @@ extern "C" int gl_build_pupil(const gl_surface* surfaces, int n_surfaces, int N,
     if (N <= 0 || N > 8192) return fail(GL_ERR_INVALID, "build_pupil: N must be 1..8192");
     if (!(pupil_fill > 0.0f) || pupil_fill > 1.0f) return fail(GL_ERR_INVALID, "build_pupil: pupil_fill must lie in (0, 1]");
     const PupilMask m = resolve_pupil_mask(surfaces, n_surfaces, blades_override, rotation_deg);
-    PupilDev d{m.aspect, m.rot_rad, m.apothem, m.sector, m.n_blades};
+    PupilDev d{m.aspect, m.rot_rad, m.apothem, m.sector, m.n_blades, m.blade};
     const int total = N * N;
     pupil_build_kernel<<<(total + 255) / 256, 256, 0, (cudaStream_t)stream>>>(d_out, N, pupil_fill, d);
     GL_CUDA_TRY(cudaGetLastError());

@@ -18,6 +18,8 @@
 #include <math.h>
 #include <stdint.h>
 
+#include "gl_blade.h"
+
 #ifndef __CUDACC__
 #ifndef __host__
 #define __host__
@@ -46,18 +48,18 @@ enum SurfFlags : int32_t {
 struct SurfRec {
     float z, radius, semi_ap, aspect;
     float rot_rad, sector, apothem, conic;
-    float dec_x, dec_y, inv_r, pad0;
+    float dec_x, dec_y, inv_r;
     float rot[9];
     float asph[8];
     int32_t form, shape, flags, n_asph;
     int32_t coating, ar_layers, blades, cyl_axis;
     float tint_r, tint_g, tint_b, tint_s;
     float g_sigma, g_bg, g_peak, g_dx, g_dy;
-    float pad1[3];
+    BladeProfile blade;         // authored blade silhouette of a polygon stop (blade.deformed)
 };
-// 49 words: an odd stride, so lanes reading the same field of different
+// 65 words: an odd stride, so lanes reading the same field of different
 // surfaces in shared memory hit different banks.
-static_assert(sizeof(SurfRec) == 196, "SurfRec must stay 196 bytes");
+static_assert(sizeof(SurfRec) == 260, "SurfRec must stay 260 bytes");
 
 struct V3 {
     float x, y, z;
@@ -179,6 +181,8 @@ GLH bool check_aperture(V3 hit, const SurfRec& s)
     {
         float r = sqrtf(h2);
         if (r < 1e-9f) return true;
+        // authored blade shape: the profile's boundary radius (trace_core.h:153-154)
+        if (s.blade.deformed) return r <= s.semi_ap * blade_radius_at(s.blade, atan2f(hy, hx));
         const float angle = atan2f(hy, hx) - s.rot_rad;
         float off = fmodf(angle, s.sector);
         if (off < 0.0f) off += s.sector;

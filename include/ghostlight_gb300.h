@@ -142,6 +142,14 @@ int         gl_version(void);
  * lays z so the chain ends at the sensor (z = 0). */
 int gl_finalize_z(gl_surface* surfaces, int n);
 
+/* ApertureProfile::radius_at (ghostlight/src/aperture_profile.h:192-196) of
+ * make_aperture_profile (:285-358): the normalised boundary radius (1 = blade
+ * tip) of a bladed stop at each angle theta[i] (radians, absolute), for the
+ * authored curvature [-1, 1], twist [-1, 1], notch and notch angle (radians);
+ * with none authored, the regular polygon.  Host float arithmetic. */
+int gl_blade_radius(int blades, float rotation_rad, float curvature, float twist, float notch_rad,
+                    float notch_angle_rad, const float* theta, int n, float* out);
+
 /* make_rotation, ghostlight/src/optical_system.cpp:185-199 — the element
  * rotation R = Ry(tilt_y) Rx(tilt_x) Rz(roll) of the lens-file loader
  * (row-major 3x3 into out[9]; float arithmetic, C library cosf/sinf). */

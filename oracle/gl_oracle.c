@@ -31,11 +31,86 @@ static int orc_rot_identity(const float* m)
             fabsf(m[6]) < eps && fabsf(m[7]) < eps && fabsf(m[8] - 1.f) < eps);
 }
 
+/* ---- authored blade silhouette -----------------------------------------
+ * ApertureProfile / make_aperture_profile, aperture_profile.h:82-358: each
+ * half blade edge a conic arc in u = 1/r through the waist and the tip, the
+ * notch a chord across the tip.  The derived block is built in float, as the
+ * reference does; the boundary radius is evaluated in the instantiation's
+ * scalar type (impl: blade_radius). */
+typedef struct {
+    int blades, deformed, facets;
+    float rotation, sigma, half, r_w, phi_w, u_w, u_rise, qR, qL, p, beta, eA, eB;
+} orc_blade;
+
+static float orc_bclamp(float v, float lo, float hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+static float orc_blade_u_edge(const orc_blade* b, float phi)
+{
+    const float psi = phi - b->phi_w;
+    const float sh = sinf(0.5f * psi);
+    return b->u_w - b->u_rise * (sh * sh) * ((psi >= 0.0f) ? b->qR : b->qL);
+}
+
+static int orc_blade_authored(const gl_surface* s)
+{
+    return s->aperture_curvature != 0.0f || s->aperture_twist != 0.0f || s->aperture_notch_rad != 0.0f;
+}
+
+static orc_blade orc_make_blade(const gl_surface* s)
+{
+    const float pi = (float)M_PI;
+    orc_blade b;
+    memset(&b, 0, sizeof(b));
+    b.blades = s->aperture_blades;
+    const float curv = orc_bclamp(s->aperture_curvature, -1.0f, 1.0f);
+    const float twist = orc_bclamp(s->aperture_twist, -1.0f, 1.0f);
+    const float notch = orc_bclamp(s->aperture_notch_rad, -(float)(M_PI / 4.0), (float)(M_PI / 4.0));
+    const float rake = orc_bclamp(s->aperture_notch_angle_rad, 0.0f, (float)(M_PI / 4.0));
+    b.rotation = s->aperture_rotation_rad;
+    b.sigma = 2.0f * pi / (float)b.blades;
+    b.half = 0.5f * b.sigma;
+    b.deformed = !(curv == 0.0f && twist == 0.0f && notch == 0.0f);
+    const float a = cosf(b.half);
+    b.r_w = (curv >= 0.0f) ? (a + curv * (1.0f - a)) : (a * (1.0f + curv * 0.55f));
+    const float lim = fmaxf(0.0f, b.half - 4.0f * (float)(M_PI / 180.0));
+    b.phi_w = orc_bclamp(twist * b.half, -lim, lim);
+    const float dR = b.half - b.phi_w, dL = b.half + b.phi_w;
+    b.u_w = 1.0f / b.r_w;
+    b.u_rise = b.u_w - 1.0f;
+    const float sR = sinf(0.5f * dR), sL = sinf(0.5f * dL);
+    b.qR = 1.0f / (sR * sR);
+    b.qL = 1.0f / (sL * sL);
+    const float e = (fabsf(notch) / (45.0f * (float)(M_PI / 180.0))) * 0.45f * b.half;
+    const float sk = orc_bclamp(rake / (float)(M_PI / 4.0), 0.0f, 1.0f);
+    float eA = fminf(e * (1.0f + sk), 0.90f * b.half);
+    float eB = e * (1.0f - sk);
+    if (notch < 0.0f) { const float t = eA; eA = eB; eB = t; }
+    if (e > 1e-9f && b.r_w < 1.0f && (eA + eB) > 1e-9f)
+    {
+        const float pa = b.half - eA, pb = b.half + eB;
+        const float ra = 1.0f / orc_blade_u_edge(&b, pa);
+        const float rb = 1.0f / orc_blade_u_edge(&b, -b.half + eB);
+        const float ax = ra * cosf(pa), ay = ra * sinf(pa);
+        const float bx = rb * cosf(pb), by = rb * sinf(pb);
+        const float dx = bx - ax, dy = by - ay;
+        const float dl = sqrtf(dx * dx + dy * dy);
+        if (dl >= 1e-9f)
+        {
+            float nx = dy / dl, ny = -dx / dl;
+            if (ax * nx + ay * ny < 0.0f) { nx = -nx; ny = -ny; }
+            const float p = ax * nx + ay * ny;
+            if (p > 1e-6f) { b.facets = 1; b.p = p; b.beta = atan2f(ny, nx); b.eA = eA; b.eB = eB; }
+        }
+    }
+    return b;
+}
+
 /* ---- float instantiation ------------------------------------------------ */
 #define R float
 #define SFX(x) x##_f32
 #define SQRT sqrtf
 #define COS cosf
+#define SIN sinf
 #define ATAN2 atan2f
 #define FMOD fmodf
 #define FABS fabsf
@@ -48,6 +123,7 @@ static int orc_rot_identity(const float* m)
 #undef SFX
 #undef SQRT
 #undef COS
+#undef SIN
 #undef ATAN2
 #undef FMOD
 #undef FABS
@@ -61,6 +137,7 @@ static int orc_rot_identity(const float* m)
 #define SFX(x) x##_f64
 #define SQRT sqrt
 #define COS cos
+#define SIN sin
 #define ATAN2 atan2
 #define FMOD fmod
 #define FABS fabs
@@ -208,19 +285,36 @@ static float orc_halton3(uint32_t n)
     return r;
 }
 
+/* Boundary radius of a stop's blade silhouette (normalised, float) at
+ * angles theta[0..n): the profile of an authored stop, the plain n-gon's
+ * otherwise. */
+int orc_blade_radius(const gl_surface* stop, const float* theta, int n, float* out)
+{
+    if (!stop || stop->aperture_shape != GL_APERTURE_POLYGON || stop->aperture_blades < 3) return -1;
+    orc_blade b = orc_make_blade(stop);
+    for (int i = 0; i < n; ++i) out[i] = blade_radius_f32(&b, theta[i]);
+    return 0;
+}
+
 int orc_aperture_samples(const gl_surface* S, int N, int grid, int jitter, int seed,
                          int blades_override, float rotation_deg, float* out_uv, int cap)
 {
     int nb = 0; float rot = 0.0f, aspect = 1.0f;
+    int deformed = 0;
+    orc_blade blade;
+    memset(&blade, 0, sizeof(blade));
     for (int i = 0; i < N; ++i)
     {
         if (!S[i].is_stop) continue;
         aspect = S[i].aperture_aspect;
         if (S[i].aperture_shape == GL_APERTURE_POLYGON && S[i].aperture_blades >= 3)
-        { nb = S[i].aperture_blades; rot = S[i].aperture_rotation_rad; }
+        {
+            nb = S[i].aperture_blades; rot = S[i].aperture_rotation_rad;
+            if (orc_blade_authored(&S[i])) { blade = orc_make_blade(&S[i]); deformed = blade.deformed; }
+        }
         break;
     }
-    if (blades_override > 0) { nb = blades_override; rot = rotation_deg * ((float)M_PI / 180.0f); }
+    if (blades_override > 0) { nb = blades_override; rot = rotation_deg * ((float)M_PI / 180.0f); deformed = 0; }
     const int poly = nb >= 3;
     const float apothem = poly ? cosf((float)M_PI / nb) : 1.0f;
     const float sector = poly ? (2.0f * (float)M_PI / nb) : 1.0f;
@@ -240,7 +334,11 @@ int orc_aperture_samples(const gl_surface* S, int N, int grid, int jitter, int s
         }
         const float ux = u / aspect, r2 = ux * ux + v * v;
         if (r2 > 1.0f) continue;
-        if (poly)
+        if (poly && deformed)
+        {
+            if (!(sqrtf(r2) <= blade_radius_f32(&blade, atan2f(v, ux)))) continue;
+        }
+        else if (poly)
         {
             float ang = atan2f(v, ux) - rot;
             float sec = fmodf(ang, sector);

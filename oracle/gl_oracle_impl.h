@@ -176,7 +176,37 @@ static inline R SFX(surface_attenuator)(SFX(v3) hit, const gl_surface* s)
     return (R)1;
 }
 
-/* check_aperture, trace_core.h:133-170 (circle / ellipse / plain polygon) */
+/* ApertureProfile::radius_at, aperture_profile.h:124-200 (u_edge, fold,
+ * u_raw, sector_angle) on a float-built profile, in R */
+static inline R SFX(blade_u_edge)(const orc_blade* b, R phi)
+{
+    const R psi = phi - (R)b->phi_w;
+    const R sh = SIN((R)0.5f * psi);
+    return (R)b->u_w - (R)b->u_rise * (sh * sh) * (R)((psi >= (R)0) ? b->qR : b->qL);
+}
+static inline R SFX(blade_radius)(const orc_blade* b, R theta)
+{
+    const R sigma = (R)b->sigma, half = (R)b->half;
+    R phi = FMOD(theta - (R)b->rotation, sigma);
+    if (phi < (R)0) phi += sigma;
+    phi -= half;
+    R u = SFX(blade_u_edge)(b, phi);
+    if (b->facets)
+    {
+        R w = FMOD(phi - half + half, sigma);
+        if (w < (R)0) w += sigma;
+        w -= half;
+        if (w >= -(R)b->eA && w <= (R)b->eB)
+        {
+            const R uf = COS(w + half - (R)b->beta) / (R)b->p;
+            if (uf > u) u = uf;
+        }
+    }
+    return (R)1 / u;
+}
+
+/* check_aperture, trace_core.h:133-170 (circle / ellipse / polygon, plain or
+ * with its authored blade shape) */
 static inline int SFX(check_aperture)(SFX(v3) hit, const gl_surface* s)
 {
     R hx = hit.x / (R)s->aperture_aspect;
@@ -187,6 +217,11 @@ static inline int SFX(check_aperture)(SFX(v3) hit, const gl_surface* s)
     {
         R r = SQRT(h2);
         if (r < (R)1e-9f) return 1;
+        if (orc_blade_authored(s))
+        {
+            const orc_blade b = orc_make_blade(s);
+            return r <= (R)s->semi_aperture * SFX(blade_radius)(&b, ATAN2(hy, hx));
+        }
         const R sector = (R)2 * (R)(float)M_PI / (R)s->aperture_blades;
         const R angle = ATAN2(hy, hx) - (R)s->aperture_rotation_rad;
         R off = FMOD(angle, sector);

@@ -52,10 +52,12 @@ def test_pupil(n: int, seed: int = 3) -> np.ndarray:
     return a.astype(np.float32)
 
 
-def stop_pupil(aspect: float, n_blades: int, rot_rad: float, N: int, fill: float) -> np.ndarray:
+def stop_pupil(aspect: float, n_blades: int, rot_rad: float, N: int, fill: float, blade_stop=None) -> np.ndarray:
     """4 x 4 supersampled stop silhouette in float32 arithmetic, the stop term
     of build_pupil_kernel (starburst_render.cu:155-191) with
-    PupilMask::contains (aperture_sampler.h:63-82)."""
+    PupilMask::contains (aperture_sampler.h:63-82).  blade_stop: the stop
+    surface record when its blade shape is authored (the boundary is then the
+    profile's r(theta), aperture_sampler.h:70-73)."""
     f = np.float32
     apothem = f(np.cos(f(np.pi) / f(n_blades))) if n_blades >= 3 else f(1)
     sector = f(f(2) * f(np.pi) / f(n_blades)) if n_blades >= 3 else f(1)
@@ -68,7 +70,11 @@ def stop_pupil(aspect: float, n_blades: int, rot_rad: float, N: int, fill: float
             ux = (u / f(aspect)).astype(f)
             r2 = (ux * ux + v * v).astype(f)
             inside = r2 <= f(1)
-            if n_blades >= 3:
+            if n_blades >= 3 and blade_stop is not None:
+                from . import oracle as O
+                rad = O.blade_radius(blade_stop, np.arctan2(v, ux).astype(f))
+                inside &= np.sqrt(r2).astype(f) <= rad
+            elif n_blades >= 3:
                 ang = (np.arctan2(v, ux).astype(f) - f(rot_rad)).astype(f)
                 sec = np.fmod(ang, sector).astype(f)
                 sec = np.where(sec < 0, sec + sector, sec).astype(f)

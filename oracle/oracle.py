@@ -30,6 +30,7 @@ def _load():
         lib.orc_enumerate.argtypes = [P(gl_surface), i, P(i), i]
         lib.orc_filter.argtypes = [P(gl_surface), i, f, f, f, i, f, P(i), P(f), P(f), i]
         lib.orc_aperture_samples.argtypes = [P(gl_surface), i, i, i, i, i, f, P(f), i]
+        lib.orc_blade_radius.argtypes = [P(gl_surface), P(f), i, P(f)]
         lib.orc_render.argtypes = [P(gl_surface), i, P(i), P(f), P(i), i, P(f), i, P(f), P(i),
                                    P(f), i, f, f, i, i, f, i, i, P(d)]
         _lib = lib
@@ -78,6 +79,16 @@ def filter_pairs(surfs, hw, hh, min_int=1e-7, normalize=True, max_boost=100.0, f
     if footprint:
         return ab[:n].copy(), bo[:n].copy(), fp[:n].copy()
     return ab[:n].copy(), bo[:n].copy()
+
+
+def blade_radius(stop, theta):
+    """Normalised boundary radius of a bladed stop at angles theta (float32)."""
+    lib = _load()
+    th = np.ascontiguousarray(theta, np.float32).reshape(-1)
+    out = np.zeros_like(th)
+    if lib.orc_blade_radius(C.byref(stop), _fp(th), len(th), _fp(out)) != 0:
+        raise ValueError("blade_radius: not a bladed stop")
+    return out.reshape(np.shape(theta))
 
 
 def aperture_samples(surfs, grid, jitter=0, seed=0, blades_override=0, rotation_deg=0.0):
