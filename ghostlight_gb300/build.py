@@ -73,8 +73,18 @@ def _deps():
         list(CSRC.glob("*.inc")) + [REPO / "include" / "ghostlight_gb300.h", pathlib.Path(__file__)]
 
 
+STAMP = BUILD / "flags.txt"
+
+
+def _flags_stamp() -> str:
+    """The per-unit flags the library was built with: a change (an
+    environment override) forces a rebuild even when no source changed."""
+    return "\n".join("%s %s" % (u, " ".join(f)) for u, f in sorted(UNITS.items()))
+
+
 def build(force: bool = False, verbose: bool = False) -> pathlib.Path:
-    if not force and LIB.exists():
+    stamp = _flags_stamp()
+    if not force and LIB.exists() and STAMP.exists() and STAMP.read_text() == stamp:
         t = LIB.stat().st_mtime
         if all(p.stat().st_mtime <= t for p in _deps()):
             return LIB
@@ -91,6 +101,7 @@ def build(force: bool = False, verbose: bool = False) -> pathlib.Path:
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))
     os.replace(tmp, LIB)
+    STAMP.write_text(stamp)
     return LIB
 
 
