@@ -55,6 +55,7 @@ def _declare(lib):
     lib.gl_ghost_plan_set_timing.argtypes = [vp, vp, vp, vp]
     lib.gl_morton_order.argtypes = [P(gl_pupil_sample), i, P(gl_pupil_sample)]
     lib.gl_ghost_plan_set_launch.argtypes = [vp, i, i]
+    lib.gl_ghost_plan_set_lambda_split.argtypes = [vp, i]
     lib.gl_gemm_bf16_tc.argtypes = [vp, vp, vp, i, i, i, vp]
     d = C.c_double
     lib.gl_mdft_plan_create.argtypes = [i, i, i, P(d), P(d), d, d, P(f), i, vp, P(vp)]
@@ -79,6 +80,7 @@ def _declare(lib):
     lib.gl_request_create.argtypes = [vp, i, P(gl_spectral_sample), i, P(gl_flare_source), i,
                                       P(gl_ghost_render_params), vp, P(vp)]
     lib.gl_request_enqueue.argtypes = [vp, vp, vp, vp, i, vp]
+    lib.gl_request_set_lambda_split.argtypes = [vp, i]
     lib.gl_request_planes.argtypes = [vp, P(vp)]
     lib.gl_request_copy_out.argtypes = [vp, vp, vp]
     lib.gl_request_info.argtypes = [vp, P(ll), P(ll), P(i)]

@@ -20,7 +20,9 @@ import os
 import threading
 from typing import Callable, Dict, Hashable, List, Optional, Sequence
 
-GHOST_CANDIDATES = [(0, 0), (0, 6), (0, 4), (1, 0), (2, 0), (4, 0), (8, 0)]
+# (items per warp, CTAs per SM, wavelength chunks per item)
+GHOST_CANDIDATES = [(0, 0, 1), (0, 0, 2), (0, 0, 4), (0, 0, 8), (0, 0, 16), (0, 6, 4), (1, 0, 4), (1, 0, 1),
+                    (2, 0, 1), (4, 0, 1), (8, 0, 1)]
 
 
 def mdft_candidates(sms: int) -> List[int]:

@@ -331,7 +331,7 @@ template <bool PROBE>
 __device__ __forceinline__ void trace_warp(const RenderArgs& A, const SurfRec* lens, const HotRec* hot,
                                            const float* at, const float* bf, const float4* spec,
                                            const float* kdel, const PairDev& P, const SourceDev& S,
-                                           float2 uv, bool active, float* acc, int pair)
+                                           float2 uv, bool active, float* acc, int pair, int li0, int li1)
 {
     const int n = A.n_surf, a = P.a, b = P.b;
     const int L1 = b + 1, L2 = L1 + (b - a), L = L2 + (n - 1 - a);
@@ -340,11 +340,11 @@ __device__ __forceinline__ void trace_warp(const RenderArgs& A, const SurfRec* l
     const unsigned n_lanes = __popc(__ballot_sync(kFull, active));
     int n_lambda = 0;
     #pragma unroll 1
-    for (int li = 0; li < A.n_spec; ++li)
+    for (int li = li0; li < li1; ++li)
     {
         // probe: stop once any warp has found the pair on the sensor (read
         // through L2, where the other warps' atomics land)
-        if (PROBE && li > 0 && A.pair_hits != nullptr && __ldcg(A.pair_hits + pair) > 0) break;
+        if (PROBE && li > li0 && A.pair_hits != nullptr && __ldcg(A.pair_hits + pair) > 0) break;
         ++n_lambda;
         const float4 sp = spec[li];
         const float kdelta = kdel[li];
@@ -435,27 +435,36 @@ __global__ void __launch_bounds__(kRenderThreads, kRenderMinBlocks) ghost_render
     __syncthreads();
     for (int i = tid; i < A.n_surf; i += blockDim.x) hot[i] = make_hot(lens[i]);
     __syncthreads();
-    // Warp-granular work: each warp takes one (pair, source, 32-sample) item
-    // at a time, so no CTA-wide barrier sits inside the loop.
+    // Warp-granular work: each warp takes one task at a time — a (pair,
+    // source, 32-sample) item and one of its l_chunks wavelength ranges — so
+    // no CTA-wide barrier sits inside the loop, and splitting the wavelengths
+    // shortens the tasks at the queue's tail.
     const int lane = tid & 31;
     const int gwarp = (int)((blockIdx.x * blockDim.x + tid) >> 5);
     const int nwarp = (int)((gridDim.x * blockDim.x) >> 5);
-    int next_static = A.item_base + gwarp;
+    const int chunks = A.l_chunks > 1 ? A.l_chunks : 1;
+    const int l_size = (A.n_spec + chunks - 1) / chunks;
+    const long long n_tasks = (long long)A.n_items * chunks;
+    long long next_static = (long long)A.item_base * chunks + gwarp;
     for (;;)
     {
-        int item;
+        long long task;
         if (A.counter != nullptr)
         {
             int v = 0;
             if (lane == 0) v = atomicAdd(A.counter, 1);
-            item = __shfl_sync(kFull, v, 0);
+            task = __shfl_sync(kFull, v, 0);
         }
         else
         {
-            item = next_static;
+            task = next_static;
             next_static += nwarp;
         }
-        if (item >= A.n_items) break;
+        if (task >= n_tasks) break;
+        const int item = (int)(task / chunks);
+        const int chunk = (int)(task - (long long)item * chunks);
+        const int li0 = chunk * l_size, li1 = min(A.n_spec, li0 + l_size);
+        if (li0 >= li1) continue;
         int4 w;
         if (A.items != nullptr) w = A.items[item];
         else
@@ -483,7 +492,7 @@ __global__ void __launch_bounds__(kRenderThreads, kRenderMinBlocks) ghost_render
         const SourceDev S = A.sources[w.y];
         const bool active = lane < w.w;
         const float2 uv = active ? A.samples[w.z + lane] : make_float2(0.0f, 0.0f);
-        trace_warp<PROBE>(A, lens, hot, at, bf, spec, kdel, P, S, uv, active, acc, w.x);
+        trace_warp<PROBE>(A, lens, hot, at, bf, spec, kdel, P, S, uv, active, acc, w.x, li0, li1);
     }
 }
 
@@ -551,6 +560,7 @@ struct GhostPlan {
     int grid_persistent = 0;
     int per_sm = 0, n_sm = 0;           // resident render CTAs per SM, SM count
     int launch_ipw = 0;                 // 0: persistent queue; > 0: static chunks of this many items per warp
+    int l_chunks = 1;                   // wavelength ranges per item (tasks per item)
     long long rays = 0;                 // ray-wavelength traces per execute
     float front_R = 0.0f, start_z = 0.0f;
     // off-sensor cull (probe passes)
@@ -709,6 +719,14 @@ int probe_grids(const gl_surface* surfaces, int n_surf, int blades_override, flo
     return GL_OK;
 }
 
+// Wavelength ranges per item by default: about eight wavelengths per task
+// (31 -> 4, 16 -> 2, 8 -> 1), the split the autotuner picks on the
+// 31-wavelength frames; set_lambda_split overrides it.
+int default_lambda_split(int n_spec)
+{
+    return std::max(1, std::min(n_spec, (n_spec + 4) / 8));
+}
+
 int plan_create(const gl_surface* surfaces, int n_surf, const gl_ghost_pair* pairs, const float* boosts,
                 const int32_t* pair_grid, int n_pairs, const gl_flare_source* sources, int n_src,
                 const gl_pupil_sample* samples, const int32_t* grid_offsets, int n_grids,
@@ -746,6 +764,9 @@ int plan_create(const gl_surface* surfaces, int n_surf, const gl_ghost_pair* pai
     p->front_R = surfaces[0].semi_aperture;              // ghost_render.cu:738-739
     p->start_z = surfaces[0].z - kSpawnOffset;
     p->width = prm->width; p->height = prm->height; p->prm = *prm;
+    // the per-pair form keeps the reference kernel's shape: every thread loops
+    // over all wavelengths (ghost_render.cu:372)
+    p->l_chunks = prm->plain_per_pair ? 1 : default_lambda_split(n_spec);
 
     std::vector<float> lams((size_t)n_spec), at((size_t)n_spec * n_surf), bf((size_t)n_spec * n_surf);
     std::vector<float4> sp((size_t)n_spec);
@@ -898,6 +919,7 @@ int plan_execute(GhostPlan* p, float* d_out_r, float* d_out_g, float* d_out_b, c
     A.items = p->items; A.pairs = p->pairs; A.sources = p->sources; A.samples = p->samples;
     A.counter = nullptr; A.accum = p->accum;
     A.n_surf = p->n_surf; A.n_spec = p->n_spec; A.n_items = p->n_items; A.item_base = 0;
+    A.l_chunks = p->l_chunks;
     A.width = p->width; A.height = p->height;
     A.fmt_w = (float)p->prm.fmt_w; A.fmt_h = (float)p->prm.fmt_h;
     A.fmt_x0 = (float)p->prm.fmt_x0; A.fmt_y0 = (float)p->prm.fmt_y0;
@@ -1095,6 +1117,14 @@ int gl_ghost_plan_set_launch(gl_ghost_plan* plan, int items_per_warp, int ctas_p
 {
     if (!plan) return fail(GL_ERR_INVALID, "ghost_plan_set_launch: null plan");
     return plan_set_launch(plan->p, items_per_warp, ctas_per_sm);
+}
+
+int gl_ghost_plan_set_lambda_split(gl_ghost_plan* plan, int chunks)
+{
+    if (!plan) return fail(GL_ERR_INVALID, "ghost_plan_set_lambda_split: null plan");
+    if (chunks < 1) return fail(GL_ERR_INVALID, "ghost_plan_set_lambda_split: chunks must be >= 1");
+    plan->p->l_chunks = std::min(chunks, plan->p->n_spec);
+    return GL_OK;
 }
 
 int gl_ghost_plan_info(const gl_ghost_plan* plan, long long* rays, int* n_items, int* grid)

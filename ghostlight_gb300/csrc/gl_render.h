@@ -39,6 +39,7 @@ struct RenderArgs {
     int* pair_hits;           // off-sensor cull: per-pair probe hits (null = no cull)
     unsigned long long* traced;   // ray-wavelength traces executed (null = not counted)
     int n_surf, n_spec, n_items, item_base;
+    int l_chunks;             // wavelength ranges per item (tasks = items x l_chunks); <= 1: one
     // Uniform-grid items (items == null): every pair x source traces the same
     // grid, item i = (pair, source, 32-sample tile) in pair-major order,
     // computed from the index; w_uniform replaces the pairs' per-ray weight.
@@ -54,6 +55,8 @@ struct RenderArgs {
     float hw2, hh2, gain, front_R, start_z;
 };
 
+// Default wavelength split of a render's items (tasks per item) for n_spec wavelengths.
+int default_lambda_split(int n_spec);
 // Shared memory of one render CTA for a lens of n_surf surfaces and n_spec wavelengths.
 size_t render_smem(int n_surf, int n_spec);
 // Opt the render kernels in to `smem` bytes of dynamic shared memory and

@@ -114,6 +114,7 @@ struct ResidentLens {
 struct Request {
     ResidentLens* lens = nullptr;
     int width = 0, height = 0, n_spec = 0, n_src = 0, grid_n = 0, tiles = 0, n_items = 0;
+    int l_chunks = 1;                 // wavelength ranges per item (tasks per item), set at create
     gl_ghost_render_params prm{};
     IorSet ior;
     const float2* samples = nullptr;
@@ -302,6 +303,7 @@ int gl_request_create(gl_lens* lens, int ray_grid, const gl_spectral_sample* spe
     r->lens = L;
     r->prm = *prm;
     r->width = prm->width; r->height = prm->height; r->n_spec = n_spec; r->n_src = n_sources;
+    r->l_chunks = default_lambda_split(n_spec);
     int rc = lens_ior(L, spec, n_spec, &r->ior);
     GridSet g;
     if (!rc) rc = lens_grid(L, ray_grid, &g);
@@ -364,6 +366,14 @@ int gl_request_create(gl_lens* lens, int ray_grid, const gl_spectral_sample* spe
     return GL_OK;
 }
 
+int gl_request_set_lambda_split(gl_request* req, int chunks)
+{
+    if (!req) return fail(GL_ERR_INVALID, "request_set_lambda_split: null request");
+    if (chunks < 1) return fail(GL_ERR_INVALID, "request_set_lambda_split: chunks must be >= 1");
+    req->p->l_chunks = std::min(chunks, std::max(1, req->p->n_spec));
+    return GL_OK;
+}
+
 int gl_request_enqueue(gl_request* req, float* d_out_r, float* d_out_g, float* d_out_b, int items_per_warp,
                        void* stream)
 {
@@ -387,16 +397,21 @@ int gl_request_enqueue(gl_request* req, float* d_out_r, float* d_out_g, float* d
     GL_CUDA_TRY(render_prepare(r->smem, &per_sm, &n_sm));
     const int slots = std::max(1, per_sm) * n_sm;
     const int wpb = kRenderThreads / 32;
+    // CTAs are sized by tasks (items x wavelength ranges): each CTA's warps
+    // take items_per_warp tasks, so a split request runs more, shorter CTAs
+    const long long chunks = std::max(1, r->l_chunks);
     auto grid_for = [&](int n_items) {
-        if (items_per_warp == 0) return std::max(1, std::min((n_items + wpb - 1) / wpb, slots));
+        const long long n_tasks = (long long)n_items * chunks;
+        if (items_per_warp == 0) return (int)std::max(1LL, std::min((n_tasks + wpb - 1) / wpb, (long long)slots));
         const long long per_cta = (long long)wpb * items_per_warp;
-        return (int)std::max(1LL, ((long long)n_items + per_cta - 1) / per_cta);
+        return (int)std::max(1LL, (n_tasks + per_cta - 1) / per_cta);
     };
     RenderArgs A{};
     A.recs = L->recs; A.ior_at = r->ior.at; A.ior_bf = r->ior.bf; A.spec = r->spec;
     A.items = nullptr; A.pairs = L->pairs; A.sources = r->sources; A.samples = r->samples;
     A.accum = r->accum; A.traced = r->traced; A.pair_hits = nullptr;
     A.n_surf = L->n_surf; A.n_spec = r->n_spec; A.n_items = r->n_items; A.item_base = 0;
+    A.l_chunks = (int)chunks;
     A.width = r->width; A.height = r->height;
     A.fmt_w = (float)r->prm.fmt_w; A.fmt_h = (float)r->prm.fmt_h;
     A.fmt_x0 = (float)r->prm.fmt_x0; A.fmt_y0 = (float)r->prm.fmt_y0;

@@ -286,13 +286,15 @@ class GhostRenderPlan:
                                                       out_b.data_ptr(), st), "render_ghosts")
         return _native.last_launch_count()
 
-    def set_launch(self, items_per_warp: int = 0, ctas_per_sm: int = 0):
+    def set_launch(self, items_per_warp: int = 0, ctas_per_sm: int = 0, lambda_chunks: int = 1):
         """Launch shape of the batched render: 0 = persistent work queue over
         ctas_per_sm CTAs per SM (0 = all resident), > 0 = one-shot CTAs of that
-        many 32-sample items per warp."""
+        many 32-sample items per warp; lambda_chunks splits each item's
+        wavelengths into that many tasks."""
         _native.check(self._lib.gl_ghost_plan_set_launch(self._h, int(items_per_warp), int(ctas_per_sm)),
                       "set_launch")
-        self.launch = (int(items_per_warp), int(ctas_per_sm))
+        _native.check(self._lib.gl_ghost_plan_set_lambda_split(self._h, int(lambda_chunks)), "set_launch")
+        self.launch = (int(items_per_warp), int(ctas_per_sm), int(lambda_chunks))
 
     def traced(self) -> int:
         """Ray-wavelength traces the last execute ran (render + probes)."""

@@ -162,6 +162,12 @@ def priority_class(est_rays: int, rays_per_s: float = 7e9, policy: str = "sjf") 
     return -c if policy == "lsf" else c - 3
 
 
+def lambda_split(n_spec: int) -> int:
+    """Wavelength ranges per 32-sample item the library uses by default (about
+    eight wavelengths per task: 31 -> 4, 16 -> 2, 8 -> 1)."""
+    return max(1, min(int(n_spec), (int(n_spec) + 4) // 8))
+
+
 def request_bytes(width: int, height: int, n_pairs: int, host_copy: bool = True) -> int:
     """HBM a request holds: RGBA accumulator + three output planes + tables."""
     px = int(width) * int(height)
@@ -264,11 +270,12 @@ class CudaExecutor:
     its result is copied into pinned host memory on that stream."""
 
     def __init__(self, lenses: Dict[int, ResidentLens], max_inflight: int, items_per_warp: int = 8,
-                 host_output: bool = True, device=None, policy: str = "sjf"):
+                 host_output: bool = True, device=None, policy: str = "sjf", lambda_chunks: Optional[int] = None):
         import torch
         if policy not in POLICIES:
             raise ValueError("priority policy must be one of %s" % (POLICIES,))
         self.policy = policy
+        self.lambda_chunks = lambda_chunks      # None: the library's default split per request
         self.torch = torch
         lo, hi = torch.cuda.Stream.priority_range()
         self.least, self.greatest = max(lo, hi), min(lo, hi)      # e.g. 0 and -5
@@ -288,13 +295,16 @@ class CudaExecutor:
         self._pinned: Dict[tuple, list] = collections.defaultdict(list)
 
     def cta_items(self, req: FlareRequest) -> int:
-        """Items per warp for this request's CTAs: about the same CTA lifetime
-        for every request (an item costs ~ wavelengths x surfaces), so the
-        CTA scheduler can hand SMs to a higher-priority stream often."""
+        """Tasks per warp for this request's CTAs: about the same CTA lifetime
+        for every request (a task costs ~ its wavelengths x surfaces; the
+        library splits an item's wavelengths into lambda_split(n_spec)
+        tasks), so the CTA scheduler can hand SMs to a higher-priority stream
+        often."""
         if self.items_per_warp <= 0:
             return 0
         n_surf = len(self.lenses[req.lens_id].lens.surfaces)
-        cost = max(1.0, req.n_spec * n_surf / 80.0)
+        split = self.lambda_chunks if self.lambda_chunks is not None else lambda_split(req.n_spec)
+        cost = max(1.0, (req.n_spec / min(split, req.n_spec)) * n_surf / 80.0)
         return max(1, int(round(self.items_per_warp / cost)))
 
     def estimate(self, req: FlareRequest) -> None:
@@ -342,6 +352,9 @@ class CudaExecutor:
         run = _Running()
         run.req, run.handle, run.stream = req, h, (lv, stream)
         # the request renders into its own pool-allocated planes
+        if self.lambda_chunks is not None:
+            _native.check(self._lib.gl_request_set_lambda_split(h, min(int(self.lambda_chunks), req.n_spec)),
+                          "request_set_lambda_split")
         _native.check(self._lib.gl_request_enqueue(h, None, None, None, self.cta_items(req), st), "request_enqueue")
         run.host = None
         run.outs = None
@@ -394,11 +407,13 @@ class FlareServer:
 
     def __init__(self, lenses: Dict[int, ResidentLens], budget_bytes: int = 120 * 10 ** 9,
                  max_inflight: int = 16, items_per_warp: int = 8, host_output: bool = True,
-                 executor=None, clock: Callable[[], float] = time.perf_counter, policy: str = "sjf"):
+                 executor=None, clock: Callable[[], float] = time.perf_counter, policy: str = "sjf",
+                 lambda_chunks: Optional[int] = None):
         self.lenses = lenses
         self.sched = Scheduler(budget_bytes, max_inflight)
         self.exec = executor if executor is not None else CudaExecutor(lenses, max_inflight, items_per_warp,
-                                                                       host_output, policy=policy)
+                                                                       host_output, policy=policy,
+                                                                       lambda_chunks=lambda_chunks)
         self.clock = clock
         self.t0 = clock()
         self.running: list = []             # (request, executor handle)

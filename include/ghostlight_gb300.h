@@ -275,6 +275,12 @@ int gl_ghost_plan_info(const gl_ghost_plan* plan, long long* rays, int* n_items,
  * items_per_warp = 0 -> persistent work queue over ctas_per_sm CTAs per SM
  * (0 = all resident); > 0 -> one-shot CTAs of that many 32-sample items per warp. */
 int gl_ghost_plan_set_launch(gl_ghost_plan* plan, int items_per_warp, int ctas_per_sm);
+/* Wavelength split of the render and probe work (the autotuner's other knob;
+ * no counterpart in the reference): each 32-sample item becomes `chunks`
+ * tasks over consecutive wavelength ranges, so the tasks left at the end of
+ * the queue are shorter.  >= 1, clamped to n_spec; the default is about eight
+ * wavelengths per task (31 -> 4, 16 -> 2, 8 -> 1). */
+int gl_ghost_plan_set_lambda_split(gl_ghost_plan* plan, int chunks);
 /* Ray-wavelength traces the last execute ran (render + cull probes; a probe
  * warp stops at its first on-sensor hit).  Synchronous. */
 int gl_ghost_plan_traced(const gl_ghost_plan* plan, long long* out);
@@ -412,6 +418,11 @@ int gl_request_create(gl_lens* lens, int ray_grid, const gl_spectral_sample* spe
  * W x H float32 each): gl_request_planes gives their device address and
  * gl_request_copy_out enqueues one copy of all three to host memory (pinned
  * for an asynchronous copy) or to device memory. */
+/* Wavelength split of the request's probe and render work (as
+ * gl_ghost_plan_set_lambda_split): each item becomes `chunks` tasks over
+ * consecutive wavelength ranges, and one-shot CTAs are sized by tasks, so a
+ * long request runs as more, shorter CTAs.  Before gl_request_enqueue. */
+int gl_request_set_lambda_split(gl_request* req, int chunks);
 int gl_request_enqueue(gl_request* req, float* d_out_r, float* d_out_g, float* d_out_b,
                        int items_per_warp, void* stream);
 int gl_request_planes(const gl_request* req, float** d_rgb);

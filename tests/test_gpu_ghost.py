@@ -280,7 +280,7 @@ def test_autotuned_launch_shapes_give_the_same_image(pins, meta, ref_images, tmp
     plan.execute(*ref)
     torch.cuda.synchronize()
     want = torch.stack(ref).cpu().numpy()
-    for shape in ((0, 4), (1, 0), (8, 0)):
+    for shape in ((0, 4), (1, 0), (8, 0), (0, 0, 4), (2, 0, 3), (0, 0, 8)):
         plan.set_launch(*shape)
         outs = [torch.zeros((256, 256), device="cuda") for _ in range(3)]
         plan.execute(*outs)

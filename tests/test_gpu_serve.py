@@ -77,6 +77,23 @@ def test_work_modes_agree(pool, ipw):
         assert rel_l2(b[r.rid].numpy(), a[r.rid].numpy()) < 1e-5
 
 
+def test_wavelength_split_agrees(pool):
+    """A request split into wavelength ranges (the default: 31 -> 4, 16 -> 2)
+    renders the image of the unsplit request."""
+    p, _ = pool
+    reqs = _reqs()[1:4]
+    a = _run_server(p, reqs, lambda_chunks=1)
+    for r in reqs:
+        r.start = r.finish = 0.0
+    b = _run_server(p, reqs)
+    for r in reqs:
+        r.start = r.finish = 0.0
+    c = _run_server(p, reqs, lambda_chunks=3)
+    for r in reqs:
+        assert rel_l2(b[r.rid].numpy(), a[r.rid].numpy()) < 1e-5
+        assert rel_l2(c[r.rid].numpy(), a[r.rid].numpy()) < 1e-5
+
+
 def test_alone_and_in_the_mix_agree(pool):
     p, _ = pool
     reqs = _reqs()

@@ -140,3 +140,8 @@ def test_latency_stats():
         rs.append(r)
     st = latency_stats(rs)
     assert st["n"] == 100 and abs(st["p50_ms"] - 50.5) < 1e-6 and 99.0 <= st["p99_ms"] <= 100.0
+
+
+def test_default_wavelength_split():
+    from ghostlight_gb300.serve import lambda_split
+    assert [lambda_split(n) for n in (1, 3, 8, 16, 31, 64)] == [1, 1, 1, 2, 4, 8]
