@@ -229,14 +229,14 @@ def run_gpu(args, rank, world):
             prev = None
             for k in range(n):
                 p = prepare_ghost_render(lens, src, W, H, cfg, hw, hh)
-                if prev is not None:                     # frame k-1 finished: release its plan
-                    done[(k - 1) % 2].synchronize()
-                    prev.close()
                 o = outs2[k % 2]
-                p.execute(*o, stream=stream.cuda_stream)
+                p.execute(*o, stream=stream.cuda_stream)       # queued behind frame k-1
                 for c in range(3):
                     host2[k % 2][c].copy_(o[c], non_blocking=True)
                 done[k % 2].record(stream)
+                if prev is not None:                     # frame k-1 landed in host memory: release its plan
+                    done[(k - 1) % 2].synchronize()
+                    prev.close()
                 prev = p
             done[(n - 1) % 2].synchronize()
             prev.close()

@@ -575,26 +575,60 @@ struct GhostPlan {
     unsigned long long* traced = nullptr;   // [render, probe] traces executed by the last execute
     // optional timing events recorded around the probe and render launches
     cudaEvent_t ev_probe = nullptr, ev_render = nullptr, ev_end = nullptr;
+    // Device memory comes from the device's stream-ordered pool: creating and
+    // destroying a plan then costs no device-wide synchronisation (a
+    // cudaFree waits for every stream).  `done` is recorded after each
+    // execute; destroy waits for it (or, after a stream capture, for the
+    // device) and releases the blocks in stream order.
+    cudaMemPool_t pool = nullptr;
+    cudaStream_t own = nullptr;         // the device's plan stream (uploads, releases)
+    cudaEvent_t done = nullptr;
+    bool executed = false, captured = false;
 };
+
+// One non-blocking stream per device for plan uploads and releases.
+static cudaStream_t plan_stream(int dev)
+{
+    static std::mutex mu;
+    static cudaStream_t st[64] = {};
+    if (dev < 0 || dev >= 64) return nullptr;
+    std::lock_guard<std::mutex> lk(mu);
+    if (!st[dev] && cudaStreamCreateWithFlags(&st[dev], cudaStreamNonBlocking) != cudaSuccess) st[dev] = nullptr;
+    return st[dev];
+}
 
 static void plan_free(GhostPlan* p)
 {
     if (!p) return;
-    cudaFree(p->recs); cudaFree(p->ior_at); cudaFree(p->ior_bf); cudaFree(p->spec);
-    cudaFree(p->items); cudaFree(p->pairs); cudaFree(p->sources); cudaFree(p->samples);
-    cudaFree(p->counter); cudaFree(p->accum);
-    cudaFree(p->probe_items); cudaFree(p->probe_samples); cudaFree(p->pair_hits); cudaFree(p->probe_counters);
-    cudaFree(p->traced); cudaFree(p->pair_hits_init);
+    if (p->captured) cudaDeviceSynchronize();               // graph replays may still use the blocks
+    else if (p->executed && p->done) cudaEventSynchronize(p->done);
+    void* blocks[] = {p->recs, p->ior_at, p->ior_bf, p->spec, p->items, p->pairs, p->sources, p->samples,
+                      p->counter, p->accum, p->probe_items, p->probe_samples, p->pair_hits, p->probe_counters,
+                      p->traced, p->pair_hits_init};
+    for (void* b : blocks)
+    {
+        if (!b) continue;
+        if (p->own) cudaFreeAsync(b, p->own);
+        else cudaFree(b);
+    }
+    if (p->done) cudaEventDestroy(p->done);
     delete p;
 }
 
 template <class T>
-static cudaError_t upload(T** dst, const T* src, size_t count)
+static cudaError_t upload(T** dst, const T* src, size_t count, cudaMemPool_t pool, cudaStream_t st)
 {
-    cudaError_t e = cudaMalloc(dst, std::max<size_t>(count, 1) * sizeof(T));
+    cudaError_t e = cudaMallocFromPoolAsync(reinterpret_cast<void**>(dst), std::max<size_t>(count, 1) * sizeof(T),
+                                            pool, st);
     if (e != cudaSuccess) return e;
-    if (count) e = cudaMemcpy(*dst, src, count * sizeof(T), cudaMemcpyHostToDevice);
+    if (count) e = cudaMemcpyAsync(*dst, src, count * sizeof(T), cudaMemcpyHostToDevice, st);
     return e;
+}
+
+template <class T>
+static cudaError_t alloc(T** dst, size_t bytes, cudaMemPool_t pool, cudaStream_t st)
+{
+    return cudaMallocFromPoolAsync(reinterpret_cast<void**>(dst), bytes, pool, st);
 }
 
 size_t render_smem(int n_surf, int n_spec)
@@ -846,26 +880,40 @@ int plan_create(const gl_surface* surfaces, int n_surf, const gl_ghost_pair* pai
 
     cudaError_t e = cudaSuccess;
     auto chk = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
-    chk(upload(&p->recs, recs.data(), recs.size()));
-    chk(upload(&p->ior_at, at.data(), at.size()));
-    chk(upload(&p->ior_bf, bf.data(), bf.size()));
-    chk(upload(&p->spec, sp.data(), sp.size()));
-    chk(upload(&p->items, items.data(), items.size()));
-    chk(upload(&p->pairs, pd.data(), pd.size()));
-    chk(upload(&p->sources, src.data(), src.size()));
-    chk(upload(&p->samples, reinterpret_cast<const float2*>(ordered.data()), (size_t)n_samples));
-    chk(cudaMalloc(&p->counter, sizeof(int)));
-    chk(cudaMalloc(&p->traced, 2 * sizeof(unsigned long long)));
+    chk(shared_device_pool(p->device, &p->pool));
+    p->own = plan_stream(p->device);
+    if (e == cudaSuccess && !p->own) e = cudaErrorInvalidResourceHandle;
+    if (e == cudaSuccess) chk(cudaEventCreateWithFlags(&p->done, cudaEventDisableTiming));
+    if (e != cudaSuccess)
+    {
+        p->own = nullptr;
+        plan_free(p);
+        return fail(GL_ERR_CUDA, std::string("render_ghosts: ") + cudaGetErrorString(e));
+    }
+    cudaMemPool_t pool = p->pool;
+    cudaStream_t ost = p->own;
+    chk(upload(&p->recs, recs.data(), recs.size(), pool, ost));
+    chk(upload(&p->ior_at, at.data(), at.size(), pool, ost));
+    chk(upload(&p->ior_bf, bf.data(), bf.size(), pool, ost));
+    chk(upload(&p->spec, sp.data(), sp.size(), pool, ost));
+    chk(upload(&p->items, items.data(), items.size(), pool, ost));
+    chk(upload(&p->pairs, pd.data(), pd.size(), pool, ost));
+    chk(upload(&p->sources, src.data(), src.size(), pool, ost));
+    chk(upload(&p->samples, reinterpret_cast<const float2*>(ordered.data()), (size_t)n_samples, pool, ost));
+    chk(alloc(&p->counter, sizeof(int), pool, ost));
+    chk(alloc(&p->traced, 2 * sizeof(unsigned long long), pool, ost));
     if (p->cull)
     {
-        chk(upload(&p->probe_items, pitems.data(), pitems.size()));
-        chk(upload(&p->probe_samples, reinterpret_cast<const float2*>(psamples.data()), psamples.size()));
-        chk(cudaMalloc(&p->pair_hits, sizeof(int) * std::max(1, n_pairs)));
-        chk(upload(&p->pair_hits_init, hits_init.data(), hits_init.size()));
-        chk(cudaMalloc(&p->probe_counters, sizeof(int) * 4));
+        chk(upload(&p->probe_items, pitems.data(), pitems.size(), pool, ost));
+        chk(upload(&p->probe_samples, reinterpret_cast<const float2*>(psamples.data()), psamples.size(), pool, ost));
+        chk(alloc(&p->pair_hits, sizeof(int) * std::max(1, n_pairs), pool, ost));
+        chk(upload(&p->pair_hits_init, hits_init.data(), hits_init.size(), pool, ost));
+        chk(alloc(&p->probe_counters, sizeof(int) * 4, pool, ost));
     }
-    chk(cudaMalloc(&p->accum, (size_t)prm->width * prm->height * sizeof(float4)));
-    if (e == cudaSuccess) chk(cudaMemset(p->accum, 0, (size_t)prm->width * prm->height * sizeof(float4)));
+    chk(alloc(&p->accum, (size_t)prm->width * prm->height * sizeof(float4), pool, ost));
+    if (e == cudaSuccess) chk(cudaMemsetAsync(p->accum, 0, (size_t)prm->width * prm->height * sizeof(float4), ost));
+    // the host vectors above go out of scope: the uploads must have landed
+    chk(cudaStreamSynchronize(ost));
     p->smem = render_smem(n_surf, n_spec);
     int per_sm = 0, n_sm = 0;
     if (e == cudaSuccess) chk(render_prepare(p->smem, &per_sm, &n_sm));
@@ -1006,6 +1054,16 @@ int plan_execute(GhostPlan* p, float* d_out_r, float* d_out_g, float* d_out_b, c
         C[0], C[1], C[2], C[3], C[4], C[5], C[6], C[7], C[8]);
     GL_CUDA_TRY(cudaGetLastError());
     ++launches;
+    // completion marker for destroy (see GhostPlan::done)
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    GL_CUDA_TRY(cudaStreamIsCapturing(st, &cs));
+    if (cs == cudaStreamCaptureStatusActive)
+        p->captured = true;
+    else
+    {
+        GL_CUDA_TRY(cudaEventRecord(p->done, st));
+        p->executed = true;
+    }
     g_last_launches = launches;
     return GL_OK;
 }

@@ -55,6 +55,8 @@ struct RenderArgs {
     float hw2, hh2, gain, front_R, start_z;
 };
 
+// The device's stream-ordered memory pool (freed blocks stay reserved).
+cudaError_t shared_device_pool(int dev, cudaMemPool_t* out);
 // Default wavelength split of a render's items (tasks per item) for n_spec wavelengths.
 int default_lambda_split(int n_spec);
 // Shared memory of one render CTA for a lens of n_surf surfaces and n_spec wavelengths.

@@ -93,6 +93,10 @@ unsigned long long* traced_slot()
 
 }  // namespace
 
+// The device's stream-ordered pool (shared by requests and plans).
+cudaError_t shared_device_pool(int dev, cudaMemPool_t* out) { return device_pool(dev, out); }
+
+
 struct ResidentLens {
     int device = 0;
     int n_surf = 0, n_pairs = 0;
