@@ -505,41 +505,71 @@ def run_serving(args):
     """Poisson arrivals at 200 req/s; each request a seeded lens of 8-30
     surfaces from a resident pool, an output of 512^2..4096^2, 8/16/31
     wavelengths, a pupil grid of 32^2..256^2 and a source at 0-20 deg;
-    admitted against a 120 GB HBM budget.  Against serial plain renders
-    (per-call plan, per-pair launches, blocking) of a sample of the same
-    requests."""
+    admitted against a 120 GB HBM budget.  Two mixes over the same lens pool:
+    the ghost layer of every request (the headline), then (--serve-starburst,
+    on by default) the same arrivals with each request's starburst layer
+    added from resident DFT matrices.  Each against serial plain renders
+    (per-call plan, per-pair launches, per-call DFT matrices, blocking) of a
+    sample of its requests."""
     import torch
     import ghostlight_gb300 as gl
-    from ghostlight_gb300.flare import GhostRenderPlan, pupil_grid
-    from ghostlight_gb300.serve import (FlareServer, _spectral, latency_stats, poisson_requests,
-                                        serving_lens_pool)
+    from ghostlight_gb300.serve import _spectral, serving_lens_pool
     cfg = gl.FlareConfig(min_ghost_intensity=MIN_INTENSITY)
     t0 = time.perf_counter()
     pool = serving_lens_pool(SERVE_LENSES, cfg, seed=100, n_min=8, n_max=30)
-    reqs = poisson_requests(args.serve_rate, args.serve_seconds, pool.keys(), seed=5)
+    grids = range(32, 257, 16)
     for rl in pool.values():                      # resident tables: grids and IOR slices of the mix
-        for g in sorted({r.ray_grid for r in reqs}):
+        for g in grids:
             rl.prepare(g)
         for ns in (8, 16, 31):
             rl.prepare(0, _spectral(ns, cfg)[0])
     setup_s = time.perf_counter() - t0
+    out = _serve_mix(args, pool, cfg, False, args.serve_seconds, args.serve_dump)
+    out["lens_setup_s"] = setup_s
+    if args.serve_starburst:
+        out["with_starburst"] = _serve_mix(args, pool, cfg, True, args.serve_sb_seconds, "")
+    for rl in pool.values():
+        rl.close()
+    return out
+
+
+def _serve_mix(args, pool, cfg, sb_on, seconds, dump):
+    import torch
+    import ghostlight_gb300 as gl
+    from ghostlight_gb300.flare import GhostRenderPlan, pupil_grid
+    from ghostlight_gb300.serve import (STARBURST_PUPIL, FlareRequest, FlareServer, _spectral, latency_stats,
+                                        poisson_requests)
+    reqs = poisson_requests(args.serve_rate, seconds, pool.keys(), seed=5, starburst=sb_on)
     # warm: one request per lens
-    from ghostlight_gb300.serve import FlareRequest
     srv = FlareServer(pool, budget_bytes=SERVE_BUDGET, max_inflight=args.serve_slots, items_per_warp=8)
-    srv.run_trace([FlareRequest(lens_id=i, width=512, height=512, n_spec=8, ray_grid=32, field_deg=5.0, rid=i)
-                   for i in pool])
+    srv.run_trace([FlareRequest(lens_id=i, width=512, height=512, n_spec=8, ray_grid=32, field_deg=5.0, rid=i,
+                                starburst=sb_on) for i in pool])
     torch.cuda.synchronize()
+    warm_exec = srv.exec
     srv = FlareServer(pool, budget_bytes=SERVE_BUDGET, max_inflight=args.serve_slots, items_per_warp=8,
                       policy=args.serve_policy)
-    srv.exec.prewarm([(w, w) for w in (512, 1024, 2048, 4096)], 8)
-    with ClockSampler(torch.cuda.current_device()) as clk:
-        t1 = time.perf_counter()
-        srv.run_trace(reqs)
+    # a pinned result buffer per slot and size: no host allocation while serving
+    srv.exec.prewarm([(w, w) for w in (512, 1024, 2048, 4096)], args.serve_slots)
+    sb_bytes = 0
+    if sb_on:                                     # resident DFT matrices of every (size, wavelength count)
+        srv.exec.starburst = warm_exec.starburst
+        srv.exec.prewarm_starburst([(w, w) for w in (512, 1024, 2048, 4096)], (8, 16, 31), cfg)
         torch.cuda.synchronize()
-        wall = time.perf_counter() - t1
+        sb_bytes = sum(p.device_bytes() for p, _ in srv.exec.starburst.plans.values())
+    import gc
+    gc.collect()
+    gc.disable()                                  # no collector pauses inside the request loop
+    try:
+        with ClockSampler(torch.cuda.current_device()) as clk:
+            t1 = time.perf_counter()
+            srv.run_trace(reqs)
+            torch.cuda.synchronize()
+            wall = time.perf_counter() - t1
+    finally:
+        gc.enable()
     traced = sum(r.traced for r in reqs)
-    if args.serve_dump:
-        with open(args.serve_dump, "w") as f:
+    if dump:
+        with open(dump, "w") as f:
             f.write("rid,lens,n_surf,n_pairs,width,n_spec,grid,field,priority,est_rays,traced,arrival,start,finish\n")
             for r in reqs:
                 rl = pool[r.lens_id]
@@ -563,25 +593,37 @@ def run_serving(args):
                                apply_correction=True, plain_per_pair=True)
         outs = torch.empty((3, r.height, r.width), device="cuda")
         plan.execute(outs[0], outs[1], outs[2])
-        host = outs.cpu()
+        if r.starburst:                           # DFT matrices built for this call
+            cx, cy = rl.image_point(r.field_deg, r.width, r.height)
+            lam = spec[:, 0].astype(np.float64)
+            sc = lam.min() / lam
+            mp = gl.MdftPlan(STARBURST_PUPIL, (r.width, r.height), sc / r.width, sc / r.height, spec[:, 1:4],
+                             "split_bf16", center_x=cx, center_y=cy)
+            mp.execute(rl.starburst_pupil(), outs[0], outs[1], outs[2], accumulate=True)
+            mp.close()
+        outs.cpu()
         plan.close()
         ts.append(time.perf_counter() - tt)
     serial_req_s = len(ts) / sum(ts)
     served_req_s = len(reqs) / wall
-    for rl in pool.values():
-        rl.close()
+    if sb_on:
+        srv.exec.starburst.close()
     return {"workload": "Poisson %.0f req/s for %.0f s (%d requests), %d resident lenses of 8-30 surfaces, "
                         "outputs 512^2-4096^2, 8/16/31 wavelengths, pupil grids 32^2-256^2, field 0-20 deg, "
                         "%d slots, %.0f GB HBM budget, %s priorities" % (
-                            args.serve_rate, args.serve_seconds, len(reqs), SERVE_LENSES, args.serve_slots,
+                            args.serve_rate, seconds, len(reqs), SERVE_LENSES, args.serve_slots,
                             SERVE_BUDGET / 1e9, args.serve_policy),
-            "throughput_req_s": served_req_s, "wall_s": wall, "offered_req_s": len(reqs) / args.serve_seconds,
+            "layers": ("ghost + starburst: every request whose source images within a frame width of the frame "
+                       "(%d of %d) adds the split-BF16 matrix DFT of its lens's 256^2 stop pupil from resident "
+                       "plans per (size, wavelength count), %.2f GB" % (sum(bool(r.starburst) for r in reqs),
+                                                                      len(reqs), sb_bytes / 1e9))
+            if sb_on else "ghost",
+            "throughput_req_s": served_req_s, "wall_s": wall, "offered_req_s": len(reqs) / seconds,
             "rays_per_s": traced / wall, "ray_lambda_traces": traced,
             "latency_all": latency_stats(reqs), "latency_by_size": by_size,
             "peak_inflight": srv.sched.peak_inflight, "peak_budget_bytes": srv.sched.peak_used,
             "serial_plain": {"sample": len(ts), "req_s": serial_req_s, "mean_ms": 1e3 * sum(ts) / len(ts)},
-            "speedup_served_vs_serial_plain": served_req_s / serial_req_s,
-            "lens_setup_s": setup_s, "clocks": clk.summary()}
+            "speedup_served_vs_serial_plain": served_req_s / serial_req_s, "clocks": clk.summary()}
 
 
 # ---- anamorphic source sweep (120 frames, one graph) ---------------------------
@@ -800,6 +842,9 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=30.0)
     ap.add_argument("--serve-slots", type=int, default=32)
     ap.add_argument("--serve-rate", type=float, default=SERVE_RATE, help="Poisson arrival rate (requests/s)")
+    ap.add_argument("--serve-starburst", type=int, default=1,
+                    help="1: also serve the mix with every request's starburst layer")
+    ap.add_argument("--serve-sb-seconds", type=float, default=15.0, help="arrival window of the starburst mix")
     ap.add_argument("--serve-policy", default="sjf", choices=("sjf", "lsf", "sjf_fifo"),
                     help="stream priority of a request: shortest first; longest (least slack) first; or "
                          "shortest first with the long requests ranked by arrival")

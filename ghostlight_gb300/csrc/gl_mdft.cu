@@ -741,6 +741,8 @@ __global__ void __launch_bounds__(256) mdft_simt_step2(const float* __restrict__
 }  // namespace
 
 // ---- MDFT plan ----------------------------------------------------------------
+constexpr double kMaxCentre = 12288.0;   // pattern centre range (pixels)
+
 struct MdftPlan {
     int n = 0, Kx = 0, Ky = 0, n_lambda = 0, form = 0, Kp = 0, elem = 2;
     void* wx = nullptr;     // W_x' [lam][2][Kx][Kp]
@@ -806,8 +808,10 @@ extern "C" int gl_mdft_plan_create2(int n, int Kx, int Ky, int n_lambda, const d
     if (n_lambda < 1 || n_lambda > 1024) return fail(GL_ERR_INVALID, "mdft_plan_create: 1..1024 wavelengths");
     if (form < 0 || form > 2)
         return fail(GL_ERR_UNSUPPORTED, "mdft_plan_create: form must be 0 (split BF16), 1 (TF32) or 2 (FP32 CUDA cores)");
-    if (!(std::fabs(center_x) < 4096.0) || !(std::fabs(center_y) < 4096.0))
-        return fail(GL_ERR_INVALID, "mdft_plan_create: centre coordinates must lie within +-4096 pixels");
+    // |k - c| < 8192 + 12288 and |j - cj| <= 2048 keep the phase product
+    // a (k - c) below 2^26, whose float rounding error the FMA captures exactly
+    if (!(std::fabs(center_x) < kMaxCentre) || !(std::fabs(center_y) < kMaxCentre))
+        return fail(GL_ERR_INVALID, "mdft_plan_create: centre coordinates must lie within +-12288 pixels");
     cudaStream_t st = (cudaStream_t)stream;
     MdftPlan* p = new MdftPlan();
     p->n = n; p->Kx = Kx; p->Ky = Ky; p->n_lambda = n_lambda; p->form = form;
@@ -895,8 +899,8 @@ extern "C" int gl_mdft_plan_set_center(gl_mdft_plan* plan, double center_x, doub
 {
     using namespace gl;
     if (!plan) return fail(GL_ERR_INVALID, "mdft_plan_set_center: null plan");
-    if (!(std::fabs(center_x) < 4096.0) || !(std::fabs(center_y) < 4096.0))
-        return fail(GL_ERR_INVALID, "mdft_plan_set_center: centre coordinates must lie within +-4096 pixels");
+    if (!(std::fabs(center_x) < kMaxCentre) || !(std::fabs(center_y) < kMaxCentre))
+        return fail(GL_ERR_INVALID, "mdft_plan_set_center: centre coordinates must lie within +-12288 pixels");
     plan->p->cx = center_x;
     plan->p->cy = center_y;
     GL_CUDA_TRY(mdft_build_matrices(plan->p, (cudaStream_t)stream));

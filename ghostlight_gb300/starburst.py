@@ -92,6 +92,16 @@ class MdftPlan:
         _native.check(self._lib.gl_mdft_plan_status(self._h, C.byref(v)), "mdft")
         return int(v.value)
 
+    def device_bytes(self) -> int:
+        """HBM the plan holds: the two DFT matrices, the operand mask and the
+        intermediate T' in the form's element type (split-BF16: three bf16
+        terms per element along K)."""
+        kp = 3 * self.n if self.form == "split_bf16" else self.n
+        elem = 2 if self.form == "split_bf16" else 4
+        nl = self.n_lambda
+        return (nl * 2 * (self.Kx + self.Ky) * kp * elem + self.n * kp * elem +
+                nl * (self.Kx // 128) * 3 * 128 * kp * elem + 32 * nl + 4)
+
     def close(self):
         if getattr(self, "_h", None):
             self._lib.gl_mdft_plan_destroy(self._h)

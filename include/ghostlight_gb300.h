@@ -338,7 +338,7 @@ int gl_mdft_plan_destroy(gl_mdft_plan* plan);
 int gl_mdft_plan_create2(int n, int Kx, int Ky, int n_lambda, const double* scale_x,
                          const double* scale_y, double center_x, double center_y,
                          const float* weights_rgb, int form, void* stream, gl_mdft_plan** out);
-/* Move the pattern's centre (output pixels, |c| < 4096): enqueues the
+/* Move the pattern's centre (output pixels, |c| < 12288): enqueues the
  * rebuild of the plan's DFT matrices on `stream` (graph-capturable), as the
  * reference rebuilds its phase matrices per source (mdft_render.cu:109-135). */
 int gl_mdft_plan_set_center(gl_mdft_plan* plan, double center_x, double center_y, void* stream);

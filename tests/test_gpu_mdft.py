@@ -105,6 +105,26 @@ def test_rectangular_recentred_and_accumulated(form, tol):
     assert got.shape == (3, Ky, Kx) and err < tol, err
 
 
+def test_far_centre_matches_oracle():
+    """A centre far outside the frame (a source imaged beyond the sensor):
+    the pattern's tail that reaches the frame, against the FP64 oracle."""
+    import ghostlight_gb300 as gl
+    from oracle import mdft_oracle as MO
+    n, Kx, Ky, L = 128, 256, 256, 2
+    A, sx, sy, w = _inputs(n, L, seed=5)
+    dA = torch.from_numpy(A).cuda()
+    for cx, cy in ((-9000.4, 130.0), (11800.75, -6000.5)):
+        plan = gl.MdftPlan(n, (Kx, Ky), sx, sy, w, "split_bf16", center_x=cx, center_y=cy)
+        out = [torch.zeros((Ky, Kx), device="cuda") for _ in range(3)]
+        plan.execute(dA, *out)
+        torch.cuda.synchronize()
+        assert plan.status() == 0
+        plan.close()
+        got = np.stack([o.cpu().numpy() for o in out]).astype(np.float64)
+        want = MO.eform(A, (Kx, Ky), sx, sy, cx, cy, w)
+        assert np.linalg.norm(got - want) / np.linalg.norm(want) < 1e-3
+
+
 def test_set_center_matches_fresh_plan():
     import ghostlight_gb300 as gl
     n, K, L = 128, 256, 2

@@ -94,9 +94,38 @@ def test_wavelength_split_agrees(pool):
         assert rel_l2(c[r.rid].numpy(), a[r.rid].numpy()) < 1e-5
 
 
+def test_request_starburst_layer(pool):
+    """A request with the starburst layer = its ghost layer + the resident
+    plan's pattern of the lens's stop pupil at the source's image point."""
+    import ghostlight_gb300 as gl
+    from ghostlight_gb300.serve import STARBURST_PUPIL, _spectral
+    p, cfg = pool
+    base = _reqs()[3]                                  # 512^2, 31 wavelengths
+    ghost = _run_server(p, [base])[base.rid].numpy()
+    base.start = base.finish = 0.0
+    base.starburst = True
+    both = _run_server(p, [base])[base.rid].numpy()
+    rl = p[base.lens_id]
+    spec, _ = _spectral(base.n_spec, cfg)
+    lam = spec[:, 0].astype(np.float64)
+    sc = lam.min() / lam
+    cx, cy = rl.image_point(base.field_deg, base.width, base.height)
+    plan = gl.MdftPlan(STARBURST_PUPIL, (base.width, base.height), sc / base.width, sc / base.height,
+                       spec[:, 1:4], "split_bf16", center_x=cx, center_y=cy)
+    out = [torch.zeros((base.height, base.width), device="cuda") for _ in range(3)]
+    plan.execute(rl.starburst_pupil(), *out)
+    torch.cuda.synchronize()
+    want = torch.stack(out).cpu().numpy()
+    plan.close()
+    assert want.max() > 0.1 * np.abs(ghost).max()
+    assert rel_l2(both - ghost, want) < 1e-4
+
+
 def test_alone_and_in_the_mix_agree(pool):
     p, _ = pool
     reqs = _reqs()
+    for r in reqs[::2]:
+        r.starburst = True
     alone = {}
     for r in reqs:
         alone.update(_run_server(p, [r]))
