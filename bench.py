@@ -917,8 +917,8 @@ def roofline(res, plan):
 # 2.02e11 FLOP over 1.793e8 traces) and frozen as the algorithmic count.
 FLOPS_PER_RAY_LAMBDA = 1126.0
 # DRAM bytes (read + write) of one render launch on this frame, from one ncu
-# capture: 7.726 GB/s x 5.685 ms.
-RENDER_DRAM_BYTES = 43.9e6
+# capture of the tuned launch: 8.502 GB/s x 5.231 ms.
+RENDER_DRAM_BYTES = 44.5e6
 FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.070e9 / 1e12
 
 
