@@ -80,7 +80,7 @@ __device__ __forceinline__ bool sphere_hit(V3 o, V3 d, float z_s, float c, float
     if (fabsf(d.z) < 1e-12f) return false;
     const float t0 = (z_s - o.z) / d.z;
     const float px = o.x + d.x * t0, py = o.y + d.y * t0;
-    const float A = c * (d.x * d.x + d.y * d.y + d.z * d.z);
+    const float A = c;                      // c |d|^2: the walk's directions are unit
     const float B = c * (px * d.x + py * d.y) - d.z;
     const float C = c * (px * px + py * py);
     const float disc = B * B - A * C;
@@ -241,8 +241,8 @@ __device__ __forceinline__ bool surface_step(V3& o, V3& d, const HotRec& h, cons
         if (!(h2 <= h.sa2)) return false;
         if ((h.bits & HB_POLYGON) && !check_polygon(hx, hy, h2, s)) return false;
         // outward normal (c q_x, c q_y, c q_z - 1), turned to oppose the ray
+        // (for a plane, c = 0, it is (0, 0, -1) as it stands)
         nrm = v3(c * q.x, c * q.y, c * q.z - 1.0f);
-        if (c == 0.0f) nrm = v3(0.0f, 0.0f, -1.0f);
         hit = v3(q.x, q.y, q.z + h.z);
     }
     else
