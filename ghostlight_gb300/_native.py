@@ -30,6 +30,12 @@ def _declare(lib):
     lib.gl_last_launch_count.restype = i
     lib.gl_finalize_z.argtypes = [P(gl_surface), i]
     lib.gl_euler_rotation.argtypes = [C.c_float, C.c_float, C.c_float, P(C.c_float)]
+    fp = P(C.c_float)
+    lib.gl_coating_table_create.argtypes = [i, fp, i, fp, i, fp, C.c_float, i, P(i)]
+    lib.gl_coating_table_info.argtypes = [i, P(i), P(i), P(i), fp, P(i)]
+    lib.gl_coating_table_read.argtypes = [i, fp, fp, fp]
+    lib.gl_coating_table_prepare.argtypes = [i]
+    lib.gl_coating_bake_layers.argtypes = [P(gl_surface), i, i, i, fp, P(i), fp, fp, fp, P(i)]
     lib.gl_blade_radius.argtypes = [i, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, P(C.c_float), i,
                                     P(C.c_float)]
     lib.gl_enumerate_ghost_pairs.argtypes = [P(gl_surface), i, P(gl_ghost_pair), i, P(i)]

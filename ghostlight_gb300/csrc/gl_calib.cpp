@@ -394,7 +394,7 @@ int open_lens(const gl_surface* s, int n, ProbeLens& L)
     L.s = s;
     L.n = n;
     L.recs.resize((size_t)n);
-    const int rc = pack_lens(s, n, L.recs.data());
+    const int rc = pack_lens(s, n, L.recs.data(), kTablesHost);
     if (rc) return rc;
     L.mask = resolve_pupil_mask(s, n, 0, 0.0f);
     L.front_R = s[0].semi_aperture;

@@ -119,7 +119,7 @@ extern "C" int gl_filter_ghost_pairs(const gl_surface* surfaces, int n, float hw
 {
     if (!surfaces || n <= 0 || !prm || !n_out) return fail(GL_ERR_INVALID, "filter_ghost_pairs: bad arguments");
     std::vector<SurfRec> recs((size_t)n);
-    int rc = pack_lens(surfaces, n, recs.data());
+    int rc = pack_lens(surfaces, n, recs.data(), kTablesHost);     // the host re-check's records
     if (rc) return rc;
 
     // Enumerate (ghost.cpp:17-31) and apply the IOR-contrast test
@@ -155,6 +155,12 @@ extern "C" int gl_filter_ghost_pairs(const gl_surface* surfaces, int n, float hw
         int dev = 0;
         chk(cudaGetDevice(&dev));
         if (e == cudaSuccess && (dev < 0 || dev >= 64)) e = cudaErrorInvalidDevice;
+        std::vector<SurfRec> drecs((size_t)n);                      // the device probes' records
+        if (e == cudaSuccess)
+        {
+            rc = pack_lens(surfaces, n, drecs.data(), dev);
+            if (rc) return rc;
+        }
         std::unique_lock<std::mutex> lock(g_scratch_mu);
         Scratch& sc = g_scratch[e == cudaSuccess ? dev : 0];
         if (e == cudaSuccess && sc.bytes < need)
@@ -173,7 +179,7 @@ extern "C" int gl_filter_ghost_pairs(const gl_surface* surfaces, int n, float hw
         ProbeOut* d_out = reinterpret_cast<ProbeOut*>(base + o_out);
         if (e == cudaSuccess)
         {
-            chk(cudaMemcpy(d_recs, recs.data(), sizeof(SurfRec) * n, cudaMemcpyHostToDevice));
+            chk(cudaMemcpy(d_recs, drecs.data(), sizeof(SurfRec) * n, cudaMemcpyHostToDevice));
             chk(cudaMemcpy(d_at, at.data(), sizeof(float) * 3 * n, cudaMemcpyHostToDevice));
             chk(cudaMemcpy(d_bf, bf.data(), sizeof(float) * 3 * n, cudaMemcpyHostToDevice));
             chk(cudaMemcpy(d_pairs, cand.data(), sizeof(int2) * np, cudaMemcpyHostToDevice));

@@ -788,8 +788,10 @@ int plan_create(const gl_surface* surfaces, int n_surf, const gl_ghost_pair* pai
         if (grid_offsets[g + 1] < grid_offsets[g] || grid_offsets[g] < 0)
             return fail(GL_ERR_INVALID, "render_ghosts: grid offsets must be non-decreasing");
 
+    int plan_dev = 0;
+    GL_CUDA_TRY(cudaGetDevice(&plan_dev));
     std::vector<SurfRec> recs((size_t)n_surf);
-    int rc = pack_lens(surfaces, n_surf, recs.data());
+    int rc = pack_lens(surfaces, n_surf, recs.data(), plan_dev);
     if (rc) return rc;
 
     GhostPlan* p = new GhostPlan();
@@ -1265,8 +1267,10 @@ int gl_trace_rays(const gl_surface* surfaces, int n, int bounce_a, int bounce_b,
         return fail(GL_ERR_INVALID, "bounce indices must satisfy 0 <= bounce_a < bounce_b < num_surfaces");
     if (n_rays < 0 || (n_rays > 0 && (!d_rays || !d_out))) return fail(GL_ERR_INVALID, "trace_rays: bad ray buffers");
     if (n_rays == 0) return GL_OK;
+    int dev = 0;
+    GL_CUDA_TRY(cudaGetDevice(&dev));
     std::vector<SurfRec> recs((size_t)n);
-    int rc = pack_lens(surfaces, n, recs.data());
+    int rc = pack_lens(surfaces, n, recs.data(), dev);
     if (rc) return rc;
     std::vector<DispRec> disp((size_t)n);
     for (int i = 0; i < n; ++i)
@@ -1360,7 +1364,7 @@ extern "C" int gl_trace_rays_noalloc(const gl_surface* surfaces, int n, int boun
     int rc = trace_tables_address(device, &base);
     if (rc) return rc;
     NoAllocTables host;   // staged on the stack: no heap, no device allocation
-    rc = pack_lens(surfaces, n, host.recs);
+    rc = pack_lens(surfaces, n, host.recs, device, false);
     if (rc) return rc;
     for (int i = 0; i < n; ++i)
     {

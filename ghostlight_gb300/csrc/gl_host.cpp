@@ -35,7 +35,7 @@ static bool rot_identity(const float* m)
             fabsf(m[6]) < eps && fabsf(m[7]) < eps && fabsf(m[8] - 1.f) < eps);
 }
 
-int pack_lens(const gl_surface* in, int n, SurfRec* out)
+int pack_lens(const gl_surface* in, int n, SurfRec* out, int tables, bool may_upload)
 {
     if (in == nullptr || n <= 0) return fail(GL_ERR_INVALID, "lens has no surfaces");
     if (n > kMaxSurfaces) return fail(GL_ERR_INVALID, "lens has more than 64 surfaces");
@@ -46,9 +46,8 @@ int pack_lens(const gl_surface* in, int n, SurfRec* out)
         std::memset(&r, 0, sizeof(r));
         if (g.aperture_shape == GL_APERTURE_IMAGE)
             return fail(GL_ERR_UNSUPPORTED, "image apertures are outside the flare path");
-        if (g.coating_model != GL_COATING_SIMPLE && g.coating_model != GL_COATING_ARTIST &&
-            g.coating_model != GL_COATING_ATTENUATOR)
-            return fail(GL_ERR_UNSUPPORTED, "table-backed coatings are outside the flare path");
+        if (g.coating_model < GL_COATING_SIMPLE || g.coating_model > GL_COATING_ARTIST)
+            return fail(GL_ERR_INVALID, "unknown coating model " + std::to_string(g.coating_model));
         if (g.aperture_shape == GL_APERTURE_POLYGON && g.aperture_blades < 3)
             return fail(GL_ERR_INVALID, "polygon aperture needs >= 3 blades");
         r.z = g.z;
@@ -83,6 +82,21 @@ int pack_lens(const gl_surface* in, int n, SurfRec* out)
                   ((g.decenter_x != 0.0f || g.decenter_y != 0.0f || !rot_identity(g.rot)) ? SF_TRANSFORMED : 0);
         r.coating = g.coating_model;
         r.ar_layers = g.ar_layers;
+        if (g.coating_model >= GL_COATING_SPECTRAL && g.coating_model <= GL_COATING_SPECTRAL_ANGULAR)
+        {
+            // ar_layers names the table; 0 = none (bare Fresnel)
+            r.ar_layers = 0;
+            if (g.ar_layers != 0)
+            {
+                const float* t = nullptr;
+                int rc = coating_table_address(g.ar_layers, g.coating_model, tables, may_upload, &t, &r.tab_n0,
+                                               &r.tab_n1, &r.tab_discard, &r.tab_ref_ior);
+                if (rc) return rc;
+                const uint64_t a = (uint64_t)(uintptr_t)t;
+                r.tab_lo = (uint32_t)a;
+                r.tab_hi = (uint32_t)(a >> 32);
+            }
+        }
         r.tint_r = g.tint_r; r.tint_g = g.tint_g; r.tint_b = g.tint_b; r.tint_s = g.tint_strength;
         r.g_sigma = g.gauss_sigma; r.g_bg = g.gauss_background; r.g_peak = g.gauss_peak;
         r.g_dx = g.gauss_decenter_x; r.g_dy = g.gauss_decenter_y;

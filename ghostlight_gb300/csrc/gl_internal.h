@@ -24,7 +24,14 @@ struct PupilMask {
     BladeProfile blade{};       // the stop's authored blade shape (blade.deformed), dropped under an override
 };
 
-int pack_lens(const gl_surface* in, int n, SurfRec* out);
+// Pack the trace records of a lens.  Table coatings resolve to their table
+// in the memory space of the trace that reads the records: the host
+// (kTablesHost) or device `tables` (copied there on first use unless
+// `may_upload` is false).
+constexpr int kTablesHost = -1;
+int pack_lens(const gl_surface* in, int n, SurfRec* out, int tables, bool may_upload = true);
+int coating_table_address(int id, int model, int device, bool may_upload, const float** out, int* n0, int* n1,
+                          int* discard, float* ref_ior);
 float ior_at(const gl_surface& s, float lam);
 float ior_before_nd(const gl_surface* s, int idx);
 void build_ior_tables(const gl_surface* s, int n, const float* lambdas, int n_lam, float* at, float* bf);

@@ -157,8 +157,10 @@ extern "C" int gl_psf_render(const gl_surface* surfaces, int n_surfaces, const g
     if (!d_out_r || (!monochromatic && (!d_out_g || !d_out_b))) return fail(GL_ERR_INVALID, "psf_render: null output");
     if (splat_radius_px < 0 || splat_radius_px > 16) return fail(GL_ERR_INVALID, "psf_render: splat radius must be 0..16");
     if (n_sources == 0 || n_grid == 0) return GL_OK;
+    int dev = 0;
+    GL_CUDA_TRY(cudaGetDevice(&dev));
     std::vector<SurfRec> recs((size_t)n_surfaces);
-    int rc = pack_lens(surfaces, n_surfaces, recs.data());
+    int rc = pack_lens(surfaces, n_surfaces, recs.data(), dev);
     if (rc) return rc;
     std::vector<float> lams((size_t)n_spec), at((size_t)n_spec * n_surfaces), bf((size_t)n_spec * n_surfaces);
     std::vector<float4> sp((size_t)n_spec);

@@ -220,8 +220,10 @@ int gl_lens_create(const gl_surface* surfaces, int n_surfaces, const gl_ghost_pa
         if (a < 0 || b <= a || b >= n_surfaces)
             return fail(GL_ERR_INVALID, "lens_create: bounce indices must satisfy 0 <= a < b < n");
     }
+    int dev = 0;
+    GL_CUDA_TRY(cudaGetDevice(&dev));
     std::vector<SurfRec> recs((size_t)n_surfaces);
-    int rc = pack_lens(surfaces, n_surfaces, recs.data());
+    int rc = pack_lens(surfaces, n_surfaces, recs.data(), dev);
     if (rc) return rc;
     ResidentLens* L = new ResidentLens();
     cudaGetDevice(&L->device);

@@ -56,10 +56,17 @@ struct SurfRec {
     float tint_r, tint_g, tint_b, tint_s;
     float g_sigma, g_bg, g_peak, g_dx, g_dy;
     BladeProfile blade;         // authored blade silhouette of a polygon stop (blade.deformed)
+    // table-backed coating (SPECTRAL / ANGULAR / SPECTRAL_ANGULAR): address
+    // of the table in the memory space of the trace that reads the record
+    // (split in two words so the record keeps 4-byte alignment), its
+    // extents, the clamp/discard rule and the angle axis' medium index
+    uint32_t tab_lo, tab_hi;
+    int32_t tab_n0, tab_n1, tab_discard;
+    float tab_ref_ior;
 };
-// 65 words: an odd stride, so lanes reading the same field of different
+// 71 words: an odd stride, so lanes reading the same field of different
 // surfaces in shared memory hit different banks.
-static_assert(sizeof(SurfRec) == 260, "SurfRec must stay 260 bytes");
+static_assert(sizeof(SurfRec) == 284, "SurfRec must stay 284 bytes");
 
 struct V3 {
     float x, y, z;
@@ -146,13 +153,117 @@ GLH float surface_reflectance(float cos_i, float n1, float n2, int layers, float
     return fminf(fmaxf(R, 0.0f), 1.0f);
 }
 
-// surface_weight (trace_core.h:635-783) for the SIMPLE / ARTIST / ATTENUATOR models
+// ---- table-backed coatings (trace_core.h:566-622, 655-760) ----------------
+// Table layout: 1-D models [keys n0 | r n0] (keys ascending: nm or degrees);
+// SPECTRAL_ANGULAR [wavelengths n0 | angles n1 | r n0*n1, wavelength-major].
+GLH const float* coating_table(const SurfRec& s)
+{
+    return reinterpret_cast<const float*>(((uint64_t)s.tab_hi << 32) | (uint64_t)s.tab_lo);
+}
+
+// Bracket `key` on an ascending axis: the lower index and the fraction
+// towards the next sample; keys outside the axis clamp to its ends and, in
+// discard mode, flag the lookup as discarded.
+GLH void coating_bracket(const float* ax, int n, float key, bool discard, int& i0, float& f, bool& dropped)
+{
+    i0 = 0;
+    f = 0.0f;
+    if (key <= ax[0])
+    {
+        if (discard && key < ax[0]) dropped = true;
+        return;
+    }
+    if (key >= ax[n - 1])
+    {
+        if (discard && key > ax[n - 1]) dropped = true;
+        i0 = (n > 1) ? n - 2 : 0;
+        f = (n > 1) ? 1.0f : 0.0f;
+        return;
+    }
+    for (int i = 1; i < n; ++i)
+    {
+        if (key <= ax[i])
+        {
+            i0 = i - 1;
+            const float span = ax[i] - ax[i - 1];
+            f = (span > 0.0f) ? (key - ax[i - 1]) / span : 0.0f;
+            return;
+        }
+    }
+}
+
+// 1-D lookup: the end samples are returned as they are (no blend), the
+// interior as r[i-1] + f (r[i] - r[i-1])
+GLH float coating_lerp(const float* t, int n, float key, bool discard, bool& dropped)
+{
+    const float* r = t + n;
+    if (key <= t[0])
+    {
+        if (discard && key < t[0]) dropped = true;
+        return r[0];
+    }
+    if (key >= t[n - 1])
+    {
+        if (discard && key > t[n - 1]) dropped = true;
+        return r[n - 1];
+    }
+    int i0;
+    float f;
+    coating_bracket(t, n, key, false, i0, f, dropped);
+    return r[i0] + f * (r[i0 + 1] - r[i0]);
+}
+
+// The table's angle axis is measured in a medium of index ref_ior: carry the
+// local incidence over by the Snell invariant n sin(theta); past grazing the
+// lookup reads the 90-degree end.
+GLH float coating_table_angle(float cos_i, float n1, float ref_ior)
+{
+    const float sin_i = sqrtf(fmaxf(0.0f, 1.0f - cos_i * cos_i));
+    const float s_ref = (ref_ior > 0.0f) ? (n1 * sin_i / ref_ior) : sin_i;
+    if (s_ref >= 1.0f) return 90.0f;
+    return asinf(s_ref) * (180.0f / kPi);
+}
+
+// Reflectance of a table-backed coating; `dropped` is set when a discard-mode
+// lookup falls outside the table (the interaction then carries no energy).
+GLH float table_reflectance(const SurfRec& s, float cos_i, float n1, float n2, float lam, bool& dropped)
+{
+    const float* t = coating_table(s);
+    if (t == nullptr || s.tab_n0 <= 0 || (s.coating == 3 && s.tab_n1 <= 0))
+        return fresnel_reflectance(cos_i, n1, n2);
+    const bool discard = s.tab_discard != 0;
+    if (s.coating == 1) return coating_lerp(t, s.tab_n0, lam, discard, dropped);
+    const float ang = coating_table_angle(cos_i, n1, s.tab_ref_ior);
+    if (s.coating == 2) return coating_lerp(t, s.tab_n0, ang, discard, dropped);
+    const int nw = s.tab_n0, na = s.tab_n1;
+    int iw, ia;
+    float fw, fa;
+    coating_bracket(t, nw, lam, discard, iw, fw, dropped);
+    coating_bracket(t + nw, na, ang, discard, ia, fa, dropped);
+    if (dropped) return 0.0f;
+    const float* r = t + nw + na;
+    const int iw1 = (iw + 1 < nw) ? iw + 1 : iw;
+    const int ia1 = (ia + 1 < na) ? ia + 1 : ia;
+    const float r00 = r[iw * na + ia], r01 = r[iw * na + ia1];
+    const float r10 = r[iw1 * na + ia], r11 = r[iw1 * na + ia1];
+    return (1.0f - fw) * ((1.0f - fa) * r00 + fa * r01) + fw * ((1.0f - fa) * r10 + fa * r11);
+}
+
+// surface_weight (trace_core.h:635-783): SIMPLE, ARTIST, the three table
+// models, and bare Fresnel for the attenuator (its positional factor is
+// surface_attenuator's)
 GLH float surface_weight(V3 dir, V3 nrm, float n1, float n2, const SurfRec& s, float lam, bool reflecting)
 {
     float cos_i = fabsf(dot(nrm, dir));
     float R;
     if (s.coating == 0)      R = surface_reflectance(cos_i, n1, n2, s.ar_layers, lam);
     else if (s.coating == 5) R = artist_reflectance(s.tint_r, s.tint_g, s.tint_b, s.tint_s, lam);
+    else if (s.coating >= 1 && s.coating <= 3)
+    {
+        bool dropped = false;
+        R = table_reflectance(s, cos_i, n1, n2, lam, dropped);
+        if (dropped) return 0.0f;
+    }
     else                     R = fresnel_reflectance(cos_i, n1, n2);
     R = fminf(fmaxf(R, 0.0f), 1.0f);
     return reflecting ? R : (1.0f - R);

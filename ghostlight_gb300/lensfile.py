@@ -12,12 +12,12 @@ cosf/sinf through ``gl_euler_rotation``).  Files the reference rejects raise
 ``RuntimeError("OpticalSystem.load() failed: ...")`` (bind_geometry.cpp:386-389);
 where the reference only warns, this reader warns too.
 
-Not carried by this build's surface record: table-backed coatings
-(``spectral``, ``angular``, ``spectral_angular``) and thin-film stacks
-(``layers``, baked by the reference into a spectral-angular table), and bitmap
-(``image``) apertures.  Such a surface loads uncoated / circular with a
-warning and is listed in ``OpticalSystem.unsupported`` so a caller can refuse
-the lens.
+Table-backed coatings (``spectral``, ``angular``, ``spectral_angular``) go
+to the coating store (``ghostlight_gb300.coatings``), the surface record
+naming its table; thin-film stacks (``layers``) are baked after flattening,
+as the reference does.  Not carried by this build: bitmap (``image``)
+apertures, which load circular with a warning and are listed in
+``OpticalSystem.unsupported`` so a caller can refuse the lens.
 """
 from __future__ import annotations
 
@@ -204,10 +204,14 @@ def _apply_glass(name, catalogue, s: gl_surface, path):
 # ---- surface modifiers -----------------------------------------------------
 def _extract_coating(mods, s: gl_surface, path, unsupported: List[str]):
     """extract_coating (optical_system.cpp:351-527): the last coating modifier
-    wins; the default is SIMPLE with no AR layers (bare Fresnel)."""
+    wins; the default is SIMPLE with no AR layers (bare Fresnel).  Tables go
+    to the coating store (the record names them in ar_layers); a ``layers``
+    stack is returned for the bake after flattening, when the glasses are
+    final (optical_system.cpp:1407-1415)."""
+    from . import coatings as K
     coat = dict(model=_COATING_SIMPLE, ar_layers=0, tint=[f32(1.0)] * 3, strength=f32(0.04),
                 gauss=[f32(0.0)] * 5)
-    note = None
+    layers = None
     if isinstance(mods, list):
         for m in mods:
             if not isinstance(m, dict) or m.get("type", "") != "coating":
@@ -217,57 +221,73 @@ def _extract_coating(mods, s: gl_surface, path, unsupported: List[str]):
                 _fail(path, "coating modifier has no 'model' field.")
             fresh = dict(model=_COATING_SIMPLE, ar_layers=0, tint=[f32(1.0)] * 3, strength=f32(0.04),
                          gauss=[f32(0.0)] * 5)
+            discard = m.get("out_of_range", "clamp") == "discard"
             if model == "layers":
-                layers = m.get("layers")
-                if not isinstance(layers, list):
+                jls = m.get("layers")
+                if not isinstance(jls, list):
                     _fail(path, "coating model 'layers' has no 'layers' array.")
-                ok = bool(layers)
-                for jl in layers:
+                specs = []
+                for jl in jls:
                     if not isinstance(jl, dict):
-                        ok = False
+                        specs = None
                         break
-                    nk = [e for e in (jl.get("nk_table") or []) if isinstance(e, dict) and "lambda_um" in e]
-                    if not nk or _value(jl, "thickness_nm", 0.0) <= f32(0.0):
-                        ok = False
+                    nk = [(_num(e["lambda_um"]), _value(e, "n", 1.0), _value(e, "k", 0.0))
+                          for e in (jl.get("nk_table") or []) if isinstance(e, dict) and "lambda_um" in e] \
+                        if isinstance(jl.get("nk_table"), list) else []
+                    th = _value(jl, "thickness_nm", 0.0)
+                    if not nk or th <= f32(0.0):
+                        specs = None
                         break
-                if not ok:
+                    specs.append({"material": str(jl.get("material", "")), "thickness_nm": th,
+                                  "nk_table": np.array(nk, np.float32)})
+                if not specs:
                     _fail(path, "coating 'layers' stack is empty or has a layer with no nk_table / "
                                 "non-positive thickness.")
-                coat, note = fresh, "layers"
+                coat, layers = fresh, specs
             elif model == "simple":
                 fresh["ar_layers"] = int(m.get("ar_layers", 0))
-                coat, note = fresh, None
+                coat, layers = fresh, None
             elif model == "artist":
                 t = m.get("tint")
                 if isinstance(t, list) and len(t) == 3:
                     fresh["tint"] = [_clamp01(_num(x)) for x in t]
                 fresh["strength"] = _clamp01(_value(m, "strength", 0.04))
                 fresh["model"] = _COATING_ARTIST
-                coat, note = fresh, None
+                coat, layers = fresh, None
             elif model in ("spectral", "angular"):
                 key = "lambda_nm" if model == "spectral" else "angle_deg"
-                rows = [e for e in (m.get("data") or []) if isinstance(e, dict) and key in e and "r" in e] \
-                    if isinstance(m.get("data"), list) else []
+                rows = [(_num(e[key]), _clamp01(_num(e["r"]))) for e in m["data"]
+                        if isinstance(e, dict) and key in e and "r" in e] if isinstance(m.get("data"), list) else []
                 if not rows:
                     warnings.warn("%s: coating modifier has an empty/invalid 'data' table; treating as "
                                   "uncoated." % path)
                     continue
-                coat, note = fresh, model
+                d = K.sort_1d(rows)
+                kind = K.SPECTRAL if model == "spectral" else K.ANGULAR
+                ref = _value(m, "angle_ref_ior", 1.0) if model == "angular" else f32(1.0)
+                fresh["model"] = kind
+                fresh["ar_layers"] = K.create_table(kind, d[:, 0], d[:, 1], angle_ref_ior=float(ref),
+                                                    out_of_range_discard=discard)
+                coat, layers = fresh, None
             elif model == "spectral_angular":
                 wl = [_num(v) for v in (m.get("wavelengths_nm") or [])]
                 ang = [_num(v) for v in (m.get("angles_deg") or [])]
-                r = [v for row in (m.get("r") or []) if isinstance(row, list) for v in row]
+                r = [_clamp01(_num(v)) for row in (m.get("r") or []) if isinstance(row, list) for v in row]
                 if (not wl or not ang or len(r) != len(wl) * len(ang) or wl != sorted(wl)
                         or ang != sorted(ang)):
                     warnings.warn("%s: spectral_angular coating has inconsistent or unsorted "
                                   "wavelengths/angles/r arrays; treating as uncoated." % path)
                     continue
-                coat, note = fresh, model
+                fresh["model"] = K.SPECTRAL_ANGULAR
+                fresh["ar_layers"] = K.create_table(K.SPECTRAL_ANGULAR, wl, np.array(r, np.float32), axis1=ang,
+                                                    angle_ref_ior=float(_value(m, "angle_ref_ior", 1.0)),
+                                                    out_of_range_discard=discard)
+                coat, layers = fresh, None
             elif model == "attenuator_gaussian":
                 fresh["model"] = _COATING_ATTENUATOR_GAUSS
                 fresh["gauss"] = [_value(m, k, 0.0) for k in ("sigma", "attenuation_background",
                                                             "attenuation_peak", "decenter_x", "decenter_y")]
-                coat, note = fresh, None
+                coat, layers = fresh, None
             else:
                 _fail(path, "coating model '%s' is not recognised." % model)
     s.coating_model = coat["model"]
@@ -276,8 +296,7 @@ def _extract_coating(mods, s: gl_surface, path, unsupported: List[str]):
     s.tint_strength = float(coat["strength"])
     (s.gauss_sigma, s.gauss_background, s.gauss_peak, s.gauss_decenter_x,
      s.gauss_decenter_y) = (float(v) for v in coat["gauss"])
-    if note is not None:
-        unsupported.append("coating '%s' (table-backed; loaded uncoated)" % note)
+    return layers
 
 
 def _set_circular(s: gl_surface, aspect):
@@ -377,7 +396,7 @@ def _parse_form(jf, s: gl_surface, path):
         s.cyl_axis = 1 if ax in ("y", "Y") else 0
 
 
-def _flatten_element(jel, M: _Transform, nominal_z, catalogue, path, surfaces, notes):
+def _flatten_element(jel, M: _Transform, nominal_z, catalogue, path, surfaces, notes, layer_stacks):
     """flatten_element (optical_system.cpp:801-912); returns the nominal z of
     the element's last surface vertex."""
     js_list, jm_list = jel.get("surfaces"), jel.get("materials")
@@ -400,7 +419,7 @@ def _flatten_element(jel, M: _Transform, nominal_z, catalogue, path, surfaces, n
         s.semi_aperture = float(_value(js, "semi_aperture", 0.0))
         unsupported: List[str] = []
         mods = js.get("modifiers", [])
-        _extract_coating(mods, s, path, unsupported)
+        stack = _extract_coating(mods, s, path, unsupported)
         _parse_form(js.get("form", {}), s, path)
         _apply_apertures(mods, s, path, unsupported)
         thickness = _value(js, "thickness", 0.0)
@@ -420,6 +439,8 @@ def _flatten_element(jel, M: _Transform, nominal_z, catalogue, path, surfaces, n
                           % (path, name, i))
         for u in unsupported:
             notes.append((len(surfaces), u))
+        if stack is not None:
+            layer_stacks[len(surfaces)] = stack
         surfaces.append(s)
         last_nominal = cum_nominal
         cum_local = cum_local + thickness
@@ -549,11 +570,12 @@ def read_lens(path) -> Tuple[List[gl_surface], str, float, List[Tuple[int, str]]
     # pass 3: surfaces, then the inter-element air gaps from nominal z
     surfaces: List[gl_surface] = []
     notes: List[Tuple[int, str]] = []
+    layer_stacks: Dict[int, list] = {}
     emits = []
     for r in records:
         z_nom = r["xform"].pos[2]
         first = len(surfaces)
-        last_z = _flatten_element(r["node"], r["xform"], z_nom, catalogue, path, surfaces, notes)
+        last_z = _flatten_element(r["node"], r["xform"], z_nom, catalogue, path, surfaces, notes, layer_stacks)
         emits.append((z_nom, first, len(surfaces) - first, last_z))
     for k in range(len(emits) - 1):
         _, first, n, last_z = emits[k]
@@ -568,6 +590,11 @@ def read_lens(path) -> Tuple[List[gl_surface], str, float, List[Tuple[int, str]]
             s.z = float(f32(s.z) - total)
     if not surfaces:
         _fail(path, "optical_system produced no surfaces")
+    # post-flatten pass: thin-film stacks bake against the final glasses
+    from . import coatings as K
+    for idx in sorted(layer_stacks):
+        tid = K.bake_layers(surfaces, idx, layer_stacks[idx])
+        K.reset_coating(surfaces[idx], K.SPECTRAL_ANGULAR, tid)
     for idx, what in notes:
         warnings.warn("%s: surface %d: %s is not supported by this build" % (path, idx, what))
     return surfaces, name, float(focal), notes
@@ -617,8 +644,30 @@ def _modifiers(s: gl_surface):
                      "attenuation_background": float(s.gauss_background),
                      "attenuation_peak": float(s.gauss_peak), "decenter_x": float(s.gauss_decenter_x),
                      "decenter_y": float(s.gauss_decenter_y)})
-    else:
-        raise ValueError("save_lens: coating model %d has no table data in this build" % s.coating_model)
+    elif s.coating_model in (1, 2, 3) and s.ar_layers:
+        from . import coatings as K
+        model, a0, a1, r, ref, discard = K.read_table(s.ar_layers)
+        stack = K.layers_of(s.ar_layers) if model == K.SPECTRAL_ANGULAR else None
+        if stack:
+            mods.append({"type": "coating", "model": "layers", "layers": [
+                {"material": d["material"], "thickness_nm": float(d["thickness_nm"]),
+                 "nk_table": [{"lambda_um": float(a), "n": float(b), "k": float(c)} for a, b, c in d["nk_table"]]}
+                for d in stack]})
+        else:
+            m = {"type": "coating", "out_of_range": "discard" if discard else "clamp"}
+            if model == K.SPECTRAL_ANGULAR:
+                m.update(model="spectral_angular", wavelengths_nm=[float(v) for v in a0],
+                         angles_deg=[float(v) for v in a1], r=[[float(v) for v in row] for row in r],
+                         angle_ref_ior=float(ref))
+            else:
+                key = "lambda_nm" if model == K.SPECTRAL else "angle_deg"
+                m.update(model="spectral" if model == K.SPECTRAL else "angular",
+                         data=[{key: float(k), "r": float(v)} for k, v in zip(a0, r)])
+                if model == K.ANGULAR:
+                    m["angle_ref_ior"] = float(ref)
+            mods.append(m)
+    elif s.coating_model not in (1, 2, 3):
+        raise ValueError("save_lens: unknown coating model %d" % s.coating_model)
     ap = {"type": "aperture"}
     if s.aperture_shape == _APERTURE_POLYGON:
         import math

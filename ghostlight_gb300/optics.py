@@ -250,6 +250,92 @@ class OpticalSystem:
                 return float(np.float32(s.ior)) if lambda_nm is None else s.ior_at(lambda_nm)
         return 1.0
 
+    # ---- coating tables (bind_geometry.cpp:412-627) ------------------------
+    def _surface_index(self, i: int) -> int:
+        if i < 0 or i >= len(self.surfaces):
+            raise IndexError("surface index out of range")
+        return i
+
+    def set_coating_spectral_table(self, index: int, data, out_of_range_discard: bool = False) -> None:
+        """R(lambda) from an (N, 2) array of (lambda_nm, r), sorted by key."""
+        from . import coatings as K
+        d = K.sort_1d(data)
+        rec = self.surfaces[self._surface_index(index)].record
+        tid = K.create_table(K.SPECTRAL, d[:, 0], d[:, 1], out_of_range_discard=out_of_range_discard)
+        K.reset_coating(rec, K.SPECTRAL, tid)
+
+    def set_coating_angular_table(self, index: int, data, angle_ref_ior: float = 1.0,
+                                  out_of_range_discard: bool = False) -> None:
+        """R(angle) from an (N, 2) array of (angle_deg, r) measured in a
+        medium of index ``angle_ref_ior``."""
+        from . import coatings as K
+        d = K.sort_1d(data)
+        rec = self.surfaces[self._surface_index(index)].record
+        tid = K.create_table(K.ANGULAR, d[:, 0], d[:, 1], angle_ref_ior=angle_ref_ior,
+                             out_of_range_discard=out_of_range_discard)
+        K.reset_coating(rec, K.ANGULAR, tid)
+
+    def get_coating_table(self, index: int):
+        """The (N, 2) (key, r) table of a SPECTRAL / ANGULAR surface; (0, 2)
+        otherwise."""
+        from . import coatings as K
+        rec = self.surfaces[self._surface_index(index)].record
+        if rec.coating_model in (K.SPECTRAL, K.ANGULAR) and rec.ar_layers:
+            _, a0, _, r, _, _ = K.read_table(rec.ar_layers)
+            return np.stack([a0, r], 1)
+        return np.zeros((0, 2), np.float32)
+
+    def set_coating_sa_table(self, index: int, wavelengths_nm, angles_deg, r, angle_ref_ior: float = 1.0,
+                             out_of_range_discard: bool = False) -> None:
+        """R(lambda, angle) on ascending axes; r is (n_wavelengths, n_angles)."""
+        from . import coatings as K
+        rec = self.surfaces[self._surface_index(index)].record
+        wl = np.asarray(wavelengths_nm, np.float32)
+        ang = np.asarray(angles_deg, np.float32)
+        rr = np.asarray(r, np.float32)
+        if wl.ndim != 1 or ang.ndim != 1 or wl.size < 1 or ang.size < 1:
+            raise ValueError("wavelengths and angles must be 1-D non-empty arrays")
+        if rr.ndim != 2 or rr.shape != (wl.size, ang.size):
+            raise ValueError("r must be an (n_wavelengths, n_angles) array")
+        if np.any(np.diff(wl) < 0) or np.any(np.diff(ang) < 0):
+            raise ValueError("wavelengths and angles must be sorted ascending")
+        tid = K.create_table(K.SPECTRAL_ANGULAR, wl, rr, axis1=ang, angle_ref_ior=angle_ref_ior,
+                             out_of_range_discard=out_of_range_discard)
+        K.reset_coating(rec, K.SPECTRAL_ANGULAR, tid)
+
+    def get_coating_sa_table(self, index: int):
+        """(wavelengths_nm, angles_deg, r) of a SPECTRAL_ANGULAR surface;
+        empty arrays otherwise."""
+        from . import coatings as K
+        rec = self.surfaces[self._surface_index(index)].record
+        if rec.coating_model == K.SPECTRAL_ANGULAR and rec.ar_layers:
+            _, a0, a1, r, _, _ = K.read_table(rec.ar_layers)
+            return a0, a1, r
+        return np.zeros(0, np.float32), np.zeros(0, np.float32), np.zeros((0, 0), np.float32)
+
+    def set_coating_layers(self, index: int, layers) -> None:
+        """A thin-film stack (dicts of material, thickness_nm, nk_table (K, 3)
+        of lambda_um, n, k), baked against the lens's current glasses."""
+        from . import coatings as K
+        i = self._surface_index(index)
+        try:
+            tid = K.bake_layers(self.records(), i, layers)
+        except Exception as e:
+            raise ValueError("set_coating_layers: %s" % e) from None
+        K.reset_coating(self.surfaces[i].record, K.SPECTRAL_ANGULAR, tid)
+
+    def get_coating_layers(self, index: int):
+        from . import coatings as K
+        rec = self.surfaces[self._surface_index(index)].record
+        if rec.coating_model == K.SPECTRAL_ANGULAR and rec.ar_layers:
+            return [dict(d, nk_table=d["nk_table"].copy()) for d in (K.layers_of(rec.ar_layers) or [])]
+        return []
+
+    def clear_coating(self, index: int) -> None:
+        """Uncoated SIMPLE (bare Fresnel)."""
+        from . import coatings as K
+        K.reset_coating(self.surfaces[self._surface_index(index)].record)
+
     # Cached helpers mirroring ghostlight/bindings/python/ghostlight/optical_system.py
     def calibration(self, *, d_line_nm: float = 587.56):
         from .calibration import calibrate_lens

@@ -44,6 +44,9 @@ extern "C" {
 #define GL_DISP_ABBE          1
 #define GL_DISP_SELLMEIER     2
 #define GL_COATING_SIMPLE     0
+#define GL_COATING_SPECTRAL   1   /* ar_layers = gl_coating_table id   */
+#define GL_COATING_ANGULAR    2   /* ar_layers = gl_coating_table id   */
+#define GL_COATING_SPECTRAL_ANGULAR 3 /* ar_layers = gl_coating_table id */
 #define GL_COATING_ATTENUATOR 4
 #define GL_COATING_ARTIST     5
 
@@ -149,6 +152,40 @@ int gl_finalize_z(gl_surface* surfaces, int n);
  * with none authored, the regular polygon.  Host float arithmetic. */
 int gl_blade_radius(int blades, float rotation_rad, float curvature, float twist, float notch_rad,
                     float notch_angle_rad, const float* theta, int n, float* out);
+
+/* ---- table-backed coatings ----------------------------------------------
+ * OpticalSystem::coating_tables (ghostlight/src/optical_system.h:285-301) and
+ * its Python setters set_coating_spectral_table / set_coating_angular_table /
+ * set_coating_sa_table / set_coating_layers (bindings/python/src/
+ * bind_geometry.cpp:412-590).  A table is an immutable entry of a
+ * process-wide store, named by a positive id; a surface selects it with
+ * coating_model = GL_COATING_SPECTRAL / ANGULAR / SPECTRAL_ANGULAR and
+ * ar_layers = id (ar_layers = 0: no table, bare Fresnel as the reference's
+ * null-table fallback, trace_core.h:657-660).  Identical content gives the
+ * same id; entries live for the process.
+ *
+ * gl_coating_table_create: 1-D models take keys axis0[n0] (nm or degrees,
+ * ascending) and r[n0], axis1 = NULL, n1 = 0; SPECTRAL_ANGULAR takes
+ * wavelengths axis0[n0], angles axis1[n1] (both ascending) and
+ * r[n0 * n1] wavelength-major.  angle_ref_ior: index of the medium the angle
+ * axis is measured in (ignored by SPECTRAL); out_of_range_discard: a lookup
+ * outside the table carries no energy instead of clamping. */
+int gl_coating_table_create(int32_t model, const float* axis0, int32_t n0, const float* axis1, int32_t n1,
+                            const float* r, float angle_ref_ior, int32_t out_of_range_discard, int32_t* out_id);
+int gl_coating_table_info(int32_t id, int32_t* model, int32_t* n0, int32_t* n1, float* angle_ref_ior,
+                          int32_t* out_of_range_discard);
+int gl_coating_table_read(int32_t id, float* axis0, float* axis1, float* r);
+/* Copy a table to the current device ahead of an allocation-free render
+ * (the other entry points copy it on first use). */
+int gl_coating_table_prepare(int32_t id);
+/* OpticalSystem::bake_coating_layers (ghostlight/src/optical_system.cpp:
+ * 1483-1575): the thin-film stack of n_layers layers (thickness_nm[l]; n,k
+ * samples at nk_lambda_um in um, nk_count[l] of them per layer, concatenated)
+ * on surface `index`, baked on 400..700 nm x 0..85 degrees into a
+ * SPECTRAL_ANGULAR table whose angle axis is the medium before the surface. */
+int gl_coating_bake_layers(const gl_surface* surfaces, int32_t n, int32_t index, int32_t n_layers,
+                           const float* thickness_nm, const int32_t* nk_count, const float* nk_lambda_um,
+                           const float* nk_n, const float* nk_k, int32_t* out_id);
 
 /* make_rotation, ghostlight/src/optical_system.cpp:185-199 — the element
  * rotation R = Ry(tilt_y) Rx(tilt_x) Rz(roll) of the lens-file loader

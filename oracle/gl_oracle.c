@@ -105,10 +105,40 @@ static orc_blade orc_make_blade(const gl_surface* s)
     return b;
 }
 
+/* ---- coating tables ------------------------------------------------------
+ * OpticalSystem::coating_tables (optical_system.h:288-295) keyed by the id a
+ * table-coated surface carries in ar_layers: the test registers each table
+ * under the id the product's store gave it.  Layout per entry: axis0[n0]
+ * (nm or degrees), axis1[n1] (SPECTRAL_ANGULAR angles), r (n0 or n0*n1,
+ * wavelength-major). */
+#define ORC_MAX_TABLES 256
+typedef struct { int model, n0, n1, discard; float ref_ior; float* data; } orc_table;
+static orc_table orc_tables[ORC_MAX_TABLES];
+
+int orc_coating_register(int id, int model, int n0, int n1, const float* data, float ref_ior, int discard)
+{
+    if (id < 1 || id >= ORC_MAX_TABLES || n0 < 1 || n1 < 0) return -1;
+    const size_t len = (size_t)n0 + (size_t)n1 + (n1 ? (size_t)n0 * n1 : (size_t)n0);
+    float* d = (float*)malloc(len * sizeof(float));
+    if (!d) return -1;
+    memcpy(d, data, len * sizeof(float));
+    free(orc_tables[id].data);
+    orc_tables[id].model = model; orc_tables[id].n0 = n0; orc_tables[id].n1 = n1;
+    orc_tables[id].discard = discard; orc_tables[id].ref_ior = ref_ior; orc_tables[id].data = d;
+    return 0;
+}
+
+static const orc_table* orc_coating_find(int id)
+{
+    if (id < 1 || id >= ORC_MAX_TABLES || !orc_tables[id].data) return NULL;
+    return &orc_tables[id];
+}
+
 /* ---- float instantiation ------------------------------------------------ */
 #define R float
 #define SFX(x) x##_f32
 #define SQRT sqrtf
+#define ASIN asinf
 #define COS cosf
 #define SIN sinf
 #define ATAN2 atan2f
@@ -122,6 +152,7 @@ static orc_blade orc_make_blade(const gl_surface* s)
 #undef R
 #undef SFX
 #undef SQRT
+#undef ASIN
 #undef COS
 #undef SIN
 #undef ATAN2
@@ -136,6 +167,7 @@ static orc_blade orc_make_blade(const gl_surface* s)
 #define R double
 #define SFX(x) x##_f64
 #define SQRT sqrt
+#define ASIN asin
 #define COS cos
 #define SIN sin
 #define ATAN2 atan2

@@ -144,17 +144,88 @@ static inline R SFX(surface_reflectance)(R cos_i, R n1, R n2, int layers, R lam)
     return FMIN(FMAX(Rr, (R)0), (R)1);
 }
 
-/* surface_weight, trace_core.h:635-783 (SIMPLE / ARTIST / ATTENUATOR) */
+/* coating_lerp_1d, trace_core.h:575-602: the end rows are returned as they
+ * are, the interior linearly; *dropped in discard mode outside the keys */
+static inline R SFX(table_lerp)(const float* key, const float* r, int n, R x, int discard, int* dropped)
+{
+    if (x <= (R)key[0]) { if (discard && x < (R)key[0]) *dropped = 1; return (R)r[0]; }
+    if (x >= (R)key[n - 1]) { if (discard && x > (R)key[n - 1]) *dropped = 1; return (R)r[n - 1]; }
+    for (int i = 1; i < n; ++i)
+        if (x <= (R)key[i])
+        {
+            R span = (R)key[i] - (R)key[i - 1];
+            R f = (span > 0) ? (x - (R)key[i - 1]) / span : (R)0;
+            return (R)r[i - 1] + f * ((R)r[i] - (R)r[i - 1]);
+        }
+    return (R)r[n - 1];
+}
+
+/* the bracketing of one SPECTRAL_ANGULAR axis, trace_core.h:699-752 */
+static inline void SFX(table_axis)(const float* ax, int n, R x, int discard, int* i0, R* f, int* dropped)
+{
+    *i0 = 0; *f = 0;
+    if (x <= (R)ax[0]) { if (discard && x < (R)ax[0]) *dropped = 1; return; }
+    if (x >= (R)ax[n - 1])
+    {
+        *i0 = (n > 1) ? n - 2 : 0; *f = (n > 1) ? (R)1 : (R)0;
+        if (discard && x > (R)ax[n - 1]) *dropped = 1;
+        return;
+    }
+    for (int i = 1; i < n; ++i)
+        if (x <= (R)ax[i])
+        {
+            R span = (R)ax[i] - (R)ax[i - 1];
+            *i0 = i - 1;
+            *f = (span > 0) ? (x - (R)ax[i - 1]) / span : (R)0;
+            return;
+        }
+}
+
+/* coating_ref_angle_deg, trace_core.h:614-621 */
+static inline R SFX(table_angle)(R cos_i, R n1, R ref_ior)
+{
+    R sin_i = SQRT(FMAX((R)0, (R)1 - cos_i * cos_i));
+    R s_ref = (ref_ior > 0) ? (n1 * sin_i / ref_ior) : sin_i;
+    if (s_ref >= (R)1) return (R)90.0f;
+    return ASIN(s_ref) * ((R)180.0f / (R)(float)M_PI);
+}
+
+/* surface_weight, trace_core.h:635-783 */
 static inline R SFX(surface_weight)(SFX(v3) dir, SFX(v3) nrm, R n1, R n2,
                                      const gl_surface* s, R lam, int reflecting)
 {
     R cos_i = FABS(SFX(dot)(nrm, dir));
     R Rr;
+    const orc_table* t = (s->coating_model >= 1 && s->coating_model <= 3) ? orc_coating_find(s->ar_layers) : NULL;
     if (s->coating_model == GL_COATING_SIMPLE)
         Rr = SFX(surface_reflectance)(cos_i, n1, n2, s->ar_layers, lam);
     else if (s->coating_model == GL_COATING_ARTIST)
         Rr = SFX(artist_reflectance)((R)s->tint_r, (R)s->tint_g, (R)s->tint_b,
                                      (R)s->tint_strength, lam);
+    else if (t && t->model == s->coating_model)
+    {
+        int dropped = 0;
+        if (t->model == 1)
+            Rr = SFX(table_lerp)(t->data, t->data + t->n0, t->n0, lam, t->discard, &dropped);
+        else if (t->model == 2)
+            Rr = SFX(table_lerp)(t->data, t->data + t->n0, t->n0, SFX(table_angle)(cos_i, n1, (R)t->ref_ior),
+                                 t->discard, &dropped);
+        else
+        {
+            const int nw = t->n0, na = t->n1;
+            const float* rr = t->data + nw + na;
+            const R ang = SFX(table_angle)(cos_i, n1, (R)t->ref_ior);
+            int iw, ia;
+            R fw, fa;
+            SFX(table_axis)(t->data, nw, lam, t->discard, &iw, &fw, &dropped);
+            SFX(table_axis)(t->data + nw, na, ang, t->discard, &ia, &fa, &dropped);
+            if (dropped) return 0;
+            const int iw1 = (iw + 1 < nw) ? iw + 1 : iw, ia1 = (ia + 1 < na) ? ia + 1 : ia;
+            Rr = ((R)1 - fw) * (((R)1 - fa) * (R)rr[iw * na + ia] + fa * (R)rr[iw * na + ia1])
+               + fw * (((R)1 - fa) * (R)rr[iw1 * na + ia] + fa * (R)rr[iw1 * na + ia1]);
+        }
+        if (dropped) return 0;
+    }
     else
         Rr = SFX(fresnel)(cos_i, n1, n2);
     Rr = FMIN(FMAX(Rr, (R)0), (R)1);

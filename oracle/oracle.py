@@ -31,6 +31,7 @@ def _load():
         lib.orc_filter.argtypes = [P(gl_surface), i, f, f, f, i, f, P(i), P(f), P(f), i]
         lib.orc_aperture_samples.argtypes = [P(gl_surface), i, i, i, i, i, f, P(f), i]
         lib.orc_blade_radius.argtypes = [P(gl_surface), P(f), i, P(f)]
+        lib.orc_coating_register.argtypes = [i, i, i, i, P(f), f, i]
         lib.orc_render.argtypes = [P(gl_surface), i, P(i), P(f), P(i), i, P(f), i, P(f), P(i),
                                    P(f), i, f, f, i, i, f, i, i, P(d)]
         _lib = lib
@@ -47,6 +48,20 @@ def _ip(a):
 
 def _dp(a):
     return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def register_coating(table_id, model, axis0, r, axis1=None, angle_ref_ior=1.0, discard=False):
+    """Give the oracle the table a surface names by ``ar_layers = table_id``
+    (OpticalSystem::coating_tables, optical_system.h:288-295): 1-D models
+    take keys ``axis0`` and ``r``; SPECTRAL_ANGULAR (model 3) wavelengths
+    ``axis0``, angles ``axis1`` and ``r`` of shape (len(axis0), len(axis1))."""
+    lib = _load()
+    a0 = np.asarray(axis0, np.float32).ravel()
+    a1 = np.zeros(0, np.float32) if axis1 is None else np.asarray(axis1, np.float32).ravel()
+    data = np.ascontiguousarray(np.concatenate([a0, a1, np.asarray(r, np.float32).ravel()]), np.float32)
+    if lib.orc_coating_register(int(table_id), int(model), len(a0), len(a1), _fp(data), float(angle_ref_ior),
+                                int(bool(discard))) != 0:
+        raise ValueError("oracle: bad coating table %d" % table_id)
 
 
 def trace(surfs, a, b, rays, fp64=True):

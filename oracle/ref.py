@@ -53,6 +53,9 @@ def _load():
     lib.ref_render_ghosts_cpu.argtypes = [P(gl_surface), i, P(i), P(f), i, P(f), i,
                                           P(f), i, P(f), i, f, f, i, i, f, i, P(f)]
     lib.ref_render_ghosts_cpu.restype = i
+    lib.ref_coating_register.argtypes = [i, i, i, i, P(f), f, i]
+    lib.ref_bake_layers.argtypes = [P(gl_surface), i, i, i, P(f), P(i), P(f), P(f), P(f), P(f), P(f), P(f), P(f)]
+    lib.ref_load_lens_coating.argtypes = [C.c_char_p, i, P(i), P(f), P(f), i]
     assert lib.ref_sizeof_surface() == C.sizeof(gl_surface)
     _lib = lib
     return lib
@@ -75,6 +78,53 @@ def load_lens(path):
     arr = (gl_surface * n)()
     lib.ref_load_lens(str(path).encode(), arr, n, C.byref(fl))
     return list(arr), float(fl.value)
+
+
+def register_coating(table_id, model, axis0, r, axis1=None, angle_ref_ior=1.0, discard=False):
+    """Attach a coating table to every flat record that names ``table_id``
+    in ar_layers (as OpticalSystem::coating_tables for the reference)."""
+    lib = _load()
+    a0 = np.asarray(axis0, np.float32).ravel()
+    a1 = np.zeros(0, np.float32) if axis1 is None else np.asarray(axis1, np.float32).ravel()
+    data = np.ascontiguousarray(np.concatenate([a0, a1, np.asarray(r, np.float32).ravel()]), np.float32)
+    lib.ref_coating_register(int(table_id), int(model), len(a0), len(a1), _fp(data), float(angle_ref_ior),
+                             int(bool(discard)))
+
+
+def bake_layers(surfs, index, layers):
+    """OpticalSystem::bake_coating_layers: layers = [(thickness_nm, nk (K,3)
+    of lambda_um, n, k)] -> (wavelengths, angles, r (31, 18), angle_ref_ior)."""
+    lib = _load()
+    th = np.array([t for t, _ in layers], np.float32)
+    cnt = np.array([len(nk) for _, nk in layers], np.int32)
+    nk = np.concatenate([np.asarray(nk, np.float32).reshape(-1, 3) for _, nk in layers])
+    lam, nn, kk = (np.ascontiguousarray(nk[:, c]) for c in range(3))
+    wl, ang, r = np.zeros(31, np.float32), np.zeros(18, np.float32), np.zeros((31, 18), np.float32)
+    ref = C.c_float()
+    if lib.ref_bake_layers(surface_array(surfs), len(surfs), index, len(layers), _fp(th), _ip(cnt), _fp(lam),
+                           _fp(nn), _fp(kk), _fp(wl), _fp(ang), _fp(r), C.byref(ref)) != 0:
+        raise RuntimeError("reference bake failed")
+    return wl, ang, r, float(ref.value)
+
+
+def load_lens_coating(path, index):
+    """The reference loader's coating of surface ``index``: (model, axis0,
+    axis1, r, angle_ref_ior, discard); empty arrays when it has no table."""
+    lib = _load()
+    meta = np.zeros(4, np.int32)
+    ref = C.c_float()
+    n = lib.ref_load_lens_coating(str(path).encode(), index, _ip(meta), C.byref(ref), None, 0)
+    if n < 0:
+        raise RuntimeError("reference loader rejected %s" % path)
+    data = np.zeros(max(n, 1), np.float32)
+    lib.ref_load_lens_coating(str(path).encode(), index, _ip(meta), C.byref(ref), _fp(data), n)
+    m, n0, n1, disc = (int(v) for v in meta)
+    a0 = data[:n0].copy()
+    a1 = data[n0:n0 + n1].copy()
+    r = data[n0 + n1:n].copy()
+    if n1:
+        r = r.reshape(n0, n1)
+    return m, a0, a1, r, float(ref.value), bool(disc)
 
 
 def trace(surfs, a, b, rays):

@@ -23,10 +23,18 @@
 
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <vector>
 #include <omp.h>
 
 namespace {
+
+// Coating tables by the id a table-coated flat record carries in ar_layers
+// (the test registers each one with ref_coating_register); make_lens puts
+// them into OpticalSystem::coating_tables the way the reference's own
+// setters do (bind_geometry.cpp:412-513).
+struct RefTable { int model, n0, n1, discard; float ref_ior; std::vector<float> data; };
+std::map<int, RefTable> g_ref_tables;
 
 void to_ref(const gl_surface& g, Surface& s)
 {
@@ -91,6 +99,29 @@ OpticalSystem* make_lens(const gl_surface* surfs, int n)
     L->surface_ids.resize(n);
     L->aperture_images.resize(n);
     L->coating_tables.resize(n);
+    for (int i = 0; i < n; ++i)
+    {
+        const int m = surfs[i].coating_model;
+        if (m < 1 || m > 3) continue;
+        Coating& c = L->surfaces[i].coating;
+        c.ar_layers = 0;
+        auto it = g_ref_tables.find(surfs[i].ar_layers);
+        if (it == g_ref_tables.end() || it->second.model != m) continue;
+        const RefTable& t = it->second;
+        CoatingTables& ct = L->coating_tables[i];
+        if (m == 3)
+        {
+            ct.sa_wavelengths.assign(t.data.begin(), t.data.begin() + t.n0);
+            ct.sa_angles.assign(t.data.begin() + t.n0, t.data.begin() + t.n0 + t.n1);
+            ct.sa_r.assign(t.data.begin() + t.n0 + t.n1, t.data.end());
+        }
+        else
+        {
+            for (int k = 0; k < t.n0; ++k) ct.table.push_back({t.data[k], t.data[t.n0 + k]});
+        }
+        c.out_of_range_discard = t.discard != 0;
+        c.angle_ref_ior = t.ref_ior;
+    }
     L->sync_coating_pointers();
     return L;
 }
@@ -109,6 +140,85 @@ FlareConfig make_filter_cfg(float min_int, int normalize, float max_boost)
 extern "C" {
 
 int ref_sizeof_surface() { return (int)sizeof(gl_surface); }
+
+int ref_coating_register(int id, int model, int n0, int n1, const float* data, float ref_ior, int discard)
+{
+    RefTable t{model, n0, n1, discard, ref_ior, {}};
+    const size_t len = (size_t)n0 + n1 + (n1 ? (size_t)n0 * n1 : (size_t)n0);
+    t.data.assign(data, data + len);
+    g_ref_tables[id] = std::move(t);
+    return 0;
+}
+
+// OpticalSystem::bake_coating_layers on surface `index` of a flat table:
+// out_wl[31], out_ang[18], out_r[31*18], *ref_ior.  Layers as
+// gl_coating_bake_layers takes them.
+int ref_bake_layers(const gl_surface* surfs, int n, int index, int n_layers, const float* thickness_nm,
+                    const int* nk_count, const float* nk_lambda_um, const float* nk_n, const float* nk_k,
+                    float* out_wl, float* out_ang, float* out_r, float* ref_ior)
+{
+    OpticalSystem* L = make_lens(surfs, n);
+    int o = 0;
+    for (int l = 0; l < n_layers; ++l)
+    {
+        CoatingLayerSpec spec;
+        spec.thickness_nm = thickness_nm[l];
+        for (int k = 0; k < nk_count[l]; ++k)
+        {
+            spec.nk_lambda_um.push_back(nk_lambda_um[o + k]);
+            spec.nk_n.push_back(nk_n[o + k]);
+            spec.nk_k.push_back(nk_k[o + k]);
+        }
+        o += nk_count[l];
+        L->coating_tables[index].layers.push_back(spec);
+    }
+    std::string err;
+    const bool ok = L->bake_coating_layers(index, &err);
+    int rc = -1;
+    const CoatingTables& t = L->coating_tables[index];
+    if (ok && t.sa_wavelengths.size() == 31 && t.sa_angles.size() == 18)
+    {
+        std::memcpy(out_wl, t.sa_wavelengths.data(), 31 * 4);
+        std::memcpy(out_ang, t.sa_angles.data(), 18 * 4);
+        std::memcpy(out_r, t.sa_r.data(), 31 * 18 * 4);
+        *ref_ior = L->surfaces[index].coating.angle_ref_ior;
+        rc = 0;
+    }
+    delete L;
+    return rc;
+}
+
+// The coating tables the reference loader gives surface `index` of a lens
+// file: model, extents, discard flag and angle medium into meta
+// (model, n0, n1, discard), ref_ior; the table as axis0 | axis1 | r into
+// data (cap floats).  Returns the float count, or -1.
+int ref_load_lens_coating(const char* path, int index, int* meta, float* ref_ior, float* data, int cap)
+{
+    OpticalSystem L;
+    if (!L.load(path) || index < 0 || index >= L.num_surfaces()) return -1;
+    const Coating& c = L.surfaces[index].coating;
+    const CoatingTables& t = L.coating_tables[index];
+    std::vector<float> d;
+    int n0 = 0, n1 = 0;
+    if (!t.table.empty())
+    {
+        n0 = (int)t.table.size();
+        for (const auto& e : t.table) d.push_back(e.key);
+        for (const auto& e : t.table) d.push_back(e.r);
+    }
+    else if (!t.sa_r.empty())
+    {
+        n0 = (int)t.sa_wavelengths.size();
+        n1 = (int)t.sa_angles.size();
+        d.insert(d.end(), t.sa_wavelengths.begin(), t.sa_wavelengths.end());
+        d.insert(d.end(), t.sa_angles.begin(), t.sa_angles.end());
+        d.insert(d.end(), t.sa_r.begin(), t.sa_r.end());
+    }
+    meta[0] = (int)c.model; meta[1] = n0; meta[2] = n1; meta[3] = c.out_of_range_discard ? 1 : 0;
+    *ref_ior = c.angle_ref_ior;
+    if (data) for (int k = 0; k < (int)d.size() && k < cap; ++k) data[k] = d[(size_t)k];
+    return (int)d.size();
+}
 
 // Load a .lens file with the reference loader; returns the surface count, or
 // -1 on failure.  out may be NULL to query the count.

@@ -21,9 +21,7 @@ from ghostlight_gb300.lensfile import LensFileError
 GOLDEN = pathlib.Path(__file__).resolve().parent / "golden"
 LENSES = GOLDEN / "lenses"
 
-# fields a table-backed coating (not carried by this build) sets in the reference
-COATING_FIELDS = ("coating_model", "ar_layers", "tint_r", "tint_g", "tint_b", "tint_strength",
-                  "gauss_sigma", "gauss_background", "gauss_peak", "gauss_decenter_x", "gauss_decenter_y")
+TABLE_MODELS = (1, 2, 3)
 
 
 def _table(lens):
@@ -31,15 +29,32 @@ def _table(lens):
 
 
 def _compare(ours, ref, unsupported):
+    """Field-for-field equality; a table-coated record names its table in
+    ar_layers (the reference keeps the table beside the surface)."""
     assert len(ours) == len(ref)
-    masked = {i for i, _ in unsupported}
     for name in SURFACE_DTYPE.names:
         a, b = ours[name], ref[name]
         for i in range(len(ours)):
-            if i in masked and name in COATING_FIELDS:
+            if name == "ar_layers" and ours["coating_model"][i] in TABLE_MODELS:
                 continue
             assert np.array_equal(np.asarray(a[i]).view(np.uint32), np.asarray(b[i]).view(np.uint32)), \
                 "surface %d field %s: %r != %r" % (i, name, a[i], b[i])
+
+
+def _compare_tables(lens, path):
+    """Each table-coated surface's table against the live reference loader's."""
+    from ghostlight_gb300 import coatings as K
+    from oracle import ref
+    for i, s in enumerate(lens.surfaces):
+        m, a0, a1, r, rior, disc = ref.load_lens_coating(path, i)
+        if s.coating_model not in TABLE_MODELS or not s.ar_layers:
+            assert len(a0) == 0, "surface %d: the reference has a table" % i
+            continue
+        got = K.read_table(s.ar_layers)
+        assert got[0] == m and got[5] == disc and np.float32(got[4]) == np.float32(rior), i
+        for x, y in ((got[1], a0), (got[2], a1), (got[3], r)):
+            np.testing.assert_array_equal(np.asarray(x, np.float32).view(np.uint32),
+                                          np.asarray(y, np.float32).view(np.uint32))
 
 
 @pytest.mark.parametrize("name", ["fixture_rig", "fixture_modifiers", "fixture_minimal"])
@@ -57,11 +72,13 @@ def test_fixture_warnings_and_unsupported():
         lens = OpticalSystem.load(LENSES / "fixture_modifiers.lens")
     msgs = " ".join(str(w.message) for w in rec)
     for frag in ("truncating to 8", "curvature must be within", "blades >= 3", "empty/invalid 'data'",
-                 "aperture_aspect must be > 0", "unknown aperture shape", "not supported by this build"):
+                 "aperture_aspect must be > 0", "unknown aperture shape"):
         assert frag in msgs
     # the valid spectral table (surface 4) is table-backed; the later simple
     # coating after the layer stack (surface 5) replaces it
-    assert [i for i, _ in lens.unsupported] == [4]
+    assert lens.unsupported == []
+    assert lens.surfaces[4].coating_model == 1
+    np.testing.assert_array_equal(lens.get_coating_table(4), np.float32([[450.0, 0.01], [650.0, 0.02]]))
     s = lens.surfaces
     assert s[1].n_asphere_terms == 8 and s[2].cyl_axis == 1 and not s[4].is_active
     assert s[1].aperture_blades == 9 and s[1].aperture_curvature == 1.0
@@ -146,4 +163,16 @@ def test_reference_library_lens(path):
         warnings.simplefilter("ignore")
         lens = load_lens(path)
     _compare(_table(lens), np.frombuffer(bytes(surface_array(surfs)), dtype=SURFACE_DTYPE), lens.unsupported)
+    _compare_tables(lens, path)
     assert np.float32(lens.focal_length) == np.float32(fl)
+
+
+@pytest.mark.parametrize("name", ["fixture_rig", "fixture_modifiers", "fixture_minimal", "fixture_coatings"])
+def test_fixture_tables_match_live_reference(name):
+    from oracle import ref
+    if not ref.available():
+        pytest.skip("reference loader not built")
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        lens = load_lens(LENSES / (name + ".lens"))
+    _compare_tables(lens, LENSES / (name + ".lens"))
