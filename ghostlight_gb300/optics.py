@@ -111,9 +111,31 @@ class Coating:
     def model(self, v):
         self._rec.coating_model = int(v)
 
+    # table attributes (bind_geometry.cpp:153-164) live with the table the
+    # record names; reading them on a coating without a table gives the
+    # defaults
+    _TABLE_ATTRS = ("angle_ref_ior", "out_of_range_discard", "table_count", "sa_n_wavelengths", "sa_n_angles")
+
+    def _table(self):
+        if self._rec.coating_model in (1, 2, 3) and self._rec.ar_layers:
+            from .coatings import table_info
+            return table_info(self._rec.ar_layers)
+        return None
+
     def __getattr__(self, k):
         if k in Coating._MAP:
             return getattr(self._rec, Coating._MAP[k])
+        if k in Coating._TABLE_ATTRS:
+            t = self._table()
+            if k == "angle_ref_ior":
+                return t["angle_ref_ior"] if t else 1.0
+            if k == "out_of_range_discard":
+                return t["out_of_range_discard"] if t else False
+            if t is None:
+                return 0
+            if k == "table_count":
+                return t["n0"] if t["model"] in (1, 2) else 0
+            return (t["n0"] if k == "sa_n_wavelengths" else t["n1"]) if t["model"] == 3 else 0
         raise AttributeError(k)
 
     def __setattr__(self, k, v):
@@ -121,6 +143,16 @@ class Coating:
             self._rec.coating_model = int(v)
         elif k in Coating._MAP:
             setattr(self._rec, Coating._MAP[k], v)
+        elif k in ("angle_ref_ior", "out_of_range_discard"):
+            # tables are immutable: the record moves to the table with the new attribute
+            if self._table() is not None:
+                from .coatings import create_table, read_table
+                model, a0, a1, r, ref, disc = read_table(self._rec.ar_layers)
+                if k == "angle_ref_ior":
+                    ref = float(v)
+                else:
+                    disc = bool(v)
+                self._rec.ar_layers = create_table(model, a0, r, a1 if len(a1) else None, ref, disc)
         else:
             raise AttributeError("Coating has no field %r" % k)
 

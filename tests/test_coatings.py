@@ -191,6 +191,12 @@ def test_accessors_round_trip(tmp_path):
     for i in (2, 4, 6, 9):
         a, b = lens.surfaces[i], back.surfaces[i]
         assert (a.coating_model, a.ar_layers) == (b.coating_model, b.ar_layers), i
+    c = lens.surfaces[4].coating
+    assert c.table_count == 2 and c.sa_n_wavelengths == 0 and not c.out_of_range_discard
+    c.out_of_range_discard = True
+    assert lens.surfaces[4].coating.out_of_range_discard
+    assert lens.surfaces[4].coating.angle_ref_ior == pytest.approx(1.6)
+    assert lens.surfaces[6].coating.sa_n_wavelengths == 2 and lens.surfaces[6].coating.sa_n_angles == 3
     lens.clear_coating(6)
     assert lens.surfaces[6].coating_model == 0 and lens.surfaces[6].ar_layers == 0
     assert lens.get_coating_sa_table(6)[0].size == 0
