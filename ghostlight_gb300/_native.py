@@ -31,6 +31,13 @@ def _declare(lib):
     lib.gl_finalize_z.argtypes = [P(gl_surface), i]
     lib.gl_euler_rotation.argtypes = [C.c_float, C.c_float, C.c_float, P(C.c_float)]
     fp = P(C.c_float)
+    vp_ = C.c_void_p
+    lib.gl_sprite_plan_create.argtypes = [i, P(gl_spectral_sample), i, C.c_float, P(vp_)]
+    lib.gl_sprite_plan_bake.argtypes = [vp_, vp_, i, vp_]
+    lib.gl_sprite_plan_splat.argtypes = [vp_, fp, i, C.c_float, C.c_float, C.c_float, C.c_float, i, i, C.c_float,
+                                         vp_, vp_, vp_, i, i, vp_]
+    lib.gl_sprite_plan_read.argtypes = [vp_, vp_, vp_, P(C.c_double), P(i), vp_]
+    lib.gl_sprite_plan_destroy.argtypes = [vp_]
     lib.gl_coating_table_create.argtypes = [i, fp, i, fp, i, fp, C.c_float, i, P(i)]
     lib.gl_coating_table_info.argtypes = [i, P(i), P(i), P(i), fp, P(i)]
     lib.gl_coating_table_read.argtypes = [i, fp, fp, fp]

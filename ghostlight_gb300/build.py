@@ -41,6 +41,7 @@ UNITS = {
     "gl_serve.cu": FAST,
     "gl_veil.cu": FAST,
     "gl_psf.cu": FAST,
+    "gl_sprite.cu": FAST,
 }
 # Occupancy target of the render kernel (CTAs of 128 threads per SM); an
 # environment override lets a tuning sweep rebuild with another value.

@@ -459,8 +459,16 @@ def render_source_flare(offsets, width: int, height: int, lens: OpticalSystem,
                     * calibration.sensor_half_h / hh
             pos[i] = (sx * width, sy * height, src[i, 2], src[i, 3], src[i, 4])
     if want_sb:
-        from .starburst import starburst_layer
-        out.update(starburst_layer(lens, calibration, config, pos, width, height, hw, hh))
+        # engine choice as render_starburst (starburst_render.cu:646-711): the
+        # SPRITE engine by default and whenever the pattern is prominent or
+        # the grid grows; the matrix-DFT field form otherwise when asked for
+        from .starburst import sprite_geometry, sprite_starburst_layer, starburst_layer
+        geo = sprite_geometry(calibration, config, pos, width, height, hw, hh,
+                              front_R=lens.surfaces[0].semi_aperture if lens.surfaces else 0.0)
+        if geo["engine"] == "sprite":
+            out.update(sprite_starburst_layer(lens, calibration, config, pos, width, height, hw, hh, geometry=geo))
+        else:
+            out.update(starburst_layer(lens, calibration, config, pos, width, height, hw, hh))
     if want_veil:
         from .veil import render_veil
         out.update(render_veil(pos, width, height, hw, hh, dc.veil_spread, dc.veil_falloff, dc.veil_gain))

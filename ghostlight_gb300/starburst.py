@@ -202,3 +202,217 @@ def starburst_layer(lens, calibration, config, sources_px, width: int, height: i
         raise _native.GhostlightError("starburst: device pipeline wait timed out (code %d)" % code)
     return {"starburst_r": out[0, :height, :width].contiguous(), "starburst_g": out[1, :height, :width].contiguous(),
             "starburst_b": out[2, :height, :width].contiguous()}
+
+
+# ---------------------------------------------------------------------------
+# SPRITE engine (render_starburst's default path, starburst_render.cu:594-1073)
+# ---------------------------------------------------------------------------
+LAMBDA_REF_NM = 550.0       # wavelength of the one FFT
+SPRITE_OVERSAMPLE = 3       # sprite texels kept per output pixel after the box sum
+APERTURE_REF_FNUMBER = 2.8
+
+
+class SpritePlan:
+    """Resident sprite pipeline for one grid and spectral table: FFT of the
+    pupil, PSF, wavelength bake + box sum, splat (gl_sprite_plan_*)."""
+
+    def __init__(self, N: int, spec, lambda_ref: float = LAMBDA_REF_NM):
+        from ._abi import gl_spectral_sample
+        lib = _native.load()
+        spec = np.ascontiguousarray(spec, np.float32).reshape(-1, 4)
+        arr = (gl_spectral_sample * len(spec))()
+        C.memmove(arr, spec.ctypes.data, spec.nbytes)
+        h = C.c_void_p()
+        _native.check(lib.gl_sprite_plan_create(int(N), arr, len(spec), float(lambda_ref), C.byref(h)),
+                      "sprite_plan_create")
+        self._h, self.N, self.M = h, int(N), 0
+
+    def bake(self, pupil, ds: int, stream=None) -> None:
+        import torch
+        st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        pupil = pupil.to(torch.float32).contiguous()
+        if tuple(pupil.shape) != (self.N, self.N):
+            raise ValueError("sprite: pupil must be (N, N)")
+        self._pupil = pupil      # kept alive until the stream has read it
+        _native.check(_native.load().gl_sprite_plan_bake(self._h, C.c_void_p(pupil.data_ptr()), int(ds),
+                                                         C.c_void_p(st)), "sprite_bake")
+        self.M = self.N // int(ds)
+
+    def splat(self, sources, sx_ds, sy_ds, px_mm_x, px_mm_y, rx, ry, gain, out_r, out_g, out_b, stream=None):
+        import torch
+        st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        src = np.ascontiguousarray(sources, np.float32).reshape(-1, 5)
+        H, W = out_r.shape
+        _native.check(_native.load().gl_sprite_plan_splat(
+            self._h, src.ctypes.data_as(C.POINTER(C.c_float)), len(src), float(sx_ds), float(sy_ds),
+            float(px_mm_x), float(px_mm_y), int(rx), int(ry), float(gain), C.c_void_p(out_r.data_ptr()),
+            C.c_void_p(out_g.data_ptr()), C.c_void_p(out_b.data_ptr()), int(W), int(H), C.c_void_p(st)),
+            "sprite_splat")
+
+    def read(self):
+        """(PSF (N, N) before normalisation, sprite (M, M, 3), PSF energy)."""
+        import torch
+        psf = torch.empty((self.N, self.N), dtype=torch.float32, device="cuda")
+        spr = torch.empty((self.M, self.M, 3), dtype=torch.float32, device="cuda")
+        e, m = C.c_double(), C.c_int()
+        st = torch.cuda.current_stream().cuda_stream
+        _native.check(_native.load().gl_sprite_plan_read(self._h, C.c_void_p(psf.data_ptr()),
+                                                         C.c_void_p(spr.data_ptr()), C.byref(e), C.byref(m),
+                                                         C.c_void_p(st)), "sprite_read")
+        return psf, spr, float(e.value)
+
+    def close(self):
+        if self._h:
+            _native.load().gl_sprite_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _po2_floor(x: float, hi: int) -> int:
+    p = 1
+    while p * 2 <= x and p * 2 <= hi:
+        p *= 2
+    return max(p, 1)
+
+
+def starburst_spectrum(config):
+    """The starburst's spectral table (render_starburst :712-736): the
+    output-space CMF with the sample spacing premultiplied, each channel then
+    normalised so a flat spectrum sums to one (white in, white out)."""
+    from .flare import spectral_table
+    dc = config.diffraction
+    ns = int(dc.spectral_samples) if int(dc.spectral_samples) > 0 else int(config.spectral_samples)
+    ns = max(3, ns)
+    spec, _ = spectral_table(ns, int(config.output_cs), config.custom_xyz_to_output)
+    f = np.float32
+    d_lambda = f(f(700.0 - 400.0) / f(ns))
+    spec = spec.copy()
+    spec[:, 1:4] = (spec[:, 1:4] * d_lambda).astype(np.float32)
+    sums = spec[:, 1:4].astype(np.float64).sum(0)
+    for c in range(3):
+        if sums[c] > 0.0:
+            spec[:, 1 + c] = (spec[:, 1 + c] / np.float32(sums[c])).astype(np.float32)
+    return spec
+
+
+def sprite_geometry(calibration, config, sources_px, width: int, height: int, sensor_half_w: float,
+                    sensor_half_h: float, fmt_w=None, fmt_h=None, front_R: float = 0.0):
+    """The sprite path's scalars (render_starburst :620-711, :1003-1070) in
+    the reference's float32: grid N (grown to cover the frame when the pattern
+    is prominent or the sensor oversized), engine ('sprite' / 'mdft'), fine
+    texel pitch, box-sum factor ds, M, footprint rx / ry and the gain."""
+    f = np.float32
+    dc = config.diffraction
+    fmt_w = int(fmt_w or width)
+    fmt_h = int(fmt_h or height)
+    efl_x, efl_y = f(calibration.focal_length_x), f(calibration.focal_length_y)
+    ep_x, ep_y = f(calibration.entrance_pupil_semi_x), f(calibration.entrance_pupil_semi_y)
+    if efl_x <= 0 and calibration.max_half_angle_h > 0:
+        efl_x = f(f(sensor_half_w) / f(np.tan(f(calibration.max_half_angle_h))))
+    if efl_y <= 0 and calibration.max_half_angle_v > 0:
+        efl_y = f(f(sensor_half_h) / f(np.tan(f(calibration.max_half_angle_v))))
+    if ep_x <= 0:
+        ep_x = f(front_R)
+    if ep_y <= 0:
+        ep_y = f(front_R)
+    if efl_x <= 0 or efl_y <= 0 or ep_x <= 0 or ep_y <= 0:
+        raise ValueError("render_starburst: degenerate first-order optics (no focal length / pupil)")
+    fnum_x = f(efl_x / (f(2.0) * ep_x))
+    fnum_y = f(efl_y / (f(2.0) * ep_y))
+    N = int(dc.starburst_grid)
+    if N < 256 or (N & (N - 1)) != 0:
+        raise ValueError("starburst_grid must be a power of two >= 256")
+    fill = f(dc.pupil_fill) if f(0.02) < f(dc.pupil_fill) < f(0.9) else f(0.30)
+    lam_mm = f(f(LAMBDA_REF_NM) * f(1e-6))
+    dx_fine_x = f(f(lam_mm * fnum_x) * fill)
+    dx_fine_y = f(f(lam_mm * fnum_y) * fill)
+    engine = "mdft" if int(dc.starburst_engine) == 1 else "sprite"
+    trim0 = f(dc.scale_trim) if f(dc.scale_trim) > 0 else f(1.0)
+    dx0_x, dx0_y = f(trim0 * dx_fine_x), f(trim0 * dx_fine_y)
+    frame_w, frame_h = f(f(2.0) * f(sensor_half_w)), f(f(2.0) * f(sensor_half_h))
+    frac = max(f(f(N) * dx0_x / frame_w) if frame_w > 0 else f(0.0),
+               f(f(N) * dx0_y / frame_h) if frame_h > 0 else f(0.0))
+    grid_cap = int(dc.starburst_grid_cap) if int(dc.starburst_grid_cap) >= 256 else 8192
+    grid_cap = min(grid_cap, 16384)
+    p = 256
+    while (p << 1) <= grid_cap:
+        p <<= 1
+    grid_cap = max(p, N)
+    circle_w = f(calibration.image_circle_semi_w) if calibration.image_circle_semi_w > 0 else f(calibration.sensor_half_w)
+    circle_h = f(calibration.image_circle_semi_h) if calibration.image_circle_semi_h > 0 else f(calibration.sensor_half_h)
+    oversized = ((circle_w > 0 and f(sensor_half_w) > f(1.5) * circle_w) or
+                 (circle_h > 0 and f(sensor_half_h) > f(1.5) * circle_h))
+    prominent = frac >= f(0.20)
+    if prominent:
+        engine = "sprite"
+    src = np.asarray(sources_px, np.float32).reshape(-1, 5)
+    if frac < 1.0 and (prominent or oversized) and len(src) and width > 0 and height > 0 and grid_cap > N:
+        reach_x = reach_y = f(0.0)
+        for (px, py, _r, _g, _b) in src:
+            reach_x = max(reach_x, max(f(px), f(f(width) - f(px))))
+            reach_y = max(reach_y, max(f(py), f(f(height) - f(py))))
+        px_buf_x, px_buf_y = f(frame_w / f(width)), f(frame_h / f(height))
+        covN = max(2.0 * float(reach_x) * float(px_buf_x) / float(dx0_x),
+                   2.0 * float(reach_y) * float(px_buf_y) / float(dx0_y))
+        want = int(np.ceil(covN)) if covN > N else N
+        want = min(want, grid_cap)
+        Ne = 256
+        while Ne < want:
+            Ne <<= 1
+        if Ne > N:
+            N, engine = Ne, "sprite"
+    px_mm_x = f(f(f(2.0) * f(sensor_half_w)) / f(fmt_w))
+    px_mm_y = f(f(f(2.0) * f(sensor_half_h)) / f(fmt_h))
+    trim = trim0
+    sx, sy = f(trim * dx_fine_x), f(trim * dx_fine_y)
+    ds_target = min(float(px_mm_x) / float(f(sx * f(SPRITE_OVERSAMPLE))),
+                    float(px_mm_y) / float(f(sy * f(SPRITE_OVERSAMPLE))))
+    ds = _po2_floor(ds_target, N // 8)
+    M = N // ds
+    sx_ds, sy_ds = f(sx * f(ds)), f(sy * f(ds))
+    aperture_scale = f(f(f(APERTURE_REF_FNUMBER) * f(APERTURE_REF_FNUMBER)) * f(calibration.pupil_area_frac)
+                       / max(f(fnum_x * fnum_y), f(1e-6)))
+    gain = f(f(f(dc.starburst_gain) * f(1.0)) * aperture_scale)     # pupil throughput T = 1 (plain stop)
+    rx = int(np.ceil(0.5 * M * float(sx_ds) / float(px_mm_x))) + 1
+    ry = int(np.ceil(0.5 * M * float(sy_ds) / float(px_mm_y))) + 1
+    rx, ry = min(rx, width), min(ry, height)
+    return dict(N=N, engine=engine, fill=float(fill), sx=float(sx), sy=float(sy), ds=ds, M=M, sx_ds=float(sx_ds),
+                sy_ds=float(sy_ds), px_mm_x=float(px_mm_x), px_mm_y=float(px_mm_y), rx=rx, ry=ry,
+                gain=float(gain), fnum_x=float(fnum_x), fnum_y=float(fnum_y))
+
+
+def sprite_starburst_layer(lens, calibration, config, sources_px, width: int, height: int, sensor_half_w: float,
+                           sensor_half_h: float, fmt_w=None, fmt_h=None, geometry=None):
+    """The starburst layer by the reference's default SPRITE engine: one FFT
+    of the device-built stop pupil at 550 nm, baked over the config's
+    wavelengths, box-summed toward the output pitch and resampled
+    area-weighted at every source (sources_px: (N, 5) px, py, r, g, b in
+    buffer pixels).  Returns {"starburst_r", "starburst_g", "starburst_b"}."""
+    import torch
+    g = geometry or sprite_geometry(calibration, config, sources_px, width, height, sensor_half_w, sensor_half_h,
+                                    fmt_w, fmt_h, front_R=lens.surfaces[0].semi_aperture if lens.surfaces else 0.0)
+    if g["N"] > 8192:
+        raise ValueError("render_starburst: sprite grids above 8192 are not supported (starburst_grid_cap)")
+    out = {k: torch.zeros((height, width), dtype=torch.float32, device="cuda")
+           for k in ("starburst_r", "starburst_g", "starburst_b")}
+    src = np.asarray(sources_px, np.float32).reshape(-1, 5)
+    if len(src) == 0:
+        return out
+    spec = starburst_spectrum(config)
+    pupil = build_pupil(lens, g["N"], g["fill"], int(config.aperture_blades), float(config.aperture_rotation))
+    if not float(pupil.sum()) > 0.0:
+        raise ValueError("render_starburst: degenerate pupil (zero energy)")
+    plan = SpritePlan(g["N"], spec)
+    try:
+        plan.bake(pupil, g["ds"])
+        plan.splat(src, g["sx_ds"], g["sy_ds"], g["px_mm_x"], g["px_mm_y"], g["rx"], g["ry"], g["gain"],
+                   out["starburst_r"], out["starburst_g"], out["starburst_b"])
+        torch.cuda.synchronize()
+    finally:
+        plan.close()
+    return out

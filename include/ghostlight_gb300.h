@@ -418,6 +418,34 @@ int gl_conv2d_plan_execute2(gl_conv_plan* plan, const float* d_in_r, const float
 int gl_conv2d_plan_info(const gl_conv_plan* plan, int* P, int* Q);
 int gl_conv2d_plan_destroy(gl_conv_plan* plan);
 
+/* ---- SPRITE starburst engine ---------------------------------------------
+ * The reference's default starburst engine, render_starburst's sprite path
+ * (ghostlight/src/starburst_render.cu:969-1073; kernels psf_from_fft :202,
+ * bake_sprite :255, downsample :283, splat_resample :316).
+ *
+ * gl_sprite_plan_create: N x N grid (power of two, 256..8192) and the
+ * spectral table the bake integrates over (cmf already scaled as the caller
+ * wants them: the reference premultiplies the sample spacing and white-
+ * balances), lambda_ref the wavelength of the one FFT (550 nm).
+ * gl_sprite_plan_bake: d_pupil = N x N real stop amplitude on the device
+ * (gl_build_pupil); FFT, |.|^2 fftshifted, normalised to unit sum, baked over
+ * wavelength and box-summed by ds (power of two <= N/8) into the M x M RGB
+ * sprite, M = N / ds.  Stream-ordered, nothing read back.
+ * gl_sprite_plan_splat: sources = n_src x {px, py, r, g, b} (host; buffer
+ * pixels and colour), texel pitch sx_ds/sy_ds and pixel pitch px_mm_x/y (mm),
+ * footprint half-extent rx/ry (pixels), gain; ADDS into the three planes.
+ * gl_sprite_plan_read: copies of the PSF (N x N, |FFT|^2 before the 1/energy
+ * scale) and the sprite (M x M x 3) into device buffers, and the
+ * PSF energy (FP64) to the host. */
+typedef struct gl_sprite_plan gl_sprite_plan;
+int gl_sprite_plan_create(int N, const gl_spectral_sample* spec, int n_spec, float lambda_ref, gl_sprite_plan** out);
+int gl_sprite_plan_bake(gl_sprite_plan* plan, const float* d_pupil, int ds, void* stream);
+int gl_sprite_plan_splat(gl_sprite_plan* plan, const float* sources, int n_src, float sx_ds, float sy_ds,
+                         float px_mm_x, float px_mm_y, int rx, int ry, float gain, float* d_out_r, float* d_out_g,
+                         float* d_out_b, int width, int height, void* stream);
+int gl_sprite_plan_read(gl_sprite_plan* plan, float* d_psf, float* d_sprite, double* energy, int* M, void* stream);
+int gl_sprite_plan_destroy(gl_sprite_plan* plan);
+
 /* ---- Serving: resident lenses and stream-ordered requests -----------------
  * The reference renders one flare per blocking call under process-wide
  * mutexes (ghost_render.cu:504-511, entered from bind_renderers.cpp:85-134)

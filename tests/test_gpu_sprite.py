@@ -1,0 +1,147 @@
+"""The SPRITE starburst engine on the GPU against its FP64 restatement
+(oracle/sprite_oracle.py, render_starburst's sprite path): the PSF, the
+wavelength-baked and box-summed sprite, the area-weighted splat, and the
+layer through render_point_flare."""
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+from oracle import sprite_oracle as SO
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+def _lens():
+    from ghostlight_gb300 import prescriptions as P
+    from ghostlight_gb300.optics import OpticalSystem
+    lens = OpticalSystem.from_records(P.double_gauss_12(seed=1))
+    for s in lens.surfaces:
+        if s.is_stop:
+            s.aperture_shape, s.aperture_blades = 1, 9
+            s.aperture_rotation_rad = 0.2
+            s.aperture_curvature = 0.3
+    return lens
+
+
+def _config(ns=16):
+    import ghostlight_gb300 as gl
+    cfg = gl.PointFlareConfig(ray_grid=32, spectral_samples=ns)
+    cfg.diffraction.starburst = True
+    return cfg
+
+
+@pytest.mark.parametrize("N,ds", [(512, 1), (512, 4), (1024, 2)])
+def test_sprite_matches_oracle(N, ds):
+    from ghostlight_gb300.starburst import SpritePlan, build_pupil, starburst_spectrum
+    spec = starburst_spectrum(_config())
+    pupil = build_pupil(_lens(), N, 0.3)
+    plan = SpritePlan(N, spec)
+    plan.bake(pupil, ds)
+    psf, spr, energy = plan.read()
+    torch.cuda.synchronize()
+    plan.close()
+    p_ref = SO.psf(pupil.cpu().numpy())
+    assert energy == pytest.approx(p_ref.sum(), rel=1e-5)
+    assert rel_l2(psf.cpu().numpy(), p_ref) < 1e-5
+    s_ref = SO.sprite(pupil.cpu().numpy(), spec, ds)
+    got = spr.cpu().numpy()
+    assert got.shape == (N // ds, N // ds, 3)
+    assert rel_l2(got, s_ref) < 1e-4
+    # white in, white out: each channel of the sprite carries about unit
+    # energy (the bilinear wavelength rescale is exact only in the continuum)
+    tot = got.reshape(-1, 3).sum(0)
+    assert np.all(np.abs(tot - 1.0) < 0.08)
+
+
+@pytest.mark.parametrize("N", [4096, 8192])
+def test_large_grids_psf(N):
+    """The 2- and 1-column FFT groups of the large grids: the PSF is the
+    pupil's |FFT|^2 (checked against numpy at 4096), its energy the pupil's
+    by Parseval, and centro-symmetric for the real pupil."""
+    from ghostlight_gb300.starburst import SpritePlan, build_pupil, starburst_spectrum
+    spec = starburst_spectrum(_config(8))
+    pupil = build_pupil(_lens(), N, 0.3)
+    plan = SpritePlan(N, spec)
+    plan.bake(pupil, 8)
+    psf, spr, energy = plan.read()
+    torch.cuda.synchronize()
+    plan.close()
+    a2 = float((pupil.double() ** 2).sum())
+    assert energy == pytest.approx(N * N * a2, rel=1e-4)
+    p = psf.cpu().numpy()
+    c = N // 2
+    assert p[c, c] == p.max()
+    np.testing.assert_allclose(p[1:, 1:], p[1:, 1:][::-1, ::-1], rtol=2e-3, atol=p.max() * 1e-5)
+    if N == 4096:
+        assert rel_l2(p, SO.psf(pupil.cpu().numpy())) < 1e-5
+    assert np.isfinite(spr.cpu().numpy()).all()
+
+
+def test_splat_matches_oracle():
+    from ghostlight_gb300.starburst import SpritePlan, build_pupil, starburst_spectrum
+    N, ds, W, H = 512, 2, 300, 220
+    spec = starburst_spectrum(_config())
+    pupil = build_pupil(_lens(), N, 0.3)
+    plan = SpritePlan(N, spec)
+    plan.bake(pupil, ds)
+    _, spr, _ = plan.read()
+    src = np.array([[150.3, 100.7, 1.0, 0.8, 0.6], [12.5, 210.2, 0.5, 1.0, 1.0], [299.9, 3.1, 2.0, 2.0, 2.0]],
+                   np.float32)
+    args = (0.011, 0.012, 0.02, 0.02, 140, 140, 1.7)
+    out = [torch.zeros((H, W), dtype=torch.float32, device="cuda") for _ in range(3)]
+    plan.splat(src, *args, *out)
+    torch.cuda.synchronize()
+    plan.close()
+    got = np.stack([o.cpu().numpy() for o in out])
+    want = SO.splat(spr.cpu().numpy().astype(np.float64), src, *args, W, H)
+    assert want.sum() > 0
+    assert rel_l2(got, want) < 1e-5
+
+
+def test_layer_through_point_flare():
+    """render_point_flare's starburst by the default SPRITE engine: against
+    the oracle pipeline on the same geometry; the brightest pixel is the
+    source's image point and the layer carries gain x colour of energy."""
+    import ghostlight_gb300 as gl
+    from ghostlight_gb300.starburst import build_pupil, sprite_geometry, starburst_spectrum
+    lens = _lens()
+    cal = lens.calibration()
+    cfg = _config(12)
+    cfg.source_x, cfg.source_y = 0.55, 0.45
+    cfg.diffraction.scale_trim = 5.0
+    W, H = 320, 240
+    out = gl.render_point_flare(W, H, lens, cal, cfg)
+    got = np.stack([out["starburst_%s" % c].cpu().numpy() for c in "rgb"])
+    assert got.shape == (3, H, W) and got.max() > 0
+    y, x = np.unravel_index(np.argmax(got[1]), got[1].shape)
+    assert abs(x - 0.55 * W) <= 2 and abs(y - 0.45 * H) <= 2
+    # the same layer from the oracle, on the geometry the render used
+    hw, hh = cal.sensor_half_w, cal.sensor_half_h
+    pos = np.array([[x + 0.5, y + 0.5, 1, 1, 1]], np.float32)
+    geo = sprite_geometry(cal, cfg, pos, W, H, hw, hh, front_R=lens.surfaces[0].semi_aperture)
+    assert geo["engine"] == "sprite"
+    spec = starburst_spectrum(cfg)
+    pupil = build_pupil(lens, geo["N"], geo["fill"]).cpu().numpy()
+    spr = SO.sprite(pupil, spec, geo["ds"])
+    # total energy: the sprite's per-channel sum x gain x the source colour,
+    # less what falls off the frame
+    from ghostlight_gb300.flare import source_rgb
+    rgb = source_rgb(cfg, cfg.source_r, cfg.source_g, cfg.source_b)
+    for c in range(3):
+        full = spr[..., c].sum() * geo["gain"] * float(rgb[c])
+        assert 0.5 * full < got[c].sum() <= full * 1.001, c
+
+
+def test_mdft_engine_still_selectable():
+    import ghostlight_gb300 as gl
+    from ghostlight_gb300.config import StarburstEngine
+    lens = _lens()
+    cal = lens.calibration()
+    cfg = _config(8)
+    cfg.source_x, cfg.source_y = 0.5, 0.5
+    cfg.diffraction.starburst_engine = StarburstEngine.MDFT
+    out = gl.render_point_flare(256, 192, lens, cal, cfg)
+    g = out["starburst_g"].cpu().numpy()
+    y, x = np.unravel_index(np.argmax(g), g.shape)
+    assert abs(x - 128) <= 2 and abs(y - 96) <= 2
