@@ -472,6 +472,19 @@ int gl_finalize_z(gl_surface* s, int n)
     return GL_OK;
 }
 
+// PupilMask::contains (aperture_sampler.h:63-82) at host points, host float
+// arithmetic; aspect_one rasterises the stop round as the starburst does.
+int gl_pupil_contains(const gl_surface* surfaces, int n, int blades_override, float rotation_deg, int aspect_one,
+                      const float* uv, int n_pts, uint8_t* out)
+{
+    if (!surfaces || n <= 0 || n_pts < 0 || (n_pts > 0 && (!uv || !out)))
+        return fail(GL_ERR_INVALID, "pupil_contains: bad arguments");
+    PupilMask m = resolve_pupil_mask(surfaces, n, blades_override, rotation_deg);
+    if (aspect_one) m.aspect = 1.0f;
+    for (int k = 0; k < n_pts; ++k) out[k] = pupil_contains(m, uv[2 * k], uv[2 * k + 1]) ? 1 : 0;
+    return GL_OK;
+}
+
 // Boundary radius (normalised; 1 = blade tip) of a bladed stop's silhouette
 // at angles theta: ApertureProfile::radius_at of make_aperture_profile
 // (aperture_profile.h:192-196, 285-358), host float arithmetic.

@@ -576,12 +576,32 @@ __device__ __forceinline__ bool pupil_in(const PupilDev& m, float u, float v)
     return true;
 }
 
-__global__ void pupil_build_kernel(float* __restrict__ out, int N, float fill, PupilDev m)
+// bilinear sample of the cat's-eye envelope (ME x ME over pupil [-1, 1]^2,
+// cell centres, clamped at the edges): sample_env, starburst_render.cu:136-149
+__device__ __forceinline__ float pupil_env(const float* __restrict__ env, int ME, float u, float v)
+{
+    float fx = (u * 0.5f + 0.5f) * ME - 0.5f;
+    float fy = (v * 0.5f + 0.5f) * ME - 0.5f;
+    fx = fminf(fmaxf(fx, 0.0f), (float)(ME - 1));
+    fy = fminf(fmaxf(fy, 0.0f), (float)(ME - 1));
+    const int x0 = (int)floorf(fx), y0 = (int)floorf(fy);
+    const int x1 = min(x0 + 1, ME - 1), y1 = min(y0 + 1, ME - 1);
+    const float tx = fx - x0, ty = fy - y0;
+    const float a = env[(size_t)y0 * ME + x0] * (1.0f - tx) + env[(size_t)y0 * ME + x1] * tx;
+    const float b = env[(size_t)y1 * ME + x0] * (1.0f - tx) + env[(size_t)y1 * ME + x1] * tx;
+    return a * (1.0f - ty) + b * ty;
+}
+
+// env == nullptr: the plain stop (coverage of the 16 supersamples); else
+// each inside supersample weighs the envelope at its own position
+__global__ void pupil_build_kernel(float* __restrict__ out, int N, float fill, PupilDev m,
+                                   const float* __restrict__ env, int ME)
 {
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= N * N) return;
     const int i = idx % N, j = idx / N;
     int cnt = 0;
+    float acc = 0.0f;
     #pragma unroll
     for (int sy = 0; sy < 4; ++sy)
         #pragma unroll
@@ -589,9 +609,11 @@ __global__ void pupil_build_kernel(float* __restrict__ out, int N, float fill, P
         {
             const float u = (((float)i + ((float)sx + 0.5f) * 0.25f) / (float)N * 2.0f - 1.0f) / fill;
             const float v = (((float)j + ((float)sy + 0.5f) * 0.25f) / (float)N * 2.0f - 1.0f) / fill;
-            cnt += pupil_in(m, u, v) ? 1 : 0;
+            if (!pupil_in(m, u, v)) continue;
+            ++cnt;
+            if (env) acc += pupil_env(env, ME, u, v);
         }
-    out[idx] = (float)cnt * (1.0f / 16.0f);
+    out[idx] = (env ? acc : (float)cnt) * (1.0f / 16.0f);
 }
 
 // Pupil amplitude A[i][j] (float, n x n) -> B operand [hi | lo | hi] or FP32.
@@ -983,20 +1005,30 @@ extern "C" int gl_mdft_plan_execute(gl_mdft_plan* plan, const float* d_pupil, fl
     return gl_mdft_plan_execute2(plan, d_pupil, d_out_r, d_out_g, d_out_b, 0, stream);
 }
 
-extern "C" int gl_build_pupil(const gl_surface* surfaces, int n_surfaces, int N, float pupil_fill,
-                              int blades_override, float rotation_deg, float* d_out, void* stream)
+extern "C" int gl_build_pupil2(const gl_surface* surfaces, int n_surfaces, int N, float pupil_fill,
+                               int blades_override, float rotation_deg, int aspect_one, const float* d_env, int env_n,
+                               float* d_out, void* stream)
 {
     using namespace gl;
     if (!surfaces || n_surfaces <= 0 || !d_out) return fail(GL_ERR_INVALID, "build_pupil: bad arguments");
     if (N <= 0 || N > 8192) return fail(GL_ERR_INVALID, "build_pupil: N must be 1..8192");
     if (!(pupil_fill > 0.0f) || pupil_fill > 1.0f) return fail(GL_ERR_INVALID, "build_pupil: pupil_fill must lie in (0, 1]");
-    const PupilMask m = resolve_pupil_mask(surfaces, n_surfaces, blades_override, rotation_deg);
+    if (d_env && (env_n < 1 || env_n > 4096)) return fail(GL_ERR_INVALID, "build_pupil: envelope side must be 1..4096");
+    PupilMask m = resolve_pupil_mask(surfaces, n_surfaces, blades_override, rotation_deg);
+    if (aspect_one) m.aspect = 1.0f;
     PupilDev d{m.aspect, m.rot_rad, m.apothem, m.sector, m.n_blades, m.blade};
     const int total = N * N;
-    pupil_build_kernel<<<(total + 255) / 256, 256, 0, (cudaStream_t)stream>>>(d_out, N, pupil_fill, d);
+    pupil_build_kernel<<<(total + 255) / 256, 256, 0, (cudaStream_t)stream>>>(d_out, N, pupil_fill, d, d_env, env_n);
     GL_CUDA_TRY(cudaGetLastError());
     g_last_launches = 1;
     return GL_OK;
+}
+
+extern "C" int gl_build_pupil(const gl_surface* surfaces, int n_surfaces, int N, float pupil_fill,
+                              int blades_override, float rotation_deg, float* d_out, void* stream)
+{
+    return gl_build_pupil2(surfaces, n_surfaces, N, pupil_fill, blades_override, rotation_deg, 0, nullptr, 0, d_out,
+                           stream);
 }
 
 extern "C" int gl_mdft_plan_status(gl_mdft_plan* plan, int* err_code)

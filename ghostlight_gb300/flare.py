@@ -466,7 +466,10 @@ def render_source_flare(offsets, width: int, height: int, lens: OpticalSystem,
         geo = sprite_geometry(calibration, config, pos, width, height, hw, hh,
                               front_R=lens.surfaces[0].semi_aperture if lens.surfaces else 0.0)
         if geo["engine"] == "sprite":
-            out.update(sprite_starburst_layer(lens, calibration, config, pos, width, height, hw, hh, geometry=geo))
+            field = (float(np.float32(np.mean(src[:, 0].astype(np.float64)))),
+                     float(np.float32(np.mean(src[:, 1].astype(np.float64)))))
+            out.update(sprite_starburst_layer(lens, calibration, config, pos, width, height, hw, hh, geometry=geo,
+                                              field=field))
         else:
             out.update(starburst_layer(lens, calibration, config, pos, width, height, hw, hh))
     if want_veil:

@@ -381,18 +381,74 @@ def sprite_geometry(calibration, config, sources_px, width: int, height: int, se
     rx = int(np.ceil(0.5 * M * float(sx_ds) / float(px_mm_x))) + 1
     ry = int(np.ceil(0.5 * M * float(sy_ds) / float(px_mm_y))) + 1
     rx, ry = min(rx, width), min(ry, height)
-    return dict(N=N, engine=engine, fill=float(fill), sx=float(sx), sy=float(sy), ds=ds, M=M, sx_ds=float(sx_ds),
+    return dict(N=N, engine=engine, fill=float(fill), ep_x=float(ep_x), ep_y=float(ep_y), sx=float(sx), sy=float(sy),
+                ds=ds, M=M, sx_ds=float(sx_ds),
                 sy_ds=float(sy_ds), px_mm_x=float(px_mm_x), px_mm_y=float(px_mm_y), rx=rx, ry=ry,
                 gain=float(gain), fnum_x=float(fnum_x), fnum_y=float(fnum_y))
 
 
+def build_pupil2(lens, N: int, pupil_fill: float, blades_override: int = 0, rotation_deg: float = 0.0,
+                 aspect_one: bool = True, envelope=None, stream=None):
+    """The starburst's effective pupil (build_pupil_kernel,
+    starburst_render.cu:155-191): the stop rasterised round (the aspect goes
+    into the per-axis pitch) and, when given, weighted by the cat's-eye
+    envelope (ME x ME host or device array over pupil [-1, 1]^2)."""
+    import torch
+    lib = _native.load()
+    arr = lens.to_array()
+    out = torch.empty((N, N), dtype=torch.float32, device="cuda")
+    st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+    env, me = None, 0
+    if envelope is not None:
+        env = torch.as_tensor(np.asarray(envelope, np.float32) if not hasattr(envelope, "is_cuda") else envelope,
+                              dtype=torch.float32).cuda().contiguous()
+        me = env.shape[0]
+    _native.check(lib.gl_build_pupil2(arr, len(arr), int(N), float(pupil_fill), int(blades_override),
+                                      float(rotation_deg), int(bool(aspect_one)),
+                                      C.c_void_p(env.data_ptr()) if env is not None else None, int(me),
+                                      C.c_void_p(out.data_ptr()), C.c_void_p(st)), "build_pupil")
+    if env is not None:
+        torch.cuda.current_stream().synchronize()
+    return out
+
+
+def effective_pupil(lens, config, g, field):
+    """The sprite's pupil and its throughput T (render_starburst :740-922):
+    on axis, or with use_survivor_mask off, the plain stop and T = 1;
+    off axis, the stop weighted by the cat's-eye envelope centred on the
+    surviving crescent, T = its energy over the plain stop's.  Returns
+    (pupil, T), or (None, 0) where nothing survives at this field."""
+    dc = config.diffraction
+    f = np.float32
+    bo, rot = int(config.aperture_blades), float(config.aperture_rotation)
+    ax, ay = (f(field[0]), f(field[1])) if field is not None else (f(0.0), f(0.0))
+    off_axis = abs(float(ax)) > 1e-5 or abs(float(ay)) > 1e-5
+    if not (bool(dc.use_survivor_mask) and off_axis):
+        return build_pupil2(lens, g["N"], g["fill"], bo, rot), 1.0
+    cx, cy, any_surv = survivor_center(lens, float(ax), float(ay))
+    if not any_surv:
+        return None, 0.0
+    me = min(max(int(dc.survivor_grid), 16), 1024)
+    env = survivor_envelope(lens, g["ep_x"], g["ep_y"], cx, cy, float(ax), float(ay), me)
+    plain = build_pupil2(lens, g["N"], g["fill"], bo, rot)
+    pupil = build_pupil2(lens, g["N"], g["fill"], bo, rot, envelope=env)
+    s_ref = float((plain.double() ** 2).sum())
+    s_eff = float((pupil.double() ** 2).sum())
+    T = min(max(s_eff / s_ref, 0.0), 1.0) if s_ref > 0 else 1.0
+    if T < 1e-3:
+        return None, T
+    return pupil, T
+
+
 def sprite_starburst_layer(lens, calibration, config, sources_px, width: int, height: int, sensor_half_w: float,
-                           sensor_half_h: float, fmt_w=None, fmt_h=None, geometry=None):
+                           sensor_half_h: float, fmt_w=None, fmt_h=None, geometry=None, field=None):
     """The starburst layer by the reference's default SPRITE engine: one FFT
-    of the device-built stop pupil at 550 nm, baked over the config's
+    of the device-built effective pupil at 550 nm, baked over the config's
     wavelengths, box-summed toward the output pitch and resampled
     area-weighted at every source (sources_px: (N, 5) px, py, r, g, b in
-    buffer pixels).  Returns {"starburst_r", "starburst_g", "starburst_b"}."""
+    buffer pixels; field: the mean source direction (radians), which sets the
+    off-axis cat's-eye).  Returns {"starburst_r", "starburst_g",
+    "starburst_b"}."""
     import torch
     g = geometry or sprite_geometry(calibration, config, sources_px, width, height, sensor_half_w, sensor_half_h,
                                     fmt_w, fmt_h, front_R=lens.surfaces[0].semi_aperture if lens.surfaces else 0.0)
@@ -403,16 +459,177 @@ def sprite_starburst_layer(lens, calibration, config, sources_px, width: int, he
     src = np.asarray(sources_px, np.float32).reshape(-1, 5)
     if len(src) == 0:
         return out
-    spec = starburst_spectrum(config)
-    pupil = build_pupil(lens, g["N"], g["fill"], int(config.aperture_blades), float(config.aperture_rotation))
+    pupil, T = effective_pupil(lens, config, g, field)
+    if pupil is None:
+        return out      # past the vignette edge: no starburst
     if not float(pupil.sum()) > 0.0:
         raise ValueError("render_starburst: degenerate pupil (zero energy)")
+    spec = starburst_spectrum(config)
+    gain = float(np.float32(np.float32(g["gain"]) * np.float32(T)))
     plan = SpritePlan(g["N"], spec)
     try:
         plan.bake(pupil, g["ds"])
-        plan.splat(src, g["sx_ds"], g["sy_ds"], g["px_mm_x"], g["px_mm_y"], g["rx"], g["ry"], g["gain"],
+        plan.splat(src, g["sx_ds"], g["sy_ds"], g["px_mm_x"], g["px_mm_y"], g["rx"], g["ry"], gain,
                    out["starburst_r"], out["starburst_g"], out["starburst_b"])
         torch.cuda.synchronize()
     finally:
         plan.close()
     return out
+
+
+# ---------------------------------------------------------------------------
+# Off-axis cat's-eye: survivor centre and envelope (starburst_render.cu:393-583)
+# ---------------------------------------------------------------------------
+SURVIVOR_EDGE_SS = 10      # envelope rim supersampling per side
+SURVIVOR_CENTER_SS = 8     # centre-solve boundary supersampling per side
+SURVIVOR_SCAN = 81         # centre-solve launch grid per side
+
+
+def _launch_dir(ax: float, ay: float):
+    """Vec3f(tan ax, tan ay, 1).normalized() in float32 (vec3.h:48-52)."""
+    f = np.float32
+    bx, by = f(np.tan(f(ax))), f(np.tan(f(ay)))
+    ln = f(np.sqrt(f(f(bx * bx) + f(by * by)) + f(1.0)))
+    inv = f(f(1.0) / ln)
+    return bx, by, (f(bx * inv), f(by * inv), f(inv))
+
+
+def _survives_device(lens, ox, oy, z, d, lam=LAMBDA_REF_NM):
+    """Primary traces of launches (ox[k], oy[k], z) along d on the device:
+    True where the ray reaches the sensor at a finite position."""
+    import torch
+    from .flare import trace_rays
+    n = len(ox)
+    if n == 0:
+        return np.zeros(0, bool)
+    rays = np.empty((n, 7), np.float32)
+    rays[:, 0], rays[:, 1], rays[:, 2] = ox, oy, z
+    rays[:, 3], rays[:, 4], rays[:, 5] = d
+    rays[:, 6] = lam
+    r = trace_rays(lens, torch.from_numpy(rays).cuda(), -1, -1).cpu().numpy()
+    return (r[:, 4] == 0) & np.isfinite(r[:, 0]) & np.isfinite(r[:, 1])
+
+
+def _boundary8(a, valid=None):
+    """Cells with an 8-neighbour of the other class (among valid cells)."""
+    S0, S1 = a.shape
+    cls = a > 0.5
+    ok = np.ones_like(cls) if valid is None else valid
+    out = np.zeros_like(cls)
+    for dj in (-1, 0, 1):
+        for di in (-1, 0, 1):
+            if not di and not dj:
+                continue
+            sh = np.zeros_like(cls)
+            shv = np.zeros_like(cls)
+            ys = slice(max(dj, 0), S0 + min(dj, 0))
+            yd = slice(max(-dj, 0), S0 + min(-dj, 0))
+            xs = slice(max(di, 0), S1 + min(di, 0))
+            xd = slice(max(-di, 0), S1 + min(-di, 0))
+            sh[yd, xd] = cls[ys, xs]
+            shv[yd, xd] = ok[ys, xs]
+            out |= shv & (sh != cls)
+    return out & ok
+
+
+def survivor_center(lens, ax: float, ay: float, survives=None):
+    """Centroid of the spawn-plane launches whose ray reaches the sensor at
+    field (ax, ay) (solve_survivor_center, starburst_render.cu:503-583):
+    an 81 x 81 scan over the front element's reach, boundary cells
+    supersampled 8 x 8.  Returns (cx, cy, any_survivor)."""
+    f = np.float32
+    survives = survives or (lambda x, y, z, d: _survives_device(lens, x, y, z, d))
+    front_R = f(lens.surfaces[0].semi_aperture) if lens.surfaces else f(0.0)
+    if front_R <= 0:
+        return 0.0, 0.0, False
+    z = f(f(lens.surfaces[0].z) - f(20.0))
+    bx, by, d = _launch_dir(ax, ay)
+    span_x = f(f(f(1.1) * front_R) + f(f(20.0) * f(abs(bx))))
+    span_y = f(f(f(1.1) * front_R) + f(f(20.0) * f(abs(by))))
+    S = SURVIVOR_SCAN
+    t = (f(2.0) * np.arange(S, dtype=np.float32) / f(S - 1) - f(1.0)).astype(np.float32)
+    lx = (span_x * t).astype(np.float32)
+    ly = (span_y * t).astype(np.float32)
+    gx, gy = np.meshgrid(lx, ly)
+    surv = survives(gx.ravel(), gy.ravel(), z, d).reshape(S, S)
+    bnd = _boundary8(surv.astype(np.float32))
+    sx = float(np.sum(gx[surv & ~bnd], dtype=np.float64))
+    sy = float(np.sum(gy[surv & ~bnd], dtype=np.float64))
+    w = float(np.count_nonzero(surv & ~bnd))
+    jb, ib = np.nonzero(bnd)
+    if len(jb):
+        K = SURVIVOR_CENTER_SS
+        hx, hy = f(span_x / f(S - 1)), f(span_y / f(S - 1))
+        off = ((f(2.0) * (np.arange(K, dtype=np.float32) + f(0.5)) / f(K)) - f(1.0)).astype(np.float32)
+        llx = (lx[ib][:, None, None] + (hx * off)[None, None, :]).astype(np.float32)
+        lly = (ly[jb][:, None, None] + (hy * off)[None, :, None]).astype(np.float32)
+        llx, lly = np.broadcast_arrays(llx, lly)
+        ok = survives(llx.ravel().copy(), lly.ravel().copy(), z, d)
+        inv_k2 = float(f(1.0) / f(K * K))
+        sx += float(np.sum(llx.ravel()[ok].astype(np.float64))) * inv_k2
+        sy += float(np.sum(lly.ravel()[ok].astype(np.float64))) * inv_k2
+        w += int(ok.sum()) * inv_k2
+    if w > 0:
+        return float(f(sx / w)), float(f(sy / w)), True
+    return 0.0, 0.0, False
+
+
+def survivor_envelope(lens, ep_x, ep_y, cx, cy, ax, ay, ME: int, survives=None, contains=None):
+    """Cat's-eye rim-vignetting envelope over pupil [-1, 1]^2, ME x ME
+    (build_survivor_envelope, starburst_render.cu:393-491): 1 where a primary
+    ray launched at (cx + u ep_x, cy + v ep_y) survives, cells on the survive
+    / clip boundary supersampled 10 x 10 to a coverage fraction, cells outside
+    the stop filled by a radius-2 dilation from inside."""
+    f = np.float32
+    from ._abi import surface_array
+    from . import _native
+    survives = survives or (lambda x, y, z, d: _survives_device(lens, x, y, z, d))
+    if contains is None:
+        arr = surface_array(lens.records())
+
+        def contains(uv):
+            uv = np.ascontiguousarray(uv, np.float32).reshape(-1, 2)
+            out = np.zeros(len(uv), np.uint8)
+            _native.check(_native.load().gl_pupil_contains(
+                arr, len(arr), 0, 0.0, 1, uv.ctypes.data_as(C.POINTER(C.c_float)), len(uv),
+                out.ctypes.data_as(C.POINTER(C.c_uint8))), "pupil_contains")
+            return out.astype(bool)
+    if not lens.surfaces:
+        return np.ones((ME, ME), np.float32)
+    z = f(f(lens.surfaces[0].z) - f(20.0))
+    _, _, d = _launch_dir(ax, ay)
+    c = ((np.arange(ME, dtype=np.float32) + f(0.5)) / f(ME) * f(2.0) - f(1.0)).astype(np.float32)
+    U, V = np.meshgrid(c, c)
+    inside = contains(np.stack([U.ravel(), V.ravel()], 1)).reshape(ME, ME)
+    env = np.full((ME, ME), -1.0, np.float32)
+    ox = (f(cx) + U[inside] * f(ep_x)).astype(np.float32)
+    oy = (f(cy) + V[inside] * f(ep_y)).astype(np.float32)
+    env[inside] = survives(ox, oy, z, d).astype(np.float32)
+    bnd = _boundary8(env, env >= 0)
+    jb, ib = np.nonzero(bnd)
+    if len(jb):
+        K = SURVIVOR_EDGE_SS
+        du = f(f(2.0) / f(ME))
+        off = (du * ((np.arange(K, dtype=np.float32) + f(0.5)) / f(K) - f(0.5))).astype(np.float32)
+        uu = (c[ib][:, None, None] + off[None, None, :]).astype(np.float32)
+        vv = (c[jb][:, None, None] + off[None, :, None]).astype(np.float32)
+        uu, vv = np.broadcast_arrays(uu, vv)
+        uu, vv = uu.reshape(len(jb), -1), vv.reshape(len(jb), -1)
+        ins = contains(np.stack([uu.ravel(), vv.ravel()], 1)).reshape(uu.shape)
+        ok = np.zeros(uu.shape, bool)
+        ox = (f(cx) + uu[ins] * f(ep_x)).astype(np.float32)
+        oy = (f(cy) + vv[ins] * f(ep_y)).astype(np.float32)
+        ok[ins] = survives(ox, oy, z, d)
+        n_in = ins.sum(1)
+        frac = np.where(n_in > 0, ok.sum(1).astype(np.float32) / np.maximum(n_in, 1).astype(np.float32),
+                        env[jb, ib])
+        env[jb, ib] = frac.astype(np.float32)
+    # dilation of the survival into the outside band (radius 2)
+    filled = env.copy()
+    pad = np.pad(np.where(env >= 0, env, 0.0).astype(np.float32), 2, constant_values=0.0)
+    best = np.zeros_like(env)
+    for dj in range(5):
+        for di in range(5):
+            best = np.maximum(best, pad[dj:dj + ME, di:di + ME])
+    filled[env < 0] = best[env < 0]
+    return filled

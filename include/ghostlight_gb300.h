@@ -394,6 +394,18 @@ int gl_mdft_plan_execute2(gl_mdft_plan* plan, const float* d_pupil, float* d_out
  * device, asynchronous. */
 int gl_build_pupil(const gl_surface* surfaces, int n_surfaces, int N, float pupil_fill,
                    int blades_override, float rotation_deg, float* d_out, void* stream);
+/* gl_build_pupil with the rest of build_pupil_kernel's modifiers
+ * (starburst_render.cu:155-191): aspect_one = 1 rasterises the stop round
+ * (the starburst takes an anamorphic pupil's aspect in the per-axis pitch,
+ * starburst_render.cu:738); d_env = the ME x ME cat's-eye envelope over pupil
+ * [-1, 1]^2 (device; NULL = none), each inside supersample weighted by its
+ * bilinear sample (sample_env :136). */
+int gl_build_pupil2(const gl_surface* surfaces, int n_surfaces, int N, float pupil_fill, int blades_override,
+                    float rotation_deg, int aspect_one, const float* d_env, int env_n, float* d_out, void* stream);
+/* PupilMask::contains (aperture_sampler.h:63-82) of the lens's stop at host
+ * points uv[2 k], uv[2 k + 1] -> out[k] (host float arithmetic). */
+int gl_pupil_contains(const gl_surface* surfaces, int n, int blades_override, float rotation_deg, int aspect_one,
+                      const float* uv, int n_pts, uint8_t* out);
 
 /* PSF / veil image convolution: out_c = in_c (*) k ('same' size, kernel
  * centred, odd kw x kh, float32).  The reference has no such operation on

@@ -383,6 +383,49 @@ int orc_aperture_samples(const gl_surface* S, int N, int grid, int jitter, int s
     return k_out;
 }
 
+/* PupilMask::contains (aperture_sampler.h:63-82) of the lens's stop at the
+ * points uv[2k], uv[2k+1] -> out[k]; aspect_one forces the ellipse round. */
+int orc_pupil_contains(const gl_surface* S, int N, int blades_override, float rotation_deg, int aspect_one,
+                       const float* uv, int n_pts, unsigned char* out)
+{
+    int nb = 0; float rot = 0.0f, aspect = 1.0f;
+    int deformed = 0;
+    orc_blade blade;
+    memset(&blade, 0, sizeof(blade));
+    for (int i = 0; i < N; ++i)
+    {
+        if (!S[i].is_stop) continue;
+        aspect = S[i].aperture_aspect;
+        if (S[i].aperture_shape == GL_APERTURE_POLYGON && S[i].aperture_blades >= 3)
+        {
+            nb = S[i].aperture_blades; rot = S[i].aperture_rotation_rad;
+            if (orc_blade_authored(&S[i])) { blade = orc_make_blade(&S[i]); deformed = blade.deformed; }
+        }
+        break;
+    }
+    if (blades_override > 0) { nb = blades_override; rot = rotation_deg * ((float)M_PI / 180.0f); deformed = 0; }
+    if (aspect_one) aspect = 1.0f;
+    const int poly = nb >= 3;
+    const float apothem = poly ? cosf((float)M_PI / nb) : 1.0f;
+    const float sector = poly ? (2.0f * (float)M_PI / nb) : 1.0f;
+    for (int k = 0; k < n_pts; ++k)
+    {
+        const float u = uv[2 * k], v = uv[2 * k + 1];
+        const float ux = u / aspect, r2 = ux * ux + v * v;
+        int in = r2 <= 1.0f;
+        if (in && poly && deformed) in = sqrtf(r2) <= blade_radius_f32(&blade, atan2f(v, ux));
+        else if (in && poly)
+        {
+            float ang = atan2f(v, ux) - rot;
+            float sec = fmodf(ang, sector);
+            if (sec < 0.0f) sec += sector;
+            in = !(sqrtf(r2) * cosf(sec - sector * 0.5f) > apothem);
+        }
+        out[k] = (unsigned char)in;
+    }
+    return 0;
+}
+
 /* Host mirror of the ghost kernel's full-pupil main path
  * (ghost_render.cu:280-463): per pair, source, pupil sample and wavelength,
  * trace and splat bilinearly.  pair_grid / grid_offsets select each pair's

@@ -32,6 +32,7 @@ def _load():
         lib.orc_aperture_samples.argtypes = [P(gl_surface), i, i, i, i, i, f, P(f), i]
         lib.orc_blade_radius.argtypes = [P(gl_surface), P(f), i, P(f)]
         lib.orc_coating_register.argtypes = [i, i, i, i, P(f), f, i]
+        lib.orc_pupil_contains.argtypes = [P(gl_surface), i, i, f, i, P(f), i, P(C.c_ubyte)]
         lib.orc_render.argtypes = [P(gl_surface), i, P(i), P(f), P(i), i, P(f), i, P(f), P(i),
                                    P(f), i, f, f, i, i, f, i, i, P(d)]
         _lib = lib
@@ -62,6 +63,16 @@ def register_coating(table_id, model, axis0, r, axis1=None, angle_ref_ior=1.0, d
     if lib.orc_coating_register(int(table_id), int(model), len(a0), len(a1), _fp(data), float(angle_ref_ior),
                                 int(bool(discard))) != 0:
         raise ValueError("oracle: bad coating table %d" % table_id)
+
+
+def pupil_contains(surfs, uv, blades_override=0, rotation_deg=0.0, aspect_one=False):
+    """PupilMask::contains of the lens's stop at (n, 2) points -> bool (n,)."""
+    lib = _load()
+    uv = np.ascontiguousarray(uv, np.float32).reshape(-1, 2)
+    out = np.zeros(len(uv), np.uint8)
+    lib.orc_pupil_contains(surface_array(surfs), len(surfs), int(blades_override), float(rotation_deg),
+                           int(bool(aspect_one)), _fp(uv), len(uv), out.ctypes.data_as(C.POINTER(C.c_ubyte)))
+    return out.astype(bool)
 
 
 def trace(surfs, a, b, rays, fp64=True):

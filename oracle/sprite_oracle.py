@@ -81,3 +81,121 @@ def splat(spr, sources, sx_ds, sy_ds, px_mm_x, px_mm_y, rx, ry, gain, width, hei
         for c, w in enumerate((r, g, b)):
             out[c][np.ix_(ys, xs)] += (Wy @ spr[..., c] @ Wx.T) * w * gain
     return out
+
+
+# ---- off-axis cat's-eye (starburst_render.cu:393-583), float launches, the
+# oracle's float host trace (the reference's host arithmetic) ----------------
+def _launch(ax, ay):
+    f = np.float32
+    bx, by = f(np.tan(f(ax))), f(np.tan(f(ay)))
+    ln = f(np.sqrt(f(f(bx * bx) + f(by * by)) + f(1.0)))
+    inv = f(f(1.0) / ln)
+    return bx, by, (f(bx * inv), f(by * inv), inv)
+
+
+def _survive(surfs, pts, z, d, lam=550.0):
+    from oracle import oracle as O
+    pts = np.asarray(pts, np.float32).reshape(-1, 2)
+    if len(pts) == 0:
+        return np.zeros(0, bool)
+    rays = np.zeros((len(pts), 7), np.float32)
+    rays[:, 0:2] = pts
+    rays[:, 2] = z
+    rays[:, 3:6] = d
+    rays[:, 6] = lam
+    r = O.trace(surfs, -1, -1, rays, fp64=False)
+    return (r[:, 4] == 0) & np.isfinite(r[:, 0]) & np.isfinite(r[:, 1])
+
+
+def survivor_center(surfs, ax, ay):
+    """solve_survivor_center: (cx, cy, any)."""
+    f = np.float32
+    front_R = f(surfs[0].semi_aperture)
+    if front_R <= 0:
+        return 0.0, 0.0, False
+    z = f(f(surfs[0].z) - f(20.0))
+    bx, by, d = _launch(ax, ay)
+    span_x = f(f(f(1.1) * front_R) + f(f(20.0) * f(abs(bx))))
+    span_y = f(f(f(1.1) * front_R) + f(f(20.0) * f(abs(by))))
+    S, K = 81, 8
+    pos = lambda span, k: f(span * f(f(f(2.0) * f(k)) / f(S - 1) - f(1.0)))
+    grid = [(pos(span_x, i), pos(span_y, j)) for j in range(S) for i in range(S)]
+    surv = _survive(surfs, grid, z, d).reshape(S, S)
+    hx, hy = f(span_x / f(S - 1)), f(span_y / f(S - 1))
+    inv_k2 = f(f(1.0) / f(K * K))
+    sx = sy = w = 0.0
+    pending = []
+    for j in range(S):
+        for i in range(S):
+            s = surv[j, i]
+            bnd = any(0 <= i + di < S and 0 <= j + dj < S and surv[j + dj, i + di] != s
+                      for dj in (-1, 0, 1) for di in (-1, 0, 1) if di or dj)
+            lx, ly = grid[j * S + i]
+            if not bnd:
+                if s:
+                    sx += float(lx)
+                    sy += float(ly)
+                    w += 1.0
+                continue
+            for a in range(K):
+                lly = f(ly + f(hy * f(f(f(2.0) * f(a + 0.5)) / f(K) - f(1.0))))
+                for b in range(K):
+                    llx = f(lx + f(hx * f(f(f(2.0) * f(b + 0.5)) / f(K) - f(1.0))))
+                    pending.append((llx, lly))
+    if pending:
+        ok = _survive(surfs, pending, z, d)
+        for (llx, lly), o in zip(pending, ok):
+            if o:
+                sx += float(llx) * float(inv_k2)
+                sy += float(lly) * float(inv_k2)
+                w += float(inv_k2)
+    if w > 0:
+        return float(f(sx / w)), float(f(sy / w)), True
+    return 0.0, 0.0, False
+
+
+def survivor_envelope(surfs, ep_x, ep_y, cx, cy, ax, ay, ME):
+    """build_survivor_envelope: (ME, ME) float32."""
+    from oracle import oracle as O
+    f = np.float32
+    z = f(f(surfs[0].z) - f(20.0))
+    _, _, d = _launch(ax, ay)
+    coord = lambda k: f(f(f(f(k) + f(0.5)) / f(ME)) * f(2.0) - f(1.0))
+    cells = [(coord(i), coord(j)) for j in range(ME) for i in range(ME)]
+    inside = O.pupil_contains(surfs, cells, aspect_one=True).reshape(ME, ME)
+    env = np.full((ME, ME), -1.0, np.float32)
+    launch = [(f(f(cx) + f(u * f(ep_x))), f(f(cy) + f(v * f(ep_y)))) for (u, v), ins in zip(cells, inside.ravel())
+              if ins]
+    env[inside] = _survive(surfs, launch, z, d).astype(np.float32)
+    base = env.copy()
+    K = 10
+    du = f(f(2.0) / f(ME))
+    for j in range(ME):
+        for i in range(ME):
+            e = base[j, i]
+            if e < 0:
+                continue
+            bnd = any(0 <= i + di < ME and 0 <= j + dj < ME and base[j + dj, i + di] >= 0
+                      and (base[j + dj, i + di] > 0.5) != (e > 0.5)
+                      for dj in (-1, 0, 1) for di in (-1, 0, 1) if di or dj)
+            if not bnd:
+                continue
+            u0, v0 = cells[j * ME + i]
+            sub = [(f(u0 + f(du * f(f(f(sx) + f(0.5)) / f(K) - f(0.5)))),
+                    f(v0 + f(du * f(f(f(sy) + f(0.5)) / f(K) - f(0.5))))) for sy in range(K) for sx in range(K)]
+            ins = O.pupil_contains(surfs, sub, aspect_one=True)
+            pts = [(f(f(cx) + f(u * f(ep_x))), f(f(cy) + f(v * f(ep_y)))) for (u, v), k in zip(sub, ins) if k]
+            if pts:
+                env[j, i] = f(f(int(_survive(surfs, pts, z, d).sum())) / f(len(pts)))
+    out = env.copy()
+    for j in range(ME):
+        for i in range(ME):
+            if env[j, i] >= 0:
+                continue
+            best = 0.0
+            for dj in range(-2, 3):
+                for di in range(-2, 3):
+                    if 0 <= i + di < ME and 0 <= j + dj < ME and env[j + dj, i + di] >= 0:
+                        best = max(best, float(env[j + dj, i + di]))
+            out[j, i] = best
+    return out

@@ -145,3 +145,51 @@ def test_mdft_engine_still_selectable():
     g = out["starburst_g"].cpu().numpy()
     y, x = np.unravel_index(np.argmax(g), g.shape)
     assert abs(x - 128) <= 2 and abs(y - 96) <= 2
+
+
+@pytest.mark.parametrize("field_deg", [(15.0, 5.0), (-22.0, 0.0)])
+def test_cats_eye_device_matches_oracle(field_deg):
+    """The cat's-eye centre and envelope from device traces against the
+    oracle's float host traces: launches that straddle an aperture edge
+    within rounding may land on either side, so the envelopes agree up to a
+    few rim cells and the centres to a small fraction of the pupil."""
+    import math
+    from ghostlight_gb300.starburst import survivor_center, survivor_envelope
+    lens = _lens()
+    surfs = lens.records()
+    ax, ay = (math.radians(a) for a in field_deg)
+    got = survivor_center(lens, ax, ay)
+    want = SO.survivor_center(surfs, ax, ay)
+    assert got[2] and want[2]
+    ep = lens.calibration().entrance_pupil_semi_x
+    assert abs(got[0] - want[0]) < 1e-3 * ep and abs(got[1] - want[1]) < 1e-3 * ep
+    env = survivor_envelope(lens, ep, ep, want[0], want[1], ax, ay, 64)
+    ref = SO.survivor_envelope(surfs, ep, ep, want[0], want[1], ax, ay, 64)
+    assert np.abs(env - ref).mean() < 2e-3 and (env != ref).mean() < 0.01
+    assert 0.0 < ref.mean() < 1.0
+
+
+def test_off_axis_sprite_uses_the_cats_eye():
+    """Off axis the sprite's pupil is the stop weighted by the envelope: it
+    never exceeds the plain stop, its throughput T < 1 scales the gain, and
+    switching use_survivor_mask off restores the plain stop."""
+    import math
+    from ghostlight_gb300.starburst import build_pupil2, effective_pupil, sprite_geometry
+    lens = _lens()
+    cal = lens.calibration()
+    cfg = _config(8)
+    g = sprite_geometry(cal, cfg, np.array([[100, 100, 1, 1, 1]], np.float32), 320, 240, cal.sensor_half_w,
+                        cal.sensor_half_h, front_R=lens.surfaces[0].semi_aperture)
+    field = (math.radians(18.0), math.radians(4.0))
+    pupil, T = effective_pupil(lens, cfg, g, field)
+    plain = build_pupil2(lens, g["N"], g["fill"])
+    assert pupil is not None and 0.01 < T < 0.999
+    p, q = pupil.cpu().numpy(), plain.cpu().numpy()
+    assert np.all(p <= q + 1e-6)
+    assert float((pupil.double() ** 2).sum() / (plain.double() ** 2).sum()) == pytest.approx(T, rel=1e-9)
+    cfg.diffraction.use_survivor_mask = False
+    p2, T2 = effective_pupil(lens, cfg, g, field)
+    assert T2 == 1.0 and torch.equal(p2, plain)
+    # far past the vignette edge nothing survives: no starburst
+    cfg.diffraction.use_survivor_mask = True
+    assert effective_pupil(lens, cfg, g, (math.radians(80.0), 0.0))[0] is None

@@ -101,3 +101,35 @@ def test_oracle_energy():
     assert np.all(np.abs(tot - 1.0) < 0.08)
     img = SO.splat(spr, [[100.2, 90.7, 1.0, 1.0, 1.0]], 0.01, 0.01, 0.02, 0.02, 80, 80, 1.0, 200, 180)
     np.testing.assert_allclose(img.reshape(3, -1).sum(1), tot, rtol=1e-9)
+
+
+@pytest.mark.parametrize("field_deg", [(15.0, 5.0), (-22.0, 0.0), (3.0, -18.0)])
+def test_survivor_structure_matches_restatement(field_deg):
+    """The product's vectorised cat's-eye centre and envelope against the
+    oracle's loop-by-loop restatement of solve_survivor_center /
+    build_survivor_envelope, both fed the oracle's float host trace: the
+    same launches, boundary cells, supersamples and dilation give the same
+    numbers bit for bit."""
+    import math
+    from ghostlight_gb300 import prescriptions as P
+    from ghostlight_gb300.optics import OpticalSystem
+    from ghostlight_gb300.starburst import survivor_center, survivor_envelope
+    lens = OpticalSystem.from_records(P.double_gauss_12(seed=1))
+    surfs = lens.records()
+    ax, ay = (math.radians(a) for a in field_deg)
+
+    def host_survives(x, y, z, d):
+        return SO._survive(surfs, np.stack([x, y], 1), z, d)
+
+    got = survivor_center(lens, ax, ay, survives=host_survives)
+    want = SO.survivor_center(surfs, ax, ay)
+    assert got[2] == want[2]
+    assert np.float32(got[0]) == np.float32(want[0]) and np.float32(got[1]) == np.float32(want[1])
+    if not want[2]:
+        return
+    cal = lens.calibration()
+    ep_x, ep_y = cal.entrance_pupil_semi_x, cal.entrance_pupil_semi_y
+    env = survivor_envelope(lens, ep_x, ep_y, got[0], got[1], ax, ay, 40, survives=host_survives)
+    ref = SO.survivor_envelope(surfs, ep_x, ep_y, want[0], want[1], ax, ay, 40)
+    np.testing.assert_array_equal(env, ref)
+    assert 0.0 < env.mean() < 1.0 and ((env > 0) & (env < 1)).any()
