@@ -147,7 +147,7 @@ def test_mdft_engine_still_selectable():
     assert abs(x - 128) <= 2 and abs(y - 96) <= 2
 
 
-@pytest.mark.parametrize("field_deg", [(15.0, 5.0), (-22.0, 0.0)])
+@pytest.mark.parametrize("field_deg", [(15.0, 5.0), (-12.0, 3.0), (-22.0, 0.0)])
 def test_cats_eye_device_matches_oracle(field_deg):
     """The cat's-eye centre and envelope from device traces against the
     oracle's float host traces: launches that straddle an aperture edge
@@ -160,7 +160,9 @@ def test_cats_eye_device_matches_oracle(field_deg):
     ax, ay = (math.radians(a) for a in field_deg)
     got = survivor_center(lens, ax, ay)
     want = SO.survivor_center(surfs, ax, ay)
-    assert got[2] and want[2]
+    assert got[2] == want[2]
+    if not want[2]:         # past this lens's vignette edge
+        return
     ep = lens.calibration().entrance_pupil_semi_x
     assert abs(got[0] - want[0]) < 1e-3 * ep and abs(got[1] - want[1]) < 1e-3 * ep
     env = survivor_envelope(lens, ep, ep, want[0], want[1], ax, ay, 64)
