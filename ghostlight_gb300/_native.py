@@ -43,6 +43,7 @@ def _declare(lib):
     lib.gl_coating_table_create.argtypes = [i, fp, i, fp, i, fp, C.c_float, i, P(i)]
     lib.gl_coating_table_info.argtypes = [i, P(i), P(i), P(i), fp, P(i)]
     lib.gl_coating_table_read.argtypes = [i, fp, fp, fp]
+    lib.gl_aperture_image_create.argtypes = [i, i, fp, C.c_float, P(i)]
     lib.gl_coating_table_prepare.argtypes = [i]
     lib.gl_coating_bake_layers.argtypes = [P(gl_surface), i, i, i, fp, P(i), fp, fp, fp, P(i)]
     lib.gl_blade_radius.argtypes = [i, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, P(C.c_float), i,

@@ -26,6 +26,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <complex>
 #include <cstring>
 #include <map>
@@ -263,6 +264,22 @@ extern "C" int gl_coating_table_create(int32_t model, const float* axis0, int32_
     return intern(std::move(e), out_id);
 }
 
+extern "C" int gl_aperture_image_create(int32_t width, int32_t height, const float* pixels, float semi_diameter,
+                                        int32_t* out_id)
+{
+    if (!out_id || !pixels || width < 1 || height < 1 || (long long)width * height > (1LL << 28))
+        return fail(GL_ERR_INVALID, "aperture_image_create: bad arguments");
+    if (!std::isfinite(semi_diameter) || semi_diameter < 0.0f)
+        return fail(GL_ERR_INVALID, "aperture_image_create: semi_diameter must be finite and non-negative");
+    auto e = std::make_unique<TableEntry>();
+    e->model = kStoreImage;
+    e->n0 = width;
+    e->n1 = height;
+    e->ref_ior = semi_diameter;
+    e->data.assign(pixels, pixels + (size_t)width * height);
+    return intern(std::move(e), out_id);
+}
+
 extern "C" int gl_coating_table_info(int32_t id, int32_t* model, int32_t* n0, int32_t* n1, float* angle_ref_ior,
                                      int32_t* out_of_range_discard)
 {
@@ -281,6 +298,11 @@ extern "C" int gl_coating_table_read(int32_t id, float* axis0, float* axis1, flo
     TableEntry* e = lookup(id);
     if (!e) return fail(GL_ERR_INVALID, "unknown coating table id " + std::to_string(id));
     const float* d = e->data.data();
+    if (e->model == kStoreImage)
+    {
+        if (r) std::memcpy(r, d, (size_t)e->n0 * e->n1 * 4);
+        return GL_OK;
+    }
     if (axis0) std::memcpy(axis0, d, (size_t)e->n0 * 4);
     if (axis1 && e->n1) std::memcpy(axis1, d + e->n0, (size_t)e->n1 * 4);
     const size_t nr = (e->n1 ? (size_t)e->n0 * e->n1 : (size_t)e->n0);

@@ -119,6 +119,7 @@ __device__ __forceinline__ bool aperture_ok(float x, float y, const SurfRec& s)
     const float h2 = hx * hx + hy * hy;
     if (!(h2 <= s.semi_ap * s.semi_ap)) return false;
     if (s.shape == 1) return check_polygon(hx, hy, h2, s);
+    if (s.shape == 2) return image_aperture_ok(x, y, s);
     return true;
 }
 
@@ -147,7 +148,7 @@ struct __align__(16) HotRec {
     float ar_scale;                 // 0.25^(ar_layers - 1): the extra AR layers of the SIMPLE model
     int pad;
 };
-enum HotBits { HB_ACTIVE = 1, HB_GENERAL = 2, HB_POLYGON = 4, HB_SIMPLE = 8, HB_ATTEN = 16 };
+enum HotBits { HB_ACTIVE = 1, HB_GENERAL = 2, HB_POLYGON = 4, HB_SIMPLE = 8, HB_ATTEN = 16, HB_IMAGE = 32 };
 
 __device__ __forceinline__ HotRec make_hot(const SurfRec& s)
 {
@@ -159,7 +160,7 @@ __device__ __forceinline__ HotRec make_hot(const SurfRec& s)
     h.bits = ((s.flags & SF_ACTIVE) ? HB_ACTIVE : 0) |
              ((s.form != 0 || (s.flags & SF_TRANSFORMED)) ? HB_GENERAL : 0) |
              ((s.shape == 1) ? HB_POLYGON : 0) | ((s.coating == 0) ? HB_SIMPLE : 0) |
-             ((s.coating == 4) ? HB_ATTEN : 0);
+             ((s.coating == 4) ? HB_ATTEN : 0) | ((s.shape == 2) ? HB_IMAGE : 0);
     h.ar_layers = s.ar_layers;
     h.ar_scale = 1.0f;
     for (int i = 1; i < s.ar_layers; ++i) h.ar_scale *= 0.25f;
@@ -240,6 +241,7 @@ __device__ __forceinline__ bool surface_step(V3& o, V3& d, const HotRec& h, cons
         const float h2 = hx * hx + hy * hy;
         if (!(h2 <= h.sa2)) return false;
         if ((h.bits & HB_POLYGON) && !check_polygon(hx, hy, h2, s)) return false;
+        if ((h.bits & HB_IMAGE) && !image_aperture_ok(q.x, q.y, s)) return false;
         // outward normal (c q_x, c q_y, c q_z - 1), turned to oppose the ray
         // (for a plane, c = 0, it is (0, 0, -1) as it stands)
         nrm = v3(c * q.x, c * q.y, c * q.z - 1.0f);

@@ -44,8 +44,8 @@ int pack_lens(const gl_surface* in, int n, SurfRec* out, int tables, bool may_up
         const gl_surface& g = in[i];
         SurfRec& r = out[i];
         std::memset(&r, 0, sizeof(r));
-        if (g.aperture_shape == GL_APERTURE_IMAGE)
-            return fail(GL_ERR_UNSUPPORTED, "image apertures are outside the flare path");
+        if (g.aperture_shape < GL_APERTURE_CIRCLE || g.aperture_shape > GL_APERTURE_IMAGE)
+            return fail(GL_ERR_INVALID, "unknown aperture shape " + std::to_string(g.aperture_shape));
         if (g.coating_model < GL_COATING_SIMPLE || g.coating_model > GL_COATING_ARTIST)
             return fail(GL_ERR_INVALID, "unknown coating model " + std::to_string(g.coating_model));
         if (g.aperture_shape == GL_APERTURE_POLYGON && g.aperture_blades < 3)
@@ -55,8 +55,20 @@ int pack_lens(const gl_surface* in, int n, SurfRec* out, int tables, bool may_up
         r.semi_ap = g.semi_aperture;
         r.aspect = g.aperture_aspect;
         r.rot_rad = g.aperture_rotation_rad;
-        r.shape = (g.aperture_shape == GL_APERTURE_POLYGON) ? 1 : 0;
-        r.blades = g.aperture_blades;
+        r.shape = (g.aperture_shape == GL_APERTURE_POLYGON) ? 1 : (g.aperture_shape == GL_APERTURE_IMAGE ? 2 : 0);
+        r.blades = (g.aperture_shape == GL_APERTURE_IMAGE) ? 0 : g.aperture_blades;
+        if (g.aperture_shape == GL_APERTURE_IMAGE && g.aperture_blades != 0)
+        {
+            // aperture_blades names the bitmap in the store; 0 = not loaded
+            const float* px = nullptr;
+            int disc = 0;
+            int rc = coating_table_address(g.aperture_blades, kStoreImage, tables, may_upload, &px, &r.img_w,
+                                           &r.img_h, &disc, &r.img_semi);
+            if (rc) return rc;
+            const uint64_t a = (uint64_t)(uintptr_t)px;
+            r.img_lo = (uint32_t)a;
+            r.img_hi = (uint32_t)(a >> 32);
+        }
         if (r.shape == 1)
         {
             // check_aperture (trace_core.h:159-166) evaluates these per hit;

@@ -29,6 +29,7 @@ struct PupilMask {
 // (kTablesHost) or device `tables` (copied there on first use unless
 // `may_upload` is false).
 constexpr int kTablesHost = -1;
+constexpr int kStoreImage = 100;     // store entries that hold an aperture bitmap
 int pack_lens(const gl_surface* in, int n, SurfRec* out, int tables, bool may_upload = true);
 int coating_table_address(int id, int model, int device, bool may_upload, const float** out, int* n0, int* n1,
                           int* discard, float* ref_ior);

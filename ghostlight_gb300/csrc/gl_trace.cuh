@@ -63,10 +63,17 @@ struct SurfRec {
     uint32_t tab_lo, tab_hi;
     int32_t tab_n0, tab_n1, tab_discard;
     float tab_ref_ior;
+    // bitmap aperture (shape 2): address of its w x h luminance pixels (row
+    // major, 0 = not loaded: passthrough), and the world radius of the
+    // image boundary
+    uint32_t img_lo, img_hi;
+    int32_t img_w, img_h;
+    float img_semi;
+    int32_t img_pad;
 };
-// 71 words: an odd stride, so lanes reading the same field of different
+// 77 words: an odd stride, so lanes reading the same field of different
 // surfaces in shared memory hit different banks.
-static_assert(sizeof(SurfRec) == 284, "SurfRec must stay 284 bytes");
+static_assert(sizeof(SurfRec) == 308, "SurfRec must stay 308 bytes");
 
 struct V3 {
     float x, y, z;
@@ -282,6 +289,23 @@ GLH float surface_attenuator(V3 hit, const SurfRec& s)
 }
 
 // ---- geometry (trace_core.h:133-564) -------------------------------------
+// Bitmap aperture (sample_aperture_image, trace.cpp:31-48): the surface
+// point (x, y) in the image's frame, nearest pixel, open where > 0.5; outside
+// the image closed; no pixels loaded: open.
+GLH bool image_aperture_ok(float x, float y, const SurfRec& s)
+{
+    const float* px = reinterpret_cast<const float*>(((uint64_t)s.img_hi << 32) | (uint64_t)s.img_lo);
+    if (px == nullptr) return true;
+    if (s.img_w <= 0 || s.img_h <= 0 || !(s.aspect > 0.0f) || !(s.img_semi > 0.0f)) return false;
+    const float hx = x / s.aspect;
+    const float u = 0.5f + hx / (2.0f * s.img_semi);
+    const float v = 0.5f + y / (2.0f * s.img_semi);
+    if (u < 0.0f || u > 1.0f || v < 0.0f || v > 1.0f) return false;
+    const int ix = (int)(u * (float)(s.img_w - 1) + 0.5f);
+    const int iy = (int)(v * (float)(s.img_h - 1) + 0.5f);
+    return px[(size_t)iy * s.img_w + ix] > 0.5f;
+}
+
 GLH bool check_aperture(V3 hit, const SurfRec& s)
 {
     float hx = hit.x / s.aspect;
@@ -300,6 +324,7 @@ GLH bool check_aperture(V3 hit, const SurfRec& s)
         off -= 0.5f * s.sector;
         return r <= s.apothem / cosf(off);
     }
+    if (s.shape == 2) return image_aperture_ok(hit.x, hit.y, s);
     return true;
 }
 

@@ -15,9 +15,9 @@ where the reference only warns, this reader warns too.
 Table-backed coatings (``spectral``, ``angular``, ``spectral_angular``) go
 to the coating store (``ghostlight_gb300.coatings``), the surface record
 naming its table; thin-film stacks (``layers``) are baked after flattening,
-as the reference does.  Not carried by this build: bitmap (``image``)
-apertures, which load circular with a warning and are listed in
-``OpticalSystem.unsupported`` so a caller can refuse the lens.
+as the reference does.  Bitmap (``image``) apertures load as IMAGE surfaces
+with their path and semi-diameter recorded; the pixels are decoded by
+``OpticalSystem.load_aperture_images`` as in the reference.
 """
 from __future__ import annotations
 
@@ -324,8 +324,8 @@ def _apply_apertures(mods, s: gl_surface, path, unsupported: List[str]):
     """apply_aperture_modifiers (optical_system.cpp:572-689): last one wins;
     default circle of aspect 1."""
     if not isinstance(mods, list):
-        return
-    image = False
+        return None
+    image = None
     for m in mods:
         if not isinstance(m, dict) or m.get("type", "") != "aperture":
             continue
@@ -336,7 +336,7 @@ def _apply_apertures(mods, s: gl_surface, path, unsupported: List[str]):
             if not (aspect > f32(0.0)):
                 warnings.warn("%s: aperture_aspect must be > 0; got %g - clamping to 1.0." % (path, aspect))
                 aspect = f32(1.0)
-        image = False
+        image = None
         if shape == "circular":
             _set_circular(s, aspect)
         elif shape == "polygon":
@@ -363,12 +363,14 @@ def _apply_apertures(mods, s: gl_surface, path, unsupported: List[str]):
                 _set_circular(s, aspect)
                 continue
             _set_circular(s, aspect)
-            image = True
+            # the pixels are decoded later (OpticalSystem.load_aperture_images);
+            # until then the bitmap passes every ray, as in the reference
+            s.aperture_shape = _APERTURE_IMAGE
+            image = (str(m["image_path"]), float(sd))
         else:
             warnings.warn("%s: unknown aperture shape '%s'; falling back to circular." % (path, shape))
             _set_circular(s, aspect)
-    if image:
-        unsupported.append("image aperture (bitmap stop; loaded circular)")
+    return image
 
 
 def _parse_form(jf, s: gl_surface, path):
@@ -396,7 +398,7 @@ def _parse_form(jf, s: gl_surface, path):
         s.cyl_axis = 1 if ax in ("y", "Y") else 0
 
 
-def _flatten_element(jel, M: _Transform, nominal_z, catalogue, path, surfaces, notes, layer_stacks):
+def _flatten_element(jel, M: _Transform, nominal_z, catalogue, path, surfaces, notes, layer_stacks, images):
     """flatten_element (optical_system.cpp:801-912); returns the nominal z of
     the element's last surface vertex."""
     js_list, jm_list = jel.get("surfaces"), jel.get("materials")
@@ -421,7 +423,9 @@ def _flatten_element(jel, M: _Transform, nominal_z, catalogue, path, surfaces, n
         mods = js.get("modifiers", [])
         stack = _extract_coating(mods, s, path, unsupported)
         _parse_form(js.get("form", {}), s, path)
-        _apply_apertures(mods, s, path, unsupported)
+        image = _apply_apertures(mods, s, path, unsupported)
+        if image is not None:
+            images[len(surfaces)] = image
         thickness = _value(js, "thickness", 0.0)
         s.thickness = float(thickness)
         s.decenter_x = float(M.pos[0] + M.piv[0] + M.rot[2] * cum_local)
@@ -485,7 +489,7 @@ def _apply_pivot(p, point, t: _Transform):
     t.piv = _mat_vec(R, t.piv)
 
 
-def read_lens(path) -> Tuple[List[gl_surface], str, float, List[Tuple[int, str]]]:
+def read_lens(path, images=None) -> Tuple[List[gl_surface], str, float, List[Tuple[int, str]]]:
     """Parse and flatten a lens file: (surface records, name, focal length
     hint, [(surface index, unsupported feature)])."""
     path = os.fspath(path)
@@ -571,11 +575,14 @@ def read_lens(path) -> Tuple[List[gl_surface], str, float, List[Tuple[int, str]]
     surfaces: List[gl_surface] = []
     notes: List[Tuple[int, str]] = []
     layer_stacks: Dict[int, list] = {}
+    if images is None:
+        images = {}
     emits = []
     for r in records:
         z_nom = r["xform"].pos[2]
         first = len(surfaces)
-        last_z = _flatten_element(r["node"], r["xform"], z_nom, catalogue, path, surfaces, notes, layer_stacks)
+        last_z = _flatten_element(r["node"], r["xform"], z_nom, catalogue, path, surfaces, notes, layer_stacks,
+                                  images)
         emits.append((z_nom, first, len(surfaces) - first, last_z))
     for k in range(len(emits) - 1):
         _, first, n, last_z = emits[k]
@@ -603,9 +610,12 @@ def read_lens(path) -> Tuple[List[gl_surface], str, float, List[Tuple[int, str]]
 def load_lens(path):
     """OpticalSystem.load(path): the flat surface table of a lens file."""
     from .optics import OpticalSystem
-    surfaces, name, focal, notes = read_lens(path)
+    images = {}
+    surfaces, name, focal, notes = read_lens(path, images)
     out = OpticalSystem.from_records(surfaces, name=name, focal_length=focal)
     out.unsupported = notes
+    for idx, (src, semi) in images.items():
+        out.set_aperture_source(idx, src, semi)
     out.source_path = os.fspath(path)
     return out
 
@@ -630,7 +640,7 @@ def _euler_from_rot(R):
     return math.degrees(tx), math.degrees(ty), math.degrees(rz)
 
 
-def _modifiers(s: gl_surface):
+def _modifiers(s: gl_surface, image=None):
     mods = []
     if s.coating_model == _COATING_SIMPLE:
         if s.ar_layers:
@@ -681,7 +691,10 @@ def _modifiers(s: gl_surface):
     elif s.aperture_shape == _APERTURE_CIRCLE:
         ap["shape"] = "circular"
     else:
-        raise ValueError("save_lens: image apertures are not carried by this build")
+        src, semi = image if image is not None else ("", 0.0)
+        if not src or not semi > 0:
+            raise ValueError("save_lens: image aperture has no source path / semi-diameter to write")
+        ap.update(shape="image", image_path=src, semi_diameter=float(semi))
     if s.aperture_aspect != 1.0:
         ap["aperture_aspect"] = float(s.aperture_aspect)
     if len(ap) > 2 or s.aperture_shape != _APERTURE_CIRCLE:
@@ -698,6 +711,9 @@ def lens_document(lens, name: str = "") -> dict:
     rounding (the loader re-accumulates element thicknesses)."""
     import uuid
     surfs = [s.record if hasattr(s, "record") else s for s in getattr(lens, "surfaces", lens)]
+    image_sources = {i: (img.source_path, img.semi_diameter)
+                     for i, img in enumerate(getattr(lens, "aperture_images", []) or [])
+                     if getattr(img, "source_path", "")}
     if not surfs:
         raise ValueError("save_lens: lens has no surfaces")
     catalogue, glass_names = {}, {}
@@ -726,7 +742,7 @@ def lens_document(lens, name: str = "") -> dict:
                 js["is_stop"] = True
             if not s.is_active:
                 js["is_active"] = False
-            mods = _modifiers(s)
+            mods = _modifiers(s, image_sources.get(i))
             if mods:
                 js["modifiers"] = mods
             jsurfs.append(js)

@@ -282,6 +282,55 @@ class OpticalSystem:
                 return float(np.float32(s.ior)) if lambda_nm is None else s.ior_at(lambda_nm)
         return 1.0
 
+    # ---- bitmap apertures (bind_geometry.cpp:311-384, optical_system.py:178) --
+    def set_aperture_source(self, index: int, source_path: str, semi_diameter: float) -> None:
+        """Declare surface ``index`` a bitmap aperture read from
+        ``source_path`` (decoded by load_aperture_images); until then it
+        passes every ray inside its clear aperture."""
+        i = self._surface_index(index)
+        paths = self.__dict__.setdefault("_aperture_sources", {})
+        paths[i] = (str(source_path), float(semi_diameter))
+        self.surfaces[i].aperture_shape = ApertureShape.IMAGE
+        self.surfaces[i].aperture_blades = 0
+
+    def set_aperture_image(self, index: int, pixels, semi_diameter: float | None = None) -> None:
+        """Surface ``index`` becomes a bitmap aperture: ``pixels`` (H, W)
+        luminance in [0, 1] (open above 0.5, nearest pixel), the image
+        spanning +-semi_diameter mm (default: the declared one)."""
+        from .aperture_images import create_image
+        i = self._surface_index(index)
+        paths = self.__dict__.setdefault("_aperture_sources", {})
+        if semi_diameter is None:
+            semi_diameter = paths.get(i, ("", 0.0))[1]
+        if not semi_diameter > 0:
+            raise ValueError("set_aperture_image: semi_diameter must be positive")
+        tid = create_image(pixels, float(semi_diameter))
+        paths[i] = (paths.get(i, ("", 0.0))[0], float(semi_diameter))
+        self.surfaces[i].aperture_shape = ApertureShape.IMAGE
+        self.surfaces[i].aperture_blades = tid
+
+    @property
+    def aperture_images(self):
+        """ApertureImage per surface (empty pixels for surfaces without a
+        loaded bitmap).  A snapshot: change a bitmap with set_aperture_image."""
+        from .aperture_images import ApertureImage, read_image
+        paths = self.__dict__.get("_aperture_sources", {})
+        out = []
+        for i, s in enumerate(self.surfaces):
+            src, semi = paths.get(i, ("", 0.0))
+            if s.aperture_shape == ApertureShape.IMAGE and s.aperture_blades:
+                img = read_image(s.aperture_blades)
+                img.source_path = src
+                out.append(img)
+            else:
+                out.append(ApertureImage(None, semi if s.aperture_shape == ApertureShape.IMAGE else 0.0, src))
+        return out
+
+    def load_aperture_images(self, *, root_dir: str | None = None) -> None:
+        """Decode the bitmaps of the IMAGE surfaces (optical_system.py:178-225)."""
+        from .aperture_images import load_aperture_images
+        load_aperture_images(self, root_dir)
+
     # ---- coating tables (bind_geometry.cpp:412-627) ------------------------
     def _surface_index(self, i: int) -> int:
         if i < 0 or i >= len(self.surfaces):

@@ -175,6 +175,18 @@ int gl_coating_table_create(int32_t model, const float* axis0, int32_t n0, const
 int gl_coating_table_info(int32_t id, int32_t* model, int32_t* n0, int32_t* n1, float* angle_ref_ior,
                           int32_t* out_of_range_discard);
 int gl_coating_table_read(int32_t id, float* axis0, float* axis1, float* r);
+/* Bitmap aperture (ApertureImage, ghostlight/src/optical_system.h:262-269;
+ * sampled by sample_aperture_image, trace.cpp:31-48): width x height
+ * row-major luminance in [0, 1] and the world radius of the image boundary
+ * (aperture_semi_diameter).  A surface selects it with aperture_shape =
+ * GL_APERTURE_IMAGE and aperture_blades = id (0: not loaded, the surface
+ * passes every ray inside its clear aperture, as the reference does before
+ * the pixels are decoded).  Same store as the coating tables:
+ * gl_coating_table_info reports model 100, n0 = width, n1 = height,
+ * angle_ref_ior = semi-diameter; gl_coating_table_read returns the pixels
+ * in r. */
+int gl_aperture_image_create(int32_t width, int32_t height, const float* pixels, float semi_diameter,
+                             int32_t* out_id);
 /* Copy a table to the current device ahead of an allocation-free render
  * (the other entry points copy it on first use). */
 int gl_coating_table_prepare(int32_t id);

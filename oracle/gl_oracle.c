@@ -128,6 +128,21 @@ int orc_coating_register(int id, int model, int n0, int n1, const float* data, f
     return 0;
 }
 
+/* ApertureImage (optical_system.h:262-269) under the id a GL_APERTURE_IMAGE
+ * surface carries in aperture_blades: w x h luminance, the boundary radius in
+ * ref_ior. */
+int orc_image_register(int id, int w, int h, const float* pixels, float semi_diameter)
+{
+    if (id < 1 || id >= ORC_MAX_TABLES || w < 1 || h < 1) return -1;
+    float* d = (float*)malloc((size_t)w * h * sizeof(float));
+    if (!d) return -1;
+    memcpy(d, pixels, (size_t)w * h * sizeof(float));
+    free(orc_tables[id].data);
+    orc_tables[id].model = 100; orc_tables[id].n0 = w; orc_tables[id].n1 = h;
+    orc_tables[id].discard = 0; orc_tables[id].ref_ior = semi_diameter; orc_tables[id].data = d;
+    return 0;
+}
+
 static const orc_table* orc_coating_find(int id)
 {
     if (id < 1 || id >= ORC_MAX_TABLES || !orc_tables[id].data) return NULL;

@@ -301,6 +301,19 @@ static inline int SFX(check_aperture)(SFX(v3) hit, const gl_surface* s)
         const R apothem = (R)s->semi_aperture * COS((R)0.5f * sector);
         return r <= apothem / COS(off);
     }
+    if (s->aperture_shape == GL_APERTURE_IMAGE)
+    {
+        /* sample_aperture_image, trace.cpp:31-48: nearest pixel > 0.5 */
+        const orc_table* t = orc_coating_find(s->aperture_blades);
+        if (!t || t->model != 100) return 1;          /* not loaded: passthrough */
+        if (!(s->aperture_aspect > 0.0f) || !(t->ref_ior > 0.0f)) return 0;
+        const R u = (R)0.5f + hit.x / (R)s->aperture_aspect / ((R)2.0f * (R)t->ref_ior);
+        const R v = (R)0.5f + hit.y / ((R)2.0f * (R)t->ref_ior);
+        if (u < 0 || u > 1 || v < 0 || v > 1) return 0;
+        const int px = (int)(u * (R)(t->n0 - 1) + (R)0.5f);
+        const int py = (int)(v * (R)(t->n1 - 1) + (R)0.5f);
+        return t->data[(size_t)py * t->n0 + px] > 0.5f;
+    }
     return 1;
 }
 

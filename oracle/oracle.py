@@ -32,6 +32,7 @@ def _load():
         lib.orc_aperture_samples.argtypes = [P(gl_surface), i, i, i, i, i, f, P(f), i]
         lib.orc_blade_radius.argtypes = [P(gl_surface), P(f), i, P(f)]
         lib.orc_coating_register.argtypes = [i, i, i, i, P(f), f, i]
+        lib.orc_image_register.argtypes = [i, i, i, P(f), f]
         lib.orc_pupil_contains.argtypes = [P(gl_surface), i, i, f, i, P(f), i, P(C.c_ubyte)]
         lib.orc_render.argtypes = [P(gl_surface), i, P(i), P(f), P(i), i, P(f), i, P(f), P(i),
                                    P(f), i, f, f, i, i, f, i, i, P(d)]
@@ -63,6 +64,14 @@ def register_coating(table_id, model, axis0, r, axis1=None, angle_ref_ior=1.0, d
     if lib.orc_coating_register(int(table_id), int(model), len(a0), len(a1), _fp(data), float(angle_ref_ior),
                                 int(bool(discard))) != 0:
         raise ValueError("oracle: bad coating table %d" % table_id)
+
+
+def register_image(image_id, pixels, semi_diameter):
+    """Give the oracle the bitmap an IMAGE surface names by aperture_blades."""
+    lib = _load()
+    px = np.ascontiguousarray(pixels, np.float32)
+    if lib.orc_image_register(int(image_id), px.shape[1], px.shape[0], _fp(px), float(semi_diameter)) != 0:
+        raise ValueError("oracle: bad aperture image %d" % image_id)
 
 
 def pupil_contains(surfs, uv, blades_override=0, rotation_deg=0.0, aspect_one=False):

@@ -54,6 +54,7 @@ def _load():
                                           P(f), i, P(f), i, f, f, i, i, f, i, P(f)]
     lib.ref_render_ghosts_cpu.restype = i
     lib.ref_coating_register.argtypes = [i, i, i, i, P(f), f, i]
+    lib.ref_image_register.argtypes = [i, i, i, P(f), f]
     lib.ref_bake_layers.argtypes = [P(gl_surface), i, i, i, P(f), P(i), P(f), P(f), P(f), P(f), P(f), P(f), P(f)]
     lib.ref_load_lens_coating.argtypes = [C.c_char_p, i, P(i), P(f), P(f), i]
     assert lib.ref_sizeof_surface() == C.sizeof(gl_surface)
@@ -89,6 +90,14 @@ def register_coating(table_id, model, axis0, r, axis1=None, angle_ref_ior=1.0, d
     data = np.ascontiguousarray(np.concatenate([a0, a1, np.asarray(r, np.float32).ravel()]), np.float32)
     lib.ref_coating_register(int(table_id), int(model), len(a0), len(a1), _fp(data), float(angle_ref_ior),
                              int(bool(discard)))
+
+
+def register_image(image_id, pixels, semi_diameter):
+    """Attach a bitmap to every IMAGE record naming ``image_id`` (as
+    OpticalSystem::aperture_images + Surface.aperture_semi_diameter)."""
+    lib = _load()
+    px = np.ascontiguousarray(pixels, np.float32)
+    lib.ref_image_register(int(image_id), px.shape[1], px.shape[0], _fp(px), float(semi_diameter))
 
 
 def bake_layers(surfs, index, layers):

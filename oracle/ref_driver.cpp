@@ -35,6 +35,9 @@ namespace {
 // setters do (bind_geometry.cpp:412-513).
 struct RefTable { int model, n0, n1, discard; float ref_ior; std::vector<float> data; };
 std::map<int, RefTable> g_ref_tables;
+// bitmap apertures by the id an IMAGE record carries in aperture_blades
+struct RefImage { int w, h; float semi; std::vector<float> px; };
+std::map<int, RefImage> g_ref_images;
 
 void to_ref(const gl_surface& g, Surface& s)
 {
@@ -122,6 +125,19 @@ OpticalSystem* make_lens(const gl_surface* surfs, int n)
         c.out_of_range_discard = t.discard != 0;
         c.angle_ref_ior = t.ref_ior;
     }
+    for (int i = 0; i < n; ++i)
+    {
+        if (surfs[i].aperture_shape != (int)APERTURE_IMAGE) continue;
+        L->surfaces[i].aperture_blades = 0;
+        auto it = g_ref_images.find(surfs[i].aperture_blades);
+        if (it == g_ref_images.end()) continue;
+        ApertureImage& img = L->aperture_images[i];
+        img.width = it->second.w;
+        img.height = it->second.h;
+        img.pixels = it->second.px;
+        img.semi_diameter = it->second.semi;
+        L->surfaces[i].aperture_semi_diameter = it->second.semi;
+    }
     L->sync_coating_pointers();
     return L;
 }
@@ -140,6 +156,12 @@ FlareConfig make_filter_cfg(float min_int, int normalize, float max_boost)
 extern "C" {
 
 int ref_sizeof_surface() { return (int)sizeof(gl_surface); }
+
+int ref_image_register(int id, int w, int h, const float* px, float semi)
+{
+    g_ref_images[id] = RefImage{w, h, semi, std::vector<float>(px, px + (size_t)w * h)};
+    return 0;
+}
 
 int ref_coating_register(int id, int model, int n0, int n1, const float* data, float ref_ior, int discard)
 {
