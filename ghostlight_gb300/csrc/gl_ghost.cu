@@ -240,8 +240,12 @@ __device__ __forceinline__ bool surface_step(V3& o, V3& d, const HotRec& h, cons
         const float hx = q.x * h.inv_aspect, hy = q.y;
         const float h2 = hx * hx + hy * hy;
         if (!(h2 <= h.sa2)) return false;
-        if ((h.bits & HB_POLYGON) && !check_polygon(hx, hy, h2, s)) return false;
-        if ((h.bits & HB_IMAGE) && !image_aperture_ok(q.x, q.y, s)) return false;
+        // one test on the common path: plain circular / elliptical stops
+        if (h.bits & (HB_POLYGON | HB_IMAGE))
+        {
+            if ((h.bits & HB_POLYGON) ? !check_polygon(hx, hy, h2, s) : !image_aperture_ok(q.x, q.y, s))
+                return false;
+        }
         // outward normal (c q_x, c q_y, c q_z - 1), turned to oppose the ray
         // (for a plane, c = 0, it is (0, 0, -1) as it stands)
         nrm = v3(c * q.x, c * q.y, c * q.z - 1.0f);
