@@ -459,22 +459,49 @@ def sprite_starburst_layer(lens, calibration, config, sources_px, width: int, he
     src = np.asarray(sources_px, np.float32).reshape(-1, 5)
     if len(src) == 0:
         return out
-    pupil, T = effective_pupil(lens, config, g, field)
-    if pupil is None:
-        return out      # past the vignette edge: no starburst
-    if not float(pupil.sum()) > 0.0:
-        raise ValueError("render_starburst: degenerate pupil (zero energy)")
     spec = starburst_spectrum(config)
-    gain = float(np.float32(np.float32(g["gain"]) * np.float32(T)))
-    plan = SpritePlan(g["N"], spec)
-    try:
+    plan, baked = _sprite_plan(g["N"], spec)
+    ax, ay = (float(np.float32(field[0])), float(np.float32(field[1]))) if field is not None else (0.0, 0.0)
+    off_axis = abs(ax) > 1e-5 or abs(ay) > 1e-5
+    # the baked sprite depends on the stop, the grid, the box sum and (off
+    # axis, with the cat's-eye) the field: an unchanged key reuses it
+    key = (lens.state_key(), g["N"], g["fill"], g["ds"], int(config.aperture_blades),
+           float(config.aperture_rotation), bool(config.diffraction.use_survivor_mask) and off_axis,
+           (ax, ay, g["ep_x"], g["ep_y"], int(config.diffraction.survivor_grid))
+           if bool(config.diffraction.use_survivor_mask) and off_axis else None)
+    if baked.get("key") != key:
+        pupil, T = effective_pupil(lens, config, g, field)
+        if pupil is None:
+            baked.clear()
+            return out      # past the vignette edge: no starburst
+        if not float(pupil.sum()) > 0.0:
+            raise ValueError("render_starburst: degenerate pupil (zero energy)")
         plan.bake(pupil, g["ds"])
-        plan.splat(src, g["sx_ds"], g["sy_ds"], g["px_mm_x"], g["px_mm_y"], g["rx"], g["ry"], gain,
-                   out["starburst_r"], out["starburst_g"], out["starburst_b"])
-        torch.cuda.synchronize()
-    finally:
-        plan.close()
+        baked.update(key=key, T=T, bakes=baked.get("bakes", 0) + 1)
+    gain = float(np.float32(np.float32(g["gain"]) * np.float32(baked["T"])))
+    plan.splat(src, g["sx_ds"], g["sy_ds"], g["px_mm_x"], g["px_mm_y"], g["rx"], g["ry"], gain,
+               out["starburst_r"], out["starburst_g"], out["starburst_b"])
+    torch.cuda.synchronize()
     return out
+
+
+# resident sprite plans by (device, grid, spectrum), least recently used
+# first; each keeps its last bake and the key it was baked for
+_SPRITE_PLANS = {}
+_SPRITE_PLAN_CAP = 4
+
+
+def _sprite_plan(N, spec):
+    import torch
+    key = (torch.cuda.current_device(), int(N), np.ascontiguousarray(spec, np.float32).tobytes())
+    hit = _SPRITE_PLANS.pop(key, None)
+    if hit is None:
+        while len(_SPRITE_PLANS) >= _SPRITE_PLAN_CAP:
+            old = _SPRITE_PLANS.pop(next(iter(_SPRITE_PLANS)))
+            old[0].close()
+        hit = (SpritePlan(N, spec), {})
+    _SPRITE_PLANS[key] = hit
+    return hit
 
 
 # ---------------------------------------------------------------------------

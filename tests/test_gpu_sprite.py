@@ -195,3 +195,25 @@ def test_off_axis_sprite_uses_the_cats_eye():
     # far past the vignette edge nothing survives: no starburst
     cfg.diffraction.use_survivor_mask = True
     assert effective_pupil(lens, cfg, g, (math.radians(80.0), 0.0))[0] is None
+
+
+def test_resident_sprite_is_reused():
+    """A second render of the same lens, grid and spectrum splats the
+    resident sprite without baking again, with the same image; another field
+    off axis (cat's-eye) bakes anew."""
+    import ghostlight_gb300 as gl
+    from ghostlight_gb300 import starburst as SB
+    lens = _lens()
+    cal = lens.calibration()
+    cfg = _config(8)
+    cfg.diffraction.scale_trim = 5.0
+    cfg.diffraction.use_survivor_mask = False
+    a = gl.render_point_flare(200, 150, lens, cal, cfg)["starburst_g"].cpu().numpy()
+    bakes = [v[1].get("bakes", 0) for v in SB._SPRITE_PLANS.values()]
+    b = gl.render_point_flare(200, 150, lens, cal, cfg)["starburst_g"].cpu().numpy()
+    assert [v[1].get("bakes", 0) for v in SB._SPRITE_PLANS.values()] == bakes
+    np.testing.assert_array_equal(a, b)
+    cfg.diffraction.use_survivor_mask = True
+    cfg.source_x = 0.8
+    gl.render_point_flare(200, 150, lens, cal, cfg)
+    assert sum(v[1].get("bakes", 0) for v in SB._SPRITE_PLANS.values()) > sum(bakes)
