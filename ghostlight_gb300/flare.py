@@ -393,11 +393,42 @@ def render_ghosts(lens: OpticalSystem, sources, width: int, height: int, config:
                                 plain_per_pair=plain_per_pair, stop_crossing_filter=stop_crossing_filter)
     out = {k: torch.zeros((height, width), dtype=torch.float32, device="cuda")
            for k in ("ghost_r", "ghost_g", "ghost_b")}
+    if int(getattr(config, "aov_mode", 0)) == 1 and len(plan.pairs):
+        plan.close()
+        out.update(_render_aov_layers(lens, plan, sources, width, height, config, sensor_half_w, sensor_half_h,
+                                      out, stream))
+        return out
     if len(plan.pairs):
         plan.execute(out["ghost_r"], out["ghost_g"], out["ghost_b"], stream)
     torch.cuda.current_stream().synchronize()
     plan.close()
     return out
+
+
+def _render_aov_layers(lens, plan, sources, width, height, config, sensor_half_w, sensor_half_h, out, stream):
+    """GhostAovMode.PER_PAIR (ghost_render.cu:1526-1563): each of the first
+    aov_max_pairs (all when < 0) active pairs rendered on its own, without
+    the off-sensor cull, into ghost_s{a}_s{b}_{r,g,b}; the combined ghost
+    planes are the sum of those layers."""
+    torch = _torch()
+    n = len(plan.pairs) if int(config.aov_max_pairs) < 0 else min(len(plan.pairs), int(config.aov_max_pairs))
+    layers = {}
+    for i in range(n):
+        a, b = (int(v) for v in plan.pairs[i])
+        planes = [torch.zeros((height, width), dtype=torch.float32, device="cuda") for _ in range(3)]
+        one = GhostRenderPlan(lens, plan.pairs[i:i + 1], plan.boosts[i:i + 1], sources, plan.grids,
+                              plan.pair_grid[i:i + 1], plan.spec, plan.correction, width, height, sensor_half_w,
+                              sensor_half_h, config.flare_gain, plan.apply_correction, False,
+                              cull_dead_pairs=False, blades_override=int(config.aperture_blades),
+                              rotation_deg=float(config.aperture_rotation))
+        one.execute(*planes, stream)
+        torch.cuda.current_stream().synchronize()
+        one.close()
+        for c, pl in zip("rgb", planes):
+            layers["ghost_s%d_s%d_%s" % (a, b, c)] = pl
+            out["ghost_" + c] += pl
+    torch.cuda.current_stream().synchronize()
+    return layers
 
 
 def _eff_half(config, calib: LensCalibration):

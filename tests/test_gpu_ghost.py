@@ -290,3 +290,34 @@ def test_autotuned_launch_shapes_give_the_same_image(pins, meta, ref_images, tmp
     choice = tune_ghost_plan(plan, ref, tuner=t)
     assert tuple(choice) in [tuple(c) for c in __import__("ghostlight_gb300.autotune").autotune.GHOST_CANDIDATES]
     plan.close()
+
+
+def test_aov_per_pair_layers():
+    """GhostAovMode.PER_PAIR: one ghost_s{a}_s{b} triplet per active pair
+    (the first aov_max_pairs of them), each the render of that pair alone,
+    and the combined planes their sum."""
+    import ghostlight_gb300 as gl
+    from ghostlight_gb300 import prescriptions as P
+    from ghostlight_gb300.flare import render_ghosts
+    lens = gl.OpticalSystem.from_records(P.double_gauss_12(seed=1))
+    cal = lens.calibration()
+    cfg = gl.FlareConfig(ray_grid=24, spectral_samples=8)
+    src = np.array([[0.05, 0.02, 1.0, 1.0, 1.0]], np.float32)
+    full = render_ghosts(lens, src, 96, 80, cfg, cal.sensor_half_w, cal.sensor_half_h)
+    cfg.aov_mode = gl.GhostAovMode.PER_PAIR
+    cfg.aov_max_pairs = 5
+    aov = render_ghosts(lens, src, 96, 80, cfg, cal.sensor_half_w, cal.sensor_half_h)
+    keys = sorted(k for k in aov if k.startswith("ghost_s"))
+    assert len(keys) == 15
+    tot = sum(aov[k].cpu().numpy() for k in keys if k.endswith("_g"))
+    np.testing.assert_allclose(aov["ghost_g"].cpu().numpy(), tot, rtol=1e-5, atol=1e-9)
+    assert float(aov["ghost_g"].sum()) <= float(full["ghost_g"].sum()) * (1 + 1e-4)
+    # one layer equals the include-filtered render of that pair alone
+    name = keys[0]
+    a, b = int(name.split("_")[1][1:]), int(name.split("_")[2][1:])
+    cfg1 = gl.FlareConfig(ray_grid=24, spectral_samples=8, cull_dead_pairs=False)
+    cfg1.ghost_filter.mode = gl.GhostFilterMode.INCLUDE
+    cfg1.ghost_filter.pairs = [(a, b)]
+    one = render_ghosts(lens, src, 96, 80, cfg1, cal.sensor_half_w, cal.sensor_half_h)
+    np.testing.assert_allclose(aov["ghost_s%d_s%d_g" % (a, b)].cpu().numpy(), one["ghost_g"].cpu().numpy(),
+                               rtol=1e-5, atol=1e-9)
