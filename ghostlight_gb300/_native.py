@@ -34,6 +34,7 @@ def _declare(lib):
     vp_ = C.c_void_p
     lib.gl_build_pupil2.argtypes = [P(gl_surface), i, i, C.c_float, i, C.c_float, i, vp_, i, vp_, vp_]
     lib.gl_pupil_contains.argtypes = [P(gl_surface), i, i, C.c_float, i, fp, i, P(C.c_uint8)]
+    lib.gl_ghost_plan_stats.argtypes = [vp_, P(C.c_ulonglong), vp_]
     lib.gl_sprite_plan_create.argtypes = [i, P(gl_spectral_sample), i, C.c_float, P(vp_)]
     lib.gl_sprite_plan_bake.argtypes = [vp_, vp_, i, vp_]
     lib.gl_sprite_plan_splat.argtypes = [vp_, fp, i, C.c_float, C.c_float, C.c_float, C.c_float, i, i, C.c_float,

@@ -380,17 +380,31 @@ __device__ __forceinline__ void trace_warp(const RenderArgs& A, const SurfRec* l
             // the 1.25 margin of :148): did this ray land inside the inflated
             // frame?  One hit anywhere keeps the pair, so the warp stops at
             // the first wavelength that produced one.
-            bool hit = false;
+            bool hit = false, surv = false;
             if (alive && fabsf(d.z) >= 1e-12f)
             {
                 const float ts = -o.z / d.z;
                 if (ts >= 0.0f)
                 {
-                    const float spx = ((o.x + d.x * ts) / A.hw2 + 0.5f) * A.fmt_w + A.fmt_x0;
-                    const float spy = ((o.y + d.y * ts) / A.hh2 + 0.5f) * A.fmt_h + A.fmt_y0;
+                    const float sx = o.x + d.x * ts, sy = o.y + d.y * ts;
+                    surv = isfinite(sx) && isfinite(sy);
+                    const float spx = (sx / A.hw2 + 0.5f) * A.fmt_w + A.fmt_x0;
+                    const float spy = (sy / A.hh2 + 0.5f) * A.fmt_h + A.fmt_y0;
                     hit = isfinite(spx) && isfinite(spy) && spx >= 0.0f && spx < (float)A.width &&
                           spy >= 0.0f && spy < (float)A.height;
                 }
+            }
+            if (A.stats != nullptr)
+            {
+                // diagnostic pass (the STATS instantiation, ghost_render.cu:402-415):
+                // count, never stop early
+                const unsigned sv = __ballot_sync(kFull, surv), hv = __ballot_sync(kFull, hit);
+                if ((threadIdx.x & 31) == 0)
+                {
+                    if (sv) atomicAdd(A.stats + 3 * pair + 1, (unsigned long long)__popc(sv));
+                    if (hv) atomicAdd(A.stats + 3 * pair + 2, (unsigned long long)__popc(hv));
+                }
+                continue;
             }
             if (__any_sync(kFull, hit))
             {
@@ -409,6 +423,8 @@ __device__ __forceinline__ void trace_warp(const RenderArgs& A, const SurfRec* l
     }
     if (!PROBE && cx != INT_MIN) flush_taps(A.accum, A.width, A.height, cx, cy, acc);
     if (A.traced && (threadIdx.x & 31) == 0) atomicAdd(A.traced, (unsigned long long)n_lanes * n_lambda);
+    if (PROBE && A.stats && (threadIdx.x & 31) == 0)
+        atomicAdd(A.stats + 3 * pair, (unsigned long long)n_lanes * n_lambda);
 }
 
 template <bool PROBE>
@@ -1208,6 +1224,50 @@ int gl_ghost_plan_traced(const gl_ghost_plan* plan, long long* out)
     unsigned long long v[2] = {0, 0};
     GL_CUDA_TRY(cudaMemcpy(v, plan->p->traced, sizeof(v), cudaMemcpyDeviceToHost));
     *out = (long long)(v[0] + v[1]);
+    return GL_OK;
+}
+
+// The diagnostic stats pass (launch_ghost_render's collect_stats launch,
+// ghost_render.cu:1357-1431): every render item of the plan traced again
+// without weights or splat and without the off-sensor cull, counting per pair
+// the ray-wavelength traces, the rays that left the lens and those landing
+// inside the frame.  out: 3 x n_pairs host counters {traces, survived, on
+// sensor}, pair-major.  Synchronises the stream.
+int gl_ghost_plan_stats(gl_ghost_plan* plan, unsigned long long* out, void* stream)
+{
+    if (!plan || !out) return fail(GL_ERR_INVALID, "ghost_plan_stats: null argument");
+    GhostPlan* p = plan->p;
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t bytes = sizeof(unsigned long long) * 3 * (size_t)std::max(1, p->n_pairs);
+    unsigned long long* d = nullptr;
+    GL_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&d), bytes, st));
+    cudaError_t e = cudaMemsetAsync(d, 0, bytes, st);
+    if (e == cudaSuccess && p->n_items > 0)
+    {
+        RenderArgs A{};
+        A.recs = p->recs; A.ior_at = p->ior_at; A.ior_bf = p->ior_bf; A.spec = p->spec;
+        A.items = p->items; A.pairs = p->pairs; A.sources = p->sources; A.samples = p->samples;
+        A.accum = p->accum;
+        A.n_surf = p->n_surf; A.n_spec = p->n_spec; A.n_items = p->n_items; A.item_base = 0;
+        A.l_chunks = 1;
+        A.width = p->width; A.height = p->height;
+        A.fmt_w = (float)p->prm.fmt_w; A.fmt_h = (float)p->prm.fmt_h;
+        A.fmt_x0 = (float)p->prm.fmt_x0; A.fmt_y0 = (float)p->prm.fmt_y0;
+        A.hw2 = 2.0f * p->prm.sensor_half_w; A.hh2 = 2.0f * p->prm.sensor_half_h;
+        A.gain = p->prm.flare_gain;
+        A.front_R = p->front_R; A.start_z = p->start_z;
+        A.stats = d;
+        const int warps_per_block = kRenderThreads / 32;
+        ghost_render_kernel<true><<<(p->n_items + warps_per_block - 1) / warps_per_block, kRenderThreads, p->smem,
+                                    st>>>(A);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, d, sizeof(unsigned long long) * 3 * p->n_pairs,
+                                              cudaMemcpyDeviceToHost, st);
+    cudaFreeAsync(d, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return fail(GL_ERR_CUDA, std::string("ghost_plan_stats: ") + cudaGetErrorString(e));
+    g_last_launches = 1;
     return GL_OK;
 }
 

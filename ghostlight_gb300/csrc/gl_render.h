@@ -38,6 +38,7 @@ struct RenderArgs {
     float4* accum;            // RGBA, width x height
     int* pair_hits;           // off-sensor cull: per-pair probe hits (null = no cull)
     unsigned long long* traced;   // ray-wavelength traces executed (null = not counted)
+    unsigned long long* stats;    // diagnostic pass: per pair {traces, survived, on sensor} (null = off)
     int n_surf, n_spec, n_items, item_base;
     int l_chunks;             // wavelength ranges per item (tasks = items x l_chunks); <= 1: one
     // Uniform-grid items (items == null): every pair x source traces the same

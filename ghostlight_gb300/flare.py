@@ -275,6 +275,17 @@ class GhostRenderPlan:
         self.n_items = int(items.value)
         self.persistent_ctas = int(grid.value)
 
+    def stats(self, stream=None):
+        """Per-pair counters of the diagnostic pass (gl_ghost_plan_stats):
+        (n_pairs, 3) uint64 {traces, survived, on sensor}."""
+        torch = _torch()
+        st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        n = max(1, len(getattr(self, "pairs", [])) or 1)
+        out = np.zeros((n, 3), np.uint64)
+        _native.check(self._lib.gl_ghost_plan_stats(self._h, out.ctypes.data_as(C.POINTER(C.c_ulonglong)),
+                                                    C.c_void_p(st)), "ghost_plan_stats")
+        return out[:len(self.pairs)] if hasattr(self, "pairs") else out
+
     def execute(self, out_r, out_g, out_b, stream=None):
         torch = _torch()
         for t in (out_r, out_g, out_b):
@@ -386,13 +397,39 @@ def render_ghosts(lens: OpticalSystem, sources, width: int, height: int, config:
                   stop_crossing_filter=None, stream=None):
     """Ghost layer for explicit field-angle sources (the FlareSource form of
     launch_ghost_render).  Returns {"ghost_r", "ghost_g", "ghost_b"} tensors."""
+    import time
     torch = _torch()
     if width <= 0 or height <= 0:
         raise ValueError("render_ghosts: width and height must be positive")
+    t0 = time.perf_counter()
     plan = prepare_ghost_render(lens, sources, width, height, config, sensor_half_w, sensor_half_h,
                                 plain_per_pair=plain_per_pair, stop_crossing_filter=stop_crossing_filter)
+    t1 = time.perf_counter()
     out = {k: torch.zeros((height, width), dtype=torch.float32, device="cuda")
            for k in ("ghost_r", "ghost_g", "ghost_b")}
+    if bool(getattr(config, "collect_stats", False)) and int(getattr(config, "aov_mode", 0)) != 1:
+        torch.cuda.current_stream().synchronize()
+        t2 = time.perf_counter()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        if len(plan.pairs):
+            plan.execute(out["ghost_r"], out["ghost_g"], out["ghost_b"], stream)
+        e1.record()
+        e1.synchronize()
+        cnt = plan.stats() if len(plan.pairs) else np.zeros((0, 3), np.uint64)
+        t3 = time.perf_counter()
+        out["stats"] = {
+            "ms_grid_build": 1e3 * (t1 - t0), "ms_upload": 1e3 * (t2 - t1), "ms_kernel": float(e0.elapsed_time(e1)),
+            "ms_download": 0.0, "ms_total": 1e3 * (t3 - t0),
+            "n_pairs": int(len(plan.pairs)), "n_sources": int(np.asarray(sources).reshape(-1, 5).shape[0]),
+            "n_grid": int(max((len(g) for g in plan.grids), default=0)), "n_spec": int(len(plan.spec)),
+            "traces_total": int(cnt[:, 0].sum()), "traces_survived": int(cnt[:, 1].sum()),
+            "traces_on_sensor": int(cnt[:, 2].sum()),
+            "pair_surf_a": [int(a) for a, _ in plan.pairs], "pair_surf_b": [int(b) for _, b in plan.pairs],
+            "pair_traces": [int(v) for v in cnt[:, 0]], "pair_survived": [int(v) for v in cnt[:, 1]],
+            "pair_on_sensor": [int(v) for v in cnt[:, 2]], "ps_hits": [], "ps_rect": [], "ps_budget": []}
+        plan.close()
+        return out
     if int(getattr(config, "aov_mode", 0)) == 1 and len(plan.pairs):
         plan.close()
         out.update(_render_aov_layers(lens, plan, sources, width, height, config, sensor_half_w, sensor_half_h,

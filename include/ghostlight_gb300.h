@@ -341,6 +341,11 @@ int gl_ghost_plan_traced(const gl_ghost_plan* plan, long long* out);
 int gl_morton_order(const gl_pupil_sample* in, int n, gl_pupil_sample* out);
 /* The same count split into the render launch and the off-sensor probe
  * launch.  Synchronous.  (No counterpart in the reference.) */
+/* collect_stats (render_config.h:33-35, ghost_render.cu:1357-1431): the
+ * plan's items traced again without weights, splat or cull; out[3 i + k] =
+ * pair i's {traces, traces that left the lens, traces landing in the frame}.
+ * Synchronises the stream. */
+int gl_ghost_plan_stats(gl_ghost_plan* plan, unsigned long long* out, void* stream);
 int gl_ghost_plan_traced_split(const gl_ghost_plan* plan, long long* render, long long* probe);
 /* Optional cudaEvent_t handles (NULL = none) that every later execute records
  * on its stream before the probe launch, before the render launch and after

@@ -321,3 +321,38 @@ def test_aov_per_pair_layers():
     one = render_ghosts(lens, src, 96, 80, cfg1, cal.sensor_half_w, cal.sensor_half_h)
     np.testing.assert_allclose(aov["ghost_s%d_s%d_g" % (a, b)].cpu().numpy(), one["ghost_g"].cpu().numpy(),
                                rtol=1e-5, atol=1e-9)
+
+
+def test_collect_stats_counts_match_oracle():
+    """collect_stats: the diagnostic pass's per-pair counters against the
+    oracle's float trace of the same rays (traces exact; survived and
+    on-sensor within the rays that graze an edge within rounding)."""
+    import ghostlight_gb300 as gl
+    from ghostlight_gb300 import prescriptions as P
+    from ghostlight_gb300.flare import render_ghosts, pupil_grid, spectral_table
+    lens = gl.OpticalSystem.from_records(P.double_gauss_12(seed=1))
+    cal = lens.calibration()
+    cfg = gl.FlareConfig(ray_grid=24, spectral_samples=8, collect_stats=True)
+    src = np.array([[0.0, 0.0, 1.0, 1.0, 1.0]], np.float32)      # on axis: launches straight down z
+    out = render_ghosts(lens, src, 96, 80, cfg, cal.sensor_half_w, cal.sensor_half_h)
+    st = out["stats"]
+    assert st["n_pairs"] == len(st["pair_traces"]) > 0 and st["n_spec"] == 8
+    grid = pupil_grid(lens, 24)
+    assert st["pair_traces"][0] == len(grid) * 8
+    assert st["traces_total"] == sum(st["pair_traces"]) >= st["traces_survived"] >= st["traces_on_sensor"] > 0
+    spec, _ = spectral_table(8)
+    surfs = lens.records()
+    for i in range(min(4, st["n_pairs"])):
+        a, b = st["pair_surf_a"][i], st["pair_surf_b"][i]
+        n = len(grid)
+        rays = np.zeros((n * 8, 7), np.float32)
+        d = np.array([0.0, 0.0, 1.0], np.float32)
+        for k, lam in enumerate(spec[:, 0]):
+            rays[k * n:(k + 1) * n, 0] = grid[:, 0] * surfs[0].semi_aperture
+            rays[k * n:(k + 1) * n, 1] = grid[:, 1] * surfs[0].semi_aperture
+            rays[k * n:(k + 1) * n, 2] = surfs[0].z - 20.0
+            rays[k * n:(k + 1) * n, 3:6] = d
+            rays[k * n:(k + 1) * n, 6] = lam
+        r = O.trace(surfs, a, b, rays, fp64=False)
+        ok = (r[:, 4] == 0) & np.isfinite(r[:, 0]) & np.isfinite(r[:, 1])
+        assert abs(int(ok.sum()) - st["pair_survived"][i]) <= max(2, 0.01 * ok.sum()), (a, b)
