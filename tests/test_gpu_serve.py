@@ -137,3 +137,41 @@ def test_alone_and_in_the_mix_agree(pool):
         a, m = alone[r.rid].numpy(), mix[r.rid].numpy()
         assert np.isfinite(m).all()
         assert rel_l2(m, a) < 1e-5, r
+
+
+def test_served_lens_with_tables_and_bitmaps():
+    """A resident lens with table coatings and bitmap apertures serves the
+    same image as the plan render of the same pairs (the tables and bitmaps
+    resolve to device-resident store entries in both)."""
+    import warnings
+    import ghostlight_gb300 as gl
+    from ghostlight_gb300 import load_lens
+    from ghostlight_gb300.flare import GhostRenderPlan, pupil_grid
+    from ghostlight_gb300.serve import FlareRequest, ResidentLens, _spectral
+    from test_coatings import LENS as COATED
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        lens = load_lens(COATED)
+    lens.set_aperture_image(0, np.where(np.hypot(*np.mgrid[-1:1:64j, -1:1:64j]) < 0.9, 1.0, 0.0),
+                            lens.surfaces[0].semi_aperture * 1.05)
+    cal = lens.calibration()
+    cfg = gl.FlareConfig(min_ghost_intensity=1e-6)
+    rl = ResidentLens(lens, cal.sensor_half_w, cal.sensor_half_h, cfg)
+    try:
+        req = FlareRequest(lens_id=0, width=256, height=256, n_spec=16, ray_grid=48, field_deg=6.0, rid=0)
+        got = _run_server({0: rl}, [req])[0].numpy()
+        spec, corr = _spectral(16, cfg)
+        grid = pupil_grid(lens, 48, 0, 0, 0, 0.0)
+        src = np.array([[math.radians(6.0), 0.0, 1.0, 1.0, 1.0]], np.float32)
+        plan = GhostRenderPlan(lens, rl.pairs, rl.boosts, src, [grid], np.zeros(len(rl.pairs), np.int32), spec,
+                               corr, 256, 256, rl.sensor_half_w, rl.sensor_half_h, req.gain,
+                               apply_correction=True, cull_dead_pairs=True)
+        outs = [torch.zeros((256, 256), device="cuda") for _ in range(3)]
+        plan.execute(*outs)
+        torch.cuda.synchronize()
+        want = torch.stack(outs).cpu().numpy()
+        plan.close()
+        assert np.abs(want).sum() > 0
+        assert rel_l2(got, want) < 1e-5
+    finally:
+        rl.close()
