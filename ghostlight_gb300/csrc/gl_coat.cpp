@@ -10,7 +10,10 @@
 // table twice gives the same id, and an entry is copied to a device once, on
 // first use there, and stays resident (tables are a few KB).  So a lens with
 // table coatings packs into the trace records without a per-render upload,
-// and the records of a captured graph keep pointing at live data.
+// and the records of a captured graph keep pointing at live data.  The same
+// store holds the bitmaps of IMAGE apertures (model kStoreImage: width x
+// height luminance, the boundary semi-diameter in the angle-medium slot),
+// named by the surface's aperture_blades.
 //
 // gl_coating_bake_layers restates OpticalSystem::bake_coating_layers
 // (optical_system.cpp:1483-1575) over the thin-film transfer matrix of
