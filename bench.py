@@ -274,12 +274,9 @@ def run_gpu(args, rank, world):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "cfg2: seeded 24-surface wide-angle (2 even aspheres), %d ghost pairs "
-                               "after the 1e-6 culler, adaptive pupil grids 16^2-256^2, %d wavelengths, "
-                               "source %.0f deg, %dx%d float32 RGB, one graph-replayed persistent launch"
-                               % (len(plan.pairs), N_SPEC, SOURCE_DEG, W, H),
-                   "pairs": int(len(plan.pairs)), "grid_sides": plan.grid_sides,
-                   "l2": "flushed (512 MB write) between timed steps", "parallelism": "replicas"},
+        "config": frame_config(len(plan.pairs)),
+        "frame": {"kept_pairs": int((plan.pair_hits() > 0).sum()) if hasattr(plan, "pair_hits") else None,
+                  "render_traces": traced_render, "probe_traces": traced_probe, "grid_sides": plan.grid_sides},
         "rays_per_s": rays_per_s,
         "kernel_ms": {"render": float(np.mean(kernel_ms["render"])), "probe": float(np.mean(kernel_ms["probe"])),
                       "how": "CUDA events captured into the replayed graph around each launch, every timed step"},
@@ -796,69 +793,113 @@ def cpu_baseline(plan, lens, cal, budget_s=8.0):
             "rays_per_s": rps}
 
 
-def reference_workload(lens, cal):
-    """The same frame for the CPU arm: the reference-exact filter (oracle),
-    the same adaptive grid rule on its probe footprints, the same spectral
-    table."""
-    from ghostlight_gb300.flare import adaptive_grid_size, spectral_table
-    from oracle import oracle as O
-    hw, hh = cal["sensor_half_w"], cal["sensor_half_h"]
-    pairs, boosts, fps = O.filter_pairs(lens.records(), hw, hh, MIN_INTENSITY, footprint=True)
-    sizes = [adaptive_grid_size(fp, hw, hh, W, H, 16, 256) for fp in fps]
-    uniq = sorted(set(sizes))
-    grids = [O.aperture_samples(lens.records(), g, 0) for g in uniq]
-    pair_grid = np.asarray([uniq.index(x) for x in sizes], np.int32)
-    spec, _ = spectral_table(N_SPEC)
-    rays = sum(len(grids[g]) for g in pair_grid) * N_SPEC
-    return pairs, boosts, grids, pair_grid, spec, rays
+def frame_config(n_pairs):
+    """The workload both arms report: identical dicts, so the two lines
+    describe the same frame."""
+    return {"workload": "cfg2: seeded 24-surface wide-angle (2 even aspheres), %d ghost pairs after the "
+                        "1e-6 culler, off-sensor cull on, adaptive pupil grids 16^2-256^2 (one pupil sample "
+                        "per two output pixels across each ghost), %d wavelengths, source %.0f deg, "
+                        "%dx%d float32 RGB with colour correction" % (n_pairs, N_SPEC, SOURCE_DEG, W, H),
+            "pairs": int(n_pairs),
+            "l2": "GPU arm: flushed (512 MB write) between timed steps; inputs resident",
+            "parallelism": "replicas"}
+
+
+def adaptive_side(fp, hw, hh, gmin=16, gmax=256):
+    """The frame's per-ghost grid rule (one pupil sample per two output
+    pixels across the ghost's landing extent, a multiple of 16 in
+    [16, 256]); the product computes the same rule in
+    ghostlight_gb300.flare.adaptive_grid_size."""
+    fx = float(fp[0]) / (2.0 * hw) * W
+    fy = float(fp[1]) / (2.0 * hh) * H
+    side = 0.5 * math.sqrt(max(fx, 1.0) * max(fy, 1.0))
+    return int(min(gmax, max(gmin, int(math.ceil(side / 16.0)) * 16)))
+
+
+def _reference_lens(name):
+    pins = np.load(GOLDEN / "ref_pins.npz")
+    meta = json.loads((GOLDEN / "ref_meta.json").read_text())
+    return pins[name + "/lens"], meta[name]["calibration"]
 
 
 def run_reference(args):
-    """CPU reference arm: the reference's own trace code when it was built
-    here (oracle/_ref), else the oracle port; every step traces a bounded
-    sample of the frame's pairs and is scaled to the full frame."""
-    from oracle import oracle as O
-    lens, cal = _workload()
+    """CPU reference arm: the reference's own code (ghostlight/src trace.cpp,
+    ghost.cpp, spectral.cpp, aperture_sampler.h, compiled from its sources by
+    oracle/build.py) renders the whole frame on every host core each step:
+    its filter_ghost_pairs, the footprint probe of estimate_ghost_spread for
+    the per-ghost grid sides, its spectral table and correction, then the
+    three-pass off-sensor cull and the main path of ghost_kernel over every
+    kept pair at 2048^2 (oracle/ref_driver.cpp:ref_render_frame_cpu).
+    Nothing from ghostlight_gb300 is imported."""
+    from oracle import ref as R
+    if not R.available():
+        return {"impl": "reference", "unavailable": "the reference sources were not staged in baseline/_ref "
+                                                    "(oracle/stage_ref.py), so its CPU code could not be built"}
+    raw, cal = _reference_lens("cfg2_wide_angle_24")
     hw, hh = cal["sensor_half_w"], cal["sensor_half_h"]
-    pairs, boosts, grids, pair_grid, spec, total_rays = reference_workload(lens, cal)
-    use_ref = False
-    try:
-        from oracle import ref as R
-        use_ref = R.available()
-    except Exception:
-        use_ref = False
+    pairs, boosts = R.filter_pairs(raw, hw, hh, MIN_INTENSITY)
+    sides = np.array([adaptive_side(fp, hw, hh) for fp in R.ghost_footprints(raw, pairs)], np.int32)
+    spec, corr = R.spectral_table(N_SPEC)
+    src = _sources()[0]
     n_threads = os.cpu_count() or 1
-    sel = np.arange(0, len(pairs), max(1, len(pairs) // 12))
-    rays = sum(len(grids[pair_grid[i]]) for i in sel) * N_SPEC
-    ts = []
+    ts, st = [], None
     for it in range(args.warmup + args.steps):
         t0 = time.perf_counter()
-        if use_ref:
-            for i in sel:   # the harness takes one grid per call
-                R.render_ghosts_cpu(lens.records(), pairs[i:i + 1], boosts[i:i + 1], _sources(),
-                                    grids[pair_grid[i]], spec, hw, hh, 512, 512, 1000.0, n_threads=n_threads)
-        else:
-            O.render(lens.records(), pairs[sel], boosts[sel], _sources(), grids, spec, hw, hh, 512, 512,
-                     1000.0, pair_grid=pair_grid[sel], fp64=False, n_threads=n_threads)
+        img, st = R.render_frame_cpu(raw, pairs, boosts, sides, src, spec, corr, hw, hh, W, H, 1000.0,
+                                     cull=True, n_threads=n_threads)
         if it >= args.warmup:
             ts.append(time.perf_counter() - t0)
     step = sum(ts) / len(ts)
-    rps = rays / step
-    fps = rps / total_rays
-    kind = "reference" if use_ref else "port"
+    fps = 1.0 / step
+    cfg1 = reference_cfg1(R, n_threads)
     return {"metric": METRIC, "value": fps, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "impl": "reference",
-            "config": {"workload": "cfg2 ghost layer (24-surface wide-angle, %d pairs, adaptive grids, "
-                                   "%d wavelengths, 2048^2); each step traces %d of the pairs on the CPU "
-                                   "and is scaled to the full frame (%d ray-wavelength traces)"
-                                   % (len(pairs), N_SPEC, len(sel), total_rays)},
-            "rays_per_s": rps,
-            "cpu_baseline": {"value": fps, "unit": UNIT, "cores": n_threads, "kind": kind,
-                             "sample": "%d of %d pairs per step (%d ray-wavelength traces)"
-                                       % (len(sel), len(pairs), rays)},
-            "e2e": {"value": fps, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "impl": "reference", "config": frame_config(len(pairs)),
+            "rays_per_s": (st["render_traces"] + st["probe_traces"]) / step,
+            "frame": {"kept_pairs": st["kept_pairs"], "render_traces": st["render_traces"],
+                      "probe_traces": st["probe_traces"], "grid_sides": np.bincount(sides).nonzero()[0].tolist()},
+            "cpu_baseline": {"value": fps, "unit": UNIT, "cores": st["threads"], "kind": "reference",
+                             "sample": "the whole frame every step (probe cull + %d kept pairs, %d "
+                                       "ray-wavelength traces) with the reference's trace_ghost_ray"
+                                       % (st["kept_pairs"], st["render_traces"] + st["probe_traces"])},
+            "e2e": {"value": fps, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "cfg1": cfg1}
+
+
+CFG1_W = CFG1_H = 512
+
+
+def reference_cfg1(R, n_threads, reps=5):
+    """Configuration 1 on the host with the reference's code: the seeded
+    12-surface double Gauss, the 2-reflection pairs that do not cross the
+    stop, a 32^2 grid, 8 wavelengths, a 10 deg source, 512^2 (frames/s)."""
+    raw, cal = _reference_lens("cfg1_double_gauss_12")
+    pairs, boosts = cfg1_pairs(R, raw, cal)
+    spec, corr = R.spectral_table(8)
+    src = np.array([math.radians(10.0), 0.0, 1.0, 1.0, 1.0], np.float32)
+    sides = np.full(len(pairs), 32, np.int32)
+    ts = []
+    for _ in range(reps + 1):
+        t0 = time.perf_counter()
+        _, st = R.render_frame_cpu(raw, pairs, boosts, sides, src, spec, corr, cal["sensor_half_w"],
+                                   cal["sensor_half_h"], CFG1_W, CFG1_H, 1000.0, cull=True, n_threads=n_threads)
+        ts.append(time.perf_counter() - t0)
+    dt = float(np.median(ts[1:]))
+    return {"value": 1.0 / dt, "unit": UNIT, "ms_per_frame": 1e3 * dt, "cores": st["threads"],
+            "pairs": int(len(pairs)), "traces": st["render_traces"] + st["probe_traces"],
+            "workload": "cfg1: seeded 12-surface double Gauss, %d non-stop-crossing pairs, 32^2 grid, "
+                        "8 wavelengths, 10 deg, 512^2" % len(pairs)}
+
+
+def cfg1_pairs(R, raw, cal):
+    """The reference filter at 1e-7, then the 2-reflection pairs whose
+    bounces lie on one side of the stop (the configuration's "pairs that do
+    not cross the stop"), in the filter's order."""
+    pairs, boosts = R.filter_pairs(raw, cal["sensor_half_w"], cal["sensor_half_h"], 1e-7)
+    stop = [i for i in range(len(raw)) if int(raw[i]["is_stop"])][0]
+    keep = np.array([(a < stop) == (b < stop) for a, b in pairs], bool)
+    return pairs[keep], boosts[keep]
 
 
 def main():

@@ -1376,11 +1376,15 @@ int gl_trace_rays(const gl_surface* surfaces, int n, int bounce_a, int bounce_b,
 // sized for the largest lens the path accepts (64 surfaces).  The caller
 // still passes the ray buffer and the result buffer.
 //
-// The array's device address is looked up once per device, with that device
-// current, on the first call made on it; make that first call before any
-// stream capture.  All calls share the array and it keeps whatever the last
-// call wrote: each call overwrites the records it uses before launching, and
-// calls that overlap on the GPU (other threads or streams) race on it.
+// Every call looks up the array's device address with cudaGetSymbolAddress
+// on the current device (the lookup allocates nothing), so the address is
+// never stale, e.g. after a cudaDeviceReset.  A call ends with a
+// cudaStreamSynchronize (the lens records are staged on its stack frame), so
+// it must not be made while `stream` is being captured: it returns
+// GL_ERR_INVALID there instead of breaking the caller's capture.  All calls
+// share the array and it keeps whatever the last call wrote: each call
+// overwrites the records it uses before launching, and calls that overlap on
+// the GPU (other threads or streams) race on it.
 // ===========================================================================
 namespace gl {
 
@@ -1393,22 +1397,13 @@ struct NoAllocTables {
 
 static __device__ __align__(256) unsigned char g_trace_tables[sizeof(NoAllocTables)];
 
-static std::mutex g_trace_tables_mutex;
-static void* g_trace_tables_addr[64] = {};
-
-static int trace_tables_address(int device, void** out)
+static int trace_tables_address(void** out)
 {
-    if (device < 0 || device >= 64) return fail(GL_ERR_INVALID, "trace_rays_noalloc: device ordinal out of range");
-    std::lock_guard<std::mutex> lock(g_trace_tables_mutex);
-    if (g_trace_tables_addr[device] == nullptr)
-    {
-        void* ptr = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&ptr, g_trace_tables);
-        if (e != cudaSuccess || ptr == nullptr)
-            return fail(GL_ERR_CUDA, std::string("trace_rays_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-        g_trace_tables_addr[device] = ptr;
-    }
-    *out = g_trace_tables_addr[device];
+    void* ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, g_trace_tables);
+    if (e != cudaSuccess || ptr == nullptr)
+        return fail(GL_ERR_CUDA, std::string("trace_rays_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    *out = ptr;
     return GL_OK;
 }
 
@@ -1424,10 +1419,15 @@ extern "C" int gl_trace_rays_noalloc(const gl_surface* surfaces, int n, int boun
         return fail(GL_ERR_INVALID, "bounce indices must satisfy 0 <= bounce_a < bounce_b < num_surfaces");
     if (n_rays < 0 || (n_rays > 0 && (!d_rays || !d_out))) return fail(GL_ERR_INVALID, "trace_rays_noalloc: bad ray buffers");
     if (n_rays == 0) return GL_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    GL_CUDA_TRY(cudaStreamIsCapturing(st, &cap));
+    if (cap != cudaStreamCaptureStatusNone)
+        return fail(GL_ERR_INVALID, "trace_rays_noalloc: the call synchronises its stream and cannot be captured");
     int device = 0;
     GL_CUDA_TRY(cudaGetDevice(&device));
     void* base = nullptr;
-    int rc = trace_tables_address(device, &base);
+    int rc = trace_tables_address(&base);
     if (rc) return rc;
     NoAllocTables host;   // staged on the stack: no heap, no device allocation
     rc = pack_lens(surfaces, n, host.recs, device, false);
@@ -1438,7 +1438,6 @@ extern "C" int gl_trace_rays_noalloc(const gl_surface* surfaces, int n, int boun
         host.disp[i].nd = surfaces[i].ior; host.disp[i].vd = surfaces[i].abbe_v; host.disp[i].pad = 0.0f;
         for (int k = 0; k < 3; ++k) { host.disp[i].B[k] = surfaces[i].sellmeier_B[k]; host.disp[i].C[k] = surfaces[i].sellmeier_C[k]; }
     }
-    cudaStream_t st = (cudaStream_t)stream;
     NoAllocTables* dev_tables = static_cast<NoAllocTables*>(base);
     GL_CUDA_TRY(cudaMemcpyAsync(dev_tables->recs, host.recs, sizeof(SurfRec) * n, cudaMemcpyHostToDevice, st));
     GL_CUDA_TRY(cudaMemcpyAsync(dev_tables->disp, host.disp, sizeof(DispRec) * n, cudaMemcpyHostToDevice, st));

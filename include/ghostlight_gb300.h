@@ -241,7 +241,8 @@ int gl_filter_ghost_pairs(const gl_surface* surfaces, int n,
 /* trace_ghost_ray / trace_primary_ray, ghostlight/src/trace.cpp:171,243,
  * batched.  d_rays: n_rays x 7 floats (ox,oy,oz, dx,dy,dz, lambda_nm);
  * d_out: n_rays x 5 floats (x,y,z, weight, status).  bounce_b < 0 traces a
- * primary ray.  Asynchronous on `stream`. */
+ * primary ray.  Synchronous on `stream`: the call waits for its copies and
+ * the launch before it returns. */
 int gl_trace_rays(const gl_surface* surfaces, int n,
                   int bounce_a, int bounce_b,
                   const float* d_rays, int n_rays, float* d_out, void* stream);
@@ -252,10 +253,11 @@ int gl_trace_rays(const gl_surface* surfaces, int n,
  * No counterpart in the reference.  Same arguments and results as
  * gl_trace_rays; the packed lens tables go to a fixed array inside the library
  * (at most 64 surfaces; larger lenses are rejected with GL_ERR_INVALID), so the
- * call allocates no device memory.  The array's address is looked up on the
- * first call on each device (make that call before any stream capture).  All
- * calls share the array; calls that overlap on the GPU race on it.
- * Synchronous on `stream`. */
+ * call allocates no device memory.  The array's device address is looked up
+ * (cudaGetSymbolAddress, no allocation) on every call.  All calls share the
+ * array; calls that overlap on the GPU race on it.  Synchronous on `stream`,
+ * so it must not be called while `stream` is being captured into a CUDA
+ * graph: it returns GL_ERR_INVALID then. */
 int gl_trace_rays_noalloc(const gl_surface* surfaces, int n,
                           int bounce_a, int bounce_b,
                           const float* d_rays, int n_rays, float* d_out, void* stream);
@@ -358,9 +360,10 @@ int gl_ghost_plan_set_timing(gl_ghost_plan* plan, void* ev_probe, void* ev_rende
 int gl_ghost_plan_pair_hits(const gl_ghost_plan* plan, int32_t* out, int n);
 int gl_ghost_plan_destroy(gl_ghost_plan* plan);
 
-/* ---- tensor-core building blocks (tcgen05) -------------------------------- */
+/* ---- TEST-ONLY: tensor-core building block (tcgen05) ---------------------- */
 
-/* C[M x N] (float32, row-major) = A[M x K] * B[N x K]^T with BF16 operands
+/* Test hook, not part of the drop-in surface: no reference caller binds it.
+ * C[M x N] (float32, row-major) = A[M x K] * B[N x K]^T with BF16 operands
  * (row-major, device) and FP32 accumulation in tensor memory: the TMA +
  * tcgen05 pipeline the matrix-DFT starburst is built on, exposed so it can
  * be checked against a library GEMM.  M, N multiples of 128, K of 64.

@@ -21,11 +21,20 @@
 
 #include "ghostlight_gb300.h"
 
+#include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <map>
 #include <vector>
 #include <omp.h>
+
+#ifdef REF_GPU
+#include "PointFlareRenderer.h"
+#include "SourceFlareRenderer.h"
+#include "render_config.h"
+#include <cuda_runtime.h>
+#endif
 
 namespace {
 
@@ -493,3 +502,320 @@ int ref_render_ghosts_cpu(const gl_surface* surfs, int n,
 }
 
 } // extern "C"
+
+// ---------------------------------------------------------------------------
+// One full frame of the ghost layer on the host, for the CPU reference arm.
+// The reference has no CPU flare renderer, so this harness restates the host
+// side of launch_ghost_render around the reference's own trace:
+//  * the off-sensor cull of probe_cull_and_concentrate (ghost_render.cu:
+//    976-1080, concentration off): pass 0 probes every pair with a 40^2
+//    wang-jittered pupil grid (jitter seed 0x9E3779B9 * (pass + 1)) at every
+//    wavelength against the sensor inflated by 1.25; passes 1-2 re-probe the
+//    pairs still without an on-sensor landing; a pair none of them lands is
+//    not rendered;
+//  * the main path of ghost_kernel (ghost_render.cu:280-463) for every kept
+//    pair over its own regular pupil grid (build_aperture_samples, no jitter)
+//    with ray weight 1 / n_grid of that grid, splatted bilinearly;
+//  * the colour correction of spectral_correct_kernel (:610-622).
+// Threads: OpenMP over (pair, pupil sample); one float image per thread,
+// summed at the end.  counts: {probe traces, render traces, kept pairs}.
+// ---------------------------------------------------------------------------
+namespace {
+
+inline void splat_point(float* img, size_t npx, int W, int H, float hw, float hh,
+                        const TraceResult& res, float base, const float* src, const float* sp)
+{
+    float px = (res.position.x / (2.0f * hw) + 0.5f) * (float)W;
+    float py = (res.position.y / (2.0f * hh) + 0.5f) * (float)H;
+    if (!std::isfinite(px) || !std::isfinite(py)) return;
+    px = std::fmax(-2.0e9f, std::fmin(2.0e9f, px));
+    py = std::fmax(-2.0e9f, std::fmin(2.0e9f, py));
+    const int x0 = (int)std::floor(px - 0.5f), y0 = (int)std::floor(py - 0.5f);
+    const float fx = (px - 0.5f) - (float)x0, fy = (py - 0.5f) - (float)y0;
+    const float wt[4] = {(1.0f - fx) * (1.0f - fy), fx * (1.0f - fy), (1.0f - fx) * fy, fx * fy};
+    const int ox[4] = {0, 1, 0, 1}, oy[4] = {0, 0, 1, 1};
+    const float P = src[2] * sp[1] + src[3] * sp[2] + src[4] * sp[3];
+    const float power = P * base;
+    const float c[3] = {power * sp[1], power * sp[2], power * sp[3]};
+    for (int k = 0; k < 4; ++k)
+    {
+        const int xi = x0 + ox[k], yi = y0 + oy[k];
+        if (xi < 0 || xi >= W || yi < 0 || yi >= H) continue;
+        const size_t pix = (size_t)yi * W + xi;
+        for (int ch = 0; ch < 3; ++ch)
+            if (std::fabs(c[ch]) > 1e-14f) img[ch * npx + pix] += c[ch] * wt[k];
+    }
+}
+
+}  // namespace
+
+extern "C" int ref_render_frame_cpu(const gl_surface* surfs, int n,
+                                    const int* pairs_ab, const float* boosts, const int* pair_side, int n_pairs,
+                                    const float* src5, const float* spec4, int n_spec, const float* corr9,
+                                    float hw, float hh, int W, int H, float gain, int cull, int n_threads,
+                                    float* out_rgb, long long* counts)
+{
+    OpticalSystem* L = make_lens(surfs, n);
+    const float front_R = L->surfaces[0].semi_aperture;
+    const float start_z = L->surfaces[0].z - SPAWN_OFFSET;
+    const size_t npx = (size_t)W * H;
+    if (n_threads > 0) omp_set_num_threads(n_threads);
+    const float bx = tanf(src5[0]), by = tanf(src5[1]);
+    const Vec3f beam = Vec3f(bx, by, 1.0f).normalized();
+    float sdx, sdy; spawn_shift(bx, by, sdx, sdy);
+
+    // pupil grids, one per distinct side
+    std::map<int, std::vector<ApertureSample>> grids;
+    for (int p = 0; p < n_pairs; ++p)
+        if (!grids.count(pair_side[p]))
+        {
+            ApertureSamplerParams sp; sp.ray_grid = pair_side[p]; sp.pupil_jitter = 0; sp.jitter_seed = 0;
+            grids[pair_side[p]] = build_aperture_samples(*L, sp);
+        }
+
+    // ---- off-sensor cull ----
+    std::vector<char> keep(n_pairs, 1);
+    long long probe_traces = 0;
+    if (cull && n_pairs > 1 && n_spec != 3)
+    {
+        std::vector<char> cand(n_pairs, 1);
+        const float mhw = hw * 1.25f, mhh = hh * 1.25f;
+        for (int pass = 0; pass < 3; ++pass)
+        {
+            ApertureSamplerParams pp; pp.ray_grid = 40; pp.pupil_jitter = 1;
+            pp.jitter_seed = (int)(0x9E3779B9u * (unsigned)(pass + 1));
+            const std::vector<ApertureSample> probe = build_aperture_samples(*L, pp);
+            const int np = (int)probe.size();
+            if (np <= 0) { if (pass == 0) break; else continue; }
+            std::vector<int> hit(n_pairs, 0);
+            long long traces = 0;
+            #pragma omp parallel for schedule(dynamic, 1) reduction(+:traces)
+            for (int p = 0; p < n_pairs; ++p)
+            {
+                if (!cand[p]) continue;
+                const int a = pairs_ab[2 * p], b = pairs_ab[2 * p + 1];
+                int h = 0;
+                for (int g = 0; g < np; ++g)
+                    for (int li = 0; li < n_spec; ++li)
+                    {
+                        Ray r;
+                        r.origin = Vec3f(probe[g].u * front_R + sdx, probe[g].v * front_R + sdy, start_z);
+                        r.dir = beam; r.lambda = spec4[4 * li];
+                        ++traces;
+                        TraceResult res = trace_ghost_ray(r, *L, a, b);
+                        if (res.status != TraceStatus::OK) continue;
+                        if (!std::isfinite(res.position.x) || !std::isfinite(res.position.y)) continue;
+                        const float spx = (res.position.x / (2.0f * mhw) + 0.5f) * (float)W;
+                        const float spy = (res.position.y / (2.0f * mhh) + 0.5f) * (float)H;
+                        if (std::isfinite(spx) && std::isfinite(spy) && spx >= 0.0f && spx < (float)W &&
+                            spy >= 0.0f && spy < (float)H) ++h;
+                    }
+                hit[p] = h;
+            }
+            probe_traces += traces;
+            int n_cand = 0;
+            for (int p = 0; p < n_pairs; ++p)
+                if (cand[p] && hit[p] > 0) cand[p] = 0;
+                else if (cand[p]) ++n_cand;
+            if (n_cand == 0) break;
+        }
+        for (int p = 0; p < n_pairs; ++p) keep[p] = cand[p] ? 0 : 1;
+    }
+
+    // ---- render: (pair, sample) work list over the kept pairs ----
+    std::vector<long long> first(n_pairs + 1, 0);
+    for (int p = 0; p < n_pairs; ++p)
+        first[p + 1] = first[p] + (keep[p] ? (long long)grids[pair_side[p]].size() : 0);
+    const long long n_work = first[n_pairs];
+    std::vector<const std::vector<ApertureSample>*> gptr(n_pairs);
+    for (int p = 0; p < n_pairs; ++p) gptr[p] = &grids[pair_side[p]];
+    int nt = 1;
+    #pragma omp parallel
+    {
+        #pragma omp single
+        nt = omp_get_num_threads();
+    }
+    std::vector<std::vector<float>> acc(nt);
+    long long render_traces = 0;
+    #pragma omp parallel reduction(+:render_traces)
+    {
+        const int tid = omp_get_thread_num();
+        acc[tid].assign(3 * npx, 0.0f);
+        float* img = acc[tid].data();
+        #pragma omp for schedule(dynamic, 512)
+        for (long long wi = 0; wi < n_work; ++wi)
+        {
+            const int p = (int)(std::upper_bound(first.begin(), first.end(), wi) - first.begin()) - 1;
+            const std::vector<ApertureSample>& g = *gptr[p];
+            const ApertureSample& s = g[(size_t)(wi - first[p])];
+            const float ray_weight = 1.0f / (float)g.size();
+            const int a = pairs_ab[2 * p], b = pairs_ab[2 * p + 1];
+            for (int li = 0; li < n_spec; ++li)
+            {
+                Ray r;
+                r.origin = Vec3f(s.u * front_R + sdx, s.v * front_R + sdy, start_z);
+                r.dir = beam; r.lambda = spec4[4 * li];
+                ++render_traces;
+                TraceResult res = trace_ghost_ray(r, *L, a, b);
+                if (res.status != TraceStatus::OK) continue;
+                if (!std::isfinite(res.position.x) || !std::isfinite(res.position.y)) continue;
+                const float base = res.weight * ray_weight * gain * boosts[p];
+                if (base < 1e-14f) continue;
+                splat_point(img, npx, W, H, hw, hh, res, base, src5, spec4 + 4 * li);
+            }
+        }
+    }
+    // sum the thread images, then the colour correction
+    #pragma omp parallel for schedule(static)
+    for (long long i = 0; i < (long long)npx; ++i)
+    {
+        float rgb[3];
+        for (int ch = 0; ch < 3; ++ch)
+        {
+            float t = 0.0f;
+            for (int k = 0; k < nt; ++k) t += acc[k][ch * npx + i];
+            rgb[ch] = t;
+        }
+        for (int ch = 0; ch < 3; ++ch)
+            out_rgb[ch * npx + i] = corr9 ? corr9[3 * ch] * rgb[0] + corr9[3 * ch + 1] * rgb[1] +
+                                            corr9[3 * ch + 2] * rgb[2]
+                                          : rgb[ch];
+    }
+    int kept = 0;
+    for (int p = 0; p < n_pairs; ++p) kept += keep[p];
+    if (counts) { counts[0] = probe_traces; counts[1] = render_traces; counts[2] = kept; }
+    delete L;
+    return nt;
+}
+
+
+// Landing extent of a ghost on the sensor (ghost_w, ghost_h; 0 when fewer than
+// two probe rays land): the 8x8 on-axis probe at 550 nm of
+// estimate_ghost_spread (ghost.cpp:53-102), traced with the reference's own
+// trace_ghost_ray, for n_pairs pairs.
+extern "C" int ref_ghost_footprints(const gl_surface* surfs, int n, const int* pairs_ab, int n_pairs,
+                                    float* out_wh)
+{
+    OpticalSystem* L = make_lens(surfs, n);
+    const float front_R = L->surfaces[0].semi_aperture;
+    const float start_z = L->surfaces[0].z - SPAWN_OFFSET;
+    for (int p = 0; p < n_pairs; ++p)
+    {
+        float mnx = 1e30f, mxx = -1e30f, mny = 1e30f, mxy = -1e30f;
+        int valid = 0;
+        for (int gy = 0; gy < 8; ++gy)
+            for (int gx = 0; gx < 8; ++gx)
+            {
+                const float u = ((gx + 0.5f) / 8) * 2.0f - 1.0f;
+                const float v = ((gy + 0.5f) / 8) * 2.0f - 1.0f;
+                if (u * u + v * v > 1.0f) continue;
+                Ray r;
+                r.origin = Vec3f(u * front_R, v * front_R, start_z);
+                r.dir = Vec3f(0, 0, 1);
+                r.lambda = 550.0f;
+                TraceResult res = trace_ghost_ray(r, *L, pairs_ab[2 * p], pairs_ab[2 * p + 1]);
+                if (res.status != TraceStatus::OK) continue;
+                mnx = std::min(mnx, res.position.x); mxx = std::max(mxx, res.position.x);
+                mny = std::min(mny, res.position.y); mxy = std::max(mxy, res.position.y);
+                ++valid;
+            }
+        out_wh[2 * p] = valid >= 2 ? mxx - mnx : 0.0f;
+        out_wh[2 * p + 1] = valid >= 2 ? mxy - mny : 0.0f;
+    }
+    delete L;
+    return 0;
+}
+
+#ifdef REF_GPU
+// ---------------------------------------------------------------------------
+// The reference's GPU renderer (render_point_flare / render_source_flare,
+// PointFlareRenderer.cpp:11, SourceFlareRenderer.cpp:24) on a lens given as
+// flat records.  Fields follow PointFlareConfig (render_config.h) by name.
+// ---------------------------------------------------------------------------
+struct RefGpuCfg {
+    int ray_grid, spectral_samples, pupil_jitter, jitter_seed;
+    float sensor_half_w, sensor_half_h, flare_gain, min_ghost_intensity;
+    int cull_dead_pairs, concentrate_samples, adaptive_sample_budgets, aperture_blades;
+    float source_x, source_y, source_r, source_g, source_b;
+    int starburst, starburst_engine, starburst_grid, sb_spectral_samples;
+    float pupil_fill, scale_trim;
+    int spectral_correction, output_cs, use_survivor_mask, collect_stats;
+};
+
+extern "C" int refgpu_sizeof_cfg() { return (int)sizeof(RefGpuCfg); }
+
+// calib13: the 13 calibration values (ref_calibrate order) or NULL to
+// calibrate here.  offsets: n_offsets x 3 (render_source_flare) or NULL
+// (render_point_flare).  out_ghost / out_star: 3 planes of W*H or NULL.
+// ms: wall time of the render call (its own uploads, kernels and D2H).
+// stats (8 doubles, or NULL; filled when collect_stats): the renderer's own
+// GhostRenderStats ms_grid_build, ms_upload, ms_kernel, ms_download,
+// ms_total, n_pairs, traces_total, traces_on_sensor.
+extern "C" int refgpu_render(const gl_surface* surfs, int n, float focal_length, const float* calib13,
+                             const RefGpuCfg* g, const float* offsets, int n_offsets, int W, int H,
+                             float* out_ghost, float* out_star, double* ms, double* stats)
+{
+    OpticalSystem* L = make_lens(surfs, n);
+    L->focal_length = focal_length;
+    LensCalibration c{};
+    if (calib13)
+    {
+        c.sensor_half_w = calib13[0]; c.sensor_half_h = calib13[1];
+        c.max_half_angle_h = calib13[2]; c.max_half_angle_v = calib13[3];
+        c.image_circle_semi_w = calib13[4]; c.image_circle_semi_h = calib13[5];
+        c.focal_length_x = calib13[6]; c.focal_length_y = calib13[7];
+        c.entrance_pupil_semi_x = calib13[8]; c.entrance_pupil_semi_y = calib13[9];
+        c.f_number_x = calib13[10]; c.f_number_y = calib13[11]; c.pupil_area_frac = calib13[12];
+    }
+    else
+        c = calibrate_lens(*L, 587.56f);
+    PointFlareConfig cfg;
+    cfg.ray_grid = g->ray_grid; cfg.spectral_samples = g->spectral_samples;
+    cfg.pupil_jitter = g->pupil_jitter; cfg.jitter_seed = g->jitter_seed;
+    cfg.sensor_half_w = g->sensor_half_w; cfg.sensor_half_h = g->sensor_half_h;
+    cfg.flare_gain = g->flare_gain; cfg.min_ghost_intensity = g->min_ghost_intensity;
+    cfg.cull_dead_pairs = g->cull_dead_pairs != 0; cfg.concentrate_samples = g->concentrate_samples != 0;
+    cfg.adaptive_sample_budgets = g->adaptive_sample_budgets != 0;
+    if (g->aperture_blades) cfg.aperture_blades = g->aperture_blades;
+    cfg.source_x = g->source_x; cfg.source_y = g->source_y;
+    cfg.source_r = g->source_r; cfg.source_g = g->source_g; cfg.source_b = g->source_b;
+    cfg.spectral_correction = g->spectral_correction != 0;
+    cfg.output_cs = (OutputColorSpace)g->output_cs;
+    cfg.diffraction.starburst = g->starburst != 0;
+    cfg.diffraction.starburst_engine = g->starburst_engine ? StarburstEngine::MDFT : StarburstEngine::SPRITE;
+    cfg.diffraction.starburst_grid = g->starburst_grid;
+    cfg.diffraction.spectral_samples = g->sb_spectral_samples;
+    cfg.diffraction.pupil_fill = g->pupil_fill; cfg.diffraction.scale_trim = g->scale_trim;
+    cfg.diffraction.use_survivor_mask = g->use_survivor_mask != 0;
+    cfg.collect_stats = g->collect_stats != 0;
+    FlareBuffers out;
+    const auto t0 = std::chrono::steady_clock::now();
+    const bool ok = offsets ? render_source_flare(W, H, offsets, n_offsets, *L, c, cfg, out)
+                            : render_point_flare(W, H, *L, c, cfg, out);
+    const auto t1 = std::chrono::steady_clock::now();
+    if (ms) *ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+    delete L;
+    if (!ok) return -1;
+    if (stats)
+    {
+        const GhostRenderStats& t = out.stats;
+        const double v[8] = {t.ms_grid_build, t.ms_upload, t.ms_kernel, t.ms_download, t.ms_total,
+                             (double)t.n_pairs, (double)t.traces_total, (double)t.traces_on_sensor};
+        for (int k = 0; k < 8; ++k) stats[k] = out.has_stats ? v[k] : -1.0;
+    }
+    const size_t npx = (size_t)W * H;
+    if (out_ghost)
+    {
+        const std::vector<float>* pl[3] = {&out.ghost_r, &out.ghost_g, &out.ghost_b};
+        for (int k = 0; k < 3; ++k)
+            for (size_t i = 0; i < npx; ++i) out_ghost[k * npx + i] = pl[k]->size() == npx ? (*pl[k])[i] : 0.0f;
+    }
+    if (out_star)
+    {
+        const std::vector<float>* pl[3] = {&out.starburst_r, &out.starburst_g, &out.starburst_b};
+        for (int k = 0; k < 3; ++k)
+            for (size_t i = 0; i < npx; ++i) out_star[k * npx + i] = pl[k]->size() == npx ? (*pl[k])[i] : 0.0f;
+    }
+    return 0;
+}
+#endif  // REF_GPU

@@ -25,7 +25,9 @@ sys.path.insert(0, str(REPO))
 from ghostlight_gb300 import prescriptions as P  # noqa: E402
 from ghostlight_gb300._abi import SURFACE_DTYPE, surface_array  # noqa: E402
 from oracle import ref  # noqa: E402
-from oracle.build import REFERENCE_ROOT  # noqa: E402
+from oracle.stage_ref import checkout  # noqa: E402
+
+REFERENCE_ROOT = checkout()
 
 
 def lens_bytes(surfs):

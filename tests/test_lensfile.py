@@ -149,8 +149,8 @@ def test_rejected_files_raise(case, tmp_path):
 
 
 def _reference_lenses():
-    from oracle.build import REFERENCE_ROOT
-    return sorted((REFERENCE_ROOT / "lenses").glob("**/*.lens"))
+    from oracle.stage_ref import checkout
+    return sorted((checkout() / "lenses").glob("**/*.lens"))
 
 
 @pytest.mark.parametrize("path", _reference_lenses(), ids=lambda p: p.stem[:40])

@@ -60,3 +60,34 @@ def test_noalloc_trace_rejects_lenses_above_the_table_size(pins):
     rays = pins["cfg2_wide_angle_24/rays_0/in"][:4]
     with pytest.raises(ValueError, match="64 surfaces"):
         _trace(lib.gl_trace_rays_noalloc, big, -1, -1, rays)
+
+
+def test_noalloc_trace_refuses_stream_capture(pins):
+    """The call waits for its own stream, so under capture it must refuse
+    (GL_ERR_INVALID -> ValueError) instead of breaking the caller's graph."""
+    from ghostlight_gb300 import _native
+    from ghostlight_gb300._abi import surface_array
+    lib = _native.load()
+    recs = lens_from_pins(pins, "cfg2_wide_angle_24")
+    arr = surface_array(recs)
+    rays = torch.from_numpy(np.ascontiguousarray(pins["cfg2_wide_angle_24/rays_0/in"][:32])).cuda()
+    out = torch.zeros((32, 5), dtype=torch.float32, device="cuda")
+    x = torch.zeros(4, device="cuda")
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    torch.cuda.synchronize()
+    with torch.cuda.stream(s):
+        with torch.cuda.graph(g, stream=s):
+            x.add_(1.0)
+            rc = lib.gl_trace_rays_noalloc(arr, len(arr), -1, -1, rays.data_ptr(), 32, out.data_ptr(),
+                                           s.cuda_stream)
+    assert rc != 0
+    with pytest.raises(ValueError, match="captured"):
+        _native.check(rc, "trace")
+    g.replay()
+    torch.cuda.synchronize()
+    assert float(x[0]) == 1.0
+    # the same call outside the capture still works
+    got = _trace(lib.gl_trace_rays_noalloc, recs, -1, -1, rays.cpu().numpy())
+    want = _trace(lib.gl_trace_rays, recs, -1, -1, rays.cpu().numpy())
+    assert (got[:, 4] == want[:, 4]).all()
