@@ -56,6 +56,10 @@ class DiffractionConfig:
     starburst_gain: float = 1.0
     scale_trim: float = 1.0
     spectral_samples: int = 0
+    # matrix-DFT engine form: "pixel" = the reference's pixel-box-integrated
+    # intensity through the pupil autocorrelation (mdft_render.cu); "field" =
+    # the field E = W_y A W_x^T sampled at pixel centres, |E|^2
+    mdft_form: str = "pixel"
     use_survivor_mask: bool = True
     use_surface_textures: bool = True
     survivor_grid: int = 192

@@ -227,6 +227,11 @@ struct MdftArgs {
     float* out_b;
     const float4* weights;            // per wavelength (w_r, w_g, w_b, 0)
     int* err;
+    // step-2 output placement: plan pixel (l, k) -> frame (y0 + l, x0 + k) of
+    // planes out_w wide, kept when l < win_h and k < win_w
+    int out_w, x0, y0, win_w, win_h;
+    int box;                          // 1: accumulate Re E (pixel-integrated form); 0: |E|^2
+    float4 tint;                      // per-launch colour factor on the weights
 };
 
 template <int FORM>
@@ -424,25 +429,45 @@ __global__ void __launch_bounds__(kMdftThreads, 1) mdft_kernel(const __grid_cons
             const uint32_t ta = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(b * 256);
             if (STEP == 2)
             {
-                const float4 w = args.weights[lam];
-                const size_t l = (size_t)(mb * 128 + row);
+                const float4 w0 = args.weights[lam];
+                const float4 w = make_float4(w0.x * args.tint.x, w0.y * args.tint.y, w0.z * args.tint.z, 0.0f);
+                const int l = mb * 128 + row;
+                const bool row_in = l < args.win_h;
+                const size_t orow = (size_t)(args.y0 + l) * (size_t)args.out_w + (size_t)args.x0;
                 #pragma unroll 1
                 for (int c = 0; c < 8; ++c)
                 {
                     float re[16], im[16];
                     tc::tmem_ld16(ta + (uint32_t)(c * 16), re);
                     tc::tmem_ld16(ta + 128u + (uint32_t)(c * 16), im);
-                    if (!ok) continue;
-                    const size_t base = l * (size_t)args.Kx + (size_t)(xb * 128 + c * 16);
+                    if (!ok || !row_in) continue;
+                    const int kc = xb * 128 + c * 16;
                     #pragma unroll
                     for (int j = 0; j < 16; j += 4)
                     {
                         float I[4];
                         #pragma unroll
-                        for (int q = 0; q < 4; ++q) I[q] = re[j + q] * re[j + q] + im[j + q] * im[j + q];
-                        atomicAdd(reinterpret_cast<float4*>(args.out_r + base + j), make_float4(w.x * I[0], w.x * I[1], w.x * I[2], w.x * I[3]));
-                        atomicAdd(reinterpret_cast<float4*>(args.out_g + base + j), make_float4(w.y * I[0], w.y * I[1], w.y * I[2], w.y * I[3]));
-                        atomicAdd(reinterpret_cast<float4*>(args.out_b + base + j), make_float4(w.z * I[0], w.z * I[1], w.z * I[2], w.z * I[3]));
+                        for (int q = 0; q < 4; ++q)
+                            I[q] = args.box ? re[j + q] : re[j + q] * re[j + q] + im[j + q] * im[j + q];
+                        const int k = kc + j;
+                        const size_t o = orow + (size_t)k;
+                        if (k + 3 < args.win_w && (o & 3) == 0)
+                        {
+                            atomicAdd(reinterpret_cast<float4*>(args.out_r + o), make_float4(w.x * I[0], w.x * I[1], w.x * I[2], w.x * I[3]));
+                            atomicAdd(reinterpret_cast<float4*>(args.out_g + o), make_float4(w.y * I[0], w.y * I[1], w.y * I[2], w.y * I[3]));
+                            atomicAdd(reinterpret_cast<float4*>(args.out_b + o), make_float4(w.z * I[0], w.z * I[1], w.z * I[2], w.z * I[3]));
+                        }
+                        else
+                        {
+                            #pragma unroll
+                            for (int q = 0; q < 4; ++q)
+                            {
+                                if (k + q >= args.win_w) break;
+                                atomicAdd(args.out_r + o + q, w.x * I[q]);
+                                atomicAdd(args.out_g + o + q, w.y * I[q]);
+                                atomicAdd(args.out_b + o + q, w.z * I[q]);
+                            }
+                        }
                     }
                 }
             }
@@ -499,10 +524,12 @@ __global__ void __launch_bounds__(kMdftThreads, 1) mdft_kernel(const __grid_cons
 // two-float sum, and the product's integer cycles are removed from
 // the leading term exactly; the reduced phase is accurate to ~1e-9 cycles,
 // then evaluated with sincospif.  (The FP64 units of this part are slow.)
+// With box set each entry also carries the pixel-box factor sinc(s (j - cj))
+// of the reference's pixel-integrated form (mdft_render.cu:109-135).
 // FORM 0 stores [hi | hi | lo] along the reduction axis, FORM 1 the FP32 value.
 template <int FORM>
 __global__ void mdft_dft_kernel(void* out, int n_lambda, int K_rows, int n, int Kp, const float2* __restrict__ scale,
-                                float ck_hi, float ck_lo, float cj)
+                                float ck_hi, float ck_lo, float cj, int box)
 {
     const size_t total = (size_t)n_lambda * K_rows * n;
     for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x)
@@ -527,7 +554,15 @@ __global__ void mdft_dft_kernel(void* out, int n_lambda, int K_rows, int n, int 
         fr -= rintf(fr);
         float sv, cv;
         sincospif(2.0f * fr, &sv, &cv);
-        const float re = cv, im = -sv;
+        float amp = 1.0f;
+        if (box)
+        {
+            // pixel-box factor of the pixel-integrated form: sinc(m s), m = j - cj
+            // the lag, s = pixel pitch / pattern period at this wavelength
+            const float x = a * (sc.x + sc.y);
+            amp = fabsf(x) < 1e-7f ? 1.0f : sinpif(x) / (3.14159265358979323846f * x);
+        }
+        const float re = amp * cv, im = -amp * sv;
         const size_t rr = ((size_t)(lam * 2 + 0) * K_rows + k) * Kp;
         const size_t ri = ((size_t)(lam * 2 + 1) * K_rows + k) * Kp;
         if (FORM == 0)
@@ -698,7 +733,9 @@ __global__ void __launch_bounds__(256) mdft_simt_step1(const float* __restrict__
 
 __global__ void __launch_bounds__(256) mdft_simt_step2(const float* __restrict__ W, const float* __restrict__ T,
                                                        const float4* __restrict__ weights, float* out_r, float* out_g,
-                                                       float* out_b, int K_rows, int K_out, int n, int NB, int n_lambda)
+                                                       float* out_b, int K_rows, int K_out, int n, int NB, int n_lambda,
+                                                       int box, int out_w, int x0, int y0, int win_w, int win_h,
+                                                       float4 tint)
 {
     // K_rows = rows of W_y per (wavelength, part) = Ky; K_out = output width Kx
     __shared__ float sWr[kSK][kSB + 4], sWi[kSK][kSB + 4], sTr[kSK][kSB + 4], sTi[kSK][kSB + 4];
@@ -745,15 +782,19 @@ __global__ void __launch_bounds__(256) mdft_simt_step2(const float* __restrict__
             __syncthreads();
         }
         // this block owns the tile across wavelengths: plain read-modify-write
-        const float4 w = weights[lam];
+        const float4 w0 = weights[lam];
+        const float4 w = make_float4(w0.x * tint.x, w0.y * tint.y, w0.z * tint.z, 0.0f);
         #pragma unroll
         for (int p = 0; p < 8; ++p)
         {
-            const size_t row = (size_t)(mb * kSB + ty * 8 + p) * K_out + nb * kSB + tx * 8;
+            const int l = mb * kSB + ty * 8 + p;
+            if (l >= win_h) continue;
+            const size_t row = (size_t)(y0 + l) * out_w + x0 + nb * kSB + tx * 8;
             #pragma unroll
             for (int q = 0; q < 8; ++q)
             {
-                const float I = er[p][q] * er[p][q] + ei[p][q] * ei[p][q];
+                if (nb * kSB + tx * 8 + q >= win_w) continue;
+                const float I = box ? er[p][q] : er[p][q] * er[p][q] + ei[p][q] * ei[p][q];
                 out_r[row + q] += w.x * I; out_g[row + q] += w.y * I; out_b[row + q] += w.z * I;
             }
         }
@@ -774,6 +815,8 @@ struct MdftPlan {
     float4* weights = nullptr;
     float2* scales = nullptr;   // [2][n_lambda] (s_hi, s_lo) device copy
     double cx = 0.0, cy = 0.0;
+    float cj = 0.0f;            // reduction-axis centre: (n - 1) / 2, or the zero lag mc of the box form
+    int box = 0;                // pixel-integrated form (the reference's MDFT engine)
     int ctas = 0;               // GEMM grid (0 = one CTA per SM)
     int* err = nullptr;
     CUtensorMap t_wx, t_wy, t_mask, t_tp;
@@ -798,32 +841,36 @@ namespace gl {
 static cudaError_t mdft_build_matrices(MdftPlan* p, cudaStream_t st)
 {
     const int blocks = 4 * p->sms;
-    const float cj = 0.5f * (float)(p->n - 1);
+    const float cj = p->cj;
+    const int box = p->box;
     const float cxh = (float)p->cx, cxl = (float)(p->cx - (double)cxh);
     const float cyh = (float)p->cy, cyl = (float)(p->cy - (double)cyh);
     if (p->form == 0)
     {
-        mdft_dft_kernel<0><<<blocks, 256, 0, st>>>(p->wx, p->n_lambda, p->Kx, p->n, p->Kp, p->scales, cxh, cxl, cj);
+        mdft_dft_kernel<0><<<blocks, 256, 0, st>>>(p->wx, p->n_lambda, p->Kx, p->n, p->Kp, p->scales, cxh, cxl, cj, box);
         mdft_dft_kernel<0><<<blocks, 256, 0, st>>>(p->wy, p->n_lambda, p->Ky, p->n, p->Kp, p->scales + p->n_lambda, cyh,
-                                                   cyl, cj);
+                                                   cyl, cj, box);
     }
     else
     {
-        mdft_dft_kernel<1><<<blocks, 256, 0, st>>>(p->wx, p->n_lambda, p->Kx, p->n, p->Kp, p->scales, cxh, cxl, cj);
+        mdft_dft_kernel<1><<<blocks, 256, 0, st>>>(p->wx, p->n_lambda, p->Kx, p->n, p->Kp, p->scales, cxh, cxl, cj, box);
         mdft_dft_kernel<1><<<blocks, 256, 0, st>>>(p->wy, p->n_lambda, p->Ky, p->n, p->Kp, p->scales + p->n_lambda, cyh,
-                                                   cyl, cj);
+                                                   cyl, cj, box);
     }
     return cudaGetLastError();
 }
 
 }  // namespace gl
 
-extern "C" int gl_mdft_plan_create2(int n, int Kx, int Ky, int n_lambda, const double* scale_x, const double* scale_y,
-                                    double center_x, double center_y, const float* weights_rgb, int form, void* stream,
-                                    gl_mdft_plan** out)
+extern "C" int gl_mdft_plan_create3(int n, int Kx, int Ky, int n_lambda, const double* scale_x, const double* scale_y,
+                                    double center_x, double center_y, const float* weights_rgb, int form, int box,
+                                    float red_center, void* stream, gl_mdft_plan** out)
 {
     using namespace gl;
     if (!out || !scale_x || !scale_y || !weights_rgb) return fail(GL_ERR_INVALID, "mdft_plan_create: null argument");
+    if (box != 0 && box != 1) return fail(GL_ERR_INVALID, "mdft_plan_create: box must be 0 or 1");
+    if (!(red_center >= 0.0f) || !(red_center <= (float)n) || red_center != std::floor(2.0f * red_center) * 0.5f)
+        return fail(GL_ERR_INVALID, "mdft_plan_create: the reduction centre must be a whole or half index in [0, n]");
     if (n <= 0 || n % 128 || Kx <= 0 || Kx % 128 || Ky <= 0 || Ky % 128)
         return fail(GL_ERR_INVALID, "mdft_plan_create: the pupil side n and output sides Kx, Ky must be multiples of 128");
     if (Kx > 8192 || Ky > 8192 || n > 4096) return fail(GL_ERR_INVALID, "mdft_plan_create: sides above 8192 (4096 for n)");
@@ -838,6 +885,7 @@ extern "C" int gl_mdft_plan_create2(int n, int Kx, int Ky, int n_lambda, const d
     MdftPlan* p = new MdftPlan();
     p->n = n; p->Kx = Kx; p->Ky = Ky; p->n_lambda = n_lambda; p->form = form;
     p->cx = center_x; p->cy = center_y;
+    p->box = box; p->cj = red_center;
     p->Kp = form == 0 ? 3 * n : n;
     p->elem = form == 0 ? 2 : 4;
     const int NBx = Kx / 128;
@@ -909,6 +957,14 @@ extern "C" int gl_mdft_plan_create2(int n, int Kx, int Ky, int n_lambda, const d
     return GL_OK;
 }
 
+extern "C" int gl_mdft_plan_create2(int n, int Kx, int Ky, int n_lambda, const double* scale_x, const double* scale_y,
+                                    double center_x, double center_y, const float* weights_rgb, int form, void* stream,
+                                    gl_mdft_plan** out)
+{
+    return gl_mdft_plan_create3(n, Kx, Ky, n_lambda, scale_x, scale_y, center_x, center_y, weights_rgb, form, 0,
+                                0.5f * (float)(n - 1), stream, out);
+}
+
 extern "C" int gl_mdft_plan_create(int n, int K_out, int n_lambda, const double* scale_x, const double* scale_y,
                                    double center_x, double center_y, const float* weights_rgb, int form,
                                    void* stream, gl_mdft_plan** out)
@@ -930,15 +986,19 @@ extern "C" int gl_mdft_plan_set_center(gl_mdft_plan* plan, double center_x, doub
     return GL_OK;
 }
 
-extern "C" int gl_mdft_plan_execute2(gl_mdft_plan* plan, const float* d_pupil, float* d_out_r, float* d_out_g,
-                                     float* d_out_b, int accumulate, void* stream)
+extern "C" int gl_mdft_plan_execute3(gl_mdft_plan* plan, const float* d_pupil, float* d_out_r, float* d_out_g,
+                                     float* d_out_b, int accumulate, int out_w, int out_h, int x0, int y0, int win_w,
+                                     int win_h, const float* tint_rgb, void* stream)
 {
     using namespace gl;
     if (!plan || !d_pupil || !d_out_r || !d_out_g || !d_out_b) return fail(GL_ERR_INVALID, "mdft_plan_execute: null argument");
     MdftPlan* p = plan->p;
+    if (out_w <= 0 || out_h <= 0 || x0 < 0 || y0 < 0 || win_w < 0 || win_h < 0 || win_w > p->Kx || win_h > p->Ky ||
+        x0 + win_w > out_w || y0 + win_h > out_h)
+        return fail(GL_ERR_INVALID, "mdft_plan_execute: the output window must lie inside the planes and the plan");
     cudaStream_t st = (cudaStream_t)stream;
     const int NBx = p->Kx / 128, NBy = p->Ky / 128, NI = p->n / 128;
-    const size_t npx = (size_t)p->Kx * p->Ky;
+    const size_t npx = (size_t)out_w * out_h;
     int launches = 0;
     GL_CUDA_TRY(cudaMemsetAsync(p->err, 0, sizeof(int), st));
     if (p->form == 0) mdft_mask_kernel<0><<<2 * p->sms, 256, 0, st>>>(d_pupil, p->mask, p->n, p->Kp);
@@ -957,6 +1017,8 @@ extern "C" int gl_mdft_plan_execute2(gl_mdft_plan* plan, const float* d_pupil, f
     a.NB = NBx; a.NI = NI;
     a.tprime = p->tprime; a.out_r = d_out_r; a.out_g = d_out_g; a.out_b = d_out_b;
     a.weights = p->weights; a.err = p->err;
+    a.out_w = out_w; a.x0 = x0; a.y0 = y0; a.win_w = win_w; a.win_h = win_h; a.box = p->box;
+    a.tint = tint_rgb ? make_float4(tint_rgb[0], tint_rgb[1], tint_rgb[2], 0.0f) : make_float4(1.0f, 1.0f, 1.0f, 0.0f);
     const size_t smem1 = 4 * 3 * (size_t)kOpTile + 1024, smem2 = 2 * 5 * (size_t)kOpTile + 1024;
     a.n_units = p->n_lambda * NBx * NI;                 // step 1: (lambda, k block, pupil-row block)
     const int gmax = p->ctas > 0 ? p->ctas : p->sms;
@@ -972,7 +1034,7 @@ extern "C" int gl_mdft_plan_execute2(gl_mdft_plan* plan, const float* d_pupil, f
                                                                     static_cast<float*>(p->tprime), p->Kx, p->n, NBx);
         mdft_simt_step2<<<dim3(NBx, NBy), 256, 0, st>>>(static_cast<const float*>(p->wy), static_cast<const float*>(p->tprime),
                                                        p->weights, d_out_r, d_out_g, d_out_b, p->Ky, p->Kx, p->n, NBx,
-                                                       p->n_lambda);
+                                                       p->n_lambda, p->box, out_w, x0, y0, win_w, win_h, a.tint);
     }
     else if (p->form == 0)
     {
@@ -988,6 +1050,15 @@ extern "C" int gl_mdft_plan_execute2(gl_mdft_plan* plan, const float* d_pupil, f
     launches += 2;
     g_last_launches = launches;
     return GL_OK;
+}
+
+extern "C" int gl_mdft_plan_execute2(gl_mdft_plan* plan, const float* d_pupil, float* d_out_r, float* d_out_g,
+                                     float* d_out_b, int accumulate, void* stream)
+{
+    if (!plan) return gl::fail(GL_ERR_INVALID, "mdft_plan_execute: null argument");
+    const gl::MdftPlan* p = plan->p;
+    return gl_mdft_plan_execute3(plan, d_pupil, d_out_r, d_out_g, d_out_b, accumulate, p->Kx, p->Ky, 0, 0, p->Kx, p->Ky,
+                                 nullptr, stream);
 }
 
 extern "C" int gl_mdft_plan_set_launch(gl_mdft_plan* plan, int ctas)

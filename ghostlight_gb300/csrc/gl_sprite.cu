@@ -122,6 +122,54 @@ __device__ __forceinline__ float psf_bilinear(const float* __restrict__ psf, flo
     return a * (1.0f - ty) + b * ty;
 }
 
+// Column pass of the second transform of the matrix-DFT engine's compact
+// autocorrelation (mdft_render.cu:88-99, 247-262): after the row pass of the
+// fftshifted PSF, transform the columns whose x lag lies within +-mc of zero
+// and write C[a][b] (a = y lag + mc, b = x lag + mc) = (-1)^(lx + ly)
+// Re X[ly][lx] / (energy N^2).  The sign undoes the fftshift of the PSF
+// (a shift by N/2 multiplies the transform by (-1)^l); energy = sum |FFT A|^2
+// = G[0][0], summed on the device by the first column pass.  A real pupil has
+// a real, point-symmetric autocorrelation: the imaginary part is rounding.
+template <int NB>
+__global__ void __launch_bounds__(kSpriteThreads) autocorr_cols(const float2* __restrict__ work, int N, FftDims d,
+                                                                const float2* __restrict__ tw, int mc,
+                                                                const double* __restrict__ energy,
+                                                                float* __restrict__ C, int ldc)
+{
+    extern __shared__ float2 sm[];
+    const int c0 = blockIdx.x * NB;
+    const int h = N / 2;
+    bool any = false;
+    #pragma unroll
+    for (int s = 0; s < NB; ++s)
+    {
+        const int c = c0 + s, lag = c <= h ? c : c - N;
+        any |= (lag >= -mc && lag <= mc);
+    }
+    if (!any) return;                          // uniform over the block
+    float2* x = sm;
+    float2* y = sm + padded((size_t)N * NB);
+    for (int it = threadIdx.x; it < N * NB; it += blockDim.x)
+    {
+        const int r = it / NB, s = it % NB;
+        x[pad(r * NB + s)] = work[(size_t)r * N + c0 + s];
+    }
+    __syncthreads();
+    const float2* X = stockham<NB>(x, y, d, tw, false);
+    const double e = *energy;
+    const float scale = e > 0.0 ? (float)(1.0 / (e * (double)N * (double)N)) : 0.0f;
+    const int Mc = 2 * mc + 1;
+    for (int it = threadIdx.x; it < Mc * NB; it += blockDim.x)
+    {
+        const int a = it / NB, s = it % NB;
+        const int c = c0 + s, lx = c <= h ? c : c - N;
+        if (lx < -mc || lx > mc) continue;
+        const int ly = a - mc, r = (ly + N) & (N - 1);
+        const float v = X[pad(r * NB + s)].x * scale;
+        C[(size_t)a * ldc + (lx + mc)] = ((lx + ly) & 1) ? -v : v;
+    }
+}
+
 // bake over wavelength + ds x ds box sum: coarse texel (a, b) of M x M
 __global__ void __launch_bounds__(kSpriteThreads) sprite_bake(const float* __restrict__ psf, int N,
                                                               const float4* __restrict__ spec, int n_spec,
@@ -289,6 +337,9 @@ extern "C" int gl_sprite_plan_create(int N, const gl_spectral_sample* spec, int 
         if (nb == 4) chk(cudaFuncSetAttribute(sprite_cols<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_cols));
         if (nb == 2) chk(cudaFuncSetAttribute(sprite_cols<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_cols));
         if (nb == 1) chk(cudaFuncSetAttribute(sprite_cols<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_cols));
+        if (nb == 4) chk(cudaFuncSetAttribute(autocorr_cols<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_cols));
+        if (nb == 2) chk(cudaFuncSetAttribute(autocorr_cols<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_cols));
+        if (nb == 1) chk(cudaFuncSetAttribute(autocorr_cols<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_cols));
     }
     if (e != cudaSuccess)
     {
@@ -371,6 +422,42 @@ extern "C" int gl_sprite_plan_splat(gl_sprite_plan* plan, const float* sources, 
     // the host sources are staged through pageable memory: the copy is done
     // when the call returns, so the caller may reuse them
     g_last_launches = 1;
+    return GL_OK;
+}
+
+extern "C" int gl_sprite_plan_autocorr(gl_sprite_plan* plan, const float* d_pupil, int mc, float* d_C, int ldc,
+                                       int rows, void* stream)
+{
+    if (!plan || !d_pupil || !d_C) return fail(GL_ERR_INVALID, "autocorr: bad arguments");
+    SpritePlan* p = plan->p;
+    const int N = p->N;
+    if (mc < 0 || mc > N / 2 - 1) return fail(GL_ERR_INVALID, "autocorr: lag radius must lie in [0, N/2 - 1]");
+    if (ldc < 2 * mc + 1 || rows < 2 * mc + 1)
+        return fail(GL_ERR_INVALID, "autocorr: the output must hold (2 mc + 1)^2 lags");
+    cudaStream_t st = (cudaStream_t)stream;
+    GL_CUDA_TRY(cudaMemsetAsync(d_C, 0, sizeof(float) * (size_t)ldc * rows, st));
+    GL_CUDA_TRY(cudaMemsetAsync(p->energy, 0, sizeof(double), st));
+    const int nb = col_group(N);
+    // |FFT A|^2 (fftshifted) and its sum, as the sprite bake computes them
+    sprite_rows<<<N, kSpriteThreads, p->smem_rows, st>>>(d_pupil, N, p->dims, p->tw, p->work);
+    if (nb == 4)
+        sprite_cols<4><<<N / 4, kSpriteThreads, p->smem_cols, st>>>(p->work, N, p->dims, p->tw, p->psf, p->energy);
+    else if (nb == 2)
+        sprite_cols<2><<<N / 2, kSpriteThreads, p->smem_cols, st>>>(p->work, N, p->dims, p->tw, p->psf, p->energy);
+    else
+        sprite_cols<1><<<N, kSpriteThreads, p->smem_cols, st>>>(p->work, N, p->dims, p->tw, p->psf, p->energy);
+    // the second transform, kept only at lags within +-mc
+    sprite_rows<<<N, kSpriteThreads, p->smem_rows, st>>>(p->psf, N, p->dims, p->tw, p->work);
+    if (nb == 4)
+        autocorr_cols<4><<<N / 4, kSpriteThreads, p->smem_cols, st>>>(p->work, N, p->dims, p->tw, mc, p->energy, d_C, ldc);
+    else if (nb == 2)
+        autocorr_cols<2><<<N / 2, kSpriteThreads, p->smem_cols, st>>>(p->work, N, p->dims, p->tw, mc, p->energy, d_C, ldc);
+    else
+        autocorr_cols<1><<<N, kSpriteThreads, p->smem_cols, st>>>(p->work, N, p->dims, p->tw, mc, p->energy, d_C, ldc);
+    GL_CUDA_TRY(cudaGetLastError());
+    // the bake's sprite no longer matches the PSF buffer's contents
+    p->M = 0;
+    g_last_launches = 4;
     return GL_OK;
 }
 

@@ -529,17 +529,22 @@ def render_source_flare(offsets, width: int, height: int, lens: OpticalSystem,
     if want_sb:
         # engine choice as render_starburst (starburst_render.cu:646-711): the
         # SPRITE engine by default and whenever the pattern is prominent or
-        # the grid grows; the matrix-DFT field form otherwise when asked for
-        from .starburst import sprite_geometry, sprite_starburst_layer, starburst_layer
+        # the grid grows; the matrix-DFT engine otherwise when asked for, in
+        # the reference's pixel-integrated form (or the field form when
+        # diffraction.mdft_form == "field")
+        from .starburst import mdft_box_starburst_layer, sprite_geometry, sprite_starburst_layer, starburst_layer
         geo = sprite_geometry(calibration, config, pos, width, height, hw, hh,
                               front_R=lens.surfaces[0].semi_aperture if lens.surfaces else 0.0)
+        field = (float(np.float32(np.mean(src[:, 0].astype(np.float64)))),
+                 float(np.float32(np.mean(src[:, 1].astype(np.float64)))))
         if geo["engine"] == "sprite":
-            field = (float(np.float32(np.mean(src[:, 0].astype(np.float64)))),
-                     float(np.float32(np.mean(src[:, 1].astype(np.float64)))))
             out.update(sprite_starburst_layer(lens, calibration, config, pos, width, height, hw, hh, geometry=geo,
                                               field=field))
-        else:
+        elif getattr(dc, "mdft_form", "pixel") == "field":
             out.update(starburst_layer(lens, calibration, config, pos, width, height, hw, hh))
+        else:
+            out.update(mdft_box_starburst_layer(lens, calibration, config, pos, width, height, hw, hh,
+                                                geometry=geo, field=field))
     if want_veil:
         from .veil import render_veil
         out.update(render_veil(pos, width, height, hw, hh, dc.veil_spread, dc.veil_falloff, dc.veil_gain))

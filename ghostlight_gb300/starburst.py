@@ -1,9 +1,16 @@
 """Matrix-DFT starburst on the tensor cores (row d of the flare path).
 
-Field form of the reference's per-wavelength triple product
-(ghostlight/src/mdft_render.cu:137-173): E_l = W_y A W_x^T, I_l = |E_l|^2,
-out_c = sum_l w_c(l) I_l, with
-W[k][j] = exp(-2 pi i s_l (j - (n-1)/2)(k - c)).
+Two forms of the per-wavelength triple product on the same GEMMs:
+
+* the reference's own engine (ghostlight/src/mdft_render.cu:199-340), the
+  exact pixel-box integral of the intensity through the compact pupil
+  autocorrelation C: I_l = Re(P_y C P_x^T), P[k][m] = sinc(s_l m)
+  exp(-2 pi i s_l m (k - c)) (``mdft_box_starburst_layer``, the MDFT engine
+  of render_source_flare);
+* the field form E_l = W_y A W_x^T, I_l = |E_l|^2, out_c = sum_l w_c(l) I_l,
+  W[k][j] = exp(-2 pi i s_l (j - (n-1)/2)(k - c)): the pupil sampled at the
+  pixel centres, without the box integral (``starburst_layer``,
+  ``mdft_starburst_eform``).
 
 Forms: ``"split_bf16"`` (three-term split-BF16 tcgen05 products, FP32
 accumulation in tensor memory), ``"tf32"`` (tcgen05 kind::tf32) and ``"fp32"``
@@ -13,6 +20,8 @@ resident in HBM.
 from __future__ import annotations
 
 import ctypes as C
+import math
+import threading
 
 import numpy as np
 
@@ -30,7 +39,7 @@ class MdftPlan:
     """K: output side, or (Kx, Ky) for a Kx-wide, Ky-high output."""
 
     def __init__(self, n: int, K, scale_x, scale_y, weights_rgb, form="split_bf16",
-                 center_x=None, center_y=None, stream=None):
+                 center_x=None, center_y=None, stream=None, box=False, red_center=None):
         import torch
         self._lib = _native.load()
         Kx, Ky = (int(K), int(K)) if np.isscalar(K) else (int(K[0]), int(K[1]))
@@ -48,9 +57,11 @@ class MdftPlan:
         st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
         D = C.c_double * self.n_lambda
         h = C.c_void_p()
-        _native.check(self._lib.gl_mdft_plan_create2(
+        self.box = bool(box)
+        rc = 0.5 * (self.n - 1) if red_center is None else float(red_center)
+        _native.check(self._lib.gl_mdft_plan_create3(
             self.n, self.Kx, self.Ky, self.n_lambda, D(*sx), D(*sy), cx, cy,
-            (C.c_float * w.size)(*w.reshape(-1)), FORMS[form], st, C.byref(h)), "mdft")
+            (C.c_float * w.size)(*w.reshape(-1)), FORMS[form], int(self.box), rc, st, C.byref(h)), "mdft")
         self._h = h
 
     def set_center(self, center_x: float, center_y: float, stream=None):
@@ -71,6 +82,26 @@ class MdftPlan:
         _native.check(self._lib.gl_mdft_plan_execute2(self._h, pupil.contiguous().data_ptr(), out_r.data_ptr(),
                                                       out_g.data_ptr(), out_b.data_ptr(), int(bool(accumulate)), st),
                       "mdft")
+        return _native.last_launch_count()
+
+    def execute_window(self, operand, out_r, out_g, out_b, x0, y0, win_w, win_h, tint=None, stream=None,
+                       accumulate=True):
+        """execute into (H, W) planes: plan pixel (l, k) -> plane pixel
+        (y0 + l, x0 + k) for l < win_h, k < win_w; ``tint`` (r, g, b) scales
+        the weights of this launch."""
+        import torch
+        if not (operand.is_cuda and operand.dtype == torch.float32 and operand.shape == (self.n, self.n)):
+            raise ValueError("mdft: operand must be a float32 CUDA (n, n) tensor")
+        H, W = out_r.shape
+        for t in (out_r, out_g, out_b):
+            if not (t.is_cuda and t.dtype == torch.float32 and t.is_contiguous() and tuple(t.shape) == (H, W)):
+                raise ValueError("mdft: outputs must be three contiguous float32 CUDA (H, W) tensors")
+        st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        tr = (C.c_float * 3)(*(tint if tint is not None else (1.0, 1.0, 1.0)))
+        _native.check(self._lib.gl_mdft_plan_execute3(self._h, operand.contiguous().data_ptr(), out_r.data_ptr(),
+                                                      out_g.data_ptr(), out_b.data_ptr(), int(bool(accumulate)),
+                                                      int(W), int(H), int(x0), int(y0), int(win_w), int(win_h), tr,
+                                                      st), "mdft")
         return _native.last_launch_count()
 
     def set_launch(self, ctas: int = 0):
@@ -248,6 +279,23 @@ class SpritePlan:
             float(px_mm_x), float(px_mm_y), int(rx), int(ry), float(gain), C.c_void_p(out_r.data_ptr()),
             C.c_void_p(out_g.data_ptr()), C.c_void_p(out_b.data_ptr()), int(W), int(H), C.c_void_p(st)),
             "sprite_splat")
+
+    def autocorr(self, pupil, mc: int, out, stream=None) -> None:
+        """The compact autocorrelation of the pupil at lags |l| <= mc into
+        ``out`` (rows x cols float32 CUDA, rows, cols >= 2 mc + 1; zeroed
+        first), scaled to one texel area per pattern period."""
+        import torch
+        st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        pupil = pupil.to(torch.float32).contiguous()
+        if tuple(pupil.shape) != (self.N, self.N):
+            raise ValueError("autocorr: pupil must be (N, N)")
+        if not (out.is_cuda and out.dtype == torch.float32 and out.is_contiguous() and out.dim() == 2):
+            raise ValueError("autocorr: output must be a contiguous float32 CUDA matrix")
+        self._pupil = pupil
+        _native.check(_native.load().gl_sprite_plan_autocorr(self._h, C.c_void_p(pupil.data_ptr()), int(mc),
+                                                             C.c_void_p(out.data_ptr()), int(out.shape[1]),
+                                                             int(out.shape[0]), C.c_void_p(st)), "autocorr")
+        self.M = 0
 
     def read(self):
         """(PSF (N, N) before normalisation, sprite (M, M, 3), PSF energy)."""
@@ -460,6 +508,12 @@ def sprite_starburst_layer(lens, calibration, config, sources_px, width: int, he
     if len(src) == 0:
         return out
     spec = starburst_spectrum(config)
+    with _PLAN_LOCK:
+        return _sprite_layer_locked(lens, config, g, spec, src, field, out)
+
+
+def _sprite_layer_locked(lens, config, g, spec, src, field, out):
+    import torch
     plan, baked = _sprite_plan(g["N"], spec)
     ax, ay = (float(np.float32(field[0])), float(np.float32(field[1]))) if field is not None else (0.0, 0.0)
     off_axis = abs(ax) > 1e-5 or abs(ay) > 1e-5
@@ -485,10 +539,98 @@ def sprite_starburst_layer(lens, calibration, config, sources_px, width: int, he
     return out
 
 
+def mdft_box_starburst_layer(lens, calibration, config, sources_px, width: int, height: int, sensor_half_w: float,
+                             sensor_half_h: float, geometry=None, field=None, form: str = "split_bf16"):
+    """The starburst layer by the reference's matrix-DFT engine
+    (render_starburst's MDFT fork, starburst_render.cu:926-967, and
+    mdft_starburst, mdft_render.cu:199-340), on the tensor cores.
+
+    The effective pupil, throughput, spectral table, texel pitch and gain are
+    the sprite engine's (the reference shares them); C is the pupil's compact
+    autocorrelation (four FFT passes on the device, gl_sprite_plan_autocorr);
+    each source adds the exact pixel-box integral of the intensity over its
+    window of half a pattern period, I_l = Re(P_y C P_x^T) per wavelength with
+    cmf (lambda_ref / lambda)^2, times (px_x px_y) / (dx_x dx_y) x gain x the
+    source colour.  ``form``: the GEMM form ("split_bf16", "tf32", "fp32").
+    Returns {"starburst_r", "starburst_g", "starburst_b"} (H, W) tensors."""
+    import torch
+    f = np.float32
+    g = geometry or sprite_geometry(calibration, config, sources_px, width, height, sensor_half_w, sensor_half_h,
+                                    front_R=lens.surfaces[0].semi_aperture if lens.surfaces else 0.0)
+    out = {k: torch.zeros((height, width), dtype=torch.float32, device="cuda")
+           for k in ("starburst_r", "starburst_g", "starburst_b")}
+    src = np.asarray(sources_px, np.float32).reshape(-1, 5)
+    if len(src) == 0:
+        return out
+    pupil, T = effective_pupil(lens, config, g, field)
+    if pupil is None:
+        return out      # past the vignette edge: no starburst
+    N = int(g["N"])
+    mc = min(int(math.ceil(float(f(g["fill"])) * float(N))) + 4, N // 2 - 1)
+    Mc = 2 * mc + 1
+    n = _round128(Mc)
+    spec = starburst_spectrum(config)
+    with _PLAN_LOCK:
+        ac = _autocorr_plan(N)
+        Cm = torch.empty((n, n), dtype=torch.float32, device="cuda")
+        ac.autocorr(pupil, mc, Cm)
+    # the reference's float32 scalars (mdft_render.cu:226-283)
+    dx_x, dx_y = f(g["sx"]), f(g["sy"])
+    px_x, px_y = f(g["px_mm_x"]), f(g["px_mm_y"])
+    Sx, Sy = f(f(N) * dx_x), f(f(N) * dx_y)
+    half_x = max(1, int(math.floor(0.5 * float(Sx) / float(px_x))))
+    half_y = max(1, int(math.floor(0.5 * float(Sy) / float(px_y))))
+    gain = f(f(g["gain"]) * f(T))
+    knorm_gain = f(f(f(px_x * px_y) / f(dx_x * dx_y)) * gain)
+    lam = spec[:, 0].astype(np.float32)
+    lam_scale = (lam / f(LAMBDA_REF_NM)).astype(np.float32)
+    k2 = ((f(LAMBDA_REF_NM) / lam) * (f(LAMBDA_REF_NM) / lam)).astype(np.float32)
+    s_x = float(px_x) / (Sx * lam_scale).astype(np.float32).astype(np.float64)
+    s_y = float(px_y) / (Sy * lam_scale).astype(np.float32).astype(np.float64)
+    w = (spec[:, 1:4] * k2[:, None]).astype(np.float32)
+    Kx, Ky = _round128(min(width, 2 * half_x + 1)), _round128(min(height, 2 * half_y + 1))
+    plan = MdftPlan(n, (Kx, Ky), s_x, s_y, w, form, center_x=0.0, center_y=0.0, box=True, red_center=float(mc))
+    try:
+        for (px, py, r, gg, b) in src:
+            kx0, kx1 = max(0, int(math.floor(px)) - half_x), min(width, int(math.floor(px)) + half_x + 1)
+            ky0, ky1 = max(0, int(math.floor(py)) - half_y), min(height, int(math.floor(py)) + half_y + 1)
+            if kx1 <= kx0 or ky1 <= ky0:
+                continue        # the source's window lies off the frame
+            plan.set_center(float(px) - 0.5 - kx0, float(py) - 0.5 - ky0)
+            tint = (float(knorm_gain * f(r)), float(knorm_gain * f(gg)), float(knorm_gain * f(b)))
+            plan.execute_window(Cm, out["starburst_r"], out["starburst_g"], out["starburst_b"], kx0, ky0,
+                                kx1 - kx0, ky1 - ky0, tint=tint)
+        torch.cuda.synchronize()
+        code = plan.status()
+    finally:
+        plan.close()
+    if code:
+        raise _native.GhostlightError("starburst: device pipeline wait timed out (code %d)" % code)
+    return out
+
+
 # resident sprite plans by (device, grid, spectrum), least recently used
-# first; each keeps its last bake and the key it was baked for
+# first; each keeps its last bake and the key it was baked for.  _PLAN_LOCK
+# guards the caches and every bake / splat / autocorrelation on a cached plan
+# (a plan evicted by one thread must not be in use by another).
 _SPRITE_PLANS = {}
 _SPRITE_PLAN_CAP = 4
+_AUTOCORR_PLANS = {}
+_PLAN_LOCK = threading.RLock()
+
+
+def _autocorr_plan(N):
+    """A resident FFT plan of grid N for the matrix-DFT autocorrelation
+    (spectrum unused), one per (device, grid)."""
+    import torch
+    key = (torch.cuda.current_device(), int(N))
+    p = _AUTOCORR_PLANS.get(key)
+    if p is None:
+        while len(_AUTOCORR_PLANS) >= _SPRITE_PLAN_CAP:
+            _AUTOCORR_PLANS.pop(next(iter(_AUTOCORR_PLANS))).close()
+        p = SpritePlan(N, np.array([[LAMBDA_REF_NM, 1.0, 1.0, 1.0]], np.float32))
+        _AUTOCORR_PLANS[key] = p
+    return p
 
 
 def _sprite_plan(N, spec):

@@ -405,6 +405,30 @@ int gl_mdft_plan_set_launch(gl_mdft_plan* plan, int ctas);
  * overwriting them (a starburst layered onto a ghost image). */
 int gl_mdft_plan_execute2(gl_mdft_plan* plan, const float* d_pupil, float* d_out_r,
                           float* d_out_g, float* d_out_b, int accumulate, void* stream);
+/* The reference's own matrix-DFT engine, mdft_starburst (mdft_render.cu:
+ * 199-340): the exact pixel-box integral of the intensity through the
+ * compact pupil autocorrelation C (Mc x Mc real, Mc = 2 mc + 1, padded with
+ * zeros to n x n; gl_sprite_plan_autocorr builds it):
+ *   W_x[k][j] = sinc(s_l (j - mc)) exp(-2 pi i s_l (j - mc)(k - center_x)),
+ *   I_l = Re(W_y C W_x^T),  out_c += weights_rgb[3l+c] tint_c I_l,
+ * s_l = pixel pitch / pattern period at wavelength l (the reference's
+ * px / S_l), center = source pixel - 0.5 - window origin.  box = 1 selects
+ * this form (Re E accumulated); box = 0 is the field form |E|^2 above;
+ * red_center is the reduction index of zero lag (mc for the box form,
+ * (n - 1) / 2 for the field form).  Same GEMMs, operand layout and forms as
+ * gl_mdft_plan_create2. */
+int gl_mdft_plan_create3(int n, int Kx, int Ky, int n_lambda, const double* scale_x,
+                         const double* scale_y, double center_x, double center_y,
+                         const float* weights_rgb, int form, int box, float red_center,
+                         void* stream, gl_mdft_plan** out);
+/* execute2 with the output placed in larger planes: plan pixel (l, k) ->
+ * plane pixel (y0 + l, x0 + k) of out_w x out_h planes, for l < win_h,
+ * k < win_w (the reference's clamped window around the source, :275-290);
+ * tint_rgb (3 floats, NULL = 1) scales the weights for this launch (the
+ * source colour).  accumulate = 0 clears the whole planes first. */
+int gl_mdft_plan_execute3(gl_mdft_plan* plan, const float* d_pupil, float* d_out_r,
+                          float* d_out_g, float* d_out_b, int accumulate, int out_w, int out_h,
+                          int x0, int y0, int win_w, int win_h, const float* tint_rgb, void* stream);
 
 /* Pupil amplitude of the lens's stop on an N x N grid, 4 x 4 supersampled
  * (build_pupil_kernel, starburst_render.cu:155-191, stop term only): grid
@@ -477,6 +501,14 @@ int gl_sprite_plan_splat(gl_sprite_plan* plan, const float* sources, int n_src, 
                          float* d_out_b, int width, int height, void* stream);
 int gl_sprite_plan_read(gl_sprite_plan* plan, float* d_psf, float* d_sprite, double* energy, int* M, void* stream);
 int gl_sprite_plan_destroy(gl_sprite_plan* plan);
+/* The matrix-DFT engine's compact autocorrelation (mdft_render.cu:233-262):
+ * G = FFT2(|FFT2(A)|^2) of the N x N pupil amplitude d_pupil, at the lags
+ * |l| <= mc, scaled by 1 / (G[0][0] N^2) so the pattern sums to one texel
+ * area per period: d_C[(ly + mc) ldc + (lx + mc)], rows x ldc floats, zeroed
+ * first (the padding of the GEMM operand).  Four FFT passes on the plan's
+ * buffers, the scale read on the device; invalidates the plan's sprite. */
+int gl_sprite_plan_autocorr(gl_sprite_plan* plan, const float* d_pupil, int mc, float* d_C, int ldc, int rows,
+                            void* stream);
 
 /* ---- Serving: resident lenses and stream-ordered requests -----------------
  * The reference renders one flare per blocking call under process-wide

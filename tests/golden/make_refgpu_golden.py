@@ -12,11 +12,14 @@ oracle/ref_driver.cpp.  Three things are written to ``--out``:
   reference;
 * ``refgpu_images.npz`` + ``refgpu_meta.json`` — its images of the seeded
   configuration-1, -2 and -4 lenses with deterministic sampling
-  (concentration off), for tests/test_gpu_refgpu.py;
+  (concentration off); ``--pack DIR`` turns them into the committed fixtures
+  ``refgpu_seeded.npz`` / ``refgpu_seeded.json`` (15 mantissa bits kept, as
+  make_refgolden.py packs) for tests/test_gpu_refgpu.py;
 * ``refgpu_timing.json`` — its wall time and kernel-stage time on the
   configuration-2 frame (24 surfaces, 31 wavelengths, 2048^2, 15 deg).
 
-    python tests/golden/make_refgpu_golden.py --out gpurun_out/refgpu
+    python tests/golden/make_refgpu_golden.py --out OUTDIR      (GPU host)
+    python tests/golden/make_refgpu_golden.py --pack OUTDIR     (packs into tests/golden)
 """
 from __future__ import annotations
 
@@ -126,11 +129,31 @@ def timing(pins, meta, reps=5):
     return res
 
 
+def pack_into_fixtures(src_dir):
+    from make_refgolden import pack   # same directory
+    src = pathlib.Path(src_dir)
+    imgs = np.load(src / "refgpu_images.npz")
+    meta = json.loads((src / "refgpu_meta.json").read_text())
+    out = {}
+    for k in imgs.files:
+        out[k] = pack(imgs[k])
+        meta[k.split("/")[0]]["shape"] = list(imgs[k].shape)
+    meta["selfcheck"] = json.loads((src / "refgpu_selfcheck.json").read_text())
+    np.savez_compressed(HERE / "refgpu_seeded.npz", **out)
+    (HERE / "refgpu_seeded.json").write_text(json.dumps(meta, indent=1))
+    print("refgpu_seeded.npz", (HERE / "refgpu_seeded.npz").stat().st_size // 1024, "KB")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default=str(HERE))
     ap.add_argument("--skip-timing", action="store_true")
+    ap.add_argument("--pack", default="")
     args = ap.parse_args()
+    if args.pack:
+        sys.path.insert(0, str(HERE))
+        pack_into_fixtures(args.pack)
+        return
     out = pathlib.Path(args.out)
     out.mkdir(parents=True, exist_ok=True)
     pins = np.load(HERE / "ref_pins.npz")
