@@ -206,6 +206,7 @@ def run_gpu(args, rank, world):
         t_batched = timed(graph.replay, args.steps, args.warmup, after=read_kernel_events)
     torch.cuda.synchronize()
     plan.set_timing()
+    frame_host = torch.stack(outs).cpu().numpy()       # the frame of the last timed replay
     traced_render, traced_probe = plan.traced_split()
     if args.quick:
         t_plain = [float("nan")]
@@ -298,7 +299,7 @@ def run_gpu(args, rank, world):
         res["starburst_psf"] = cfg3
     if frame_res is not None:
         res["full_flare_frame"] = frame_res
-    return res, plan
+    return res, plan, frame_host
 
 
 # ---- starburst precision sweep + PSF/veil convolution (cfg3) -----------------
@@ -768,29 +769,69 @@ def run_sweep(args):
     return res
 
 
-def cpu_baseline(plan, lens, cal, budget_s=8.0):
-    """The oracle port of the reference renderer (FP32, OpenMP over every host
-    core) on a bounded sample: a subset of the frame's pairs."""
+def cpu_baseline(plan, lens, cal, gpu_frame):
+    """The CPU leg, timed on the host cores and used as the checker of the
+    timed frame:
+
+    * timing: the reference's own code (oracle/_ref, built from the staged
+      reference sources: its filter, grids and trace_ghost_ray in the
+      ghost_kernel main path with the three-pass probe cull) renders the whole
+      frame once on every core ("reference"); where it is not built, the
+      oracle's FP32 port of the same path over the frame's kept pairs
+      ("port");
+    * parity: the frame the GPU rendered in the timed loop (all three planes,
+      2048^2, colour-corrected) against the FP64 oracle's render of the same
+      kept pairs over the same per-ghost grids and spectral table: relative L2
+      and the largest per-pixel error relative to the frame's peak.  Pairs the
+      off-sensor cull dropped are not rendered on either side (the cull is
+      checked against uncut renders by tests/test_gpu_ghost.py)."""
     from oracle import oracle as O
     n_threads = os.cpu_count() or 1
-    pairs, boosts = plan.pairs, plan.boosts
-    # sample: every k-th pair until the estimated work fits the budget
-    order = np.arange(len(pairs))
-    sel, rays = [], 0
-    for i in order[:: max(1, len(order) // 24)]:
-        g = plan.grids[int(plan.pair_grid[i])]
-        sel.append(i)
-        rays += len(g) * N_SPEC
+    hw, hh = cal["sensor_half_w"], cal["sensor_half_h"]
+    hits = plan.pair_hits()
+    keep = np.nonzero(hits > 0)[0]
+    src = _sources()
     t0 = time.perf_counter()
-    O.render(lens.records(), pairs[sel], boosts[sel], _sources(), plan.grids, plan.spec,
-             cal["sensor_half_w"], cal["sensor_half_h"], 512, 512, 1000.0,
-             pair_grid=plan.pair_grid[sel], fp64=False, n_threads=n_threads)
-    dt = time.perf_counter() - t0
-    rps = rays / dt
-    return {"value": rps / plan.rays, "unit": UNIT, "cores": n_threads, "kind": "port",
-            "sample": "%d of %d pairs (%d ray-wavelength traces, %.1f s), FP32 oracle port of "
-                      "ghost_kernel's main path, scaled to the full frame" % (len(sel), len(pairs), rays, dt),
-            "rays_per_s": rps}
+    want = O.render(lens.records(), plan.pairs[keep], plan.boosts[keep], src, plan.grids, plan.spec, hw, hh, W, H,
+                    1000.0, pair_grid=plan.pair_grid[keep], fp64=True, n_threads=n_threads)
+    t_fp64 = time.perf_counter() - t0
+    if plan.apply_correction:
+        want = np.einsum("ij,jhw->ihw", plan.correction.astype(np.float64), want)
+    got = gpu_frame.astype(np.float64)
+    rel = float(np.linalg.norm(got - want) / max(np.linalg.norm(want), 1e-300))
+    mx = float(np.abs(got - want).max() / max(float(np.abs(want).max()), 1e-300))
+    parity = {"rel_l2": rel, "max_err_rel_peak": mx, "tolerance": 1e-3, "pass": rel <= 1e-3,
+              "against": "FP64 oracle (oracle/gl_oracle_impl.h, double), the %d kept pairs of the timed frame, "
+                         "2048^2 x 3 planes, same grids / spectral table / colour correction" % len(keep),
+              "oracle_s": t_fp64, "oracle_cores": n_threads}
+    try:
+        from oracle import ref as R
+        use_ref = R.available()
+    except Exception:
+        use_ref = False
+    if use_ref:
+        raw, rcal = _reference_lens("cfg2_wide_angle_24")
+        rpairs, rboosts = R.filter_pairs(raw, hw, hh, MIN_INTENSITY)
+        sides = np.array([adaptive_side(fp, hw, hh) for fp in R.ghost_footprints(raw, rpairs)], np.int32)
+        spec, corr = R.spectral_table(N_SPEC)
+        t0 = time.perf_counter()
+        _, st = R.render_frame_cpu(raw, rpairs, rboosts, sides, src[0], spec, corr, hw, hh, W, H, 1000.0,
+                                   cull=True, n_threads=n_threads)
+        dt = time.perf_counter() - t0
+        base = {"value": 1.0 / dt, "unit": UNIT, "cores": st["threads"], "kind": "reference",
+                "sample": "one whole frame (probe cull + %d kept pairs, %d ray-wavelength traces, %.2f s) with the "
+                          "reference's trace_ghost_ray" % (st["kept_pairs"], st["render_traces"] + st["probe_traces"], dt),
+                "rays_per_s": (st["render_traces"] + st["probe_traces"]) / dt}
+    else:
+        rays = sum(len(plan.grids[int(plan.pair_grid[i])]) for i in keep) * N_SPEC
+        t0 = time.perf_counter()
+        O.render(lens.records(), plan.pairs[keep], plan.boosts[keep], src, plan.grids, plan.spec, hw, hh, W, H,
+                 1000.0, pair_grid=plan.pair_grid[keep], fp64=False, n_threads=n_threads)
+        dt = time.perf_counter() - t0
+        base = {"value": 1.0 / dt, "unit": UNIT, "cores": n_threads, "kind": "port",
+                "sample": "one whole frame of the %d kept pairs (%d ray-wavelength traces, %.2f s), the oracle's "
+                          "FP32 port of ghost_kernel's main path" % (len(keep), rays, dt), "rays_per_s": rays / dt}
+    return base, parity
 
 
 def frame_config(n_pairs):
@@ -852,6 +893,7 @@ def run_reference(args):
     step = sum(ts) / len(ts)
     fps = 1.0 / step
     cfg1 = reference_cfg1(R, n_threads)
+    gpu = reference_gpu_frame(R, raw, cal, pairs, sides, args) if not args.no_reference_gpu else None
     return {"metric": METRIC, "value": fps, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -864,7 +906,64 @@ def run_reference(args):
                                        "ray-wavelength traces) with the reference's trace_ghost_ray"
                                        % (st["kept_pairs"], st["render_traces"] + st["probe_traces"])},
             "e2e": {"value": fps, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "cfg1": cfg1}
+            "cfg1": cfg1, "gpu": gpu}
+
+
+def reference_gpu_frame(R, raw, cal, pairs, sides, args):
+    """The reference's own CUDA renderer (its core library built for sm_103a
+    from the staged sources, oracle/build.py:build_ref_gpu) on the same frame:
+    render_source_flare at 15 deg, concentration off, the off-sensor cull on,
+    31 wavelengths, 2048^2; its API takes one pupil grid per call, so the
+    frame is one call per grid side with a GhostFilter INCLUDE list of the
+    pairs of that side (the per-ghost adaptive grids).  Each call is timed by
+    wall clock (its host filter, uploads, probes, render, colour correction
+    and the D2H of the planes); its own stage timing (collect_stats) gives the
+    device part (ms_kernel).  Also the reference's single-call default
+    (one 256^2 grid, concentrated sampling with adaptive budgets)."""
+    try:
+        R._load_gpu()
+    except Exception as e:  # noqa: BLE001
+        return {"unavailable": "the reference's CUDA renderer did not build here: %s" % str(e).splitlines()[0]}
+    hw, hh = cal["sensor_half_w"], cal["sensor_half_h"]
+    centre = R.solve_source(raw, cal, 0.0, 0.0, hw, hh)
+    off = np.array([[math.radians(SOURCE_DEG) - centre["angle_x"], -centre["angle_y"], 1.0]], np.float32)
+    groups = {}
+    for (a, b), sd in zip(pairs, sides):
+        groups.setdefault(int(sd), []).append((int(a), int(b)))
+
+    def cfg_for(side, conc=0, stats=0):
+        return R.RefGpuCfg(ray_grid=side, spectral_samples=N_SPEC, pupil_jitter=0, jitter_seed=0,
+                           sensor_half_w=hw, sensor_half_h=hh, flare_gain=1000.0, min_ghost_intensity=MIN_INTENSITY,
+                           cull_dead_pairs=1, concentrate_samples=conc, adaptive_sample_budgets=conc,
+                           source_x=0.5, source_y=0.5, collect_stats=stats)
+
+    def frame():
+        ms = 0.0
+        for side, grp in sorted(groups.items()):
+            _, _, t, _ = R.gpu_render(raw, W, H, cfg_for(side), calib=cal, offsets=off, include=grp)
+            ms += t
+        return ms
+
+    frame()                                          # warm: allocations, caches
+    steps = max(3, min(args.steps, 10))
+    with ClockSampler(0) as clk:
+        walls = [frame() for _ in range(steps)]
+    kern = 0.0
+    for side, grp in sorted(groups.items()):
+        _, _, _, st = R.gpu_render(raw, W, H, cfg_for(side, stats=1), calib=cal, offsets=off, include=grp)
+        kern += st["ms_kernel"]
+    dflt = []
+    for _ in range(3):
+        _, _, t, st = R.gpu_render(raw, W, H, cfg_for(256, conc=1), calib=cal, offsets=off)
+        dflt.append(t)
+    wall = float(np.median(walls))
+    return {"frames_per_s": 1e3 / wall, "wall_ms_per_frame": wall, "walls_ms": walls,
+            "device_ms_per_frame": kern, "calls_per_frame": len(groups),
+            "how": "reference render_source_flare (ghostlight/src/SourceFlareRenderer.cpp:24), one call per grid "
+                   "side with a GhostFilter INCLUDE list; wall clock per call; device_ms = the renderer's own "
+                   "ms_kernel stage (probes + render + colour correction)",
+            "default_grid256_concentrated_wall_ms": float(np.median(dflt)),
+            "clocks": clk.summary()}
 
 
 CFG1_W = CFG1_H = 512
@@ -909,6 +1008,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-reference-gpu", action="store_true",
+                    help="reference arm: skip the timing of the reference's CUDA renderer")
     ap.add_argument("--quick", action="store_true",
                     help="batched timing only (no plain / e2e / CPU legs): for profiler runs")
     ap.add_argument("--serve-seconds", type=float, default=30.0)
@@ -947,11 +1048,11 @@ def main():
     if world > 1:
         import torch
         torch.distributed.init_process_group("nccl")
-    res, plan = run_gpu(args, rank, world)
+    res, plan, gpu_frame = run_gpu(args, rank, world)
     if rank == 0:
         lens, cal = _workload()
         if not (args.no_cpu_baseline or args.quick):
-            res["cpu_baseline"] = cpu_baseline(plan, lens, cal)
+            res["cpu_baseline"], res["parity"] = cpu_baseline(plan, lens, cal, gpu_frame)
         if not args.quick:
             res["anamorphic_sweep"] = run_sweep(args)
         if not args.quick and args.serve_seconds > 0:

@@ -29,6 +29,21 @@ def _psf_spectrum(config):
     return spec
 
 
+def splat_footprint(splat_sigma_um, mm_pp):
+    """(sigma, radius) of the Gaussian splat in pixels, in the reference's
+    float32 (psf_render.cu:426-440): sigma = um / (mm_pp 1000), radius =
+    ceil(2.5 sigma) in [1, 16]; (0, 0) selects the bilinear splat.  The
+    float32 product matters: 2.5 x 1.6f rounds to exactly 4, where float64
+    gives 4.00000006 and a radius of 5."""
+    f = np.float32
+    mm = f(mm_pp)
+    sigma = f(f(splat_sigma_um) / f(mm * f(1000.0))) if mm > 0 else f(0.0)
+    if not sigma > 0:
+        return 0.0, 0
+    radius = min(16, max(1, int(math.ceil(float(f(f(2.5) * sigma))))))
+    return float(sigma), radius
+
+
 def render_psf(sources, lens, config) -> dict:
     """sources: (N, 5) [angle_x, angle_y, r, g, b] or (N, 7) with
     [target_x_mm, target_y_mm] appended.  Returns the reference's keys; the
@@ -70,8 +85,7 @@ def render_psf(sources, lens, config) -> dict:
                       int(getattr(cfg, "aperture_blades", 0)), float(getattr(cfg, "aperture_rotation", 0.0)))
     grid = np.ascontiguousarray(grid, np.float32)
     spec = np.ascontiguousarray(_psf_spectrum(cfg), np.float32)
-    sigma = float(cfg.splat_sigma_um) / (mm_pp * 1000.0) if mm_pp > 0 else 0.0
-    radius = min(16, max(1, int(math.ceil(2.5 * sigma)))) if sigma > 0 else 0
+    sigma, radius = splat_footprint(cfg.splat_sigma_um, mm_pp)
     out = torch.zeros((3, comp_h, comp_w), dtype=torch.float32, device="cuda")
     P = C.POINTER
     _native.check(lib.gl_psf_render(arr, len(arr), gs, n, grid.ctypes.data_as(P(gl_pupil_sample)), len(grid),

@@ -322,14 +322,14 @@ def _load_gpu():
     vp, i, f = C.c_void_p, C.c_int, C.c_float
     lib.refgpu_sizeof_cfg.restype = i
     lib.refgpu_render.argtypes = [vp, i, f, vp, C.POINTER(RefGpuCfg), vp, i, i, i, vp, vp,
-                                  C.POINTER(C.c_double), vp]
+                                  C.POINTER(C.c_double), vp, vp, i]
     lib.refgpu_render.restype = i
     assert lib.refgpu_sizeof_cfg() == C.sizeof(RefGpuCfg)
     _gpu = lib
     return lib
 
 
-def gpu_render(surfs, W, H, cfg, calib=None, focal_length=0.0, offsets=None, starburst=False):
+def gpu_render(surfs, W, H, cfg, calib=None, focal_length=0.0, offsets=None, starburst=False, include=None):
     """render_point_flare (offsets None) or render_source_flare of the
     reference's GPU renderer.  Returns (ghost (3,H,W), starburst (3,H,W) or
     None, wall ms of the call, stats dict or None)."""
@@ -347,11 +347,13 @@ def gpu_render(surfs, W, H, cfg, calib=None, focal_length=0.0, offsets=None, sta
     ms = C.c_double()
     stats = np.full(8, -1.0)
     buf, n = _sp(surfs)
+    inc = None if include is None else np.ascontiguousarray(include, np.int32).reshape(-1, 2)
     rc = lib.refgpu_render(buf, n, focal_length, None if cal is None else cal.ctypes.data_as(C.c_void_p),
                            C.byref(cfg), None if offs is None else offs.ctypes.data_as(C.c_void_p), n_off,
                            W, H, ghost.ctypes.data_as(C.c_void_p),
                            None if star is None else star.ctypes.data_as(C.c_void_p), C.byref(ms),
-                           stats.ctypes.data_as(C.c_void_p))
+                           stats.ctypes.data_as(C.c_void_p),
+                           None if inc is None else inc.ctypes.data_as(C.c_void_p), 0 if inc is None else len(inc))
     if rc != 0:
         raise RuntimeError("reference GPU render failed")
     st = None

@@ -751,9 +751,12 @@ extern "C" int refgpu_sizeof_cfg() { return (int)sizeof(RefGpuCfg); }
 // stats (8 doubles, or NULL; filled when collect_stats): the renderer's own
 // GhostRenderStats ms_grid_build, ms_upload, ms_kernel, ms_download,
 // ms_total, n_pairs, traces_total, traces_on_sensor.
+// include_ab: n_include (a, b) pairs for GhostFilter INCLUDE (render_config.h:
+// 51-62), or NULL for every filtered pair.
 extern "C" int refgpu_render(const gl_surface* surfs, int n, float focal_length, const float* calib13,
                              const RefGpuCfg* g, const float* offsets, int n_offsets, int W, int H,
-                             float* out_ghost, float* out_star, double* ms, double* stats)
+                             float* out_ghost, float* out_star, double* ms, double* stats,
+                             const int* include_ab, int n_include)
 {
     OpticalSystem* L = make_lens(surfs, n);
     L->focal_length = focal_length;
@@ -788,6 +791,11 @@ extern "C" int refgpu_render(const gl_surface* surfs, int n, float focal_length,
     cfg.diffraction.pupil_fill = g->pupil_fill; cfg.diffraction.scale_trim = g->scale_trim;
     cfg.diffraction.use_survivor_mask = g->use_survivor_mask != 0;
     cfg.collect_stats = g->collect_stats != 0;
+    if (include_ab && n_include > 0)
+    {
+        cfg.ghost_filter.mode = GhostFilter::Mode::INCLUDE;
+        for (int i = 0; i < n_include; ++i) cfg.ghost_filter.pairs.emplace_back(include_ab[2 * i], include_ab[2 * i + 1]);
+    }
     FlareBuffers out;
     const auto t0 = std::chrono::steady_clock::now();
     const bool ok = offsets ? render_source_flare(W, H, offsets, n_offsets, *L, c, cfg, out)

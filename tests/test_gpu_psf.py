@@ -26,8 +26,8 @@ def test_psf_grid_matches_oracle(pins, mode, sigma_um, mono):
     from tests_psf_cells import cells_of
     cells = cells_of(lens, src, mode)
     mm_pp = float(np.float32(cfg.tile_extent_mm) / np.float32(cfg.tile_w))
-    sigma = sigma_um / (mm_pp * 1000.0)
-    radius = min(16, max(1, int(np.ceil(2.5 * sigma)))) if sigma > 0 else 0
+    from ghostlight_gb300.psf_grid import splat_footprint
+    sigma, radius = splat_footprint(sigma_um, mm_pp)
     want = PO.render(lens.records(), cells, src[:, 2:5], pupil_grid(lens, 24, 0, 0, 0, 0.0), _psf_spectrum(cfg),
                      48, 40, 2, 96, 80, mm_pp, mono, sigma, radius)
     assert want.sum() > 0
