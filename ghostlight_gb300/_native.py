@@ -115,6 +115,9 @@ def _declare(lib):
     lib.gl_veil_plan_execute.argtypes = [vp, vp, i, P(gl_veil_params), vp, vp, vp, vp]
     lib.gl_veil_plan_destroy.argtypes = [vp]
     lib.gl_calibrate_lens.argtypes = [P(gl_surface), i, f, f, P(gl_lens_calibration)]
+    lib.gl_calibrate_lens2.argtypes = [P(gl_surface), i, f, f, i, P(gl_lens_calibration)]
+    lib.gl_solve_source_angle2.argtypes = [P(gl_surface), i, P(gl_lens_calibration), f, f, f, f, i,
+                                           P(gl_source_solve)]
     lib.gl_solve_source_angle.argtypes = [P(gl_surface), i, P(gl_lens_calibration), f, f, f, f,
                                           P(gl_source_solve)]
     lib.gl_source_map_screen.argtypes = [P(gl_source_solve), f, f, P(f), P(f)]

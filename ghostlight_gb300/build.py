@@ -32,7 +32,7 @@ EXACT = ["-fmad=false", "-ftz=false", "-prec-div=true", "-prec-sqrt=true"]
 
 UNITS = {
     "gl_host.cpp": [],
-    "gl_calib.cpp": [],
+    "gl_setup.cpp": [],
     "gl_coat.cpp": [],
     "gl_filter.cu": EXACT,
     "gl_ghost.cu": FAST,

@@ -1,7 +1,9 @@
 """Per-lens first-order setup: calibrate_lens (lens_calibration.cpp:344) and
 the screen-position -> field-angle solve (source_map.cpp:182), both by
-tracing the spawn disc in the reference's float32 arithmetic
-(csrc/gl_calib.cpp), so the values equal the reference's."""
+tracing the spawn disc (csrc/gl_setup.cpp).  ``precision="fp32"`` runs the
+reference's float32 arithmetic, so the values equal the reference's bit for
+bit; ``precision="fp64"`` runs the same measurement with double-precision
+traces and solves."""
 from __future__ import annotations
 
 import ctypes as C
@@ -14,15 +16,22 @@ from .config import LensCalibration
 D_LINE_NM = 587.56
 
 SOLVED, CONTINUED, FALLBACK = 0, 1, 2
+PRECISIONS = {"fp32": 0, "fp64": 1}
 
 
-def calibrate_lens(lens, d_line_nm: float = D_LINE_NM) -> LensCalibration:
+def _precision(p) -> int:
+    if p not in PRECISIONS:
+        raise ValueError("precision must be 'fp32' or 'fp64'")
+    return PRECISIONS[p]
+
+
+def calibrate_lens(lens, d_line_nm: float = D_LINE_NM, precision: str = "fp32") -> LensCalibration:
     """Covered field, image circle, per-axis EFL, entrance pupil, f-number."""
     lib = _native.load()
     arr = lens.to_array()
     out = gl_lens_calibration()
-    _native.check(lib.gl_calibrate_lens(arr, len(arr), float(getattr(lens, "focal_length", 0.0) or 0.0),
-                                        float(d_line_nm), C.byref(out)), "calibrate_lens")
+    _native.check(lib.gl_calibrate_lens2(arr, len(arr), float(getattr(lens, "focal_length", 0.0) or 0.0),
+                                         float(d_line_nm), _precision(precision), C.byref(out)), "calibrate_lens")
     return LensCalibration(**{k: float(getattr(out, k)) for k in LensCalibration.FIELDS})
 
 
@@ -64,16 +73,16 @@ def _calib_struct(calib) -> gl_lens_calibration:
 
 
 def solve_source_angle(lens, calib, ndc_x: float, ndc_y: float, eff_half_w: float,
-                       eff_half_h: float) -> SourceMapSolve:
+                       eff_half_h: float, precision: str = "fp32") -> SourceMapSolve:
     """Field angle whose spawn-disc survivors land at (ndc_x, ndc_y) of a frame
     with half extents eff_half_w x eff_half_h mm."""
     lib = _native.load()
     arr = lens.to_array() if lens is not None else None
     out = gl_source_solve()
     c = _calib_struct(calib)
-    _native.check(lib.gl_solve_source_angle(arr, 0 if arr is None else len(arr), C.byref(c), float(ndc_x),
-                                            float(ndc_y), float(eff_half_w), float(eff_half_h), C.byref(out)),
-                  "solve_source_angle")
+    _native.check(lib.gl_solve_source_angle2(arr, 0 if arr is None else len(arr), C.byref(c), float(ndc_x),
+                                             float(ndc_y), float(eff_half_w), float(eff_half_h),
+                                             _precision(precision), C.byref(out)), "solve_source_angle")
     return SourceMapSolve(out.angle_x, out.angle_y, int(out.status), out.residual_mm, out.anchor_ax, out.anchor_ay,
                           out.anchor_x, out.anchor_y, tuple(out.J), out.eff_half_w, out.eff_half_h, out.inv_tan_w,
                           out.inv_tan_h, int(out.probe_evals), out)

@@ -86,6 +86,9 @@ class RenderConfig:
     verbose: bool = False
     collect_stats: bool = False
     spectral_correction: bool = True
+    # arithmetic of the per-render source-position solve: "fp32" reproduces
+    # the reference's float32 solve bit for bit; "fp64" solves in double
+    setup_precision: str = "fp32"
 
 
 @dataclass

@@ -8,11 +8,19 @@
 //
 // This translation unit is compiled IEEE-exact (-fmad=false, IEEE division
 // and square root, no flush-to-zero), so its float arithmetic equals the
-// reference host build's except inside cosf / atan2f / fmodf, which may differ
-// in the last place.  A keep/drop decision whose estimate lies within a guard
-// band of the threshold is therefore re-evaluated on the host with the
-// identical code compiled by the host compiler; the surviving set and its
-// order are the reference's bit for bit.
+// reference host build's except inside cosf / atan2f / fmodf / sinf, which may
+// differ in the last place.  Two guards make the results the reference's:
+//  * a keep/drop decision whose estimate lies within a guard band of the
+//    threshold is re-evaluated on the host with the identical code compiled
+//    by the host compiler;
+//  * the only libm-dependent tests of a probe ray are the silhouettes of
+//    polygon and curved-blade apertures (atan2f, fmodf, cosf, sinf), so on a
+//    lens that has one the probes also run with every such clear radius
+//    scaled by 1 + 1e-6 and 1 - 1e-6; a pair whose probe outcome (which rays
+//    land, their weights and landing box) changes between the two has a ray
+//    grazing a silhouette and is traced again on the host.
+// The surviving set, its order, the area boosts and the footprints are then
+// the reference's bit for bit.
 #include "gl_internal.h"
 
 #include <cuda_runtime.h>
@@ -28,18 +36,30 @@ namespace {
 
 constexpr int kProbeThreads = 96;   // 3 intensity rays + 64 spread probes, padded
 
-struct ProbeOut {
-    float w[3];        // per-wavelength weight of the axial ray
-    int wok[3];        // 1 when that ray reached the sensor
-    float mnx, mxx, mny, mxy;
-    int valid;
-};
+using ProbeOut = FilterProbe;
+constexpr float kGraze = 1e-6f;     // relative clear-radius perturbation of the graze test
+
+bool has_silhouette(const gl_surface* s, int n)
+{
+    for (int i = 0; i < n; ++i)
+        if (s[i].aperture_shape == GL_APERTURE_POLYGON && s[i].aperture_blades >= 3) return true;
+    return false;
+}
+
+bool same_probe(const ProbeOut& x, const ProbeOut& y)
+{
+    return std::memcmp(&x, &y, sizeof(ProbeOut)) == 0;
+}
 
 __global__ void __launch_bounds__(kProbeThreads)
 filter_probe_kernel(const SurfRec* __restrict__ recs, int n, const float* __restrict__ ior_at3,
                     const float* __restrict__ ior_bf3, const int2* __restrict__ pairs,
                     float front_R, float start_z, ProbeOut* __restrict__ out)
 {
+    // blockIdx.y: the record variant (exact, then the widened and narrowed
+    // silhouettes of the graze test)
+    recs += (size_t)blockIdx.y * n;
+    out += (size_t)blockIdx.y * gridDim.x;
     __shared__ SurfRec lens[kMaxSurfaces];
     __shared__ float at[3 * kMaxSurfaces], bf[3 * kMaxSurfaces];
     __shared__ float px[64], py[64];
@@ -145,21 +165,31 @@ extern "C" int gl_filter_ghost_pairs(const gl_surface* surfaces, int n, float hw
         std::vector<float> at(3 * (size_t)n), bf(3 * (size_t)n);
         build_ior_tables(surfaces, n, lams, 3, at.data(), bf.data());
         const int np = (int)cand.size();
-        std::vector<ProbeOut> res((size_t)np);
+        const int nv = has_silhouette(surfaces, n) ? 3 : 1;         // record variants of the graze test
+        std::vector<ProbeOut> res((size_t)np * nv);
         cudaError_t e = cudaSuccess;
         auto chk = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
-        const size_t o_at = align256(sizeof(SurfRec) * n), o_bf = o_at + align256(sizeof(float) * 3 * n);
+        const size_t o_at = align256(sizeof(SurfRec) * n * nv), o_bf = o_at + align256(sizeof(float) * 3 * n);
         const size_t o_pairs = o_bf + align256(sizeof(float) * 3 * n);
         const size_t o_out = o_pairs + align256(sizeof(int2) * np);
-        const size_t need = o_out + align256(sizeof(ProbeOut) * np);
+        const size_t need = o_out + align256(sizeof(ProbeOut) * np * nv);
         int dev = 0;
         chk(cudaGetDevice(&dev));
         if (e == cudaSuccess && (dev < 0 || dev >= 64)) e = cudaErrorInvalidDevice;
-        std::vector<SurfRec> drecs((size_t)n);                      // the device probes' records
+        std::vector<SurfRec> drecs((size_t)n * nv);                 // the device probes' records
         if (e == cudaSuccess)
         {
             rc = pack_lens(surfaces, n, drecs.data(), dev);
             if (rc) return rc;
+            for (int v = 1; v < nv; ++v)
+            {
+                std::vector<gl_surface> moved(surfaces, surfaces + n);
+                const float f = v == 1 ? 1.0f + kGraze : 1.0f - kGraze;
+                for (gl_surface& g : moved)
+                    if (g.aperture_shape == GL_APERTURE_POLYGON && g.aperture_blades >= 3) g.semi_aperture *= f;
+                rc = pack_lens(moved.data(), n, drecs.data() + (size_t)v * n, dev);
+                if (rc) return rc;
+            }
         }
         std::unique_lock<std::mutex> lock(g_scratch_mu);
         Scratch& sc = g_scratch[e == cudaSuccess ? dev : 0];
@@ -179,7 +209,7 @@ extern "C" int gl_filter_ghost_pairs(const gl_surface* surfaces, int n, float hw
         ProbeOut* d_out = reinterpret_cast<ProbeOut*>(base + o_out);
         if (e == cudaSuccess)
         {
-            chk(cudaMemcpy(d_recs, drecs.data(), sizeof(SurfRec) * n, cudaMemcpyHostToDevice));
+            chk(cudaMemcpy(d_recs, drecs.data(), sizeof(SurfRec) * n * nv, cudaMemcpyHostToDevice));
             chk(cudaMemcpy(d_at, at.data(), sizeof(float) * 3 * n, cudaMemcpyHostToDevice));
             chk(cudaMemcpy(d_bf, bf.data(), sizeof(float) * 3 * n, cudaMemcpyHostToDevice));
             chk(cudaMemcpy(d_pairs, cand.data(), sizeof(int2) * np, cudaMemcpyHostToDevice));
@@ -188,9 +218,10 @@ extern "C" int gl_filter_ghost_pairs(const gl_surface* surfaces, int n, float hw
         {
             const float front_R = surfaces[0].semi_aperture;
             const float start_z = surfaces[0].z - kSpawnOffset;
-            filter_probe_kernel<<<np, kProbeThreads>>>(d_recs, n, d_at, d_bf, d_pairs, front_R, start_z, d_out);
+            filter_probe_kernel<<<dim3(np, nv), kProbeThreads>>>(d_recs, n, d_at, d_bf, d_pairs, front_R, start_z,
+                                                                  d_out);
             chk(cudaGetLastError());
-            chk(cudaMemcpy(res.data(), d_out, sizeof(ProbeOut) * np, cudaMemcpyDeviceToHost));
+            chk(cudaMemcpy(res.data(), d_out, sizeof(ProbeOut) * np * nv, cudaMemcpyDeviceToHost));
         }
         lock.unlock();
         if (e != cudaSuccess)
@@ -201,7 +232,15 @@ extern "C" int gl_filter_ghost_pairs(const gl_surface* surfaces, int n, float hw
         const float thr = prm->min_ghost_intensity;
         for (int i = 0; i < np; ++i)
         {
-            const ProbeOut& r = res[i];
+            ProbeOut r = res[i];
+            if (nv == 3 && !(same_probe(res[(size_t)np + i], res[(size_t)2 * np + i]) &&
+                             same_probe(res[i], res[(size_t)np + i])))
+            {
+                // a probe ray grazes a polygon / blade silhouette: trace the
+                // pair's probes again on the host
+                host_filter_probe(surfaces, recs.data(), n, cand[i].x, cand[i].y, &r);
+                ++rechecked;
+            }
             // estimate_ghost_intensity's sum order: total += w650, w550, w450
             float total = 0.0f;
             for (int ch = 0; ch < 3; ++ch)

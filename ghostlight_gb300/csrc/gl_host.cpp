@@ -433,6 +433,35 @@ float host_intensity_estimate(const gl_surface* s, const SurfRec* recs, int n, i
     return total / 3.0f;
 }
 
+void host_filter_probe(const gl_surface* s, const SurfRec* recs, int n, int a, int b, FilterProbe* out)
+{
+    std::vector<float> at(n), bf(n);
+    const float start_z = s[0].z - kSpawnOffset, front_R = s[0].semi_aperture;
+    for (int ch = 0; ch < 3; ++ch)
+    {
+        build_ior_tables(s, n, &kProbeLambdas[ch], 1, at.data(), bf.data());
+        TraceOut r = trace_ghost(recs, n, at.data(), bf.data(), v3(0.0f, 0.0f, start_z), v3(0.0f, 0.0f, 1.0f),
+                                 kProbeLambdas[ch], a, b);
+        out->w[ch] = r.w;
+        out->wok[ch] = r.status == 0;
+    }
+    build_ior_tables(s, n, &kProbeLambdas[1], 1, at.data(), bf.data());
+    out->mnx = 1e30f; out->mxx = -1e30f; out->mny = 1e30f; out->mxy = -1e30f;
+    out->valid = 0;
+    for (int k = 0; k < 64; ++k)
+    {
+        const float u = ((k % 8 + 0.5f) / 8) * 2.0f - 1.0f;
+        const float v = ((k / 8 + 0.5f) / 8) * 2.0f - 1.0f;
+        if (u * u + v * v > 1.0f) continue;
+        TraceOut r = trace_ghost(recs, n, at.data(), bf.data(), v3(u * front_R, v * front_R, start_z),
+                                 v3(0.0f, 0.0f, 1.0f), kProbeLambdas[1], a, b);
+        if (r.status != 0) continue;
+        out->mnx = std::min(out->mnx, r.x); out->mxx = std::max(out->mxx, r.x);
+        out->mny = std::min(out->mny, r.y); out->mxy = std::max(out->mxy, r.y);
+        ++out->valid;
+    }
+}
+
 float host_spread_boost(const gl_surface* s, const SurfRec* recs, int n, int a, int b,
                         float hw, float hh, float max_boost)
 {

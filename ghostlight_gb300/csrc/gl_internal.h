@@ -45,6 +45,15 @@ int input_matrix(int cs, const float* custom, float M[9]);
 std::vector<gl_spectral_sample> spectral_table(int n, float lmin, float lmax, const float M[9]);
 void spectral_correction(const std::vector<gl_spectral_sample>& tn, float lmin, float lmax,
                          const float M[9], float C[9]);
+// The culler's per-pair probes (ghost.cpp:34-102): the three axial rays of
+// the intensity estimate and the 8 x 8 spread probe's landing box.
+struct FilterProbe {
+    float w[3];        // per-wavelength weight of the axial ray
+    int wok[3];        // 1 when that ray reached the sensor
+    float mnx, mxx, mny, mxy;
+    int valid;         // spread-probe rays that reached the sensor
+};
+void host_filter_probe(const gl_surface* s, const SurfRec* recs, int n, int a, int b, FilterProbe* out);
 float host_intensity_estimate(const gl_surface* s, const SurfRec* recs, int n, int a, int b);
 float host_spread_boost(const gl_surface* s, const SurfRec* recs, int n, int a, int b,
                         float hw, float hh, float max_boost);

@@ -498,7 +498,8 @@ def render_source_flare(offsets, width: int, height: int, lens: OpticalSystem,
         from .calibration import solve_source_angle
         f = np.float32
         smap = solve_source_angle(lens, calibration, float((f(config.source_x) - f(0.5)) * f(2.0)),
-                                  float((f(config.source_y) - f(0.5)) * f(2.0)), hw, hh)
+                                  float((f(config.source_y) - f(0.5)) * f(2.0)), hw, hh,
+                                  precision=getattr(config, "setup_precision", "fp32"))
         ax0, ay0 = smap.angle_x, smap.angle_y
     else:
         ax0, ay0 = source_angle

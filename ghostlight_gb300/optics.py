@@ -418,11 +418,11 @@ class OpticalSystem:
         K.reset_coating(self.surfaces[self._surface_index(index)].record)
 
     # Cached helpers mirroring ghostlight/bindings/python/ghostlight/optical_system.py
-    def calibration(self, *, d_line_nm: float = 587.56):
+    def calibration(self, *, d_line_nm: float = 587.56, precision: str = "fp32"):
         from .calibration import calibrate_lens
-        key = (self.state_key(), d_line_nm)
+        key = (self.state_key(), d_line_nm, precision)
         if self._calib is None or self._calib_key != key:
-            self._calib = calibrate_lens(self, d_line_nm)
+            self._calib = calibrate_lens(self, d_line_nm, precision=precision)
             self._calib_key = key
         return self._calib
 

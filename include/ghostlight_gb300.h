@@ -571,8 +571,12 @@ int gl_pool_trim(long long keep_bytes);
 /* ---- First-order calibration and the source-position solve (host) ---------
  * calibrate_lens (lens_calibration.cpp:344) — covered field, image circle,
  * per-axis EFL, entrance pupil and f-number by tracing the spawn disc — and
- * solve_source_angle / source_map_screen (source_map.cpp:182, :456), in the
- * reference's float32 arithmetic so the values equal the reference's. */
+ * solve_source_angle / source_map_screen (source_map.cpp:182, :456).
+ * GL_SETUP_FP32 runs the reference's float32 arithmetic (the values equal the
+ * reference's bit for bit); GL_SETUP_FP64 runs the same measurement with
+ * double-precision traces and solves (results rounded to float at the end). */
+#define GL_SETUP_FP32 0
+#define GL_SETUP_FP64 1
 typedef struct gl_lens_calibration {
     float sensor_half_w, sensor_half_h;        /* covered field landing (mm)    */
     float max_half_angle_h, max_half_angle_v;  /* covered field (rad)           */
@@ -601,11 +605,19 @@ typedef struct gl_source_solve {
 
 int gl_calibrate_lens(const gl_surface* surfaces, int n_surfaces, float lens_focal_length,
                       float d_line_nm, gl_lens_calibration* out);
+/* gl_calibrate_lens with a precision: GL_SETUP_FP32 (= gl_calibrate_lens) or
+ * GL_SETUP_FP64. */
+int gl_calibrate_lens2(const gl_surface* surfaces, int n_surfaces, float lens_focal_length,
+                       float d_line_nm, int precision, gl_lens_calibration* out);
 /* ndc in [-1, 1] (0 on the axis); eff_half_w/h: the rendered frame's half
  * extents in mm.  A lens with no surfaces gives the FALLBACK solve. */
 int gl_solve_source_angle(const gl_surface* surfaces, int n_surfaces,
                           const gl_lens_calibration* calib, float ndc_x, float ndc_y,
                           float eff_half_w, float eff_half_h, gl_source_solve* out);
+/* gl_solve_source_angle with a precision (GL_SETUP_FP32 or GL_SETUP_FP64). */
+int gl_solve_source_angle2(const gl_surface* surfaces, int n_surfaces,
+                           const gl_lens_calibration* calib, float ndc_x, float ndc_y,
+                           float eff_half_w, float eff_half_h, int precision, gl_source_solve* out);
 int gl_source_map_screen(const gl_source_solve* base, float angle_x, float angle_y,
                          float* out_sx, float* out_sy);
 

@@ -64,12 +64,13 @@ def _flare_cfg(g, cal):
     return cfg
 
 
-def render_golden(packed, key):
-    """The image the golden ``key`` records, rendered by this path (H, W, 3)."""
+def render_golden(packed, key, precision="fp32"):
+    """The image the golden ``key`` records, rendered by this path (H, W, 3);
+    ``precision`` is the arithmetic of the calibration and source solve."""
     import ghostlight_gb300 as gl
     g = _META["goldens"][key]
     lens = _lens(packed, g["lens"])
-    cal = lens.calibration()
+    cal = lens.calibration(precision=precision)
     if g["kind"] == "psf":
         ax = cal.max_half_angle_h * g["field_frac"]
         ay = cal.max_half_angle_v * g["field_frac"]
@@ -84,6 +85,7 @@ def render_golden(packed, key):
         keys = ("r", "g", "b")
     else:
         cfg = _flare_cfg(g, cal)
+        cfg.setup_precision = precision
         prefix = "ghost"
         if g["kind"] == "starburst":
             cfg.diffraction.starburst = True
@@ -122,3 +124,14 @@ def test_reference_golden(packed, key):
     assert float(want.sum()) > 0.0
     err = rel_l2(got, want)
     assert err <= IMG_TOL, "%s: relative L2 %.3e against the reference golden" % (key, err)
+
+
+@pytest.mark.parametrize("key", ["pfs/double_gauss_1.3_0.5_b0_c1", "pfs/sirui_1.6_0.9_b0_c1", "ab/hex_rot30__ghost_corner",
+                                 "ab/sirui__source_chunk"])
+def test_reference_golden_with_fp64_setup(packed, key):
+    """The same renders with the calibration and the source solve in FP64:
+    the frame still matches the reference's within the image bar."""
+    g = _META["goldens"][key]
+    want = unpack(packed["img/" + key], tuple(g["shape"]))
+    err = rel_l2(render_golden(packed, key, precision="fp64"), want)
+    assert err <= IMG_TOL, "%s (fp64 setup): relative L2 %.3e" % (key, err)
