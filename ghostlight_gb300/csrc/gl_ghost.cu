@@ -80,7 +80,7 @@ __device__ __forceinline__ bool sphere_hit(V3 o, V3 d, float z_s, float c, float
     if (fabsf(d.z) < 1e-12f) return false;
     const float t0 = (z_s - o.z) / d.z;
     const float px = o.x + d.x * t0, py = o.y + d.y * t0;
-    const float A = c;                      // c |d|^2: the walk's directions are unit
+    const float A = c * (d.x * d.x + d.y * d.y + d.z * d.z);   // c |d|^2
     const float B = c * (px * d.x + py * d.y) - d.z;
     const float C = c * (px * px + py * py);
     const float disc = B * B - A * C;
@@ -206,11 +206,11 @@ __device__ __forceinline__ float mgf2_reflectance(float cos_i, float n1, float n
     return R * ar_scale;
 }
 
-// Refraction for the walk's unit vectors (the source direction is
-// normalised, sphere normals are unit by construction, and a refraction of
-// unit vectors is unit): Snell's law as refract_ray (trace_core.h:533-552)
-// without its renormalisation.  ci = -dot(nrm, d) >= 0; returns the
-// transmitted cosine (for the coating), or -1 on total internal reflection.
+// Snell's law as refract_ray (trace_core.h:533-552), renormalised like it:
+// the walk's directions then stay unit to rounding over every interaction
+// (a drift in |d| would bias the next surface's root and the landing).
+// ci = -dot(nrm, d) >= 0; returns the transmitted cosine (for the coating),
+// or -1 on total internal reflection.
 __device__ __forceinline__ float refract_unit(V3& d, V3 nrm, float ci, float n1, float n2)
 {
     const float nr = n1 / n2;
@@ -218,6 +218,7 @@ __device__ __forceinline__ float refract_unit(V3& d, V3 nrm, float ci, float n1,
     if (s2t >= 1.0f) return -1.0f;
     const float ct = sqrtf(1.0f - s2t);
     d = d * nr + nrm * (nr * ci - ct);
+    d = d * rsqrtf(d.x * d.x + d.y * d.y + d.z * d.z);
     return ct;
 }
 
@@ -271,6 +272,7 @@ __device__ __forceinline__ bool surface_step(V3& o, V3& d, const HotRec& h, cons
             if (h.bits & HB_ATTEN) w *= attenuator_general(hit, s);
         }
         d = d + nrm * (2.0f * ci);
+        d = d * rsqrtf(d.x * d.x + d.y * d.y + d.z * d.z);
         cur = reflect_ior;
     }
     else

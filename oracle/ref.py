@@ -299,13 +299,16 @@ class RefGpuCfg(C.Structure):
                [(n, C.c_float) for n in ("source_x", "source_y", "source_r", "source_g", "source_b")] + \
                [(n, C.c_int) for n in ("starburst", "starburst_engine", "starburst_grid", "sb_spectral_samples")] + \
                [(n, C.c_float) for n in ("pupil_fill", "scale_trim")] + \
-               [(n, C.c_int) for n in ("spectral_correction", "output_cs", "use_survivor_mask", "collect_stats")]
+               [(n, C.c_int) for n in ("spectral_correction", "output_cs", "use_survivor_mask", "collect_stats",
+                                       "veil", "pad2")] + \
+               [(n, C.c_float) for n in ("veil_gain", "veil_spread", "veil_falloff")]
 
     def __init__(self, **kw):
         d = dict(ray_grid=64, spectral_samples=16, flare_gain=1000.0, min_ghost_intensity=1e-7,
                  cull_dead_pairs=1, concentrate_samples=1, adaptive_sample_budgets=1, source_x=0.5,
                  source_y=0.5, source_r=1.0, source_g=1.0, source_b=1.0, starburst_grid=1024,
-                 pupil_fill=0.3, scale_trim=1.0, spectral_correction=1, use_survivor_mask=1)
+                 pupil_fill=0.3, scale_trim=1.0, spectral_correction=1, use_survivor_mask=1, veil_gain=0.03,
+                 veil_spread=0.12, veil_falloff=1.5)
         d.update(kw)
         super().__init__(**d)
 
@@ -322,20 +325,22 @@ def _load_gpu():
     vp, i, f = C.c_void_p, C.c_int, C.c_float
     lib.refgpu_sizeof_cfg.restype = i
     lib.refgpu_render.argtypes = [vp, i, f, vp, C.POINTER(RefGpuCfg), vp, i, i, i, vp, vp,
-                                  C.POINTER(C.c_double), vp, vp, i]
+                                  C.POINTER(C.c_double), vp, vp, i, vp]
     lib.refgpu_render.restype = i
     assert lib.refgpu_sizeof_cfg() == C.sizeof(RefGpuCfg)
     _gpu = lib
     return lib
 
 
-def gpu_render(surfs, W, H, cfg, calib=None, focal_length=0.0, offsets=None, starburst=False, include=None):
+def gpu_render(surfs, W, H, cfg, calib=None, focal_length=0.0, offsets=None, starburst=False, include=None,
+               veil=False):
     """render_point_flare (offsets None) or render_source_flare of the
     reference's GPU renderer.  Returns (ghost (3,H,W), starburst (3,H,W) or
     None, wall ms of the call, stats dict or None)."""
     lib = _load_gpu()
     ghost = np.zeros((3, H, W), np.float32)
     star = np.zeros((3, H, W), np.float32) if starburst else None
+    vl = np.zeros((3, H, W), np.float32) if veil else None
     cal = None
     if calib is not None:
         cal = np.array([calib[k] for k in CALIB_FIELDS], np.float32)
@@ -353,11 +358,14 @@ def gpu_render(surfs, W, H, cfg, calib=None, focal_length=0.0, offsets=None, sta
                            W, H, ghost.ctypes.data_as(C.c_void_p),
                            None if star is None else star.ctypes.data_as(C.c_void_p), C.byref(ms),
                            stats.ctypes.data_as(C.c_void_p),
-                           None if inc is None else inc.ctypes.data_as(C.c_void_p), 0 if inc is None else len(inc))
+                           None if inc is None else inc.ctypes.data_as(C.c_void_p), 0 if inc is None else len(inc),
+                           None if vl is None else vl.ctypes.data_as(C.c_void_p))
     if rc != 0:
         raise RuntimeError("reference GPU render failed")
     st = None
     if cfg.collect_stats:
         st = dict(zip(("ms_grid_build", "ms_upload", "ms_kernel", "ms_download", "ms_total", "n_pairs",
                        "traces_total", "traces_on_sensor"), stats.tolist()))
+    if veil:
+        return ghost, star, float(ms.value), st, vl
     return ghost, star, float(ms.value), st

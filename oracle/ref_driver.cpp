@@ -740,6 +740,8 @@ struct RefGpuCfg {
     int starburst, starburst_engine, starburst_grid, sb_spectral_samples;
     float pupil_fill, scale_trim;
     int spectral_correction, output_cs, use_survivor_mask, collect_stats;
+    int veil, pad2;
+    float veil_gain, veil_spread, veil_falloff;
 };
 
 extern "C" int refgpu_sizeof_cfg() { return (int)sizeof(RefGpuCfg); }
@@ -756,7 +758,7 @@ extern "C" int refgpu_sizeof_cfg() { return (int)sizeof(RefGpuCfg); }
 extern "C" int refgpu_render(const gl_surface* surfs, int n, float focal_length, const float* calib13,
                              const RefGpuCfg* g, const float* offsets, int n_offsets, int W, int H,
                              float* out_ghost, float* out_star, double* ms, double* stats,
-                             const int* include_ab, int n_include)
+                             const int* include_ab, int n_include, float* out_veil)
 {
     OpticalSystem* L = make_lens(surfs, n);
     L->focal_length = focal_length;
@@ -791,6 +793,13 @@ extern "C" int refgpu_render(const gl_surface* surfs, int n, float focal_length,
     cfg.diffraction.pupil_fill = g->pupil_fill; cfg.diffraction.scale_trim = g->scale_trim;
     cfg.diffraction.use_survivor_mask = g->use_survivor_mask != 0;
     cfg.collect_stats = g->collect_stats != 0;
+    cfg.diffraction.veil = g->veil != 0;
+    if (g->veil)
+    {
+        cfg.diffraction.veil_gain = g->veil_gain;
+        cfg.diffraction.veil_spread = g->veil_spread;
+        cfg.diffraction.veil_falloff = g->veil_falloff;
+    }
     if (include_ab && n_include > 0)
     {
         cfg.ghost_filter.mode = GhostFilter::Mode::INCLUDE;
@@ -817,6 +826,12 @@ extern "C" int refgpu_render(const gl_surface* surfs, int n, float focal_length,
         const std::vector<float>* pl[3] = {&out.ghost_r, &out.ghost_g, &out.ghost_b};
         for (int k = 0; k < 3; ++k)
             for (size_t i = 0; i < npx; ++i) out_ghost[k * npx + i] = pl[k]->size() == npx ? (*pl[k])[i] : 0.0f;
+    }
+    if (out_veil)
+    {
+        const std::vector<float>* pl[3] = {&out.veil_r, &out.veil_g, &out.veil_b};
+        for (int k = 0; k < 3; ++k)
+            for (size_t i = 0; i < npx; ++i) out_veil[k * npx + i] = pl[k]->size() == npx ? (*pl[k])[i] : 0.0f;
     }
     if (out_star)
     {

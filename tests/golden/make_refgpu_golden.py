@@ -12,7 +12,8 @@ oracle/ref_driver.cpp.  Three things are written to ``--out``:
   reference;
 * ``refgpu_images.npz`` + ``refgpu_meta.json`` — its images of the seeded
   configuration-1, -2 and -4 lenses with deterministic sampling
-  (concentration off); ``--pack DIR`` turns them into the committed fixtures
+  (concentration off), and its veil and starburst layers (matrix-DFT and
+  SPRITE engines, on and off axis) on the configuration-1 lens; ``--pack DIR`` turns them into the committed fixtures
   ``refgpu_seeded.npz`` / ``refgpu_seeded.json`` (15 mantissa bits kept, as
   make_refgolden.py packs) for tests/test_gpu_refgpu.py;
 * ``refgpu_timing.json`` — its wall time and kernel-stage time on the
@@ -106,6 +107,38 @@ def seeded(pins, meta):
     return images, info
 
 
+# Layers of render_point_flare on the seeded configuration-1 lens (512^2,
+# 8 wavelengths): the veiling glare (veil_render.cu:243), and the starburst by
+# the matrix-DFT engine (a 1024 grid at scale_trim 15: an 87-pixel window,
+# below the reference's "prominent" switch) and by the SPRITE engine, on axis
+# and off axis (the cat's-eye effective pupil).
+LAYERS = {
+    "veil": dict(source_xy=(0.62, 0.44), veil=True),
+    "mdft": dict(source_xy=(0.5, 0.5), starburst=True, engine=1, grid=1024, trim=15.0),
+    "sprite": dict(source_xy=(0.5, 0.5), starburst=True, engine=0, grid=1024, trim=15.0),
+    "sprite_offaxis": dict(source_xy=(0.9, 0.3), starburst=True, engine=0, grid=1024, trim=15.0),
+}
+
+
+def layers(pins, meta):
+    images, info = {}, {}
+    raw, focal, cal = _lens(pins, meta, "cfg1_double_gauss_12")
+    for name, c in LAYERS.items():
+        cfg = R.RefGpuCfg(ray_grid=32, spectral_samples=8, pupil_jitter=0, jitter_seed=0,
+                          sensor_half_w=cal["sensor_half_w"], sensor_half_h=cal["sensor_half_h"], flare_gain=1000.0,
+                          min_ghost_intensity=1e-7, cull_dead_pairs=1, concentrate_samples=0,
+                          source_x=c["source_xy"][0], source_y=c["source_xy"][1], source_r=10.0, source_g=10.0,
+                          source_b=10.0, veil=int(c.get("veil", False)), starburst=int(c.get("starburst", False)),
+                          starburst_engine=c.get("engine", 0), starburst_grid=c.get("grid", 1024), pupil_fill=0.3,
+                          scale_trim=c.get("trim", 1.0), sb_spectral_samples=8)
+        g, star, ms, _, vl = R.gpu_render(raw, 512, 512, cfg, calib=cal, focal_length=focal,
+                                          starburst=bool(c.get("starburst")), veil=True)
+        images["layer_" + name + "/image"] = vl if c.get("veil") else star
+        info["layer_" + name] = dict(c, lens="cfg1_double_gauss_12", W=512, H=512, ms=ms, calibration=cal,
+                                     key="veil" if c.get("veil") else "starburst")
+    return images, info
+
+
 def timing(pins, meta, reps=5):
     """The configuration-2 frame: the reference at 256^2 grids with its
     deterministic sampling, and with its default concentrated sampling and
@@ -166,6 +199,9 @@ def main():
     (out / "refgpu_selfcheck.json").write_text(json.dumps(chk, indent=1))
     print(json.dumps(chk), flush=True)
     images, info = seeded(pins, meta)
+    li, lm = layers(pins, meta)
+    images.update(li)
+    info.update(lm)
     np.savez_compressed(out / "refgpu_images.npz", **images)
     (out / "refgpu_meta.json").write_text(json.dumps(info, indent=1, default=float))
     if not args.skip_timing:

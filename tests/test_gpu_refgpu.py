@@ -54,3 +54,36 @@ def test_seeded_configuration_matches_reference_gpu(pins, meta, case):
     assert float(want.sum()) > 0.0
     err = rel_l2(got, want)
     assert err <= IMG_TOL, "%s: relative L2 %.3e against the reference GPU renderer" % (case, err)
+
+
+@pytest.mark.parametrize("case", ["layer_veil", "layer_mdft", "layer_sprite", "layer_sprite_offaxis"])
+def test_flare_layers_match_reference_gpu(pins, meta, case):
+    """render_point_flare's veil and starburst layers (matrix-DFT engine on
+    the tensor cores, SPRITE engine on and off axis) against the reference's
+    CUDA renderer on the configuration-1 lens, 512^2, 8 wavelengths."""
+    import ghostlight_gb300 as gl
+    if case not in _META:
+        pytest.skip("fixture predates this layer")
+    c = _META[case]
+    lens = gl.OpticalSystem.from_records(lens_from_pins(pins, c["lens"]), name=c["lens"],
+                                         focal_length=meta[c["lens"]]["focal_length"])
+    cal = gl.LensCalibration.from_dict(c["calibration"])
+    cfg = gl.PointFlareConfig(ray_grid=32, spectral_samples=8, source_x=c["source_xy"][0], source_y=c["source_xy"][1],
+                              source_r=10.0, source_g=10.0, source_b=10.0, min_ghost_intensity=1e-7,
+                              concentrate_samples=False, sensor_half_w=cal.sensor_half_w,
+                              sensor_half_h=cal.sensor_half_h)
+    if c.get("veil"):
+        cfg.diffraction.veil = True
+    else:
+        cfg.diffraction.starburst = True
+        cfg.diffraction.starburst_engine = gl.StarburstEngine(c["engine"])
+        cfg.diffraction.starburst_grid = c["grid"]
+        cfg.diffraction.pupil_fill = 0.3
+        cfg.diffraction.scale_trim = c["trim"]
+        cfg.diffraction.spectral_samples = 8
+    out = gl.render_point_flare(c["W"], c["H"], lens, cal, cfg)
+    got = np.stack([out["%s_%s" % (c["key"], ch)].cpu().numpy() for ch in "rgb"])
+    want = unpack(np.load(GOLDEN / "refgpu_seeded.npz")[case + "/image"], tuple(c["shape"]))
+    assert float(want.sum()) > 0.0
+    err = rel_l2(got, want)
+    assert err <= IMG_TOL, "%s: relative L2 %.3e against the reference GPU renderer" % (case, err)
