@@ -232,6 +232,7 @@ struct MdftArgs {
     int out_w, x0, y0, win_w, win_h;
     int box;                          // 1: accumulate Re E (pixel-integrated form); 0: |E|^2
     float4 tint;                      // per-launch colour factor on the weights
+    int lam_base;                     // first wavelength of this launch's range
 };
 
 template <int FORM>
@@ -309,14 +310,14 @@ __global__ void __launch_bounds__(kMdftThreads, 1) mdft_kernel(const __grid_cons
         {
             // wavelength-major: all output tiles of one wavelength, then the next
             const int tiles = args.NBm * args.NB;
-            lam = u / tiles;
+            lam = args.lam_base + u / tiles;
             const int tile = u - lam * tiles;
             mb = tile / args.NB;
             xb = tile % args.NB;
         }
         else
         {
-            lam = u / (args.NBm * args.NI);
+            lam = args.lam_base + u / (args.NBm * args.NI);
             const int r = u % (args.NBm * args.NI);
             mb = r / args.NI;
             xb = r % args.NI;
@@ -682,11 +683,11 @@ __global__ void mdft_mask_kernel(const float* __restrict__ a, void* out, int n, 
 constexpr int kSB = 128, kSK = 16;
 
 __global__ void __launch_bounds__(256) mdft_simt_step1(const float* __restrict__ W, const float* __restrict__ A,
-                                                       float* __restrict__ T, int K_out, int n, int NB)
+                                                       float* __restrict__ T, int K_out, int n, int NB, int lam_base)
 {
     // K_out = rows of W_x per (wavelength, part) = Kx
     __shared__ float sWr[kSK][kSB + 4], sWi[kSK][kSB + 4], sA[kSK][kSB + 4];
-    const int lam = blockIdx.z, mb = blockIdx.y, ib = blockIdx.x;
+    const int lam = lam_base + (int)blockIdx.z, mb = blockIdx.y, ib = blockIdx.x;
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     const float* Wr = W + ((size_t)(lam * 2 + 0) * K_out + mb * kSB) * n;
     const float* Wi = W + ((size_t)(lam * 2 + 1) * K_out + mb * kSB) * n;
@@ -733,7 +734,7 @@ __global__ void __launch_bounds__(256) mdft_simt_step1(const float* __restrict__
 
 __global__ void __launch_bounds__(256) mdft_simt_step2(const float* __restrict__ W, const float* __restrict__ T,
                                                        const float4* __restrict__ weights, float* out_r, float* out_g,
-                                                       float* out_b, int K_rows, int K_out, int n, int NB, int n_lambda,
+                                                       float* out_b, int K_rows, int K_out, int n, int NB, int lam0, int lam1,
                                                        int box, int out_w, int x0, int y0, int win_w, int win_h,
                                                        float4 tint)
 {
@@ -741,7 +742,7 @@ __global__ void __launch_bounds__(256) mdft_simt_step2(const float* __restrict__
     __shared__ float sWr[kSK][kSB + 4], sWi[kSK][kSB + 4], sTr[kSK][kSB + 4], sTi[kSK][kSB + 4];
     const int mb = blockIdx.y, nb = blockIdx.x;
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-    for (int lam = 0; lam < n_lambda; ++lam)
+    for (int lam = lam0; lam < lam1; ++lam)
     {
         const float* Wr = W + ((size_t)(lam * 2 + 0) * K_rows + mb * kSB) * n;
         const float* Wi = W + ((size_t)(lam * 2 + 1) * K_rows + mb * kSB) * n;
@@ -817,6 +818,7 @@ struct MdftPlan {
     double cx = 0.0, cy = 0.0;
     float cj = 0.0f;            // reduction-axis centre: (n - 1) / 2, or the zero lag mc of the box form
     int box = 0;                // pixel-integrated form (the reference's MDFT engine)
+    int lam0 = 0, lam1 = -1;    // wavelength range of the next executes (lam1 < 0: all)
     int ctas = 0;               // GEMM grid (0 = one CTA per SM)
     int* err = nullptr;
     CUtensorMap t_wx, t_wy, t_mask, t_tp;
@@ -1020,21 +1022,23 @@ extern "C" int gl_mdft_plan_execute3(gl_mdft_plan* plan, const float* d_pupil, f
     a.out_w = out_w; a.x0 = x0; a.y0 = y0; a.win_w = win_w; a.win_h = win_h; a.box = p->box;
     a.tint = tint_rgb ? make_float4(tint_rgb[0], tint_rgb[1], tint_rgb[2], 0.0f) : make_float4(1.0f, 1.0f, 1.0f, 0.0f);
     const size_t smem1 = 4 * 3 * (size_t)kOpTile + 1024, smem2 = 2 * 5 * (size_t)kOpTile + 1024;
-    a.n_units = p->n_lambda * NBx * NI;                 // step 1: (lambda, k block, pupil-row block)
+    const int l0 = p->lam0, l1 = p->lam1 < 0 ? p->n_lambda : p->lam1, nl = l1 - l0;
+    a.lam_base = l0;
+    a.n_units = nl * NBx * NI;                          // step 1: (lambda, k block, pupil-row block)
     const int gmax = p->ctas > 0 ? p->ctas : p->sms;
     const int g1 = std::min(a.n_units, gmax);
     MdftArgs a2 = a;
     a2.KA = p->Ky; a2.NBm = NBy;
-    a2.n_units = NBy * NBx * p->n_lambda;               // step 2: (lambda, output tile)
+    a2.n_units = NBy * NBx * nl;                        // step 2: (lambda, output tile)
     const int g2 = std::min(a2.n_units, gmax);
     if (p->form == 2)
     {
-        mdft_simt_step1<<<dim3(NI, NBx, p->n_lambda), 256, 0, st>>>(static_cast<const float*>(p->wx),
-                                                                    static_cast<const float*>(p->mask),
-                                                                    static_cast<float*>(p->tprime), p->Kx, p->n, NBx);
+        mdft_simt_step1<<<dim3(NI, NBx, nl), 256, 0, st>>>(static_cast<const float*>(p->wx),
+                                                           static_cast<const float*>(p->mask),
+                                                           static_cast<float*>(p->tprime), p->Kx, p->n, NBx, l0);
         mdft_simt_step2<<<dim3(NBx, NBy), 256, 0, st>>>(static_cast<const float*>(p->wy), static_cast<const float*>(p->tprime),
                                                        p->weights, d_out_r, d_out_g, d_out_b, p->Ky, p->Kx, p->n, NBx,
-                                                       p->n_lambda, p->box, out_w, x0, y0, win_w, win_h, a.tint);
+                                                       l0, l1, p->box, out_w, x0, y0, win_w, win_h, a.tint);
     }
     else if (p->form == 0)
     {
@@ -1059,6 +1063,19 @@ extern "C" int gl_mdft_plan_execute2(gl_mdft_plan* plan, const float* d_pupil, f
     const gl::MdftPlan* p = plan->p;
     return gl_mdft_plan_execute3(plan, d_pupil, d_out_r, d_out_g, d_out_b, accumulate, p->Kx, p->Ky, 0, 0, p->Kx, p->Ky,
                                  nullptr, stream);
+}
+
+extern "C" int gl_mdft_plan_set_lambda_range(gl_mdft_plan* plan, int lam_begin, int lam_end)
+{
+    using namespace gl;
+    if (!plan) return fail(GL_ERR_INVALID, "mdft_plan_set_lambda_range: null plan");
+    MdftPlan* p = plan->p;
+    if (lam_begin == 0 && lam_end < 0) { p->lam0 = 0; p->lam1 = -1; return GL_OK; }
+    if (lam_begin < 0 || lam_end <= lam_begin || lam_end > p->n_lambda)
+        return fail(GL_ERR_INVALID, "mdft_plan_set_lambda_range: need 0 <= begin < end <= n_lambda");
+    p->lam0 = lam_begin;
+    p->lam1 = lam_end;
+    return GL_OK;
 }
 
 extern "C" int gl_mdft_plan_set_launch(gl_mdft_plan* plan, int ctas)

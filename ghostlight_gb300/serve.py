@@ -198,6 +198,17 @@ class StarburstPlans:
         self.priority = min(lo, hi)
         self.plans: Dict[tuple, tuple] = {}
 
+    @staticmethod
+    def chunks(width: int, height: int, n_spec: int) -> int:
+        """Wavelength ranges a pattern is enqueued in: one below 2048^2; the
+        larger patterns in ranges of about four (2048^2) or two (4096^2)
+        wavelengths, so their GEMM CTAs give the SMs back between ranges and
+        the smaller patterns behind them start within a fraction of a
+        millisecond instead of after the whole pattern."""
+        px = int(width) * int(height)
+        per = 0 if px < 2048 * 2048 else (4 if px < 4096 * 4096 else 2)
+        return 1 if per == 0 else max(1, -(-int(n_spec) // per))
+
     def get(self, width: int, height: int, spec: np.ndarray):
         from .starburst import MdftPlan
         spec = np.ascontiguousarray(spec, np.float32).reshape(-1, 4)
@@ -206,7 +217,13 @@ class StarburstPlans:
         if hit is None:
             lam = spec[:, 0].astype(np.float64)
             s = lam.min() / lam
-            st = self.torch.cuda.Stream(device=self.device, priority=self.priority)
+            # the smaller the pattern the higher its stream's priority
+            px = int(width) * int(height)
+            lower = 0 if px <= 1024 * 1024 else (1 if px <= 2048 * 2048 else 2)
+            lo, hi = self.torch.cuda.Stream.priority_range()
+            prio = self.priority + lower if self.priority < max(lo, hi) else self.priority
+            prio = min(prio, max(lo, hi))
+            st = self.torch.cuda.Stream(device=self.device, priority=prio)
             plan = MdftPlan(STARBURST_PUPIL, (int(width), int(height)), s / width, s / height,
                             spec[:, 1:4], "split_bf16", stream=st.cuda_stream)
             if self.ctas > 0:
@@ -471,8 +488,17 @@ class CudaExecutor:
         ghost_done.record(stream)
         pst.wait_event(ghost_done)
         plan.set_center(cx, cy, stream=pst.cuda_stream)
-        plan.execute_raw(rl.starburst_pupil().data_ptr(), base, base + 4 * npx, base + 8 * npx,
-                         stream=pst.cuda_stream, accumulate=True)
+        k = StarburstPlans.chunks(req.width, req.height, req.n_spec)
+        if k == 1:
+            plan.execute_raw(rl.starburst_pupil().data_ptr(), base, base + 4 * npx, base + 8 * npx,
+                             stream=pst.cuda_stream, accumulate=True)
+        else:
+            per = -(-req.n_spec // k)
+            for l0 in range(0, req.n_spec, per):
+                plan.set_lambda_range(l0, min(req.n_spec, l0 + per))
+                plan.execute_raw(rl.starburst_pupil().data_ptr(), base, base + 4 * npx, base + 8 * npx,
+                                 stream=pst.cuda_stream, accumulate=True)
+            plan.set_lambda_range(0, -1)
         sb_done = torch.cuda.Event()
         sb_done.record(pst)
         stream.wait_event(sb_done)

@@ -104,6 +104,10 @@ class MdftPlan:
                                                       st), "mdft")
         return _native.last_launch_count()
 
+    def set_lambda_range(self, begin: int = 0, end: int = -1):
+        """Restrict the next executes to wavelengths [begin, end) ((0, -1): all)."""
+        _native.check(self._lib.gl_mdft_plan_set_lambda_range(self._h, int(begin), int(end)), "mdft")
+
     def set_launch(self, ctas: int = 0):
         """GEMM grid of the tensor-core forms (0 = one CTA per SM)."""
         _native.check(self._lib.gl_mdft_plan_set_launch(self._h, int(ctas)), "mdft")

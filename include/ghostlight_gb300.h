@@ -401,6 +401,11 @@ int gl_mdft_plan_create2(int n, int Kx, int Ky, int n_lambda, const double* scal
 int gl_mdft_plan_set_center(gl_mdft_plan* plan, double center_x, double center_y, void* stream);
 /* GEMM grid of the tcgen05 forms (0 = one CTA per SM); autotuner knob. */
 int gl_mdft_plan_set_launch(gl_mdft_plan* plan, int ctas);
+/* Restrict the next executes to wavelengths [lam_begin, lam_end) (0, -1:
+ * all): a large pattern enqueued as several short wavelength ranges (each
+ * accumulating) frees its CTAs' SMs between the ranges, so a serving loop's
+ * smaller patterns are not held behind it. */
+int gl_mdft_plan_set_lambda_range(gl_mdft_plan* plan, int lam_begin, int lam_end);
 /* execute with accumulate != 0 adds into the output planes instead of
  * overwriting them (a starburst layered onto a ghost image). */
 int gl_mdft_plan_execute2(gl_mdft_plan* plan, const float* d_pupil, float* d_out_r,

@@ -165,3 +165,32 @@ def test_stop_pupil_matches_oracle(blades, rot, aspect):
     diff = np.abs(got - want)
     assert got.sum() > 0.2 * N * N * 0.45 ** 2
     assert diff.max() <= 2.0 / 16.0 and (diff > 0).mean() < 2e-3
+
+
+@pytest.mark.parametrize("form", [0, 2])
+def test_mdft_wavelength_ranges_sum_to_the_whole(form):
+    """A pattern enqueued as wavelength ranges (gl_mdft_plan_set_lambda_range,
+    each execute accumulating) equals one execute over every wavelength."""
+    from ghostlight_gb300.starburst import MdftPlan
+    from oracle import mdft_oracle as MO
+    n, K, nl = 128, 256, 7
+    lam = np.linspace(420.0, 680.0, nl)
+    s = (1.0 / (2.0 * n)) * 550.0 / lam
+    w = np.random.default_rng(3).uniform(0.2, 1.0, (nl, 3)).astype(np.float32)
+    A = torch.from_numpy(MO.test_pupil(n, 4)).cuda()
+    plan = MdftPlan(n, K, s, s * 1.1, w, ["split_bf16", "tf32", "fp32"][form], center_x=K / 2 - 3.25, center_y=K / 2 + 1.5)
+    whole = [torch.zeros((K, K), device="cuda") for _ in range(3)]
+    plan.execute(A, *whole)
+    parts = [torch.zeros((K, K), device="cuda") for _ in range(3)]
+    for l0, l1 in ((0, 3), (3, 5), (5, 7)):
+        plan.set_lambda_range(l0, l1)
+        plan.execute(A, *parts, accumulate=True)
+    plan.set_lambda_range(0, -1)
+    torch.cuda.synchronize()
+    assert plan.status() == 0
+    a = torch.stack(whole).cpu().numpy().astype(np.float64)
+    b = torch.stack(parts).cpu().numpy().astype(np.float64)
+    assert a.sum() > 0 and np.linalg.norm(a - b) / np.linalg.norm(a) < 1e-6
+    with pytest.raises(ValueError):
+        plan.set_lambda_range(5, 9)
+    plan.close()
