@@ -310,8 +310,9 @@ __global__ void __launch_bounds__(kMdftThreads, 1) mdft_kernel(const __grid_cons
         {
             // wavelength-major: all output tiles of one wavelength, then the next
             const int tiles = args.NBm * args.NB;
-            lam = args.lam_base + u / tiles;
-            const int tile = u - lam * tiles;
+            const int lr = u / tiles;               // wavelength within this launch's range
+            lam = args.lam_base + lr;
+            const int tile = u - lr * tiles;
             mb = tile / args.NB;
             xb = tile % args.NB;
         }
