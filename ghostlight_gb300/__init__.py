@@ -20,6 +20,7 @@ from .apertures import curved_blade_mask
 from .psf_grid import render_psf
 from .veil import render_veil
 from .lensfile import lens_format_version, load_lens, save_lens
+from .debug import _render_starburst_debug, _render_veil_debug
 
 __version__ = "0.1.0"
 

@@ -107,6 +107,11 @@ class gl_veil_params(C.Structure):
                 ("gain", C.c_float), ("accumulate", C.c_int32)]
 
 
+class gl_veil_geometry(C.Structure):
+    _fields_ = [("grid", C.c_int32), ("ds", C.c_int32), ("dx_mm", C.c_float), ("core_mm", C.c_float),
+                ("falloff", C.c_float), ("core_texels", C.c_float)]
+
+
 class gl_psf_cell(C.Structure):
     _fields_ = [("beam_ax", C.c_float), ("beam_ay", C.c_float), ("chief_x_mm", C.c_float),
                 ("chief_y_mm", C.c_float), ("status", C.c_int32), ("pupil_fraction", C.c_float),

@@ -12,7 +12,7 @@ import threading
 from . import _abi
 from ._abi import (gl_filter_params, gl_flare_source, gl_ghost_pair, gl_ghost_render_params,
                    gl_lens_calibration, gl_pupil_sample, gl_sampler_params, gl_source_solve,
-                   gl_spectral_sample, gl_surface, gl_veil_params, gl_psf_cell, gl_psf_source)
+                   gl_spectral_sample, gl_surface, gl_veil_params, gl_veil_geometry, gl_psf_cell, gl_psf_source)
 
 _lock = threading.Lock()
 _lib = None
@@ -115,6 +115,8 @@ def _declare(lib):
     lib.gl_veil_plan_create.argtypes = [f, vp, P(vp)]
     lib.gl_veil_plan_execute.argtypes = [vp, vp, i, P(gl_veil_params), vp, vp, vp, vp]
     lib.gl_veil_plan_destroy.argtypes = [vp]
+    lib.gl_veil_plan_geometry.argtypes = [vp, P(gl_veil_params), P(gl_veil_geometry)]
+    lib.gl_veil_plan_read.argtypes = [vp, vp, vp]
     lib.gl_calibrate_lens.argtypes = [P(gl_surface), i, f, f, P(gl_lens_calibration)]
     lib.gl_calibrate_lens2.argtypes = [P(gl_surface), i, f, f, i, P(gl_lens_calibration)]
     lib.gl_solve_source_angle2.argtypes = [P(gl_surface), i, P(gl_lens_calibration), f, f, f, f, i,

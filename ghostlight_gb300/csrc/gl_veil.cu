@@ -177,6 +177,45 @@ extern "C" int gl_veil_plan_create(float falloff, void* stream, gl_veil_plan** o
     return GL_OK;
 }
 
+namespace gl {
+namespace {
+
+// The scale of one execute (veil_render.cu:276-296): core radius a = spread x
+// the sensor half-height (half-width when that is unset), the fine texel
+// pitch a / (N / 32), and the power-of-two box sum ds toward three texels per
+// output pixel.
+struct VeilGeom {
+    float spread, half_ref, a_texels, dx_fine, px_mm_x, px_mm_y;
+    int ds, M;
+};
+
+int veil_geometry(const gl_veil_params* prm, VeilGeom& g)
+{
+    if (prm->width <= 0 || prm->height <= 0 || prm->fmt_w <= 0 || prm->fmt_h <= 0)
+        return fail(GL_ERR_INVALID, "veil_plan_execute: degenerate output dimensions");
+    if ((long long)prm->width * prm->height > (1LL << 31)) return fail(GL_ERR_INVALID, "veil_plan_execute: too many pixels");
+    g.half_ref = prm->sensor_half_h > 0.0f ? prm->sensor_half_h : prm->sensor_half_w;
+    if (!(g.half_ref > 0.0f) || !(prm->sensor_half_w > 0.0f) || !(prm->sensor_half_h > 0.0f))
+        return fail(GL_ERR_INVALID, "veil_plan_execute: degenerate sensor half-size");
+    float spread = prm->spread;
+    if (!(spread > 0.0f)) spread = 0.12f;
+    g.spread = spread < 1e-3f ? 1e-3f : (spread > 4.0f ? 4.0f : spread);
+    const int N = kVeilGrid;
+    g.a_texels = (float)N / (float)kVeilCoreDiv;
+    g.dx_fine = g.spread * g.half_ref / g.a_texels;                 // sensor mm per fine texel
+    g.px_mm_x = 2.0f * prm->sensor_half_w / (float)prm->fmt_w;
+    g.px_mm_y = 2.0f * prm->sensor_half_h / (float)prm->fmt_h;
+    const double target = std::min((double)g.px_mm_x / (g.dx_fine * kSpriteOversample),
+                                    (double)g.px_mm_y / (g.dx_fine * kSpriteOversample));
+    g.ds = 1;
+    while (g.ds * 2 <= target && g.ds * 2 <= N / 8) g.ds *= 2;
+    g.M = N / g.ds;
+    return GL_OK;
+}
+
+}  // namespace
+}  // namespace gl
+
 extern "C" int gl_veil_plan_execute(gl_veil_plan* plan, const gl_veil_source* d_sources, int n_sources,
                                     const gl_veil_params* prm, float* d_out_r, float* d_out_g, float* d_out_b,
                                     void* stream)
@@ -184,27 +223,13 @@ extern "C" int gl_veil_plan_execute(gl_veil_plan* plan, const gl_veil_source* d_
     if (!plan || !prm || !d_out_r || !d_out_g || !d_out_b) return fail(GL_ERR_INVALID, "veil_plan_execute: null argument");
     if (n_sources < 0 || n_sources > 65536 || (n_sources > 0 && !d_sources))
         return fail(GL_ERR_INVALID, "veil_plan_execute: bad source list");
-    if (prm->width <= 0 || prm->height <= 0 || prm->fmt_w <= 0 || prm->fmt_h <= 0)
-        return fail(GL_ERR_INVALID, "veil_plan_execute: degenerate output dimensions");
-    if ((long long)prm->width * prm->height > (1LL << 31)) return fail(GL_ERR_INVALID, "veil_plan_execute: too many pixels");
-    const float half_ref = prm->sensor_half_h > 0.0f ? prm->sensor_half_h : prm->sensor_half_w;
-    if (!(half_ref > 0.0f) || !(prm->sensor_half_w > 0.0f) || !(prm->sensor_half_h > 0.0f))
-        return fail(GL_ERR_INVALID, "veil_plan_execute: degenerate sensor half-size");
+    VeilGeom G;
+    if (int rc = veil_geometry(prm, G)) return rc;
     VeilPlan* v = plan->p;
     cudaStream_t st = (cudaStream_t)stream;
-    float spread = prm->spread;
-    if (!(spread > 0.0f)) spread = 0.12f;
-    spread = spread < 1e-3f ? 1e-3f : (spread > 4.0f ? 4.0f : spread);
     const int N = kVeilGrid;
-    const float a_texels = (float)N / (float)kVeilCoreDiv;
-    const float dx_fine = spread * half_ref / a_texels;            // sensor mm per fine texel
-    const float px_mm_x = 2.0f * prm->sensor_half_w / (float)prm->fmt_w;
-    const float px_mm_y = 2.0f * prm->sensor_half_h / (float)prm->fmt_h;
-    const double target = std::min((double)px_mm_x / (dx_fine * kSpriteOversample),
-                                    (double)px_mm_y / (dx_fine * kSpriteOversample));
-    int ds = 1;
-    while (ds * 2 <= target && ds * 2 <= N / 8) ds *= 2;
-    const int M = N / ds;
+    const int ds = G.ds, M = G.M;
+    const float dx_fine = G.dx_fine, px_mm_x = G.px_mm_x, px_mm_y = G.px_mm_y;
     int launches = 0;
     const float* sprite = v->ref;
     if (ds > 1)
@@ -243,5 +268,28 @@ extern "C" int gl_veil_plan_destroy(gl_veil_plan* plan)
     cudaFree(plan->p->coarse);
     delete plan->p;
     delete plan;
+    return GL_OK;
+}
+
+extern "C" int gl_veil_plan_geometry(const gl_veil_plan* plan, const gl_veil_params* prm, gl_veil_geometry* out)
+{
+    if (!plan || !prm || !out) return fail(GL_ERR_INVALID, "veil_plan_geometry: null argument");
+    VeilGeom G;
+    if (int rc = veil_geometry(prm, G)) return rc;
+    out->grid = kVeilGrid;
+    out->ds = G.ds;
+    out->dx_mm = G.dx_fine;
+    out->core_mm = G.spread * G.half_ref;
+    out->falloff = plan->p->falloff;
+    out->core_texels = G.a_texels;
+    return GL_OK;
+}
+
+extern "C" int gl_veil_plan_read(const gl_veil_plan* plan, float* d_reference, void* stream)
+{
+    if (!plan || !d_reference) return fail(GL_ERR_INVALID, "veil_plan_read: null argument");
+    const size_t NN = (size_t)kVeilGrid * kVeilGrid;
+    GL_CUDA_TRY(cudaMemcpyAsync(d_reference, plan->p->ref, NN * sizeof(float), cudaMemcpyDeviceToDevice,
+                                (cudaStream_t)stream));
     return GL_OK;
 }

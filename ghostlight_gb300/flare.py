@@ -528,28 +528,36 @@ def render_source_flare(offsets, width: int, height: int, lens: OpticalSystem,
                     * calibration.sensor_half_h / hh
             pos[i] = (sx * width, sy * height, src[i, 2], src[i, 3], src[i, 4])
     if want_sb:
-        # engine choice as render_starburst (starburst_render.cu:646-711): the
-        # SPRITE engine by default and whenever the pattern is prominent or
-        # the grid grows; the matrix-DFT engine otherwise when asked for, in
-        # the reference's pixel-integrated form (or the field form when
-        # diffraction.mdft_form == "field")
-        from .starburst import mdft_box_starburst_layer, sprite_geometry, sprite_starburst_layer, starburst_layer
-        geo = sprite_geometry(calibration, config, pos, width, height, hw, hh,
-                              front_R=lens.surfaces[0].semi_aperture if lens.surfaces else 0.0)
         field = (float(np.float32(np.mean(src[:, 0].astype(np.float64)))),
                  float(np.float32(np.mean(src[:, 1].astype(np.float64)))))
-        if geo["engine"] == "sprite":
-            out.update(sprite_starburst_layer(lens, calibration, config, pos, width, height, hw, hh, geometry=geo,
-                                              field=field))
-        elif getattr(dc, "mdft_form", "pixel") == "field":
-            out.update(starburst_layer(lens, calibration, config, pos, width, height, hw, hh))
-        else:
-            out.update(mdft_box_starburst_layer(lens, calibration, config, pos, width, height, hw, hh,
-                                                geometry=geo, field=field))
+        out.update(starburst_layer_for(lens, calibration, config, pos, width, height, hw, hh, field)[0])
     if want_veil:
         from .veil import render_veil
         out.update(render_veil(pos, width, height, hw, hh, dc.veil_spread, dc.veil_falloff, dc.veil_gain))
     return out
+
+
+def starburst_layer_for(lens, calibration, config, pos, width: int, height: int, hw: float, hh: float, field):
+    """The starburst layer for sources at buffer pixels ``pos`` ((N, 5) px,
+    py, r, g, b) whose mean direction is ``field``, with the engine
+    render_starburst picks (starburst_render.cu:646-711): the SPRITE engine by
+    default and whenever the pattern is prominent or the grid grows; the
+    matrix-DFT engine otherwise when asked for, in the reference's
+    pixel-integrated form (or the field form when diffraction.mdft_form ==
+    "field").  Returns (layer dict, sprite geometry)."""
+    from .starburst import mdft_box_starburst_layer, sprite_geometry, sprite_starburst_layer, starburst_layer
+    dc = config.diffraction
+    geo = sprite_geometry(calibration, config, pos, width, height, hw, hh,
+                          front_R=lens.surfaces[0].semi_aperture if lens.surfaces else 0.0)
+    if geo["engine"] == "sprite":
+        layer = sprite_starburst_layer(lens, calibration, config, pos, width, height, hw, hh, geometry=geo,
+                                       field=field)
+    elif getattr(dc, "mdft_form", "pixel") == "field":
+        layer = starburst_layer(lens, calibration, config, pos, width, height, hw, hh)
+    else:
+        layer = mdft_box_starburst_layer(lens, calibration, config, pos, width, height, hw, hh, geometry=geo,
+                                         field=field)
+    return layer, geo
 
 
 def render_point_flare(width: int, height: int, lens: OpticalSystem, calibration: LensCalibration,

@@ -436,7 +436,8 @@ def sprite_geometry(calibration, config, sources_px, width: int, height: int, se
     return dict(N=N, engine=engine, fill=float(fill), ep_x=float(ep_x), ep_y=float(ep_y), sx=float(sx), sy=float(sy),
                 ds=ds, M=M, sx_ds=float(sx_ds),
                 sy_ds=float(sy_ds), px_mm_x=float(px_mm_x), px_mm_y=float(px_mm_y), rx=rx, ry=ry,
-                gain=float(gain), fnum_x=float(fnum_x), fnum_y=float(fnum_y))
+                gain=float(gain), fnum_x=float(fnum_x), fnum_y=float(fnum_y), efl_x=float(efl_x),
+                efl_y=float(efl_y))
 
 
 def build_pupil2(lens, N: int, pupil_fill: float, blades_override: int = 0, rotation_deg: float = 0.0,
@@ -464,22 +465,24 @@ def build_pupil2(lens, N: int, pupil_fill: float, blades_override: int = 0, rota
     return out
 
 
-def effective_pupil(lens, config, g, field):
-    """The sprite's pupil and its throughput T (render_starburst :740-922):
-    on axis, or with use_survivor_mask off, the plain stop and T = 1;
-    off axis, the stop weighted by the cat's-eye envelope centred on the
-    surviving crescent, T = its energy over the plain stop's.  Returns
-    (pupil, T), or (None, 0) where nothing survives at this field."""
+def effective_pupil_info(lens, config, g, field) -> dict:
+    """The sprite's pupil, its throughput T and the survivor-centre launch
+    offset (render_starburst :740-922): on axis, or with use_survivor_mask
+    off, the plain stop, T = 1 and no offset; off axis, the stop weighted by
+    the cat's-eye envelope centred on the surviving crescent, T = its energy
+    over the plain stop's.  {"pupil", "T", "chief": (cx, cy), "survivors"};
+    pupil is None only where no launch survives at this field."""
     dc = config.diffraction
     f = np.float32
     bo, rot = int(config.aperture_blades), float(config.aperture_rotation)
     ax, ay = (f(field[0]), f(field[1])) if field is not None else (f(0.0), f(0.0))
     off_axis = abs(float(ax)) > 1e-5 or abs(float(ay)) > 1e-5
     if not (bool(dc.use_survivor_mask) and off_axis):
-        return build_pupil2(lens, g["N"], g["fill"], bo, rot), 1.0
+        return {"pupil": build_pupil2(lens, g["N"], g["fill"], bo, rot), "T": 1.0, "chief": (0.0, 0.0),
+                "survivors": True}
     cx, cy, any_surv = survivor_center(lens, float(ax), float(ay))
     if not any_surv:
-        return None, 0.0
+        return {"pupil": None, "T": 0.0, "chief": (0.0, 0.0), "survivors": False}
     me = min(max(int(dc.survivor_grid), 16), 1024)
     env = survivor_envelope(lens, g["ep_x"], g["ep_y"], cx, cy, float(ax), float(ay), me)
     plain = build_pupil2(lens, g["N"], g["fill"], bo, rot)
@@ -487,9 +490,17 @@ def effective_pupil(lens, config, g, field):
     s_ref = float((plain.double() ** 2).sum())
     s_eff = float((pupil.double() ** 2).sum())
     T = min(max(s_eff / s_ref, 0.0), 1.0) if s_ref > 0 else 1.0
-    if T < 1e-3:
-        return None, T
-    return pupil, T
+    return {"pupil": pupil, "T": T, "chief": (cx, cy), "survivors": True}
+
+
+def effective_pupil(lens, config, g, field):
+    """(pupil, T) of effective_pupil_info, or (None, T) where the starburst is
+    cut off: nothing survives, or T < 1e-3 (the field is past the lens's
+    imaged circle)."""
+    info = effective_pupil_info(lens, config, g, field)
+    if info["pupil"] is None or info["T"] < 1e-3:
+        return None, info["T"]
+    return info["pupil"], info["T"]
 
 
 def sprite_starburst_layer(lens, calibration, config, sources_px, width: int, height: int, sensor_half_w: float,

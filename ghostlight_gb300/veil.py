@@ -15,6 +15,8 @@ import numpy as np
 from . import _native
 from ._abi import gl_veil_params
 
+VEIL_GRID = 1024      # side of the plan's resident sprite (gl_veil_plan_geometry reports it)
+
 
 class VeilPlan:
     def __init__(self, falloff: float = 1.5, stream=None):
@@ -50,6 +52,26 @@ class VeilPlan:
                                                      out_r.data_ptr(), out_g.data_ptr(), out_b.data_ptr(), st),
                       "veil")
         return _native.last_launch_count()
+
+    def geometry(self, width: int, height: int, sensor_half_w: float, sensor_half_h: float, spread: float,
+                 fmt=None) -> dict:
+        """The scale an execute with these arguments uses: grid, ds, dx_mm
+        (sensor mm per sprite texel), core_mm, falloff, core_texels."""
+        from ._abi import gl_veil_geometry
+        fw, fh = (width, height) if fmt is None else fmt
+        prm = gl_veil_params(int(width), int(height), int(fw), int(fh), float(sensor_half_w), float(sensor_half_h),
+                             float(spread), 0.0, 0)
+        out = gl_veil_geometry()
+        _native.check(self._lib.gl_veil_plan_geometry(self._h, C.byref(prm), C.byref(out)), "veil")
+        return {k: getattr(out, k) for k, _ in gl_veil_geometry._fields_}
+
+    def read(self, stream=None):
+        """The resident unit-sum GSF sprite, (grid, grid) float32 CUDA tensor."""
+        import torch
+        out = torch.empty((VEIL_GRID, VEIL_GRID), dtype=torch.float32, device="cuda")
+        st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        _native.check(self._lib.gl_veil_plan_read(self._h, C.c_void_p(out.data_ptr()), C.c_void_p(st)), "veil")
+        return out
 
     def close(self):
         if getattr(self, "_h", None):

@@ -647,6 +647,21 @@ int gl_veil_plan_execute(gl_veil_plan* plan, const gl_veil_source* d_sources, in
                          const gl_veil_params* params, float* d_out_r, float* d_out_g,
                          float* d_out_b, void* stream);
 int gl_veil_plan_destroy(gl_veil_plan* plan);
+/* The scale an execute with these params uses and the resident sprite — what
+ * the reference's VeilDebug capture reports (veil_render.h:31-40, filled at
+ * veil_render.cu:400-412; Python _render_veil_debug, bind_renderers.cpp:244).
+ * gl_veil_plan_read copies the grid x grid unit-sum GSF (the reference
+ * replicates it into its neutral RGB sprite) on the stream. */
+typedef struct gl_veil_geometry {
+    int32_t grid;            /* sprite side N (1024)                        */
+    int32_t ds;              /* box-sum factor toward the output pitch      */
+    float dx_mm;             /* sensor mm per sprite texel (isotropic)      */
+    float core_mm;           /* GSF core radius a on the sensor             */
+    float falloff;           /* radial power p actually used                */
+    float core_texels;       /* core radius in sprite texels (N / 32)       */
+} gl_veil_geometry;
+int gl_veil_plan_geometry(const gl_veil_plan* plan, const gl_veil_params* params, gl_veil_geometry* out);
+int gl_veil_plan_read(const gl_veil_plan* plan, float* d_reference, void* stream);
 
 /* ---- PSF grid (render_psf: PSFRenderer.cpp:243-465, psf_render.cu) --------
  * Per source, the lens's primary-ray spot in its own tile of a composite
