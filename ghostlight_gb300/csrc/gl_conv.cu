@@ -335,9 +335,9 @@ extern "C" int gl_conv2d_plan_create(int width, int height, const float* h_kerne
     if (p->P != p->Q) chk(cudaMalloc(&p->tw_p, sizeof(float2) * (size_t)p->P));
     else p->tw_p = p->tw_q;
     chk(cudaMalloc(&kdev, sizeof(float) * kplane.size()));
-    chk(cudaFuncSetAttribute(conv_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_col));
-    chk(cudaFuncSetAttribute(conv_rows_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_row));
-    chk(cudaFuncSetAttribute(conv_rows_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_row));
+    chk((cudaError_t)raise_smem_limit((const void*)conv_cols, p->smem_col));
+    chk((cudaError_t)raise_smem_limit((const void*)conv_rows_fwd, p->smem_row));
+    chk((cudaError_t)raise_smem_limit((const void*)conv_rows_inv, p->smem_row));
     if (e == cudaSuccess)
     {
         chk(cudaMemcpyAsync(p->tw_q, twq.data(), sizeof(float2) * twq.size(), cudaMemcpyHostToDevice, st));

@@ -29,6 +29,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <vector>
 
@@ -661,24 +662,27 @@ size_t render_smem(int n_surf, int n_spec)
            (size_t)n_surf * sizeof(SurfRec) + (size_t)kRenderThreads * kAccStride * 4;
 }
 
-// The opt-in only grows (process-wide, per kernel), so a plan created earlier
+// The opt-in only grows (per device and kernel), so a plan created earlier
 // with a larger table keeps launching after a smaller one was prepared.
-static std::mutex g_smem_mutex;
-static size_t g_smem_optin = 0;
+int raise_smem_limit(const void* kernel, size_t bytes)
+{
+    static std::mutex mu;
+    static std::map<std::pair<int, const void*>, size_t> limit;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return (int)e;
+    std::lock_guard<std::mutex> lk(mu);
+    size_t& cur = limit[{dev, kernel}];
+    if (bytes <= cur) return (int)cudaSuccess;
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) cur = bytes;
+    return (int)e;
+}
 
 cudaError_t render_prepare(size_t smem, int* per_sm, int* n_sm)
 {
-    cudaError_t e = cudaSuccess;
-    {
-        std::lock_guard<std::mutex> lk(g_smem_mutex);
-        if (smem > g_smem_optin)
-        {
-            e = cudaFuncSetAttribute(ghost_render_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e == cudaSuccess)
-                e = cudaFuncSetAttribute(ghost_render_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e == cudaSuccess) g_smem_optin = smem;
-        }
-    }
+    cudaError_t e = (cudaError_t)raise_smem_limit((const void*)ghost_render_kernel<false>, smem);
+    if (e == cudaSuccess) e = (cudaError_t)raise_smem_limit((const void*)ghost_render_kernel<true>, smem);
     if (e == cudaSuccess && per_sm) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, ghost_render_kernel<false>, kRenderThreads, smem);
     int dev = 0;
     if (e == cudaSuccess && n_sm) e = cudaGetDevice(&dev);

@@ -14,6 +14,12 @@ extern thread_local std::string g_last_error;
 extern thread_local int g_last_launches;
 int fail(int code, const std::string& msg);
 
+// Raise (never lower) a kernel's dynamic shared-memory limit on the current
+// device; returns a cudaError_t.  The limit belongs to the function, shared
+// by every plan on the device, so a plan prepared for a smaller size must not
+// shrink it under the launches of a plan prepared earlier for a larger one.
+int raise_smem_limit(const void* kernel, size_t bytes);
+
 // Entrance-pupil silhouette (aperture_sampler.h:49-83), plain polygon form.
 struct PupilMask {
     float aspect = 1.0f;

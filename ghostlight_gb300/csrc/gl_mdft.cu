@@ -905,6 +905,7 @@ extern "C" int gl_mdft_plan_create3(int n, int Kx, int Ky, int n_lambda, const d
     chk(cudaMalloc(&p->weights, sizeof(float4) * n_lambda));
     chk(cudaMalloc(&p->scales, sizeof(float2) * 2 * n_lambda));
     chk(cudaMalloc(&p->err, sizeof(int)));
+    chk(cudaMemset(p->err, 0, sizeof(int)));          // a plan never executed reports no error
     int dev = 0;
     chk(cudaGetDevice(&dev));
     chk(cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, dev));

@@ -186,7 +186,7 @@ extern "C" int gl_psf_render(const gl_surface* surfaces, int n_surfaces, const g
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_grid, grid, (size_t)n_grid * sizeof(float2), cudaMemcpyHostToDevice, st);
     const size_t smem = recs.size() * sizeof(SurfRec) + at.size() * sizeof(float);
     if (e == cudaSuccess && smem > 48 * 1024)
-        e = cudaFuncSetAttribute(psf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        e = (cudaError_t)raise_smem_limit((const void*)psf_kernel, smem);
     if (e == cudaSuccess)
     {
         PsfArgs A;

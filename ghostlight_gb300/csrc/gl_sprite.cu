@@ -333,13 +333,13 @@ extern "C" int gl_sprite_plan_create(int N, const gl_spectral_sample* spec, int 
         for (int l = 0; l < n_spec; ++l) sp[l] = make_float4(spec[l].lambda, spec[l].cmf_r, spec[l].cmf_g, spec[l].cmf_b);
         chk(cudaMemcpy(p->tw, tw.data(), sizeof(float2) * N, cudaMemcpyHostToDevice));
         chk(cudaMemcpy(p->spec, sp.data(), sizeof(float4) * n_spec, cudaMemcpyHostToDevice));
-        chk(cudaFuncSetAttribute(sprite_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_rows));
-        if (nb == 4) chk(cudaFuncSetAttribute(sprite_cols<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_cols));
-        if (nb == 2) chk(cudaFuncSetAttribute(sprite_cols<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_cols));
-        if (nb == 1) chk(cudaFuncSetAttribute(sprite_cols<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_cols));
-        if (nb == 4) chk(cudaFuncSetAttribute(autocorr_cols<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_cols));
-        if (nb == 2) chk(cudaFuncSetAttribute(autocorr_cols<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_cols));
-        if (nb == 1) chk(cudaFuncSetAttribute(autocorr_cols<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_cols));
+        chk((cudaError_t)raise_smem_limit((const void*)sprite_rows, p->smem_rows));
+        if (nb == 4) chk((cudaError_t)raise_smem_limit((const void*)sprite_cols<4>, p->smem_cols));
+        if (nb == 2) chk((cudaError_t)raise_smem_limit((const void*)sprite_cols<2>, p->smem_cols));
+        if (nb == 1) chk((cudaError_t)raise_smem_limit((const void*)sprite_cols<1>, p->smem_cols));
+        if (nb == 4) chk((cudaError_t)raise_smem_limit((const void*)autocorr_cols<4>, p->smem_cols));
+        if (nb == 2) chk((cudaError_t)raise_smem_limit((const void*)autocorr_cols<2>, p->smem_cols));
+        if (nb == 1) chk((cudaError_t)raise_smem_limit((const void*)autocorr_cols<1>, p->smem_cols));
     }
     if (e != cudaSuccess)
     {

@@ -157,7 +157,12 @@ def test_starburst_capture_matches_frame_render(psf_lens, engine, sx):
     d = gl._render_starburst_debug(192, 192, psf_lens, cal, cfg)
     out = gl.render_point_flare(192, 192, psf_lens, cal, cfg)
     for c in "rgb":
-        np.testing.assert_array_equal(d["starburst_" + c], out["starburst_" + c].cpu().numpy())
+        want = out["starburst_" + c].cpu().numpy()
+        if engine == SPRITE:
+            np.testing.assert_array_equal(d["starburst_" + c], want)
+        else:
+            # the window accumulates wavelengths with float atomics: order noise
+            np.testing.assert_allclose(d["starburst_" + c], want, rtol=1e-5, atol=1e-6 * float(want.max()))
     N = d["grid"]
     assert N >= 1024 and d["pupil"].shape == (N, N) and d["psf"].shape == (N, N)
     assert d["sprite_rgb"].shape == (N, N, 3)
@@ -174,7 +179,14 @@ def test_starburst_capture_matches_frame_render(psf_lens, engine, sx):
         return
     assert float(d["psf"].sum(dtype=np.float64)) == pytest.approx(1.0, abs=1e-4)
     assert np.unravel_index(np.argmax(d["psf"]), d["psf"].shape) == (N // 2, N // 2)
-    assert d["sprite_rgb"].min() >= 0.0 and d["sprite_rgb"].sum() > 0.0
+    # each wavelength's scaled copy of the unit-sum PSF keeps (nearly) unit sum,
+    # so a channel sums to its colour-matching weights over the spectrum (the
+    # weights go negative in places, so can single texels)
+    from ghostlight_gb300.starburst import starburst_spectrum
+    spec = starburst_spectrum(cfg)
+    sums = d["sprite_rgb"].sum(axis=(0, 1), dtype=np.float64)
+    expect = spec[:, 1:4].astype(np.float64).sum(0)
+    np.testing.assert_allclose(sums, expect, rtol=0.05, atol=0.02 * float(np.abs(expect).max()))
     if sx == 0.5:
         assert d["throughput"] == 1.0 and d["chief_offset_x"] == 0.0
     else:
