@@ -17,6 +17,7 @@ the data path); value = frames of all ranks / max-over-ranks time.
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import math
 import os
@@ -43,6 +44,14 @@ N_SPEC = 31
 SOURCE_DEG = 15.0
 MIN_INTENSITY = 1e-6
 GOLDEN = REPO / "tests" / "golden"
+
+
+_T0 = time.perf_counter()
+
+
+def _progress(what: str) -> None:
+    """One line on stderr per finished section: where a long run spends its time."""
+    print("[bench +%.1fs] %s" % (time.perf_counter() - _T0, what), file=sys.stderr, flush=True)
 
 
 def _workload():
@@ -159,6 +168,7 @@ def run_gpu(args, rank, world):
     from ghostlight_gb300.autotune import Tuner, tune_ghost_plan
     tuner = Tuner(reps=3)
     tune_ghost_plan(plan, outs, stream=stream, tuner=tuner)
+    _progress("autotune")
 
     # ---- batched form: graph-captured launch ----
     # Events around the render launch are captured into the graph (external
@@ -204,6 +214,7 @@ def run_gpu(args, rank, world):
     torch.cuda.synchronize()
     with ClockSampler(dev.index) as clk:
         t_batched = timed(graph.replay, args.steps, args.warmup, after=read_kernel_events)
+        _progress("batched frames")
     torch.cuda.synchronize()
     plan.set_timing()
     frame_host = torch.stack(outs).cpu().numpy()       # the frame of the last timed replay
@@ -247,6 +258,7 @@ def run_gpu(args, rank, world):
     if n_e2e:
         e2e_run(2)                                        # warm
         te = [e2e_run(n_e2e) / n_e2e] * n_e2e
+        _progress("end-to-end frames")
     else:
         te = [float("nan")]
     h2d = int(lens.num_surfaces() * 192 + 2 * N_SPEC * lens.num_surfaces() * 4 + N_SPEC * 16 +
@@ -258,6 +270,7 @@ def run_gpu(args, rank, world):
     if not args.quick or args.only == "cfg3":
         with torch.cuda.stream(stream):
             cfg3, sb_inputs = run_cfg3(args, dev, stream, flush, timed)
+            _progress("starburst precision / convolution / sprite")
             if not args.quick:
                 frame_res = run_full_frame(args, dev, stream, timed, plan, plain, sb_inputs, sb_inputs[4])
             sb_inputs[4].close()
@@ -427,7 +440,7 @@ def run_cfg3(args, dev, stream, flush, timed):
     csec = sum(ts) / len(ts)
     cbytes = conv.traffic_bytes()
     gbs = cbytes / csec / 1e9
-    conv_res = {"ms": 1e3 * csec, "P": conv.P, "Q": conv.Q, "route": "FFT, 3 HBM passes",
+    conv_res = {"ms": 1e3 * csec, "P": conv.P, "Q": conv.Q, "route": "FFT, three passes per channel pair (two pairs), the pair's intermediate L2-resident between passes",
                 "rel_l2_64px_vs_fp64_direct": _conv_points(img, torch.from_numpy(kern).to(dev), cout),
                 "direct_equivalent_tflops": 2.0 * W * H * CONV_K * CONV_K * 3 / csec / 1e12,
                 "roofline": {"bound": "hbm", "achieved": gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
@@ -566,7 +579,7 @@ def _serve_mix(args, pool, cfg, sb_on, seconds, dump):
     import torch
     import ghostlight_gb300 as gl
     from ghostlight_gb300.flare import GhostRenderPlan, pupil_grid
-    from ghostlight_gb300.serve import (STARBURST_PUPIL, FlareRequest, FlareServer, _spectral, latency_stats,
+    from ghostlight_gb300.serve import (FlareRequest, FlareServer, SpriteStarbursts, _spectral, latency_stats,
                                         poisson_requests)
     reqs = poisson_requests(args.serve_rate, seconds, pool.keys(), seed=5, starburst=sb_on)
     # warm: one request per lens
@@ -575,16 +588,18 @@ def _serve_mix(args, pool, cfg, sb_on, seconds, dump):
                                 starburst=sb_on) for i in pool])
     torch.cuda.synchronize()
     warm_exec = srv.exec
+    _progress("serving warm-up (starburst %s)" % sb_on)
     srv = FlareServer(pool, budget_bytes=SERVE_BUDGET, max_inflight=args.serve_slots, items_per_warp=8,
                       policy=args.serve_policy)
     # a pinned result buffer per slot and size: no host allocation while serving
     srv.exec.prewarm([(w, w) for w in (512, 1024, 2048, 4096)], args.serve_slots)
     sb_bytes = 0
-    if sb_on:                                     # resident DFT matrices of every (size, wavelength count)
-        srv.exec.starburst = warm_exec.starburst
+    if sb_on:                                     # resident sprites of every (lens, size, wavelength count)
+        srv.exec.sprites = warm_exec.sprites
         srv.exec.prewarm_starburst([(w, w) for w in (512, 1024, 2048, 4096)], (8, 16, 31), cfg)
         torch.cuda.synchronize()
-        sb_bytes = sum(p.device_bytes() for p, _ in srv.exec.starburst.plans.values())
+        sb_bytes = srv.exec.sprites.device_bytes()
+        _progress("serving sprite bakes")
     import gc
     gc.collect()
     gc.disable()                                  # no collector pauses inside the request loop
@@ -596,6 +611,7 @@ def _serve_mix(args, pool, cfg, sb_on, seconds, dump):
             wall = time.perf_counter() - t1
     finally:
         gc.enable()
+    _progress("serving timed mix (starburst %s)" % sb_on)
     traced = sum(r.traced for r in reqs)
     if dump:
         with open(dump, "w") as f:
@@ -622,30 +638,35 @@ def _serve_mix(args, pool, cfg, sb_on, seconds, dump):
                                apply_correction=True, plain_per_pair=True)
         outs = torch.empty((3, r.height, r.width), device="cuda")
         plan.execute(outs[0], outs[1], outs[2])
-        if r.starburst:                           # DFT matrices built for this call
+        if r.starburst:                           # the sprite baked for this call, as the reference renders
             cx, cy = rl.image_point(r.field_deg, r.width, r.height)
-            lam = spec[:, 0].astype(np.float64)
-            sc = lam.min() / lam
-            mp = gl.MdftPlan(STARBURST_PUPIL, (r.width, r.height), sc / r.width, sc / r.height, spec[:, 1:4],
-                             "split_bf16", center_x=cx, center_y=cy)
-            mp.execute(rl.starburst_pupil(), outs[0], outs[1], outs[2], accumulate=True)
-            mp.close()
+            sb = SpriteStarbursts()
+            sprite, M, g = sb._bake(rl, r.width, r.height, r.n_spec)
+            lib = gl._native.load()
+            gl._native.check(lib.gl_sprite_splat_source(
+                ctypes.c_void_p(sprite.data_ptr()), M, float(cx), float(cy), 1.0, 1.0, 1.0, g["sx_ds"], g["sy_ds"],
+                g["px_mm_x"], g["px_mm_y"], g["rx"], g["ry"], g["gain"], ctypes.c_void_p(outs[0].data_ptr()),
+                ctypes.c_void_p(outs[1].data_ptr()), ctypes.c_void_p(outs[2].data_ptr()), r.width, r.height,
+                ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)), "starburst")
         outs.cpu()
         plan.close()
         ts.append(time.perf_counter() - tt)
     serial_req_s = len(ts) / sum(ts)
+    _progress("serving serial sample")
     served_req_s = len(reqs) / wall
     if sb_on:
-        srv.exec.starburst.close()
+        srv.exec.sprites.close()
     return {"workload": "Poisson %.0f req/s for %.0f s (%d requests), %d resident lenses of 8-30 surfaces, "
                         "outputs 512^2-4096^2, 8/16/31 wavelengths, pupil grids 32^2-256^2, field 0-20 deg, "
                         "%d slots, %.0f GB HBM budget, %s priorities" % (
                             args.serve_rate, seconds, len(reqs), SERVE_LENSES, args.serve_slots,
                             SERVE_BUDGET / 1e9, args.serve_policy),
             "layers": ("ghost + starburst: every request whose source images within a frame width of the frame "
-                       "(%d of %d) adds the split-BF16 matrix DFT of its lens's 256^2 stop pupil from resident "
-                       "plans per (size, wavelength count), %.2f GB" % (sum(bool(r.starburst) for r in reqs),
-                                                                      len(reqs), sb_bytes / 1e9))
+                       "(%d of %d) adds its lens's SPRITE starburst (the reference's default engine: the stop "
+                       "pupil's FFT baked over the request's wavelengths at the physical scale of the lens's "
+                       "calibration, box-summed to the output pitch), resident per (lens, size, wavelength "
+                       "count), splatted at the source's image point on the request's stream, %.2f GB of "
+                       "sprites" % (sum(bool(r.starburst) for r in reqs), len(reqs), sb_bytes / 1e9))
             if sb_on else "ghost",
             "throughput_req_s": served_req_s, "wall_s": wall, "offered_req_s": len(reqs) / seconds,
             "rays_per_s": traced / wall, "ray_lambda_traces": traced,
@@ -1071,10 +1092,13 @@ def main():
         lens, cal = _workload()
         if not (args.no_cpu_baseline or args.quick):
             res["cpu_baseline"], res["parity"] = cpu_baseline(plan, lens, cal, gpu_frame)
+            _progress("cpu baseline and FP64 parity")
         if not args.quick:
             res["anamorphic_sweep"] = run_sweep(args)
+            _progress("anamorphic sweep")
         if not args.quick and args.serve_seconds > 0:
             res["serving"] = run_serving(args)
+            _progress("serving")
         res["roofline"] = roofline(res, plan)
         print(json.dumps(res))
     if world > 1:

@@ -41,6 +41,7 @@ def _declare(lib):
                                          vp_, vp_, vp_, i, i, vp_]
     lib.gl_sprite_plan_read.argtypes = [vp_, vp_, vp_, P(C.c_double), P(i), vp_]
     lib.gl_sprite_plan_destroy.argtypes = [vp_]
+    lib.gl_sprite_splat_source.argtypes = [vp_, i, f, f, f, f, f, f, f, f, f, i, i, f, vp_, vp_, vp_, i, i, vp_]
     lib.gl_coating_table_create.argtypes = [i, fp, i, fp, i, fp, C.c_float, i, P(i)]
     lib.gl_coating_table_info.argtypes = [i, P(i), P(i), P(i), fp, P(i)]
     lib.gl_coating_table_read.argtypes = [i, fp, fp, fp]

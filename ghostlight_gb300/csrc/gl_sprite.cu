@@ -208,21 +208,104 @@ __global__ void __launch_bounds__(kSpriteThreads) sprite_bake(const float* __res
     sprite[3 * (size_t)idx + 2] = sb;
 }
 
-__global__ void __launch_bounds__(kSpriteThreads) sprite_splat(const float* __restrict__ sprite, int M, float sx_ds,
-                                                               float sy_ds, float px_mm_x, float px_mm_y, int rx,
-                                                               int ry, const StarSource* __restrict__ src,
-                                                               int n_src, float gain, float* __restrict__ out_r,
-                                                               float* __restrict__ out_g, float* __restrict__ out_b,
-                                                               int width, int height)
+// One output pixel of one source's footprint (offset t in its
+// (2 rx + 1) x (2 ry + 1) box): the sprite integrated over the pixel's sensor
+// footprint (texel overlap areas), tinted, added.
+// The same bake with the PSF staged in shared memory: a CTA owns a tile of
+// tm x tm coarse texels (fine span F = tm ds <= 64) and, for each wavelength,
+// first loads the window of the PSF that the tile's scaled samples read
+// (about F k + 2 texels a side, k = lambda_ref / lambda) with coalesced
+// loads, then takes every bilinear sample of the tile from it.  Each sample's
+// coordinates and arithmetic are those of sprite_bake, so it reads the same
+// four PSF values; only the order of the sum over wavelengths differs.  The
+// window carries one texel of margin on every side (the bounds and the
+// samples may round differently under contraction); a window wider than the
+// allocation (a spectrum far outside 400-700 nm) is read from global memory.
+__global__ void __launch_bounds__(kSpriteThreads) sprite_bake_tiled(const float* __restrict__ psf, int N,
+                                                                    const float4* __restrict__ spec, int n_spec,
+                                                                    float lambda_ref, int ds, int M, int tm,
+                                                                    int side, const double* __restrict__ energy,
+                                                                    float* __restrict__ sprite)
 {
-    const long long span_x = 2LL * rx + 1, span_y = 2LL * ry + 1;
-    const long long per_src = span_x * span_y;
-    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (tid >= (long long)n_src * per_src) return;
-    const int si = (int)(tid / per_src);
-    const long long t = tid % per_src;
+    extern __shared__ float win[];
+    const double e = *energy;
+    const float scale = (e > 0.0) ? (float)(1.0 / e) : 0.0f;
+    const int t = threadIdx.x;
+    const int a = blockIdx.x * tm + t % tm, b = blockIdx.y * tm + t / tm;
+    const bool own = t < tm * tm && a < M && b < M;
+    const float half = (float)(N / 2);
+    const int F = tm * ds;
+    const int i_lo = blockIdx.x * F, j_lo = blockIdx.y * F;
+    float sr = 0.0f, sg = 0.0f, sb = 0.0f;
+    for (int l = 0; l < n_spec; ++l)
+    {
+        const float4 s = spec[l];
+        const float k = lambda_ref / s.x;
+        const int rx0 = (int)floorf(half + (float)(i_lo - N / 2) * k) - 1;
+        const int ry0 = (int)floorf(half + (float)(j_lo - N / 2) * k) - 1;
+        const int RW = (int)floorf(half + (float)(i_lo + F - 1 - N / 2) * k) + 3 - rx0;
+        const int RH = (int)floorf(half + (float)(j_lo + F - 1 - N / 2) * k) + 3 - ry0;
+        const bool staged = RW <= side && RH <= side;
+        __syncthreads();                         // the previous wavelength's window is read
+        if (staged)
+            for (int q = t; q < RW * RH; q += blockDim.x)
+            {
+                const int y = ry0 + q / RW, x = rx0 + q % RW;
+                win[q] = (x >= 0 && x < N && y >= 0 && y < N) ? psf[(size_t)y * N + x] : 0.0f;
+            }
+        __syncthreads();
+        if (!own) continue;
+        for (int jj = 0; jj < ds; ++jj)
+            for (int ii = 0; ii < ds; ++ii)
+            {
+                const float dx = (float)(a * ds + ii - N / 2), dy = (float)(b * ds + jj - N / 2);
+                const float fx = half + dx * k, fy = half + dy * k;
+                float v = 0.0f;
+                if (!(fx < 0.0f || fy < 0.0f || fx >= (float)(N - 1) || fy >= (float)(N - 1)))
+                {
+                    const int x0 = (int)floorf(fx), y0 = (int)floorf(fy);
+                    const float tx = fx - x0, ty = fy - y0;
+                    const float* r0;
+                    int stride;
+                    if (staged && x0 >= rx0 && x0 + 1 < rx0 + RW && y0 >= ry0 && y0 + 1 < ry0 + RH)
+                    {
+                        r0 = win + (y0 - ry0) * RW + (x0 - rx0);
+                        stride = RW;
+                    }
+                    else
+                    {
+                        r0 = psf + (size_t)y0 * N + x0;
+                        stride = N;
+                    }
+                    const float* r1 = r0 + stride;
+                    const float pa = (r0[0] * scale) * (1.0f - tx) + (r0[1] * scale) * tx;
+                    const float pb = (r1[0] * scale) * (1.0f - tx) + (r1[1] * scale) * tx;
+                    v = pa * (1.0f - ty) + pb * ty;
+                }
+                v = v * k * k;
+                sr += s.y * v;
+                sg += s.z * v;
+                sb += s.w * v;
+            }
+    }
+    if (!own) return;
+    const size_t idx = (size_t)b * M + a;
+    sprite[3 * idx + 0] = sr;
+    sprite[3 * idx + 1] = sg;
+    sprite[3 * idx + 2] = sb;
+}
+
+// Coarse texels per side of a bake tile: the fine span stays <= 64.
+inline int bake_tile(int ds) { return ds <= 4 ? 16 : std::max(1, 64 / ds); }
+
+__device__ __forceinline__ void splat_pixel(const float* __restrict__ sprite, int M, float sx_ds, float sy_ds,
+                                            float px_mm_x, float px_mm_y, int rx, int ry, const StarSource& s,
+                                            long long t, float gain, float* __restrict__ out_r,
+                                            float* __restrict__ out_g, float* __restrict__ out_b, int width,
+                                            int height)
+{
+    const long long span_x = 2LL * rx + 1;
     const int oy = (int)(t / span_x) - ry, ox = (int)(t % span_x) - rx;
-    const StarSource s = src[si];
     const int ix = (int)floorf(s.px) + ox, iy = (int)floorf(s.py) + oy;
     if (ix < 0 || ix >= width || iy < 0 || iy >= height) return;
     // the pixel [ix, ix+1) x [iy, iy+1) in texel-cell coordinates (texel a
@@ -264,6 +347,36 @@ __global__ void __launch_bounds__(kSpriteThreads) sprite_splat(const float* __re
     if (fabsf(vb) > 1e-20f) atomicAdd(&out_b[pix], vb);
 }
 
+__global__ void __launch_bounds__(kSpriteThreads) sprite_splat(const float* __restrict__ sprite, int M, float sx_ds,
+                                                               float sy_ds, float px_mm_x, float px_mm_y, int rx,
+                                                               int ry, const StarSource* __restrict__ src,
+                                                               int n_src, float gain, float* __restrict__ out_r,
+                                                               float* __restrict__ out_g, float* __restrict__ out_b,
+                                                               int width, int height)
+{
+    const long long per_src = (2LL * rx + 1) * (2LL * ry + 1);
+    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= (long long)n_src * per_src) return;
+    const int si = (int)(tid / per_src);
+    splat_pixel(sprite, M, sx_ds, sy_ds, px_mm_x, px_mm_y, rx, ry, src[si], tid % per_src, gain, out_r, out_g,
+                out_b, width, height);
+}
+
+// One source passed by value: no staging buffer, so splats of one resident
+// sprite on many streams run side by side.
+__global__ void __launch_bounds__(kSpriteThreads) sprite_splat_one(const float* __restrict__ sprite, int M,
+                                                                   float sx_ds, float sy_ds, float px_mm_x,
+                                                                   float px_mm_y, int rx, int ry, StarSource s,
+                                                                   float gain, float* __restrict__ out_r,
+                                                                   float* __restrict__ out_g,
+                                                                   float* __restrict__ out_b, int width, int height)
+{
+    const long long per_src = (2LL * rx + 1) * (2LL * ry + 1);
+    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= per_src) return;
+    splat_pixel(sprite, M, sx_ds, sy_ds, px_mm_x, px_mm_y, rx, ry, s, tid, gain, out_r, out_g, out_b, width, height);
+}
+
 }  // namespace
 
 struct SpritePlan {
@@ -280,6 +393,7 @@ struct SpritePlan {
     StarSource* src = nullptr;
     int src_cap = 0;
     size_t smem_rows = 0, smem_cols = 0;
+    float kmax = 1.0f;           // largest lambda_ref / lambda of the spectrum
 };
 
 }  // namespace gl
@@ -313,6 +427,7 @@ extern "C" int gl_sprite_plan_create(int N, const gl_spectral_sample* spec, int 
     p->N = N;
     p->n_spec = n_spec;
     p->lambda_ref = lambda_ref;
+    for (int l = 0; l < n_spec; ++l) p->kmax = std::max(p->kmax, lambda_ref / spec[l].lambda);
     p->dims = make_dims(N);
     cudaGetDevice(&p->device);
     const size_t NN = (size_t)N * N;
@@ -381,8 +496,21 @@ extern "C" int gl_sprite_plan_bake(gl_sprite_plan* plan, const float* d_pupil, i
     else
         sprite_cols<1><<<N, kSpriteThreads, p->smem_cols, st>>>(p->work, N, p->dims, p->tw, p->psf, p->energy);
     const int MM = p->M * p->M;
-    sprite_bake<<<(MM + kSpriteThreads - 1) / kSpriteThreads, kSpriteThreads, 0, st>>>(
-        p->psf, N, p->spec, p->n_spec, p->lambda_ref, ds, p->M, p->energy, p->sprite);
+    const int tm = bake_tile(ds);
+    const int side = (int)std::ceil((double)(tm * ds - 1) * p->kmax) + 6;
+    const size_t bake_smem = (size_t)side * side * sizeof(float);
+    constexpr size_t kBakeSmemMax = 96 * 1024;
+    if (bake_smem <= kBakeSmemMax && raise_smem_limit((const void*)sprite_bake_tiled, bake_smem) == (int)cudaSuccess)
+    {
+        const unsigned tiles = (unsigned)((p->M + tm - 1) / tm);
+        const int threads = std::max(32, (tm * tm + 31) / 32 * 32);
+        sprite_bake_tiled<<<dim3(tiles, tiles), threads, bake_smem, st>>>(p->psf, N, p->spec, p->n_spec,
+                                                                         p->lambda_ref, ds, p->M, tm, side,
+                                                                         p->energy, p->sprite);
+    }
+    else
+        sprite_bake<<<(MM + kSpriteThreads - 1) / kSpriteThreads, kSpriteThreads, 0, st>>>(
+            p->psf, N, p->spec, p->n_spec, p->lambda_ref, ds, p->M, p->energy, p->sprite);
     GL_CUDA_TRY(cudaGetLastError());
     g_last_launches = 3;
     return GL_OK;
@@ -421,6 +549,26 @@ extern "C" int gl_sprite_plan_splat(gl_sprite_plan* plan, const float* sources, 
     GL_CUDA_TRY(cudaGetLastError());
     // the host sources are staged through pageable memory: the copy is done
     // when the call returns, so the caller may reuse them
+    g_last_launches = 1;
+    return GL_OK;
+}
+
+extern "C" int gl_sprite_splat_source(const float* d_sprite, int M, float px, float py, float r, float g, float b,
+                                      float sx_ds, float sy_ds, float px_mm_x, float px_mm_y, int rx, int ry,
+                                      float gain, float* d_out_r, float* d_out_g, float* d_out_b, int width,
+                                      int height, void* stream)
+{
+    if (!d_sprite || M < 1 || !d_out_r || !d_out_g || !d_out_b || width < 1 || height < 1)
+        return fail(GL_ERR_INVALID, "sprite_splat_source: bad arguments");
+    if (!(sx_ds > 0.0f) || !(sy_ds > 0.0f) || !(px_mm_x > 0.0f) || !(px_mm_y > 0.0f) || rx < 0 || ry < 0)
+        return fail(GL_ERR_INVALID, "sprite_splat_source: pitches must be positive");
+    const long long total = (2LL * rx + 1) * (2LL * ry + 1);
+    const long long blocks = (total + kSpriteThreads - 1) / kSpriteThreads;
+    if (blocks > 0x7fffffffLL) return fail(GL_ERR_INVALID, "sprite_splat_source: footprint too large");
+    const StarSource s{px, py, r, g, b};
+    sprite_splat_one<<<(unsigned)blocks, kSpriteThreads, 0, (cudaStream_t)stream>>>(
+        d_sprite, M, sx_ds, sy_ds, px_mm_x, px_mm_y, rx, ry, s, gain, d_out_r, d_out_g, d_out_b, width, height);
+    GL_CUDA_TRY(cudaGetLastError());
     g_last_launches = 1;
     return GL_OK;
 }

@@ -239,6 +239,62 @@ class StarburstPlans:
         self.plans = {}
 
 
+class SpriteStarbursts:
+    """The serving starburst layer by the reference's default SPRITE engine
+    (render_starburst, starburst_render.cu:594-1073): per (lens, output size,
+    wavelength count) the stop pupil's FFT is baked over the spectrum and
+    box-summed toward the output pitch once, with the physical scale of the
+    lens's first-order optics (sprite_geometry), and only the M x M x 3 sprite
+    stays resident.  Each request splats it at its source's image point on
+    the request's own stream (gl_sprite_splat_source: the source passed by
+    value, nothing staged or shared), so requests that use one sprite run side
+    by side.  The pupil is the plain stop, without the field-dependent
+    cat's-eye, as for the matrix-DFT serving layer."""
+
+    def __init__(self):
+        self.sprites: Dict[tuple, tuple] = {}
+
+    def get(self, lens_id: int, rl, width: int, height: int, n_spec: int):
+        key = (int(lens_id), int(width), int(height), int(n_spec))
+        hit = self.sprites.get(key)
+        if hit is None:
+            hit = self._bake(rl, int(width), int(height), int(n_spec))
+            self.sprites[key] = hit
+        return hit
+
+    @staticmethod
+    def config_for(rl, n_spec: int):
+        from .config import DiffractionConfig
+        cfg = dataclasses.replace(rl.config)
+        cfg.spectral_samples = int(n_spec)
+        cfg.diffraction = DiffractionConfig(starburst=True, spectral_samples=int(n_spec), use_survivor_mask=False)
+        return cfg
+
+    def _bake(self, rl, width: int, height: int, n_spec: int):
+        import torch
+        from .starburst import _PLAN_LOCK, _sprite_plan, build_pupil2, sprite_geometry, starburst_spectrum
+        cfg = self.config_for(rl, n_spec)
+        centre = np.array([[0.5 * width, 0.5 * height, 1.0, 1.0, 1.0]], np.float32)
+        front_r = rl.lens.surfaces[0].semi_aperture if rl.lens.surfaces else 0.0
+        g = sprite_geometry(rl.calibration, cfg, centre, width, height, rl.sensor_half_w, rl.sensor_half_h,
+                            front_R=front_r)
+        spec = starburst_spectrum(cfg)
+        with _PLAN_LOCK:
+            plan, baked = _sprite_plan(g["N"], spec)
+            pupil = build_pupil2(rl.lens, g["N"], g["fill"], int(cfg.aperture_blades), float(cfg.aperture_rotation))
+            plan.bake(pupil, g["ds"])
+            _, sprite, _ = plan.read()
+            baked.clear()                   # the shared plan no longer holds a frame render's bake
+            torch.cuda.current_stream().synchronize()
+        return sprite, int(sprite.shape[0]), g
+
+    def device_bytes(self) -> int:
+        return sum(int(sp.numel()) * 4 for sp, _, _ in self.sprites.values())
+
+    def close(self):
+        self.sprites = {}
+
+
 def request_bytes(width: int, height: int, n_pairs: int, host_copy: bool = True) -> int:
     """HBM a request holds: RGBA accumulator + three output planes + tables."""
     px = int(width) * int(height)
@@ -251,10 +307,12 @@ def request_bytes(width: int, height: int, n_pairs: int, host_copy: bool = True)
 class ResidentLens:
     """gl_lens: a lens with its filtered ghost pairs kept on the device."""
 
-    def __init__(self, lens, sensor_half_w: float, sensor_half_h: float, config, pairs=None, boosts=None):
+    def __init__(self, lens, sensor_half_w: float, sensor_half_h: float, config, pairs=None, boosts=None,
+                 calibration=None):
         from .flare import filter_ghosts_device
         self._lib = _native.load()
         self.lens = lens
+        self._calibration = calibration
         self.sensor_half_w, self.sensor_half_h = float(sensor_half_w), float(sensor_half_h)
         self.config = config
         if pairs is None:
@@ -274,6 +332,14 @@ class ResidentLens:
     @property
     def n_pairs(self) -> int:
         return len(self.pairs)
+
+    @property
+    def calibration(self):
+        """The lens's calibration (calibrate_lens), computed on first use."""
+        if self._calibration is None:
+            from .calibration import calibrate_lens
+            self._calibration = calibrate_lens(self.lens)
+        return self._calibration
 
     def starburst_pupil(self):
         """The stop pupil the starburst layer transforms (STARBURST_PUPIL^2,
@@ -375,7 +441,12 @@ class CudaExecutor:
         else:
             self.LEVELS = tuple(lv for lv in (0, -1, -2, -3) if lv >= self.greatest)
         self._heavy: Dict[int, int] = {}         # id(run) -> level of a long request in flight
-        self.starburst: Optional[StarburstPlans] = None    # created on the first starburst request
+        # the starburst layer's engine: "sprite" (the reference's default:
+        # resident baked sprites, one splat per request) or "mdft" (the
+        # split-BF16 matrix DFT of the field over the whole frame)
+        self.starburst_engine = "sprite"
+        self.sprites = SpriteStarbursts()
+        self.starburst: Optional[StarburstPlans] = None    # created on the first matrix-DFT starburst request
         self.starburst_ctas: Optional[int] = None            # None: a quarter of the SMs
         self._lib = _native.load()
         self.lenses = lenses
@@ -477,6 +548,17 @@ class CudaExecutor:
         cx, cy = rl.image_point(req.field_deg, req.width, req.height)
         if abs(cx - 0.5 * req.width) > 1.5 * req.width:
             return False
+        if self.starburst_engine == "sprite":
+            sprite, M, g = self.sprites.get(req.lens_id, rl, req.width, req.height, req.n_spec)
+            d = C.c_void_p()
+            _native.check(self._lib.gl_request_planes(h, C.byref(d)), "request_planes")
+            base, npx = int(d.value), req.width * req.height
+            _native.check(self._lib.gl_sprite_splat_source(
+                C.c_void_p(sprite.data_ptr()), M, float(cx), float(cy), 1.0, 1.0, 1.0, g["sx_ds"], g["sy_ds"],
+                g["px_mm_x"], g["px_mm_y"], g["rx"], g["ry"], g["gain"], C.c_void_p(base),
+                C.c_void_p(base + 4 * npx), C.c_void_p(base + 8 * npx), req.width, req.height,
+                C.c_void_p(stream.cuda_stream)), "starburst")
+            return True
         if self.starburst is None:
             self.starburst = StarburstPlans(self.device, self.starburst_ctas)
         spec, _ = _spectral(req.n_spec, rl.config)
@@ -505,7 +587,14 @@ class CudaExecutor:
         return True
 
     def prewarm_starburst(self, shapes, n_specs, config):
-        """Create the starburst plans of every (size, wavelength count)."""
+        """Bake the sprites of every (lens, size, wavelength count), or create
+        the matrix-DFT plans of every (size, wavelength count)."""
+        if self.starburst_engine == "sprite":
+            for lid, rl in self.lenses.items():
+                for (w, h) in shapes:
+                    for ns in n_specs:
+                        self.sprites.get(lid, rl, w, h, ns)
+            return
         if self.starburst is None:
             self.starburst = StarburstPlans(self.device, self.starburst_ctas)
         for (w, h) in shapes:
@@ -657,6 +746,7 @@ def serving_lens(seed: int, n_surfaces: int, field_deg: float = 20.0):
     lens = OpticalSystem.from_records(surfs, name="serve_%d_%d" % (seed, n_surfaces))
     cal = calibrate_lens(lens)
     lens.serving_focal_x = float(cal.focal_length_x)
+    lens.serving_calibration = cal
     return lens, cal.sensor_half_w, cal.sensor_half_h
 
 
@@ -668,6 +758,6 @@ def serving_lens_pool(n_lenses: int, config, seed: int = 100, n_min: int = 8, n_
     for i in range(n_lenses):
         n = int(rng.integers(n_min, n_max + 1))
         lens, hw, hh = serving_lens(seed + i, n)
-        pool[i] = ResidentLens(lens, hw, hh, config)
+        pool[i] = ResidentLens(lens, hw, hh, config, calibration=lens.serving_calibration)
         pool[i].focal_x = lens.serving_focal_x
     return pool

@@ -514,6 +514,14 @@ int gl_sprite_plan_destroy(gl_sprite_plan* plan);
  * buffers, the scale read on the device; invalidates the plan's sprite. */
 int gl_sprite_plan_autocorr(gl_sprite_plan* plan, const float* d_pupil, int mc, float* d_C, int ldc, int rows,
                             void* stream);
+/* The splat of one source (splat_resample_kernel, starburst_render.cu:316)
+ * from a baked M x M x 3 sprite held by the caller (a copy read out with
+ * gl_sprite_plan_read): the source is passed by value, so the call stages
+ * nothing, allocates nothing and keeps no state; splats of one sprite on
+ * several streams run side by side.  ADDS into the three planes. */
+int gl_sprite_splat_source(const float* d_sprite, int M, float px, float py, float r, float g, float b,
+                           float sx_ds, float sy_ds, float px_mm_x, float px_mm_y, int rx, int ry, float gain,
+                           float* d_out_r, float* d_out_g, float* d_out_b, int width, int height, void* stream);
 
 /* ---- Serving: resident lenses and stream-ordered requests -----------------
  * The reference renders one flare per blocking call under process-wide

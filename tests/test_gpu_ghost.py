@@ -266,6 +266,36 @@ def test_off_sensor_cull_keeps_the_image(pins, meta):
     assert rel_l2(imgs[True], imgs[False]) < 1e-4
 
 
+@pytest.mark.parametrize("deg", [0.0, 9.0, 15.0, 24.0])
+def test_probe_cohorts_keep_the_culled_set(pins, meta, deg):
+    """With more than one wavelength per probe task, the wavelengths after
+    the first are traced as compacted cohorts: the pairs the probe keeps must
+    be those it keeps with one wavelength per task (no cohort) and with every
+    wavelength in one task (the longest cohorts), and the frame the same."""
+    import ghostlight_gb300 as gl
+    from ghostlight_gb300.flare import filter_ghosts_device, prepare_ghost_render
+    lens = _lens(pins, "cfg2_wide_angle_24")
+    cal = meta["cfg2_wide_angle_24"]["calibration"]
+    hw, hh = cal["sensor_half_w"], cal["sensor_half_h"]
+    src = np.array([[np.radians(deg), np.radians(0.3 * deg), 1.0, 1.0, 1.0]], np.float32)
+    cfg = gl.FlareConfig(min_ghost_intensity=1e-6, spectral_samples=31, ray_grid=64, cull_dead_pairs=True)
+    fr = filter_ghosts_device(lens, hw, hh, cfg)
+    plan = prepare_ghost_render(lens, src, 256, 256, cfg, hw, hh, filter_result=fr)
+    kept, imgs = {}, {}
+    for chunks in (31, 1, 4, 2):
+        plan.set_launch(0, 0, chunks)
+        out = [torch.zeros((256, 256), device="cuda") for _ in range(3)]
+        plan.execute(*out)
+        torch.cuda.synchronize()
+        kept[chunks] = plan.pair_hits() > 0
+        imgs[chunks] = np.stack([o.cpu().numpy() for o in out])
+    plan.close()
+    assert kept[31].sum() > 0
+    for chunks in (1, 4, 2):
+        np.testing.assert_array_equal(kept[chunks], kept[31])
+        assert rel_l2(imgs[chunks], imgs[31]) < 1e-5
+
+
 def test_autotuned_launch_shapes_give_the_same_image(pins, meta, ref_images, tmp_path):
     from ghostlight_gb300.autotune import Tuner, tune_ghost_plan
     from ghostlight_gb300.flare import GhostRenderPlan

@@ -26,7 +26,9 @@ def pool():
 def _run_server(pool, reqs, **kw):
     from ghostlight_gb300.serve import FlareServer
     results = {}
+    engine = kw.pop("starburst_engine", "sprite")
     srv = FlareServer(pool, max_inflight=kw.pop("max_inflight", 8), **kw)
+    srv.exec.starburst_engine = engine
     srv.on_result = lambda r, out: results.__setitem__(r.rid, out.clone())
     srv.run_trace(reqs)
     torch.cuda.synchronize()
@@ -94,30 +96,41 @@ def test_wavelength_split_agrees(pool):
         assert rel_l2(c[r.rid].numpy(), a[r.rid].numpy()) < 1e-5
 
 
-def test_request_starburst_layer(pool):
-    """A request with the starburst layer = its ghost layer + the resident
-    plan's pattern of the lens's stop pupil at the source's image point."""
+@pytest.mark.parametrize("engine", ["sprite", "mdft"])
+def test_request_starburst_layer(pool, engine):
+    """A request with the starburst layer = its ghost layer + the lens's
+    starburst at the source's image point: with the SPRITE engine the frame
+    render's sprite layer of the same geometry (plain stop, T = 1), with the
+    matrix-DFT engine the resident plan's pattern of the lens's stop pupil."""
     import ghostlight_gb300 as gl
-    from ghostlight_gb300.serve import STARBURST_PUPIL, _spectral
+    from ghostlight_gb300.serve import STARBURST_PUPIL, SpriteStarbursts, _spectral
+    from ghostlight_gb300.starburst import sprite_starburst_layer
     p, cfg = pool
     base = _reqs()[3]                                  # 512^2, 31 wavelengths
     ghost = _run_server(p, [base])[base.rid].numpy()
     base.start = base.finish = 0.0
     base.starburst = True
-    both = _run_server(p, [base])[base.rid].numpy()
+    both = _run_server(p, [base], starburst_engine=engine)[base.rid].numpy()
     rl = p[base.lens_id]
-    spec, _ = _spectral(base.n_spec, cfg)
-    lam = spec[:, 0].astype(np.float64)
-    sc = lam.min() / lam
     cx, cy = rl.image_point(base.field_deg, base.width, base.height)
-    plan = gl.MdftPlan(STARBURST_PUPIL, (base.width, base.height), sc / base.width, sc / base.height,
-                       spec[:, 1:4], "split_bf16", center_x=cx, center_y=cy)
-    out = [torch.zeros((base.height, base.width), device="cuda") for _ in range(3)]
-    plan.execute(rl.starburst_pupil(), *out)
-    torch.cuda.synchronize()
-    want = torch.stack(out).cpu().numpy()
-    plan.close()
-    assert want.max() > 0.1 * np.abs(ghost).max()
+    if engine == "sprite":
+        scfg = SpriteStarbursts.config_for(rl, base.n_spec)
+        _, _, g = SpriteStarbursts()._bake(rl, base.width, base.height, base.n_spec)
+        layer = sprite_starburst_layer(rl.lens, rl.calibration, scfg, np.array([[cx, cy, 1.0, 1.0, 1.0]], np.float32),
+                                       base.width, base.height, rl.sensor_half_w, rl.sensor_half_h, geometry=g)
+        want = np.stack([layer["starburst_" + c].cpu().numpy() for c in "rgb"])
+    else:
+        spec, _ = _spectral(base.n_spec, cfg)
+        lam = spec[:, 0].astype(np.float64)
+        sc = lam.min() / lam
+        plan = gl.MdftPlan(STARBURST_PUPIL, (base.width, base.height), sc / base.width, sc / base.height,
+                           spec[:, 1:4], "split_bf16", center_x=cx, center_y=cy)
+        out = [torch.zeros((base.height, base.width), device="cuda") for _ in range(3)]
+        plan.execute(rl.starburst_pupil(), *out)
+        torch.cuda.synchronize()
+        want = torch.stack(out).cpu().numpy()
+        plan.close()
+    assert want.max() > 0.0
     assert rel_l2(both - ghost, want) < 1e-4
 
 

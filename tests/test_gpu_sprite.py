@@ -99,6 +99,36 @@ def test_splat_matches_oracle():
     assert rel_l2(got, want) < 1e-5
 
 
+def test_stateless_splat_matches_plan_splat():
+    """gl_sprite_splat_source (one source by value, the caller's copy of the
+    sprite, no staging) adds what the plan's splat adds, source by source,
+    on and off the frame, into planes that already hold an image."""
+    import ctypes as C
+    from ghostlight_gb300 import _native
+    from ghostlight_gb300.starburst import SpritePlan, build_pupil, starburst_spectrum
+    N, ds, W, H = 512, 2, 300, 220
+    plan = SpritePlan(N, starburst_spectrum(_config()))
+    plan.bake(build_pupil(_lens(), N, 0.3), ds)
+    _, spr, _ = plan.read()
+    M = spr.shape[0]
+    args = (0.011, 0.012, 0.02, 0.02, 140, 140, 1.7)
+    lib = _native.load()
+    base = torch.rand((3, H, W), device="cuda")
+    for src in ([150.3, 100.7, 1.0, 0.8, 0.6], [-40.0, 210.2, 0.5, 1.0, 1.0], [299.9, 3.1, 2.0, 2.0, 2.0]):
+        a = base.clone()
+        b = base.clone()
+        plan.splat(np.array([src], np.float32), *args, a[0], a[1], a[2])
+        _native.check(lib.gl_sprite_splat_source(C.c_void_p(spr.data_ptr()), M, *[float(v) for v in src],
+                                                 *[float(v) for v in args[:4]], args[4], args[5], float(args[6]),
+                                                 C.c_void_p(b[0].data_ptr()), C.c_void_p(b[1].data_ptr()),
+                                                 C.c_void_p(b[2].data_ptr()), W, H,
+                                                 C.c_void_p(torch.cuda.current_stream().cuda_stream)), "splat")
+        torch.cuda.synchronize()
+        assert (a - base).abs().sum() > 0
+        torch.testing.assert_close(b, a, rtol=0, atol=0)
+    plan.close()
+
+
 def test_layer_through_point_flare():
     """render_point_flare's starburst by the default SPRITE engine: against
     the oracle pipeline on the same geometry; the brightest pixel is the
