@@ -640,7 +640,7 @@ __global__ void __launch_bounds__(kRenderThreads, kRenderMinBlocks) ghost_render
         const SourceDev S = A.sources[w.y];
         const bool active = lane < w.w;
         const float2 uv = active ? A.samples[w.z + lane] : make_float2(0.0f, 0.0f);
-        if (PROBE && A.stats == nullptr && li1 - li0 > 1)
+        if (PROBE && A.stats == nullptr && A.pair_hits != nullptr && li1 - li0 > 1)
         {
             // first wavelength lane by lane (most kept pairs land there at
             // once), the rest as one compacted cohort when it missed
