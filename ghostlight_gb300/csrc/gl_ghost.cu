@@ -430,129 +430,6 @@ __device__ __forceinline__ void trace_warp(const RenderArgs& A, const SurfRec* l
         atomicAdd(A.stats + 3 * pair, (unsigned long long)n_lanes * n_lambda);
 }
 
-// The off-sensor probe's wavelengths after a task's first, traced as one
-// compacted cohort.  A probe ray's walk depends on its wavelength only
-// through the index tables, so rays of different wavelengths can share one
-// lock-step walk: each surface step runs over the cohort's live rays 32 at a
-// time, and the survivors are packed to the front of the warp's shared-memory
-// buffer (ballot prefix), so a warp step carries up to 32 live rays instead
-// of the lanes of one wavelength that are still alive.  The rays traced and
-// each ray's arithmetic are those of the per-wavelength walk (surface_step
-// without the weight, state stored and reloaded exactly), so the culled set
-// is the same; only the order of the work differs.  The cohort stops once
-// any warp has found the pair on the sensor.
-constexpr int kCohortFields = 8;    // o.xyz, d.xyz, current index, wavelength
-__device__ __forceinline__ void probe_cohort(const RenderArgs& A, const SurfRec* lens, const HotRec* hot,
-                                             const float* at, const float* bf, const PairDev& P,
-                                             const SourceDev& S, int4 w, int lq0, int lq1, float* buf)
-{
-    const int lane = threadIdx.x & 31;
-    const unsigned below = (1u << lane) - 1u;
-    const int n = A.n_surf, a = P.a, b = P.b;
-    const int L1 = b + 1, L2 = L1 + (b - a), L = L2 + (n - 1 - a);
-    const int nact = w.w;
-    const int total = nact * (lq1 - lq0);
-    // field f of ray i at buf[f * kCohort + i]: o.xyz, d.xyz, index, wavelength
-    auto F = [buf](int f, int i) -> float& { return buf[f * kCohort + i]; };
-    for (int r0 = 0; r0 < total; r0 += kCohort)
-    {
-        int h = 0;
-        if (lane == 0) h = __ldcg(A.pair_hits + w.x);
-        if (__shfl_sync(kFull, h, 0) > 0) return;
-        const int R = min(kCohort, total - r0);
-        int live = R;
-        bool fresh = true;
-        #pragma unroll 1
-        for (int k = 0; k < L && live > 0; ++k)
-        {
-            int s; bool refl; bool back = false;
-            if (k < L1)      { s = k;                refl = (s == b); }
-            else if (k < L2) { s = 2 * b - k;        refl = (s == a); back = true; }
-            else             { s = a + 1 + (k - L2); refl = false; }
-            const HotRec hr = hot[s];
-            if (!(hr.bits & HB_ACTIVE)) continue;
-            int wr = 0;
-            #pragma unroll 1
-            for (int base = 0; base < live; base += 32)
-            {
-                const int i = base + lane;
-                bool alive = i < live;
-                V3 o = v3(0.0f, 0.0f, 0.0f), d = v3(0.0f, 0.0f, 1.0f);
-                float cur = 1.0f;
-                int lq = lq0;
-                if (alive)
-                {
-                    if (fresh)
-                    {
-                        const int r = r0 + i, smp = r % nact;
-                        lq = lq0 + r / nact;
-                        const float2 uv = A.samples[w.z + smp];
-                        o = v3(uv.x * A.front_R + S.sdx, uv.y * A.front_R + S.sdy, A.start_z);
-                        d = v3(S.dx, S.dy, S.dz);
-                    }
-                    else
-                    {
-                        o = v3(F(0, i), F(1, i), F(2, i));
-                        d = v3(F(3, i), F(4, i), F(5, i));
-                        cur = F(6, i);
-                        lq = __float_as_int(F(7, i));
-                    }
-                }
-                __syncwarp();
-                if (alive)
-                {
-                    const float n2 = back ? bf[lq * n + s] : at[lq * n + s];
-                    const float rior = (back && refl) ? at[lq * n + a] : cur;
-                    float wt = 1.0f;
-                    alive = surface_step<false>(o, d, hr, lens[s], 0.0f, 0.0f, n2, refl, rior, cur, wt);
-                }
-                const unsigned m = __ballot_sync(kFull, alive);
-                if (alive)
-                {
-                    const int q = wr + __popc(m & below);
-                    F(0, q) = o.x; F(1, q) = o.y; F(2, q) = o.z;
-                    F(3, q) = d.x; F(4, q) = d.y; F(5, q) = d.z;
-                    F(6, q) = cur; F(7, q) = __int_as_float(lq);
-                }
-                wr += __popc(m);
-            }
-            live = wr;
-            fresh = false;
-            __syncwarp();
-        }
-        // the landing test of the per-wavelength probe, on the survivors
-        bool hit = false;
-        if (!fresh)
-        {
-            #pragma unroll 1
-            for (int base = 0; base < live && !__any_sync(kFull, hit); base += 32)
-            {
-                const int i = base + lane;
-                if (i < live && fabsf(F(5, i)) >= 1e-12f)
-                {
-                    const float ts = -F(2, i) / F(5, i);
-                    if (ts >= 0.0f)
-                    {
-                        const float sx = F(0, i) + F(3, i) * ts, sy = F(1, i) + F(4, i) * ts;
-                        const float spx = (sx / A.hw2 + 0.5f) * A.fmt_w + A.fmt_x0;
-                        const float spy = (sy / A.hh2 + 0.5f) * A.fmt_h + A.fmt_y0;
-                        hit = isfinite(spx) && isfinite(spy) && spx >= 0.0f && spx < (float)A.width &&
-                              spy >= 0.0f && spy < (float)A.height;
-                    }
-                }
-            }
-        }
-        __syncwarp();
-        const bool found = __any_sync(kFull, hit);
-        if (lane == 0)
-        {
-            if (A.traced) atomicAdd(A.traced, (unsigned long long)R);
-            if (found) atomicAdd(A.pair_hits + w.x, 1);
-        }
-        if (found) return;
-    }
-}
-
 template <bool PROBE>
 __global__ void __launch_bounds__(kRenderThreads, kRenderMinBlocks) ghost_render_kernel(const RenderArgs A)
 {
@@ -640,18 +517,6 @@ __global__ void __launch_bounds__(kRenderThreads, kRenderMinBlocks) ghost_render
         const SourceDev S = A.sources[w.y];
         const bool active = lane < w.w;
         const float2 uv = active ? A.samples[w.z + lane] : make_float2(0.0f, 0.0f);
-        if (PROBE && A.stats == nullptr && A.pair_hits != nullptr && li1 - li0 > 1)
-        {
-            // first wavelength lane by lane (most kept pairs land there at
-            // once), the rest as one compacted cohort when it missed
-            trace_warp<true>(A, lens, hot, at, bf, spec, kdel, P, S, uv, active, acc, w.x, li0, li0 + 1);
-            int h = 0;
-            if (lane == 0) h = __ldcg(A.pair_hits + w.x);
-            if (__shfl_sync(kFull, h, 0) == 0)
-                probe_cohort(A, lens, hot, at, bf, P, S, w, li0 + 1, li1,
-                             acc_base + (size_t)(tid >> 5) * kCohortFields * kCohort);
-            continue;
-        }
         trace_warp<PROBE>(A, lens, hot, at, bf, spec, kdel, P, S, uv, active, acc, w.x, li0, li1);
     }
 }
@@ -791,13 +656,6 @@ static cudaError_t alloc(T** dst, size_t bytes, cudaMemPool_t pool, cudaStream_t
     return cudaMallocFromPoolAsync(reinterpret_cast<void**>(dst), bytes, pool, st);
 }
 
-size_t probe_extra_smem()
-{
-    const size_t cohort = (size_t)(kRenderThreads / 32) * kCohortFields * kCohort * 4;
-    const size_t taps = (size_t)kRenderThreads * kAccStride * 4;
-    return cohort > taps ? cohort - taps : 0;
-}
-
 size_t render_smem(int n_surf, int n_spec)
 {
     return (size_t)n_surf * 32 + (size_t)n_spec * 16 + (size_t)n_spec * 4 + 2 * (size_t)n_spec * n_surf * 4 +
@@ -824,8 +682,7 @@ int raise_smem_limit(const void* kernel, size_t bytes)
 cudaError_t render_prepare(size_t smem, int* per_sm, int* n_sm)
 {
     cudaError_t e = (cudaError_t)raise_smem_limit((const void*)ghost_render_kernel<false>, smem);
-    if (e == cudaSuccess)
-        e = (cudaError_t)raise_smem_limit((const void*)ghost_render_kernel<true>, smem + probe_extra_smem());
+    if (e == cudaSuccess) e = (cudaError_t)raise_smem_limit((const void*)ghost_render_kernel<true>, smem);
     if (e == cudaSuccess && per_sm) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, ghost_render_kernel<false>, kRenderThreads, smem);
     int dev = 0;
     if (e == cudaSuccess && n_sm) e = cudaGetDevice(&dev);
@@ -835,7 +692,7 @@ cudaError_t render_prepare(size_t smem, int* per_sm, int* n_sm)
 
 cudaError_t render_launch(const RenderArgs& A, bool probe, int grid, size_t smem, cudaStream_t st)
 {
-    if (probe) ghost_render_kernel<true><<<grid, kRenderThreads, smem + probe_extra_smem(), st>>>(A);
+    if (probe) ghost_render_kernel<true><<<grid, kRenderThreads, smem, st>>>(A);
     else ghost_render_kernel<false><<<grid, kRenderThreads, smem, st>>>(A);
     return cudaGetLastError();
 }
@@ -1177,7 +1034,7 @@ int plan_execute(GhostPlan* p, float* d_out_r, float* d_out_g, float* d_out_b, c
             B.n_items = n_it;
             B.counter = p->probe_counters;
             const int grid = std::max(1, std::min((n_it + warps_per_block - 1) / warps_per_block, p->grid_persistent));
-            ghost_render_kernel<true><<<grid, kRenderThreads, p->smem + probe_extra_smem(), st>>>(B);
+            ghost_render_kernel<true><<<grid, kRenderThreads, p->smem, st>>>(B);
             ++launches;
         }
         GL_CUDA_TRY(cudaGetLastError());

@@ -14,7 +14,6 @@ namespace gl {
 constexpr int kRenderThreads = 128;
 constexpr int kTile = 32;          // pupil samples per work item = one warp
 constexpr int kMaxSpec = 256;
-constexpr int kCohort = 96;        // rays one probe warp keeps in flight in a compacted cohort
 
 struct PairDev {
     int a, b;
@@ -63,9 +62,6 @@ cudaError_t shared_device_pool(int dev, cudaMemPool_t* out);
 int default_lambda_split(int n_spec);
 // Shared memory of one render CTA for a lens of n_surf surfaces and n_spec wavelengths.
 size_t render_smem(int n_surf, int n_spec);
-// What a probe CTA needs beyond that: its warps' cohort buffers, which take
-// the place of the render's splat taps (render_launch adds it).
-size_t probe_extra_smem();
 // Opt the render kernels in to `smem` bytes of dynamic shared memory and
 // report resident CTAs per SM and the SM count.
 cudaError_t render_prepare(size_t smem, int* per_sm, int* n_sm);

@@ -267,11 +267,10 @@ def test_off_sensor_cull_keeps_the_image(pins, meta):
 
 
 @pytest.mark.parametrize("deg", [0.0, 9.0, 15.0, 24.0])
-def test_probe_cohorts_keep_the_culled_set(pins, meta, deg):
-    """With more than one wavelength per probe task, the wavelengths after
-    the first are traced as compacted cohorts: the pairs the probe keeps must
-    be those it keeps with one wavelength per task (no cohort) and with every
-    wavelength in one task (the longest cohorts), and the frame the same."""
+def test_probe_cull_independent_of_wavelength_split(pins, meta, deg):
+    """The pairs the off-sensor probe keeps, and the frame, do not depend on
+    how an item's wavelengths are split into tasks: one wavelength per task,
+    all of them in one task, and splits between."""
     import ghostlight_gb300 as gl
     from ghostlight_gb300.flare import filter_ghosts_device, prepare_ghost_render
     lens = _lens(pins, "cfg2_wide_angle_24")
