@@ -440,7 +440,7 @@ def run_cfg3(args, dev, stream, flush, timed):
     csec = sum(ts) / len(ts)
     cbytes = conv.traffic_bytes()
     gbs = cbytes / csec / 1e9
-    conv_res = {"ms": 1e3 * csec, "P": conv.P, "Q": conv.Q, "route": "FFT, three passes per channel pair (two pairs), the pair's intermediate L2-resident between passes",
+    conv_res = {"ms": 1e3 * csec, "P": conv.P, "Q": conv.Q, "route": "FFT, 3 HBM passes",
                 "rel_l2_64px_vs_fp64_direct": _conv_points(img, torch.from_numpy(kern).to(dev), cout),
                 "direct_equivalent_tflops": 2.0 * W * H * CONV_K * CONV_K * 3 / csec / 1e12,
                 "roofline": {"bound": "hbm", "achieved": gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",

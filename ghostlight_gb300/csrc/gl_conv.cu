@@ -55,13 +55,13 @@ constexpr int kRowLoads = 8;   // per-thread loads in flight per row pass
 __global__ void __launch_bounds__(1024) conv_rows_fwd(const float* __restrict__ in0, const float* __restrict__ in1,
                               const float* __restrict__ in2, const float* __restrict__ add0,
                               const float* __restrict__ add1, const float* __restrict__ add2, int W, int rows,
-                              float2* __restrict__ buf, FftDims dq, const float2* __restrict__ tw, int pair_base)
+                              float2* __restrict__ buf, FftDims dq, const float2* __restrict__ tw)
 {
     extern __shared__ float2 sm[];
     const int Q = dq.n, G = (Q + 3) >> 2;
     float2* x = sm;
     float2* y = sm + padded((size_t)Q * kRowsPerCta);
-    const int pair = pair_base + (int)blockIdx.y;
+    const int pair = blockIdx.y;
     const int row0 = blockIdx.x * kRowsPerCta;
     const float* re = pair == 0 ? in0 : in2;
     const float* im = pair == 0 ? in1 : nullptr;
@@ -123,14 +123,14 @@ constexpr int kColsPerCta = 2;    // columns per CTA: half a group, so two CTAs 
 // neighbouring CTAs, so each 32-byte sector they share is read from DRAM once.
 __global__ void __launch_bounds__(1024) conv_cols(float2* __restrict__ buf, const float2* __restrict__ khat,
                                                   int rows_in, int rows_out, FftDims dp, int Q, int mode,
-                                                  const float2* __restrict__ tw, int pair_base)
+                                                  const float2* __restrict__ tw)
 {
     extern __shared__ float2 sm[];
     const int P = dp.n, G = (Q + 3) >> 2;
     float2* x = sm;
     float2* y = sm + padded((size_t)P * kColsPerCta);
     const int g = blockIdx.x >> 1, hcol = (blockIdx.x & 1) * kColsPerCta;
-    float2* base = buf + ((size_t)(pair_base + (int)blockIdx.y) * G + g) * rows_in * kColGroup;
+    float2* base = buf + ((size_t)blockIdx.y * G + g) * rows_in * kColGroup;
     const int valid = max(0, min(kColsPerCta, Q - g * kColGroup - hcol));
     if (valid == 0) return;
     {
@@ -189,13 +189,13 @@ __global__ void __launch_bounds__(1024) conv_cols(float2* __restrict__ buf, cons
 // out0 (pair 0) / out2 (pair 1), imaginary part -> out1 (pair 0).  Crop to W.
 __global__ void __launch_bounds__(1024) conv_rows_inv(const float2* __restrict__ buf, int W, int H, float* __restrict__ out0,
                               float* __restrict__ out1, float* __restrict__ out2, FftDims dq,
-                              const float2* __restrict__ tw, int pair_base)
+                              const float2* __restrict__ tw)
 {
     extern __shared__ float2 sm[];
     const int Q = dq.n, G = (Q + 3) >> 2;
     float2* x = sm;
     float2* y = sm + padded((size_t)Q * kRowsPerCta);
-    const int pair = pair_base + (int)blockIdx.y;
+    const int pair = blockIdx.y;
     const int row0 = blockIdx.x * kRowsPerCta;
     const int half = (Q + 1) / 2;
     const int total = half * kRowsPerCta;
@@ -350,9 +350,9 @@ extern "C" int gl_conv2d_plan_create(int width, int height, const float* h_kerne
             // kernel spectrum: row FFTs of the real plane into tiles, then forward column FFTs in place
             conv_rows_fwd<<<dim3((p->P + kRowsPerCta - 1) / kRowsPerCta, 1), p->thr_row, p->smem_row, st>>>(kdev, nullptr, nullptr, nullptr, nullptr,
                                                                             nullptr, p->Q, p->P, p->khat, dq,
-                                                                            p->tw_q, 0);
+                                                                            p->tw_q);
             conv_cols<<<dim3(2 * p->G, 1), p->thr_col, p->smem_col, st>>>(p->khat, nullptr, p->P, p->P, dp, p->Q, 1,
-                                                                       p->tw_p, 0);
+                                                                       p->tw_p);
             chk(cudaGetLastError());
         }
         chk(cudaStreamSynchronize(st));
@@ -380,21 +380,13 @@ extern "C" int gl_conv2d_plan_execute2(gl_conv_plan* plan, const float* d_in_r, 
     cudaStream_t st = (cudaStream_t)stream;
     const FftDims dq = make_dims(p->Q), dp = make_dims(p->P);
     const unsigned rb = (unsigned)((p->H + kRowsPerCta - 1) / kRowsPerCta);
-    // One channel pair at a time through the three passes: a pair's
-    // intermediate (H x Q complex, 37.7 MB at 2048^2 + 257^2) and the kernel
-    // spectrum then stay in L2 from one pass to the next instead of both
-    // pairs' going through DRAM.
-    for (int pair = 0; pair < 2; ++pair)
-    {
-        conv_rows_fwd<<<dim3(rb, 1), p->thr_row, p->smem_row, st>>>(d_in_r, d_in_g, d_in_b, d_add_r, d_add_g,
-                                                                    d_add_b, p->W, p->H, p->buf, dq, p->tw_q, pair);
-        conv_cols<<<dim3(2 * p->G, 1), p->thr_col, p->smem_col, st>>>(p->buf, p->khat, p->H, p->H, dp, p->Q, 0,
-                                                                      p->tw_p, pair);
-        conv_rows_inv<<<dim3(rb, 1), p->thr_row, p->smem_row, st>>>(p->buf, p->W, p->H, d_out_r, d_out_g, d_out_b,
-                                                                    dq, p->tw_q, pair);
-    }
+    conv_rows_fwd<<<dim3(rb, 2), p->thr_row, p->smem_row, st>>>(d_in_r, d_in_g, d_in_b, d_add_r, d_add_g, d_add_b,
+                                                                    p->W, p->H, p->buf, dq, p->tw_q);
+    conv_cols<<<dim3(2 * p->G, 2), p->thr_col, p->smem_col, st>>>(p->buf, p->khat, p->H, p->H, dp, p->Q, 0, p->tw_p);
+    conv_rows_inv<<<dim3(rb, 2), p->thr_row, p->smem_row, st>>>(p->buf, p->W, p->H, d_out_r, d_out_g, d_out_b, dq,
+                                                                    p->tw_q);
     GL_CUDA_TRY(cudaGetLastError());
-    g_last_launches = 6;
+    g_last_launches = 3;
     return GL_OK;
 }
 

@@ -211,93 +211,6 @@ __global__ void __launch_bounds__(kSpriteThreads) sprite_bake(const float* __res
 // One output pixel of one source's footprint (offset t in its
 // (2 rx + 1) x (2 ry + 1) box): the sprite integrated over the pixel's sensor
 // footprint (texel overlap areas), tinted, added.
-// The same bake with the PSF staged in shared memory: a CTA owns a tile of
-// tm x tm coarse texels (fine span F = tm ds <= 64) and, for each wavelength,
-// first loads the window of the PSF that the tile's scaled samples read
-// (about F k + 2 texels a side, k = lambda_ref / lambda) with coalesced
-// loads, then takes every bilinear sample of the tile from it.  Each sample's
-// coordinates and arithmetic are those of sprite_bake, so it reads the same
-// four PSF values; only the order of the sum over wavelengths differs.  The
-// window carries one texel of margin on every side (the bounds and the
-// samples may round differently under contraction); a window wider than the
-// allocation (a spectrum far outside 400-700 nm) is read from global memory.
-__global__ void __launch_bounds__(kSpriteThreads) sprite_bake_tiled(const float* __restrict__ psf, int N,
-                                                                    const float4* __restrict__ spec, int n_spec,
-                                                                    float lambda_ref, int ds, int M, int tm,
-                                                                    int side, const double* __restrict__ energy,
-                                                                    float* __restrict__ sprite)
-{
-    extern __shared__ float win[];
-    const double e = *energy;
-    const float scale = (e > 0.0) ? (float)(1.0 / e) : 0.0f;
-    const int t = threadIdx.x;
-    const int a = blockIdx.x * tm + t % tm, b = blockIdx.y * tm + t / tm;
-    const bool own = t < tm * tm && a < M && b < M;
-    const float half = (float)(N / 2);
-    const int F = tm * ds;
-    const int i_lo = blockIdx.x * F, j_lo = blockIdx.y * F;
-    float sr = 0.0f, sg = 0.0f, sb = 0.0f;
-    for (int l = 0; l < n_spec; ++l)
-    {
-        const float4 s = spec[l];
-        const float k = lambda_ref / s.x;
-        const int rx0 = (int)floorf(half + (float)(i_lo - N / 2) * k) - 1;
-        const int ry0 = (int)floorf(half + (float)(j_lo - N / 2) * k) - 1;
-        const int RW = (int)floorf(half + (float)(i_lo + F - 1 - N / 2) * k) + 3 - rx0;
-        const int RH = (int)floorf(half + (float)(j_lo + F - 1 - N / 2) * k) + 3 - ry0;
-        const bool staged = RW <= side && RH <= side;
-        __syncthreads();                         // the previous wavelength's window is read
-        if (staged)
-            for (int q = t; q < RW * RH; q += blockDim.x)
-            {
-                const int y = ry0 + q / RW, x = rx0 + q % RW;
-                win[q] = (x >= 0 && x < N && y >= 0 && y < N) ? psf[(size_t)y * N + x] : 0.0f;
-            }
-        __syncthreads();
-        if (!own) continue;
-        for (int jj = 0; jj < ds; ++jj)
-            for (int ii = 0; ii < ds; ++ii)
-            {
-                const float dx = (float)(a * ds + ii - N / 2), dy = (float)(b * ds + jj - N / 2);
-                const float fx = half + dx * k, fy = half + dy * k;
-                float v = 0.0f;
-                if (!(fx < 0.0f || fy < 0.0f || fx >= (float)(N - 1) || fy >= (float)(N - 1)))
-                {
-                    const int x0 = (int)floorf(fx), y0 = (int)floorf(fy);
-                    const float tx = fx - x0, ty = fy - y0;
-                    const float* r0;
-                    int stride;
-                    if (staged && x0 >= rx0 && x0 + 1 < rx0 + RW && y0 >= ry0 && y0 + 1 < ry0 + RH)
-                    {
-                        r0 = win + (y0 - ry0) * RW + (x0 - rx0);
-                        stride = RW;
-                    }
-                    else
-                    {
-                        r0 = psf + (size_t)y0 * N + x0;
-                        stride = N;
-                    }
-                    const float* r1 = r0 + stride;
-                    const float pa = (r0[0] * scale) * (1.0f - tx) + (r0[1] * scale) * tx;
-                    const float pb = (r1[0] * scale) * (1.0f - tx) + (r1[1] * scale) * tx;
-                    v = pa * (1.0f - ty) + pb * ty;
-                }
-                v = v * k * k;
-                sr += s.y * v;
-                sg += s.z * v;
-                sb += s.w * v;
-            }
-    }
-    if (!own) return;
-    const size_t idx = (size_t)b * M + a;
-    sprite[3 * idx + 0] = sr;
-    sprite[3 * idx + 1] = sg;
-    sprite[3 * idx + 2] = sb;
-}
-
-// Coarse texels per side of a bake tile: the fine span stays <= 64.
-inline int bake_tile(int ds) { return ds <= 4 ? 16 : std::max(1, 64 / ds); }
-
 __device__ __forceinline__ void splat_pixel(const float* __restrict__ sprite, int M, float sx_ds, float sy_ds,
                                             float px_mm_x, float px_mm_y, int rx, int ry, const StarSource& s,
                                             long long t, float gain, float* __restrict__ out_r,
@@ -393,7 +306,6 @@ struct SpritePlan {
     StarSource* src = nullptr;
     int src_cap = 0;
     size_t smem_rows = 0, smem_cols = 0;
-    float kmax = 1.0f;           // largest lambda_ref / lambda of the spectrum
 };
 
 }  // namespace gl
@@ -427,7 +339,6 @@ extern "C" int gl_sprite_plan_create(int N, const gl_spectral_sample* spec, int 
     p->N = N;
     p->n_spec = n_spec;
     p->lambda_ref = lambda_ref;
-    for (int l = 0; l < n_spec; ++l) p->kmax = std::max(p->kmax, lambda_ref / spec[l].lambda);
     p->dims = make_dims(N);
     cudaGetDevice(&p->device);
     const size_t NN = (size_t)N * N;
@@ -496,21 +407,8 @@ extern "C" int gl_sprite_plan_bake(gl_sprite_plan* plan, const float* d_pupil, i
     else
         sprite_cols<1><<<N, kSpriteThreads, p->smem_cols, st>>>(p->work, N, p->dims, p->tw, p->psf, p->energy);
     const int MM = p->M * p->M;
-    const int tm = bake_tile(ds);
-    const int side = (int)std::ceil((double)(tm * ds - 1) * p->kmax) + 6;
-    const size_t bake_smem = (size_t)side * side * sizeof(float);
-    constexpr size_t kBakeSmemMax = 96 * 1024;
-    if (bake_smem <= kBakeSmemMax && raise_smem_limit((const void*)sprite_bake_tiled, bake_smem) == (int)cudaSuccess)
-    {
-        const unsigned tiles = (unsigned)((p->M + tm - 1) / tm);
-        const int threads = std::max(32, (tm * tm + 31) / 32 * 32);
-        sprite_bake_tiled<<<dim3(tiles, tiles), threads, bake_smem, st>>>(p->psf, N, p->spec, p->n_spec,
-                                                                         p->lambda_ref, ds, p->M, tm, side,
-                                                                         p->energy, p->sprite);
-    }
-    else
-        sprite_bake<<<(MM + kSpriteThreads - 1) / kSpriteThreads, kSpriteThreads, 0, st>>>(
-            p->psf, N, p->spec, p->n_spec, p->lambda_ref, ds, p->M, p->energy, p->sprite);
+    sprite_bake<<<(MM + kSpriteThreads - 1) / kSpriteThreads, kSpriteThreads, 0, st>>>(
+        p->psf, N, p->spec, p->n_spec, p->lambda_ref, ds, p->M, p->energy, p->sprite);
     GL_CUDA_TRY(cudaGetLastError());
     g_last_launches = 3;
     return GL_OK;

@@ -68,7 +68,7 @@ def test_conv_plan_composite_add_matches_fp64():
     ta = [torch.from_numpy(x).cuda() for x in a]
     tb = [torch.from_numpy(x).cuda() for x in b]
     out = [torch.full((H, W), float("nan"), device="cuda") for _ in range(3)]
-    assert plan.execute(ta, out, add=tb) == 6        # three passes per channel pair
+    assert plan.execute(ta, out, add=tb) == 3
     torch.cuda.synchronize()
     for o, x, y in zip(out, a, b):
         assert rel_l2(o.cpu().numpy(), CO.conv_same(x.astype(np.float64) + y, k)) < 1e-5
