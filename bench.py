@@ -569,7 +569,8 @@ def run_serving(args):
     out = _serve_mix(args, pool, cfg, False, args.serve_seconds, args.serve_dump)
     out["lens_setup_s"] = setup_s
     if args.serve_starburst:
-        out["with_starburst"] = _serve_mix(args, pool, cfg, True, args.serve_sb_seconds, "")
+        out["with_starburst"] = _serve_mix(args, pool, cfg, True, args.serve_sb_seconds,
+                                           args.serve_dump + ".starburst.csv" if args.serve_dump else "")
     for rl in pool.values():
         rl.close()
     return out
