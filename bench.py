@@ -571,18 +571,23 @@ def run_serving(args):
     if args.serve_starburst:
         out["with_starburst"] = _serve_mix(args, pool, cfg, True, args.serve_sb_seconds,
                                            args.serve_dump + ".starburst.csv" if args.serve_dump else "")
+    if args.serve_budget_gb > 0:
+        # the same arrivals against a budget that binds: requests wait for memory
+        out["binding_budget"] = _serve_mix(args, pool, cfg, False, args.serve_budget_seconds, "",
+                                           budget=int(args.serve_budget_gb * 1e9))
     for rl in pool.values():
         rl.close()
     return out
 
 
-def _serve_mix(args, pool, cfg, sb_on, seconds, dump):
+def _serve_mix(args, pool, cfg, sb_on, seconds, dump, budget=SERVE_BUDGET):
     import torch
     import ghostlight_gb300 as gl
     from ghostlight_gb300.flare import GhostRenderPlan, pupil_grid
     from ghostlight_gb300.serve import (FlareRequest, FlareServer, SpriteStarbursts, _spectral, latency_stats,
                                         poisson_requests)
-    reqs = poisson_requests(args.serve_rate, seconds, pool.keys(), seed=5, starburst=sb_on)
+    reqs = poisson_requests(args.serve_rate, seconds, pool.keys(), seed=5, starburst=sb_on,
+                            psf_frac=args.serve_psf_frac)
     # warm: one request per lens
     srv = FlareServer(pool, budget_bytes=SERVE_BUDGET, max_inflight=args.serve_slots, items_per_warp=8)
     srv.run_trace([FlareRequest(lens_id=i, width=512, height=512, n_spec=8, ray_grid=32, field_deg=5.0, rid=i,
@@ -590,10 +595,10 @@ def _serve_mix(args, pool, cfg, sb_on, seconds, dump):
     torch.cuda.synchronize()
     warm_exec = srv.exec
     _progress("serving warm-up (starburst %s)" % sb_on)
-    srv = FlareServer(pool, budget_bytes=SERVE_BUDGET, max_inflight=args.serve_slots, items_per_warp=8,
+    srv = FlareServer(pool, budget_bytes=budget, max_inflight=args.serve_slots, items_per_warp=8,
                       policy=args.serve_policy)
     # a pinned result buffer per slot and size: no host allocation while serving
-    srv.exec.prewarm([(w, w) for w in (512, 1024, 2048, 4096)], args.serve_slots)
+    srv.exec.prewarm([(w, w) for w in (256, 512, 1024, 2048, 4096)], args.serve_slots)
     sb_bytes = 0
     if sb_on:                                     # resident sprites of every (lens, size, wavelength count)
         srv.exec.sprites = warm_exec.sprites
@@ -622,7 +627,9 @@ def _serve_mix(args, pool, cfg, sb_on, seconds, dump):
                 f.write("%d,%d,%d,%d,%d,%d,%d,%.3f,%d,%d,%d,%.6f,%.6f,%.6f\n" % (
                     r.rid, r.lens_id, len(rl.lens.surfaces), rl.n_pairs, r.width, r.n_spec, r.ray_grid, r.field_deg,
                     r.priority, r.est_rays, r.traced, r.arrival, r.start, r.finish))
-    by_size = {"%dx%d" % (w, w): latency_stats(reqs, lambda r, w=w: r.width == w) for w in (512, 1024, 2048, 4096)}
+    by_size = {"%dx%d" % (w, w): latency_stats(reqs, lambda r, w=w: r.kind == "flare" and r.width == w)
+               for w in (512, 1024, 2048, 4096)}
+    by_size["psf"] = latency_stats(reqs, lambda r: r.kind == "psf")
     # serial plain renders of a sample of the same requests
     rng = np.random.default_rng(9)
     sample = [reqs[i] for i in sorted(rng.choice(len(reqs), size=min(len(reqs), args.serial_sample),
@@ -631,6 +638,12 @@ def _serve_mix(args, pool, cfg, sb_on, seconds, dump):
     for r in sample:
         rl = pool[r.lens_id]
         tt = time.perf_counter()
+        if r.kind == "psf":                       # render_psf, blocking, as the reference serves one
+            pcfg, psrc = srv.exec.psf_config(r, rl)
+            po = gl.render_psf(psrc, rl.lens, pcfg)
+            po["r"].cpu()
+            ts.append(time.perf_counter() - tt)
+            continue
         spec, corr = _spectral(r.n_spec, cfg)
         grid = pupil_grid(rl.lens, r.ray_grid, 0, 0, 0, 0.0)
         src = np.array([[math.radians(r.field_deg), 0.0, 1.0, 1.0, 1.0]], np.float32)
@@ -659,9 +672,10 @@ def _serve_mix(args, pool, cfg, sb_on, seconds, dump):
         srv.exec.sprites.close()
     return {"workload": "Poisson %.0f req/s for %.0f s (%d requests), %d resident lenses of 8-30 surfaces, "
                         "outputs 512^2-4096^2, 8/16/31 wavelengths, pupil grids 32^2-256^2, field 0-20 deg, "
+                        "%.0f%% of the requests PSF atlases (4x4 or 8x8 tiles of 64^2), "
                         "%d slots, %.0f GB HBM budget, %s priorities" % (
-                            args.serve_rate, seconds, len(reqs), SERVE_LENSES, args.serve_slots,
-                            SERVE_BUDGET / 1e9, args.serve_policy),
+                            args.serve_rate, seconds, len(reqs), SERVE_LENSES, 100.0 * args.serve_psf_frac,
+                            args.serve_slots, budget / 1e9, args.serve_policy),
             "layers": ("ghost + starburst: every request whose source images within a frame width of the frame "
                        "(%d of %d) adds its lens's SPRITE starburst (the reference's default engine: the stop "
                        "pupil's FFT baked over the request's wavelengths at the physical scale of the lens's "
@@ -673,6 +687,8 @@ def _serve_mix(args, pool, cfg, sb_on, seconds, dump):
             "rays_per_s": traced / wall, "ray_lambda_traces": traced,
             "latency_all": latency_stats(reqs), "latency_by_size": by_size,
             "peak_inflight": srv.sched.peak_inflight, "peak_budget_bytes": srv.sched.peak_used,
+            "budget_bytes": budget, "deferred": sum(bool(r.deferred) for r in reqs),
+            "rejected": len(srv.rejected), "psf_requests": sum(r.kind == "psf" for r in reqs),
             "serial_plain": {"sample": len(ts), "req_s": serial_req_s, "mean_ms": 1e3 * sum(ts) / len(ts)},
             "speedup_served_vs_serial_plain": served_req_s / serial_req_s, "clocks": clk.summary()}
 
@@ -1063,6 +1079,11 @@ def main():
                          "shortest first with the long requests ranked by arrival")
     ap.add_argument("--serial-sample", type=int, default=40)
     ap.add_argument("--serve-dump", default="", help="write per-request timings (CSV) here")
+    ap.add_argument("--serve-psf-frac", type=float, default=0.1,
+                    help="fraction of the serving requests that are PSF atlases (render_psf)")
+    ap.add_argument("--serve-budget-gb", type=float, default=6.0,
+                    help="HBM budget of the extra serving run whose budget binds (0: no such run)")
+    ap.add_argument("--serve-budget-seconds", type=float, default=10.0)
     ap.add_argument("--only", default="all", choices=["all", "cfg3", "serve", "sweep"],
                     help="with --quick: also run the starburst / convolution section (profiler runs)")
     args = ap.parse_args()

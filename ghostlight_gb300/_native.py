@@ -113,6 +113,7 @@ def _declare(lib):
     lib.gl_psf_prepass.argtypes = [P(gl_surface), i, P(f), i, i, P(gl_psf_cell)]
     lib.gl_psf_render.argtypes = [P(gl_surface), i, P(gl_psf_source), i, P(gl_pupil_sample), i,
                                   P(gl_spectral_sample), i, i, i, i, i, f, i, f, i, vp, vp, vp, vp]
+    lib.gl_psf_render_async.argtypes = lib.gl_psf_render.argtypes
     lib.gl_veil_plan_create.argtypes = [f, vp, P(vp)]
     lib.gl_veil_plan_execute.argtypes = [vp, vp, i, P(gl_veil_params), vp, vp, vp, vp]
     lib.gl_veil_plan_destroy.argtypes = [vp]

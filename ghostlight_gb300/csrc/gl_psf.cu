@@ -8,6 +8,7 @@
 // splat is bilinear, or a normalised Gaussian of the configured physical
 // width, clipped to the source's tile.
 #include "gl_internal.h"
+#include "gl_render.h"
 
 #include <cuda_runtime.h>
 
@@ -142,11 +143,15 @@ __global__ void __launch_bounds__(kPsfThreads) psf_kernel(PsfArgs A)
 
 using namespace gl;
 
-extern "C" int gl_psf_render(const gl_surface* surfaces, int n_surfaces, const gl_psf_source* sources, int n_sources,
-                             const gl_pupil_sample* grid, int n_grid, const gl_spectral_sample* spec, int n_spec,
-                             int tile_w, int tile_h, int composite_w, int composite_h, float mm_per_pixel,
-                             int monochromatic, float splat_sigma_px, int splat_radius_px, float* d_out_r,
-                             float* d_out_g, float* d_out_b, void* stream)
+// The render of both entries: `ordered` takes the scratch (lens records,
+// index table, spectrum, sources, pupil grid: one block) from the device's
+// stream-ordered pool and frees it in stream order without waiting; otherwise
+// plain allocations and a wait on the stream before they are freed.
+static int psf_render_impl(const gl_surface* surfaces, int n_surfaces, const gl_psf_source* sources, int n_sources,
+                           const gl_pupil_sample* grid, int n_grid, const gl_spectral_sample* spec, int n_spec,
+                           int tile_w, int tile_h, int composite_w, int composite_h, float mm_per_pixel,
+                           int monochromatic, float splat_sigma_px, int splat_radius_px, float* d_out_r,
+                           float* d_out_g, float* d_out_b, void* stream, bool ordered)
 {
     if (!surfaces || n_surfaces <= 0) return fail(GL_ERR_INVALID, "psf_render: lens has no surfaces");
     if (n_sources < 0 || n_grid < 0 || n_spec < 1 || (n_sources > 0 && !sources) || (n_grid > 0 && !grid) || !spec)
@@ -171,14 +176,29 @@ extern "C" int gl_psf_render(const gl_surface* surfaces, int n_surfaces, const g
     }
     build_ior_tables(surfaces, n_surfaces, lams.data(), n_spec, at.data(), bf.data());
     cudaStream_t st = (cudaStream_t)stream;
-    SurfRec* d_recs = nullptr; float* d_at = nullptr; float4* d_spec = nullptr;
-    gl_psf_source* d_src = nullptr; float2* d_grid = nullptr;
-    cudaError_t e = cudaMalloc(&d_recs, recs.size() * sizeof(SurfRec));
-    if (e == cudaSuccess) e = cudaMalloc(&d_at, at.size() * sizeof(float));
-    if (e == cudaSuccess) e = cudaMalloc(&d_spec, sp.size() * sizeof(float4));
-    if (e == cudaSuccess) e = cudaMalloc(&d_src, (size_t)n_sources * sizeof(gl_psf_source));
-    if (e == cudaSuccess) e = cudaMalloc(&d_grid, (size_t)n_grid * sizeof(float2));
-    if (e == cudaSuccess) e = cudaMemcpyAsync(d_recs, recs.data(), recs.size() * sizeof(SurfRec), cudaMemcpyHostToDevice, st);
+    // one scratch block, each part 256-byte aligned
+    auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const size_t o_recs = 0, o_at = o_recs + up(recs.size() * sizeof(SurfRec)), o_spec = o_at + up(at.size() * sizeof(float)),
+                 o_src = o_spec + up(sp.size() * sizeof(float4)), o_grid = o_src + up((size_t)n_sources * sizeof(gl_psf_source)),
+                 total = o_grid + up((size_t)n_grid * sizeof(float2));
+    char* block = nullptr;
+    cudaError_t e;
+    if (ordered)
+    {
+        cudaMemPool_t pool;
+        e = shared_device_pool(dev, &pool);
+        if (e == cudaSuccess) e = cudaMallocFromPoolAsync(reinterpret_cast<void**>(&block), total, pool, st);
+    }
+    else
+        e = cudaMalloc(&block, total);
+    if (e != cudaSuccess)
+        return fail(e == cudaErrorMemoryAllocation ? GL_ERR_OOM : GL_ERR_CUDA, std::string("psf_render: ") + cudaGetErrorString(e));
+    SurfRec* d_recs = reinterpret_cast<SurfRec*>(block + o_recs);
+    float* d_at = reinterpret_cast<float*>(block + o_at);
+    float4* d_spec = reinterpret_cast<float4*>(block + o_spec);
+    gl_psf_source* d_src = reinterpret_cast<gl_psf_source*>(block + o_src);
+    float2* d_grid = reinterpret_cast<float2*>(block + o_grid);
+    e = cudaMemcpyAsync(d_recs, recs.data(), recs.size() * sizeof(SurfRec), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_at, at.data(), at.size() * sizeof(float), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_spec, sp.data(), sp.size() * sizeof(float4), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess)
@@ -202,10 +222,41 @@ extern "C" int gl_psf_render(const gl_surface* surfaces, int n_surfaces, const g
         psf_kernel<<<g, kPsfThreads, smem, st>>>(A);
         e = cudaGetLastError();
     }
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    cudaFree(d_recs); cudaFree(d_at); cudaFree(d_spec); cudaFree(d_src); cudaFree(d_grid);
+    if (ordered)
+    {
+        const cudaError_t f = cudaFreeAsync(block, st);
+        if (e == cudaSuccess) e = f;
+    }
+    else
+    {
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        cudaFree(block);
+    }
     if (e != cudaSuccess)
         return fail(e == cudaErrorMemoryAllocation ? GL_ERR_OOM : GL_ERR_CUDA, std::string("psf_render: ") + cudaGetErrorString(e));
     g_last_launches = 1;
     return GL_OK;
+}
+
+extern "C" int gl_psf_render(const gl_surface* surfaces, int n_surfaces, const gl_psf_source* sources, int n_sources,
+                             const gl_pupil_sample* grid, int n_grid, const gl_spectral_sample* spec, int n_spec,
+                             int tile_w, int tile_h, int composite_w, int composite_h, float mm_per_pixel,
+                             int monochromatic, float splat_sigma_px, int splat_radius_px, float* d_out_r,
+                             float* d_out_g, float* d_out_b, void* stream)
+{
+    return psf_render_impl(surfaces, n_surfaces, sources, n_sources, grid, n_grid, spec, n_spec, tile_w, tile_h,
+                           composite_w, composite_h, mm_per_pixel, monochromatic, splat_sigma_px, splat_radius_px,
+                           d_out_r, d_out_g, d_out_b, stream, false);
+}
+
+extern "C" int gl_psf_render_async(const gl_surface* surfaces, int n_surfaces, const gl_psf_source* sources,
+                                   int n_sources, const gl_pupil_sample* grid, int n_grid,
+                                   const gl_spectral_sample* spec, int n_spec, int tile_w, int tile_h,
+                                   int composite_w, int composite_h, float mm_per_pixel, int monochromatic,
+                                   float splat_sigma_px, int splat_radius_px, float* d_out_r, float* d_out_g,
+                                   float* d_out_b, void* stream)
+{
+    return psf_render_impl(surfaces, n_surfaces, sources, n_sources, grid, n_grid, spec, n_spec, tile_w, tile_h,
+                           composite_w, composite_h, mm_per_pixel, monochromatic, splat_sigma_px, splat_radius_px,
+                           d_out_r, d_out_g, d_out_b, stream, true);
 }

@@ -44,11 +44,10 @@ def splat_footprint(splat_sigma_um, mm_pp):
     return float(sigma), radius
 
 
-def render_psf(sources, lens, config) -> dict:
-    """sources: (N, 5) [angle_x, angle_y, r, g, b] or (N, 7) with
-    [target_x_mm, target_y_mm] appended.  Returns the reference's keys; the
-    images r, g, b are torch CUDA tensors (composite_h, composite_w)."""
-    import torch
+def psf_inputs(sources, lens, config) -> dict:
+    """The host side of render_psf (PSFRenderer.cpp:243-330): checks, the
+    pre-pass centring each tile, the per-tile sources, the pupil grid, the
+    spectrum and the splat footprint, ready for gl_psf_render(_async)."""
     from .flare import pupil_grid
     cfg = config
     if cfg.grid_nx <= 0 or cfg.grid_ny <= 0 or cfg.tile_w <= 0 or cfg.tile_h <= 0:
@@ -86,13 +85,36 @@ def render_psf(sources, lens, config) -> dict:
     grid = np.ascontiguousarray(grid, np.float32)
     spec = np.ascontiguousarray(_psf_spectrum(cfg), np.float32)
     sigma, radius = splat_footprint(cfg.splat_sigma_um, mm_pp)
-    out = torch.zeros((3, comp_h, comp_w), dtype=torch.float32, device="cuda")
+    return dict(arr=arr, n=n, cells=cells, sources=gs, grid=grid, spec=spec, comp_w=comp_w, comp_h=comp_h,
+                mm_pp=mm_pp, sigma=sigma, radius=radius, mono=int(bool(getattr(cfg, "monochromatic", 0))),
+                tile_w=int(cfg.tile_w), tile_h=int(cfg.tile_h))
+
+
+def psf_launch(inp: dict, out, stream, ordered: bool = False) -> None:
+    """Enqueue the atlas of psf_inputs into `out` ((3, H, W) zeroed float32
+    CUDA tensor) on `stream`: gl_psf_render_async when `ordered` (scratch from
+    the device pool, no wait), else gl_psf_render."""
+    lib = _native.load()
     P = C.POINTER
-    _native.check(lib.gl_psf_render(arr, len(arr), gs, n, grid.ctypes.data_as(P(gl_pupil_sample)), len(grid),
-                                     spec.ctypes.data_as(P(gl_spectral_sample)), len(spec), int(cfg.tile_w),
-                                     int(cfg.tile_h), comp_w, comp_h, mm_pp, int(bool(getattr(cfg, "monochromatic", 0))),
-                                     sigma, radius, out[0].data_ptr(), out[1].data_ptr(), out[2].data_ptr(),
-                                     torch.cuda.current_stream().cuda_stream), "render_psf")
+    fn = lib.gl_psf_render_async if ordered else lib.gl_psf_render
+    _native.check(fn(inp["arr"], len(inp["arr"]), inp["sources"], inp["n"],
+                     inp["grid"].ctypes.data_as(P(gl_pupil_sample)), len(inp["grid"]),
+                     inp["spec"].ctypes.data_as(P(gl_spectral_sample)), len(inp["spec"]), inp["tile_w"],
+                     inp["tile_h"], inp["comp_w"], inp["comp_h"], inp["mm_pp"], inp["mono"], inp["sigma"],
+                     inp["radius"], out[0].data_ptr(), out[1].data_ptr(), out[2].data_ptr(), stream), "render_psf")
+
+
+def render_psf(sources, lens, config) -> dict:
+    """sources: (N, 5) [angle_x, angle_y, r, g, b] or (N, 7) with
+    [target_x_mm, target_y_mm] appended.  Returns the reference's keys; the
+    images r, g, b are torch CUDA tensors (composite_h, composite_w)."""
+    import torch
+    cfg = config
+    inp = psf_inputs(sources, lens, cfg)
+    n, cells = inp["n"], inp["cells"]
+    comp_w, comp_h = inp["comp_w"], inp["comp_h"]
+    out = torch.zeros((3, comp_h, comp_w), dtype=torch.float32, device="cuda")
+    psf_launch(inp, out, torch.cuda.current_stream().cuda_stream)
     return {"composite_w": comp_w, "composite_h": comp_h, "tile_w": int(cfg.tile_w), "tile_h": int(cfg.tile_h),
             "grid_nx": int(cfg.grid_nx), "grid_ny": int(cfg.grid_ny), "tile_extent_mm": float(cfg.tile_extent_mm),
             "r": out[0], "g": out[1], "b": out[2],

@@ -45,8 +45,16 @@ class FlareRequest:
     field_deg: float
     gain: float = 1000.0
     rid: int = 0
-    starburst: bool = False         # add the starburst layer (matrix DFT of the lens's stop pupil)
+    starburst: bool = False         # add the starburst layer (the lens's resident SPRITE starburst)
     arrival: float = 0.0            # seconds on the serving clock
+    # kind "psf": a PSF atlas (render_psf, PSFRenderer.cpp:260) of psf_grid^2
+    # sources on a regular grid over psf_field_frac of the lens's covered
+    # field, each in its own psf_tile^2 tile (width = height = psf_grid psf_tile)
+    kind: str = "flare"
+    psf_grid: int = 4
+    psf_tile: int = 64
+    psf_extent_mm: float = 0.4
+    psf_field_frac: float = 0.7
     # filled by the server
     est_rays: int = 0
     device_bytes: int = 0
@@ -54,6 +62,8 @@ class FlareRequest:
     start: float = 0.0
     finish: float = 0.0
     traced: int = 0                 # ray-wavelength traces the device ran
+    deferred: bool = False          # waited at least once for HBM budget
+    rejected: bool = False          # needs more than the whole budget: never admitted
 
     @property
     def latency(self) -> float:
@@ -98,6 +108,8 @@ class Scheduler:
                 self.inflight += 1
                 out.append(r)
             else:
+                if self.inflight < self.max_inflight:
+                    r.deferred = True       # a slot was free: the budget held it back
                 keep.append(r)
         self.pending = keep
         self.peak_used = max(self.peak_used, self.used)
@@ -418,7 +430,7 @@ def render_params(rl: ResidentLens, req: FlareRequest, correction, apply_correct
 # CUDA executor
 # ---------------------------------------------------------------------------
 class _Running:
-    __slots__ = ("req", "handle", "stream", "outs", "host", "event")
+    __slots__ = ("req", "handle", "stream", "outs", "host", "event", "psf")
 
 
 class CudaExecutor:
@@ -474,6 +486,13 @@ class CudaExecutor:
     def estimate(self, req: FlareRequest) -> None:
         rl = self.lenses[req.lens_id]
         masked = 0.8 * req.ray_grid * req.ray_grid
+        if req.kind == "psf":
+            # primary rays only: the atlas's tiles x pupil samples x wavelengths
+            req.est_rays = int(req.psf_grid * req.psf_grid * masked * req.n_spec)
+            req.priority = max(self.greatest, priority_class(req.est_rays, policy="sjf" if self.policy != "lsf"
+                                                             else "lsf"))
+            req.device_bytes = 3 * 4 * req.width * req.height * 2 + (1 << 20)
+            return
         req.est_rays = int(rl.n_pairs * masked * req.n_spec)
         if self.policy == "sjf_fifo":
             c = size_class(req.est_rays)
@@ -502,6 +521,8 @@ class CudaExecutor:
         lv = req.priority if req.priority in self.free_streams else self.least
         pool = self.free_streams[lv]
         stream = pool.pop() if pool else torch.cuda.Stream(device=self.device, priority=lv)
+        if req.kind == "psf":
+            return self._start_psf(req, rl, lv, stream)
         spec, corr = _spectral(req.n_spec, rl.config)
         apply_corr = bool(rl.config.spectral_correction) and req.n_spec != 3
         prm = render_params(rl, req, corr, apply_corr)
@@ -514,7 +535,7 @@ class CudaExecutor:
                                                   len(sp), src.ctypes.data_as(P(gl_flare_source)), 1, C.byref(prm),
                                                   st, C.byref(h)), "request_create")
         run = _Running()
-        run.req, run.handle, run.stream = req, h, (lv, stream)
+        run.req, run.handle, run.stream, run.psf = req, h, (lv, stream), None
         # the request renders into its own pool-allocated planes
         if self.lambda_chunks is not None:
             _native.check(self._lib.gl_request_set_lambda_split(h, min(int(self.lambda_chunks), req.n_spec)),
@@ -536,6 +557,44 @@ class CudaExecutor:
         run.event.record(stream)
         if heavy:
             self._heavy[id(run)] = lv
+        return run
+
+    def psf_config(self, req: FlareRequest, rl: ResidentLens):
+        """The PSFConfig of a PSF request (and its sources), as render_psf takes them."""
+        from .config import PSFConfig
+        cfg = PSFConfig(grid_nx=req.psf_grid, grid_ny=req.psf_grid, tile_w=req.psf_tile, tile_h=req.psf_tile,
+                        tile_extent_mm=req.psf_extent_mm, spectral_samples=req.n_spec, ray_grid=req.ray_grid)
+        cal = rl.calibration
+        f = np.float32
+        ax, ay = f(cal.max_half_angle_h) * f(req.psf_field_frac), f(cal.max_half_angle_v) * f(req.psf_field_frac)
+        xs = np.linspace(-ax, ax, req.psf_grid, dtype=np.float32)
+        ys = np.linspace(-ay, ay, req.psf_grid, dtype=np.float32)
+        s2 = np.stack(np.meshgrid(xs, ys, indexing="xy"), -1).reshape(-1, 2)
+        src = np.concatenate([s2, np.ones((len(s2), 3), np.float32)], 1)
+        return cfg, src
+
+    def _start_psf(self, req: FlareRequest, rl: ResidentLens, lv, stream) -> _Running:
+        """A PSF request: the host pre-pass, then the atlas on the request's
+        stream (gl_psf_render_async: scratch from the device pool, no wait)
+        into a tensor allocated on that stream, copied out like a flare."""
+        from .psf_grid import psf_inputs, psf_launch
+        torch = self.torch
+        cfg, src = self.psf_config(req, rl)
+        inp = psf_inputs(src, rl.lens, cfg)
+        run = _Running()
+        run.req, run.handle, run.stream = req, None, (lv, stream)
+        with torch.cuda.stream(stream):
+            run.psf = torch.zeros((3, inp["comp_h"], inp["comp_w"]), dtype=torch.float32, device=self.device)
+            psf_launch(inp, run.psf, stream.cuda_stream, ordered=True)
+            run.host, run.outs = None, None
+            if self.host_output:
+                run.host = self._pinned_buf(tuple(run.psf.shape))
+                run.host.copy_(run.psf, non_blocking=True)
+            else:
+                run.outs = run.psf
+        req.traced = int(inp["n"] * len(inp["grid"]) * len(inp["spec"]))
+        run.event = torch.cuda.Event()
+        run.event.record(stream)
         return run
 
     def _add_starburst(self, req: FlareRequest, rl: ResidentLens, h, stream) -> bool:
@@ -616,11 +675,13 @@ class CudaExecutor:
         returns the host planes (or the device tensor)."""
         lv, stream = run.stream
         self._heavy.pop(id(run), None)
-        v = C.c_longlong()
-        if self._lib.gl_request_traced(run.handle, C.byref(v), None) == 0:
-            run.req.traced = int(v.value)          # the stream is idle: no wait
-        self._lib.gl_request_destroy(run.handle, stream.cuda_stream)
-        run.handle = None
+        if run.handle is not None:
+            v = C.c_longlong()
+            if self._lib.gl_request_traced(run.handle, C.byref(v), None) == 0:
+                run.req.traced = int(v.value)          # the stream is idle: no wait
+            self._lib.gl_request_destroy(run.handle, stream.cuda_stream)
+            run.handle = None
+        run.psf = None
         self.free_streams[lv].append(stream)
         out = run.host if run.host is not None else run.outs
         run.outs = None
@@ -647,14 +708,21 @@ class FlareServer:
         self.t0 = clock()
         self.running: list = []             # (request, executor handle)
         self.completed: List[FlareRequest] = []
+        self.rejected: List[FlareRequest] = []
         self.on_result: Optional[Callable] = None
 
     def now(self) -> float:
         return self.clock() - self.t0
 
     def submit(self, req: FlareRequest):
+        """Queue a request; one that needs more than the whole HBM budget is
+        marked rejected and kept out of the queue."""
         self.exec.estimate(req)
-        self.sched.submit(req)
+        try:
+            self.sched.submit(req)
+        except ValueError:
+            req.rejected = True
+            self.rejected.append(req)
 
     def step(self) -> int:
         """Complete finished requests, then admit and start new ones.
@@ -702,7 +770,7 @@ class FlareServer:
 
 
 def latency_stats(reqs: List[FlareRequest], where: Optional[Callable] = None) -> dict:
-    sel = [r for r in reqs if where is None or where(r)]
+    sel = [r for r in reqs if not r.rejected and (where is None or where(r))]
     if not sel:
         return {"n": 0}
     lat = np.array([r.latency for r in sel]) * 1e3
@@ -713,11 +781,13 @@ def latency_stats(reqs: List[FlareRequest], where: Optional[Callable] = None) ->
 def poisson_requests(rate_hz: float, duration_s: float, lens_ids, seed: int = 5,
                      sizes=((512, 512), (1024, 1024), (2048, 2048), (4096, 4096)),
                      n_specs=(8, 16, 31), grid_min: int = 32, grid_max: int = 256,
-                     field_max_deg: float = 20.0, starburst: bool = False) -> List[FlareRequest]:
+                     field_max_deg: float = 20.0, starburst: bool = False,
+                     psf_frac: float = 0.0) -> List[FlareRequest]:
     """The serving mix: Poisson arrivals; per request a lens from the pool,
     an output size, a wavelength count, a pupil grid side (multiple of 16 in
     [grid_min, grid_max]) and a source field angle, all seeded; starburst
-    adds the starburst layer to every request."""
+    adds the starburst layer to every flare request; a fraction psf_frac of
+    the requests are PSF atlases (4 x 4 or 8 x 8 tiles of 64^2) instead."""
     rng = np.random.default_rng(seed)
     t, out = 0.0, []
     lens_ids = list(lens_ids)
@@ -727,11 +797,16 @@ def poisson_requests(rate_hz: float, duration_s: float, lens_ids, seed: int = 5,
         if t >= duration_s:
             break
         w, h = sizes[int(rng.integers(len(sizes)))]
-        out.append(FlareRequest(lens_id=lens_ids[int(rng.integers(len(lens_ids)))], width=w, height=h,
-                                n_spec=int(n_specs[int(rng.integers(len(n_specs)))]),
-                                ray_grid=int(grids[int(rng.integers(len(grids)))]),
-                                field_deg=float(rng.uniform(0.0, field_max_deg)), rid=len(out), arrival=t,
-                                starburst=bool(starburst)))
+        req = FlareRequest(lens_id=lens_ids[int(rng.integers(len(lens_ids)))], width=w, height=h,
+                           n_spec=int(n_specs[int(rng.integers(len(n_specs)))]),
+                           ray_grid=int(grids[int(rng.integers(len(grids)))]),
+                           field_deg=float(rng.uniform(0.0, field_max_deg)), rid=len(out), arrival=t,
+                           starburst=bool(starburst))
+        if psf_frac > 0.0 and rng.random() < psf_frac:
+            req.kind, req.starburst = "psf", False
+            req.psf_grid = 4 if rng.random() < 0.5 else 8
+            req.width = req.height = req.psf_grid * req.psf_tile
+        out.append(req)
     return out
 
 

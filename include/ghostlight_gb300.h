@@ -705,6 +705,17 @@ int gl_psf_render(const gl_surface* surfaces, int n_surfaces, const gl_psf_sourc
                   int composite_w, int composite_h, float mm_per_pixel, int monochromatic,
                   float splat_sigma_px, int splat_radius_px, float* d_out_r, float* d_out_g,
                   float* d_out_b, void* stream);
+/* The same render, stream-ordered for a serving loop (a PSF request among
+ * flare requests): its device scratch comes from the device's memory pool and
+ * is freed in stream order, and the call returns without waiting; the planes
+ * are complete when the stream reaches this point.  (gl_psf_render frees
+ * with cudaFree, which waits for the whole device.) */
+int gl_psf_render_async(const gl_surface* surfaces, int n_surfaces, const gl_psf_source* sources,
+                        int n_sources, const gl_pupil_sample* grid, int n_grid,
+                        const gl_spectral_sample* spec, int n_spec, int tile_w, int tile_h,
+                        int composite_w, int composite_h, float mm_per_pixel, int monochromatic,
+                        float splat_sigma_px, int splat_radius_px, float* d_out_r, float* d_out_g,
+                        float* d_out_b, void* stream);
 
 /* Number of kernel launches issued by the last device call on this thread. */
 int gl_last_launch_count(void);

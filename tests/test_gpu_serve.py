@@ -188,3 +188,39 @@ def test_served_lens_with_tables_and_bitmaps():
         assert rel_l2(got, want) < 1e-5
     finally:
         rl.close()
+
+
+def test_psf_request_matches_render_psf(pool):
+    """A PSF request (render_psf, PSFRenderer.cpp:260, as a served request:
+    the pre-pass on the host, the atlas stream-ordered on the request's own
+    stream) equals render_psf of the same configuration, alone and in a mix
+    with flare requests."""
+    import ghostlight_gb300 as gl
+    from ghostlight_gb300.serve import CudaExecutor, FlareRequest
+    p, _ = pool
+    reqs = []
+    for i, (g, ns, grid) in enumerate(((4, 8, 48), (8, 16, 32))):
+        r = FlareRequest(lens_id=i % len(p), width=0, height=0, n_spec=ns, ray_grid=grid, field_deg=0.0,
+                         rid=100 + i, kind="psf", psf_grid=g)
+        r.width = r.height = g * r.psf_tile
+        reqs.append(r)
+    ex = CudaExecutor(p, 4)
+    wants = {}
+    for r in reqs:
+        cfg, src = ex.psf_config(r, p[r.lens_id])
+        out = gl.render_psf(src, p[r.lens_id].lens, cfg)
+        torch.cuda.synchronize()
+        wants[r.rid] = np.stack([out[c].cpu().numpy() for c in "rgb"])
+        assert wants[r.rid].sum() > 0
+    alone = {}
+    for r in reqs:
+        alone.update(_run_server(p, [r]))
+    mix_reqs = _reqs()[:4] + reqs
+    for r in mix_reqs:
+        r.arrival, r.start, r.finish = 0.0, 0.0, 0.0
+    mix = _run_server(p, mix_reqs, max_inflight=6)
+    for r in reqs:
+        assert alone[r.rid].shape == (3, r.height, r.width)
+        assert rel_l2(alone[r.rid].numpy(), wants[r.rid]) < 1e-6
+        assert rel_l2(mix[r.rid].numpy(), wants[r.rid]) < 1e-6
+        assert r.traced > 0

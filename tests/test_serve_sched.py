@@ -145,3 +145,26 @@ def test_latency_stats():
 def test_default_wavelength_split():
     from ghostlight_gb300.serve import lambda_split
     assert [lambda_split(n) for n in (1, 3, 8, 16, 31, 64)] == [1, 1, 1, 2, 4, 8]
+
+
+def test_poisson_mix_with_psf_requests():
+    from ghostlight_gb300.serve import poisson_requests
+    reqs = poisson_requests(200.0, 5.0, [0, 1, 2], seed=3, psf_frac=0.2)
+    psf = [r for r in reqs if r.kind == "psf"]
+    assert 0.1 * len(reqs) < len(psf) < 0.3 * len(reqs)
+    for r in psf:
+        assert r.psf_grid in (4, 8) and r.width == r.height == r.psf_grid * r.psf_tile and not r.starburst
+
+
+def test_binding_budget_defers_and_rejects():
+    """With a budget that binds, requests wait for memory (marked deferred),
+    the budget holds at every step, and a request above the whole budget is
+    rejected instead of queued; the rest complete."""
+    from ghostlight_gb300.serve import request_bytes
+    reqs = [FlareRequest(0, 2048, 2048, 8, 32, 0.0, rid=i) for i in range(8)]
+    big = FlareRequest(0, 16384, 16384, 8, 32, 0.0, rid=99)
+    budget = 2 * request_bytes(2048, 2048, 100)
+    srv, ex, peak_used, _ = _serve(reqs + [big], budget, slots=8)
+    assert big.rejected and big not in srv.completed
+    assert len(srv.completed) == len(reqs)
+    assert any(r.deferred for r in reqs) and peak_used <= budget
