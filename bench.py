@@ -672,7 +672,7 @@ def _serve_mix(args, pool, cfg, sb_on, seconds, dump, budget=SERVE_BUDGET):
         srv.exec.sprites.close()
     return {"workload": "Poisson %.0f req/s for %.0f s (%d requests), %d resident lenses of 8-30 surfaces, "
                         "outputs 512^2-4096^2, 8/16/31 wavelengths, pupil grids 32^2-256^2, field 0-20 deg, "
-                        "%.0f%% of the requests PSF atlases (4x4 or 8x8 tiles of 64^2), "
+                        "%.0f%% of the requests PSF atlases (4x4 or 8x8 tiles of 64^2, 64^2 pupil grid), "
                         "%d slots, %.0f GB HBM budget, %s priorities" % (
                             args.serve_rate, seconds, len(reqs), SERVE_LENSES, 100.0 * args.serve_psf_frac,
                             args.serve_slots, budget / 1e9, args.serve_policy),
@@ -1081,7 +1081,7 @@ def main():
     ap.add_argument("--serve-dump", default="", help="write per-request timings (CSV) here")
     ap.add_argument("--serve-psf-frac", type=float, default=0.1,
                     help="fraction of the serving requests that are PSF atlases (render_psf)")
-    ap.add_argument("--serve-budget-gb", type=float, default=6.0,
+    ap.add_argument("--serve-budget-gb", type=float, default=1.5,
                     help="HBM budget of the extra serving run whose budget binds (0: no such run)")
     ap.add_argument("--serve-budget-seconds", type=float, default=10.0)
     ap.add_argument("--only", default="all", choices=["all", "cfg3", "serve", "sweep"],

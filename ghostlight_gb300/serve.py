@@ -787,7 +787,8 @@ def poisson_requests(rate_hz: float, duration_s: float, lens_ids, seed: int = 5,
     an output size, a wavelength count, a pupil grid side (multiple of 16 in
     [grid_min, grid_max]) and a source field angle, all seeded; starburst
     adds the starburst layer to every flare request; a fraction psf_frac of
-    the requests are PSF atlases (4 x 4 or 8 x 8 tiles of 64^2) instead."""
+    the requests are PSF atlases (4 x 4 or 8 x 8 tiles of 64^2, the 64^2
+    pupil grid of the reference's default render config) instead."""
     rng = np.random.default_rng(seed)
     t, out = 0.0, []
     lens_ids = list(lens_ids)
@@ -805,6 +806,7 @@ def poisson_requests(rate_hz: float, duration_s: float, lens_ids, seed: int = 5,
         if psf_frac > 0.0 and rng.random() < psf_frac:
             req.kind, req.starburst = "psf", False
             req.psf_grid = 4 if rng.random() < 0.5 else 8
+            req.ray_grid = 64
             req.width = req.height = req.psf_grid * req.psf_tile
         out.append(req)
     return out
