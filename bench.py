@@ -1144,18 +1144,20 @@ def roofline(res, plan):
             "kernel": "ghost_render_kernel", "kernel_ms": res["kernel_ms"]["render"],
             "flop_per_launch": res["traces_render"] * flops_per_trace,
             "peak_note": "GB300 FP32 CUDA-core peak: 152 SMs x 128 lanes x 2 FLOP x max SM clock",
-            "traffic_note": "DRAM bytes of one render launch from ncu (dram__bytes.sum.per_second x "
-                            "gpu__time_duration on this frame): the image accumulator stays in L2"}
+            "traffic_note": "DRAM bytes of one render launch from ncu (dram__bytes_read.sum + "
+                            "dram__bytes_write.sum on this frame): the image accumulator stays in L2"}
 
 
 # FP32 operations per traced ray-wavelength (FADD + FMUL + 2 x FFMA, thread
-# level) of the reference-formulation render kernel on this workload, measured
-# once with ncu (smsp__sass_thread_inst_executed_op_{fadd,fmul,ffma}_pred_on:
-# 2.02e11 FLOP over 1.793e8 traces) and frozen as the algorithmic count.
-FLOPS_PER_RAY_LAMBDA = 1126.0
-# DRAM bytes (read + write) of one render launch on this frame, from one ncu
-# capture of the tuned launch: 8.502 GB/s x 5.231 ms.
-RENDER_DRAM_BYTES = 44.5e6
+# level, predicated on) of the timed render kernel on this workload, measured
+# with ncu on one launch of the tuned shape
+# (smsp__sass_thread_inst_executed_op_{fadd,fmul,ffma}_pred_on.sum:
+# 4.926e9 + 20.971e9 + 2 x 18.993e9 = 6.388e10 FLOP over 6.007e7 traces)
+# and frozen as the algorithmic count.
+FLOPS_PER_RAY_LAMBDA = 1063.5
+# DRAM bytes (read + write) of one render launch on this frame, from the same
+# capture (dram__bytes_read.sum + dram__bytes_write.sum: 41.03 + 3.09 MB).
+RENDER_DRAM_BYTES = 44.12e6
 FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.070e9 / 1e12
 
 
