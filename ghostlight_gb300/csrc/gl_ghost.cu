@@ -340,7 +340,8 @@ template <bool PROBE>
 __device__ __forceinline__ void trace_warp(const RenderArgs& A, const SurfRec* lens, const HotRec* hot,
                                            const float* at, const float* bf, const float4* spec,
                                            const float* kdel, const PairDev& P, const SourceDev& S,
-                                           float2 uv, bool active, float* acc, int pair, int li0, int li1)
+                                           float2 uv, bool active, float* acc, int pair, int li0, int li1,
+                                           int sidx)
 {
     const int n = A.n_surf, a = P.a, b = P.b;
     const int L1 = b + 1, L2 = L1 + (b - a), L = L2 + (n - 1 - a);
@@ -363,6 +364,7 @@ __device__ __forceinline__ void trace_warp(const RenderArgs& A, const SurfRec* l
         V3 d = v3(S.dx, S.dy, S.dz);
         float w = 1.0f, cur = 1.0f;
         bool alive = active;
+        int kdead = L;                          // the step the ray died at (L: it left the lens)
         #pragma unroll 1
         for (int k = 0; k < L; ++k)
         {
@@ -375,8 +377,14 @@ __device__ __forceinline__ void trace_warp(const RenderArgs& A, const SurfRec* l
             if (!(hr.bits & HB_ACTIVE)) continue;
             n2 = back ? bfl[s] : atl[s];
             const float rior = (back && refl) ? atl[a] : cur;
-            if (alive) alive = surface_step<!PROBE>(o, d, hr, lens[s], sp.x, kdelta, n2, refl, rior, cur, w);
+            if (alive)
+            {
+                alive = surface_step<!PROBE>(o, d, hr, lens[s], sp.x, kdelta, n2, refl, rior, cur, w);
+                if (PROBE && !alive) kdead = k;
+            }
         }
+        if (PROBE && A.death != nullptr && active)
+            A.death[(size_t)pair * A.perm_stride + sidx] = (unsigned char)min(kdead, 255);
         if (PROBE)
         {
             // Off-sensor probe (the STATS pass of ghost_render.cu:402-415 with
@@ -488,7 +496,12 @@ __global__ void __launch_bounds__(kRenderThreads, kRenderMinBlocks) ghost_render
         if (task >= n_tasks) break;
         const int item = (int)(task / chunks);
         const int chunk = (int)(task - (long long)item * chunks);
-        const int li0 = chunk * l_size, li1 = min(A.n_spec, li0 + l_size);
+        int li0 = chunk * l_size, li1 = min(A.n_spec, li0 + l_size);
+        if (PROBE && A.lam_hi > 0)
+        {
+            li0 = max(li0, A.lam_lo);
+            li1 = min(li1, A.lam_hi);
+        }
         if (li0 >= li1) continue;
         int4 w;
         if (A.items != nullptr) w = A.items[item];
@@ -516,8 +529,55 @@ __global__ void __launch_bounds__(kRenderThreads, kRenderMinBlocks) ghost_render
         if (A.items == nullptr) P.w_ray = A.w_uniform;
         const SourceDev S = A.sources[w.y];
         const bool active = lane < w.w;
-        const float2 uv = active ? A.samples[w.z + lane] : make_float2(0.0f, 0.0f);
-        trace_warp<PROBE>(A, lens, hot, at, bf, spec, kdel, P, S, uv, active, acc, w.x, li0, li1);
+        int sidx = w.z + lane;
+        if (PROBE && A.perm != nullptr && active) sidx = A.perm[(size_t)w.x * A.perm_stride + sidx];
+        const float2 uv = active ? A.samples[sidx] : make_float2(0.0f, 0.0f);
+        trace_warp<PROBE>(A, lens, hot, at, bf, spec, kdel, P, S, uv, active, acc, w.x, li0, li1, sidx);
+    }
+}
+
+// Between the probe's two stages: each (pair, pass) still without a hit gets
+// its samples sorted by the death step of their first-wavelength ray (stable
+// counting sort, one warp), so the second stage's warps hold rays that leave
+// the lens together.  The set of samples is unchanged; only their order.
+__global__ void __launch_bounds__(32) probe_sort_kernel(const unsigned char* __restrict__ death,
+                                                        unsigned short* __restrict__ perm,
+                                                        const int* __restrict__ pair_hits, int stride, int b0,
+                                                        int b1, int b2, int b3)
+{
+    __shared__ int off[257];
+    const int pair = blockIdx.x, pass = blockIdx.y, lane = threadIdx.x;
+    if (pair_hits[pair] > 0) return;              // found on the sensor: stage 2 skips it
+    const int lo = pass == 0 ? b0 : (pass == 1 ? b1 : b2);
+    const int hi = pass == 0 ? b1 : (pass == 1 ? b2 : b3);
+    const unsigned char* d = death + (size_t)pair * stride;
+    unsigned short* out = perm + (size_t)pair * stride;
+    for (int b = lane; b < 257; b += 32) off[b] = 0;
+    __syncwarp();
+    for (int i = lo + lane; i < hi; i += 32) atomicAdd(&off[d[i]], 1);
+    __syncwarp();
+    if (lane == 0)
+    {
+        int run = lo;
+        for (int b = 0; b < 256; ++b)
+        {
+            const int c = off[b];
+            off[b] = run;
+            run += c;
+        }
+    }
+    __syncwarp();
+    for (int c0 = lo; c0 < hi; c0 += 32)
+    {
+        const int i = c0 + lane;
+        const bool v = i < hi;
+        const int key = v ? (int)d[i] : 256;
+        const unsigned m = __match_any_sync(kFull, key);
+        const int rank = __popc(m & ((1u << lane) - 1u));
+        if (v) out[off[key] + rank] = (unsigned short)i;
+        __syncwarp();
+        if (v && rank == 0) off[key] += __popc(m);
+        __syncwarp();
     }
 }
 
@@ -592,6 +652,10 @@ struct GhostPlan {
     bool cull = false;
     int4* probe_items = nullptr;
     float2* probe_samples = nullptr;
+    unsigned char* probe_death = nullptr;     // two-stage probe (one source): death steps
+    unsigned short* probe_perm = nullptr;     // and the sorted sample order, per pair
+    int probe_samples_n = 0;
+    int probe_sample_begin[4] = {0, 0, 0, 0}; // sample range of each pass
     int probe_begin[4] = {0, 0, 0, 0};   // item range of each pass
     int* pair_hits = nullptr;
     int* probe_counters = nullptr;
@@ -629,7 +693,7 @@ static void plan_free(GhostPlan* p)
     else if (p->executed && p->done) cudaEventSynchronize(p->done);
     void* blocks[] = {p->recs, p->ior_at, p->ior_bf, p->spec, p->items, p->pairs, p->sources, p->samples,
                       p->counter, p->accum, p->probe_items, p->probe_samples, p->pair_hits, p->probe_counters,
-                      p->traced, p->pair_hits_init};
+                      p->traced, p->pair_hits_init, p->probe_death, p->probe_perm};
     for (void* b : blocks)
     {
         if (!b) continue;
@@ -885,6 +949,8 @@ int plan_create(const gl_surface* surfaces, int n_surf, const gl_ghost_pair* pai
             if (rcs) { plan_free(p); return rcs; }
         }
         const int n_probe_samples = pbeg[3];
+        p->probe_samples_n = n_probe_samples;
+        for (int q = 0; q < 4; ++q) p->probe_sample_begin[q] = pbeg[q];
         for (int i = 0; i < n_pairs; ++i)
         {
             const int gi = pair_grid ? pair_grid[i] : 0;
@@ -939,6 +1005,15 @@ int plan_create(const gl_surface* surfaces, int n_surf, const gl_ghost_pair* pai
         chk(alloc(&p->pair_hits, sizeof(int) * std::max(1, n_pairs), pool, ost));
         chk(upload(&p->pair_hits_init, hits_init.data(), hits_init.size(), pool, ost));
         chk(alloc(&p->probe_counters, sizeof(int) * 4, pool, ost));
+        if (n_src == 1 && n_spec > 1 && p->probe_samples_n > 0 && p->probe_samples_n < 65536)
+        {
+            const size_t cells = (size_t)std::max(1, n_pairs) * p->probe_samples_n;
+            chk(alloc(&p->probe_death, cells, pool, ost));
+            // the identity order to start from: every entry a valid sample of its own pass
+            std::vector<unsigned short> ident(cells);
+            for (size_t c = 0; c < cells; ++c) ident[c] = (unsigned short)(c % (size_t)p->probe_samples_n);
+            chk(upload(&p->probe_perm, ident.data(), ident.size(), pool, ost));
+        }
     }
     chk(alloc(&p->accum, (size_t)prm->width * prm->height * sizeof(float4), pool, ost));
     if (e == cudaSuccess) chk(cudaMemsetAsync(p->accum, 0, (size_t)prm->width * prm->height * sizeof(float4), ost));
@@ -1034,8 +1109,29 @@ int plan_execute(GhostPlan* p, float* d_out_r, float* d_out_g, float* d_out_b, c
             B.n_items = n_it;
             B.counter = p->probe_counters;
             const int grid = std::max(1, std::min((n_it + warps_per_block - 1) / warps_per_block, p->grid_persistent));
-            ghost_render_kernel<true><<<grid, kRenderThreads, p->smem, st>>>(B);
-            ++launches;
+            if (p->probe_perm != nullptr)
+            {
+                // stage 1: every probe ray's first wavelength, recording where it died
+                RenderArgs B1 = B;
+                B1.lam_lo = 0; B1.lam_hi = 1; B1.l_chunks = 1;
+                B1.death = p->probe_death; B1.perm_stride = p->probe_samples_n;
+                ghost_render_kernel<true><<<grid, kRenderThreads, p->smem, st>>>(B1);
+                const int* sb = p->probe_sample_begin;
+                probe_sort_kernel<<<dim3((unsigned)p->n_pairs, 3), 32, 0, st>>>(
+                    p->probe_death, p->probe_perm, p->pair_hits, p->probe_samples_n, sb[0], sb[1], sb[2], sb[3]);
+                // stage 2: the other wavelengths of the pairs still without a hit, samples in sorted order
+                RenderArgs B2 = B;
+                B2.lam_lo = 1; B2.lam_hi = p->n_spec;
+                B2.perm = p->probe_perm; B2.perm_stride = p->probe_samples_n;
+                B2.counter = p->probe_counters + 1;
+                ghost_render_kernel<true><<<grid, kRenderThreads, p->smem, st>>>(B2);
+                launches += 3;
+            }
+            else
+            {
+                ghost_render_kernel<true><<<grid, kRenderThreads, p->smem, st>>>(B);
+                ++launches;
+            }
         }
         GL_CUDA_TRY(cudaGetLastError());
         A.pair_hits = p->pair_hits;

@@ -54,6 +54,15 @@ struct RenderArgs {
     int width, height;
     float fmt_w, fmt_h, fmt_x0, fmt_y0;
     float hw2, hh2, gain, front_R, start_z;
+    // Probe in two stages (plan path, one source): stage 1 traces wavelength
+    // lam_lo..lam_hi (the first) and writes each ray's death step to
+    // death[pair * perm_stride + sample]; stage 2 traces the rest with each
+    // pair's samples read through perm[pair * perm_stride + i] (sorted by
+    // that death step).  lam_hi = 0: the task's own wavelength range.
+    int lam_lo, lam_hi;
+    unsigned char* death;
+    const unsigned short* perm;
+    int perm_stride;
 };
 
 // The device's stream-ordered memory pool (freed blocks stay reserved).
