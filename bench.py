@@ -621,11 +621,11 @@ def _serve_mix(args, pool, cfg, sb_on, seconds, dump, budget=SERVE_BUDGET):
     traced = sum(r.traced for r in reqs)
     if dump:
         with open(dump, "w") as f:
-            f.write("rid,lens,n_surf,n_pairs,width,n_spec,grid,field,priority,est_rays,traced,arrival,start,finish\n")
+            f.write("rid,kind,lens,n_surf,n_pairs,width,n_spec,grid,field,priority,est_rays,traced,arrival,start,finish\n")
             for r in reqs:
                 rl = pool[r.lens_id]
-                f.write("%d,%d,%d,%d,%d,%d,%d,%.3f,%d,%d,%d,%.6f,%.6f,%.6f\n" % (
-                    r.rid, r.lens_id, len(rl.lens.surfaces), rl.n_pairs, r.width, r.n_spec, r.ray_grid, r.field_deg,
+                f.write("%d,%s,%d,%d,%d,%d,%d,%d,%.3f,%d,%d,%d,%.6f,%.6f,%.6f\n" % (
+                    r.rid, r.kind, r.lens_id, len(rl.lens.surfaces), rl.n_pairs, r.width, r.n_spec, r.ray_grid, r.field_deg,
                     r.priority, r.est_rays, r.traced, r.arrival, r.start, r.finish))
     by_size = {"%dx%d" % (w, w): latency_stats(reqs, lambda r, w=w: r.kind == "flare" and r.width == w)
                for w in (512, 1024, 2048, 4096)}
