@@ -36,10 +36,30 @@ struct PsfArgs {
     float* out_r;
     float* out_g;
     float* out_b;
+    int tile_smem;       // 1: the CTA's source tile is accumulated in shared memory
 };
 
-__device__ __forceinline__ void deposit(const PsfArgs& A, int pix, float lum, float cr, float cg, float cb, float wt)
+// Adds a ray-wavelength's weighted colour to one composite pixel: into the
+// CTA's shared-memory copy of its source's tile (planes of tile_w x tile_h),
+// or straight into the composite with global atomics.
+__device__ __forceinline__ void deposit(const PsfArgs& A, float* tile, int tx, int ty, int pix, float lum,
+                                       float cr, float cg, float cb, float wt)
 {
+    if (tile != nullptr)
+    {
+        const int t = ty * A.tile_w + tx, plane = A.tile_w * A.tile_h;
+        if (A.mono)
+        {
+            if (fabsf(lum) > 1e-14f) atomicAdd(tile + t, lum * wt);
+        }
+        else
+        {
+            if (fabsf(cr) > 1e-14f) atomicAdd(tile + t, cr * wt);
+            if (fabsf(cg) > 1e-14f) atomicAdd(tile + plane + t, cg * wt);
+            if (fabsf(cb) > 1e-14f) atomicAdd(tile + 2 * plane + t, cb * wt);
+        }
+        return;
+    }
     if (A.mono)
     {
         if (fabsf(lum) > 1e-14f) atomicAdd(A.out_r + pix, lum * wt);
@@ -51,6 +71,9 @@ __device__ __forceinline__ void deposit(const PsfArgs& A, int pix, float lum, fl
         if (fabsf(cb) > 1e-14f) atomicAdd(A.out_b + pix, cb * wt);
     }
 }
+
+__device__ __forceinline__ void psf_trace_one(const PsfArgs& A, const SurfRec* lens, const float* at, float* tile,
+                                              int si, int gi);
 
 __global__ void __launch_bounds__(kPsfThreads) psf_kernel(PsfArgs A)
 {
@@ -64,10 +87,40 @@ __global__ void __launch_bounds__(kPsfThreads) psf_kernel(PsfArgs A)
         for (int i = threadIdx.x; i < words; i += blockDim.x) d[i] = s[i];
         for (int i = threadIdx.x; i < A.n_spec * A.n_surf; i += blockDim.x) at[i] = A.ior_at[i];
     }
+    // every ray of this CTA belongs to source blockIdx.x and deposits only in
+    // its tile: accumulate the tile in shared memory, add it to the composite once
+    float* tile = nullptr;
+    const int planes = A.mono ? 1 : 3, tile_px = A.tile_w * A.tile_h;
+    if (A.tile_smem)
+    {
+        tile = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(at + A.n_spec * A.n_surf) +
+                                        ((16 - (((uintptr_t)(at + A.n_spec * A.n_surf)) & 15)) & 15));
+        for (int i = threadIdx.x; i < planes * tile_px; i += blockDim.x) tile[i] = 0.0f;
+    }
     __syncthreads();
     const int si = blockIdx.x;
     const int gi = blockIdx.y * kPsfThreads + threadIdx.x;
-    if (si >= A.n_src || gi >= A.n_grid) return;
+    if (si < A.n_src && gi < A.n_grid) psf_trace_one(A, lens, at, tile, si, gi);
+    if (!A.tile_smem || si >= A.n_src) return;
+    __syncthreads();
+    const gl_psf_source S = A.src[si];
+    float* outs[3] = {A.out_r, A.out_g, A.out_b};
+    for (int i = threadIdx.x; i < planes * tile_px; i += blockDim.x)
+    {
+        const float v = tile[i];
+        if (v == 0.0f) continue;
+        const int pl = i / tile_px, t = i - pl * tile_px;
+        const int xi = S.tile_x0 + t % A.tile_w, yi = S.tile_y0 + t / A.tile_w;
+        if (xi < 0 || xi >= A.comp_w || yi < 0 || yi >= A.comp_h) continue;
+        atomicAdd(outs[pl] + (size_t)yi * A.comp_w + xi, v);
+    }
+}
+
+// One pupil sample of one source through every wavelength, splatted into the
+// source's tile (tile != nullptr: the CTA's shared-memory copy of it).
+__device__ __forceinline__ void psf_trace_one(const PsfArgs& A, const SurfRec* lens, const float* at, float* tile,
+                                              int si, int gi)
+{
     const gl_psf_source S = A.src[si];
     const float2 uv = A.grid[gi];
     const float bx = tanf(S.angle_x), by = tanf(S.angle_y);
@@ -99,7 +152,7 @@ __global__ void __launch_bounds__(kPsfThreads) psf_kernel(PsfArgs A)
                 if (xi < tx_min || xi >= tx_max || yi < ty_min || yi >= ty_max || xi < 0 || xi >= A.comp_w ||
                     yi < 0 || yi >= A.comp_h)
                     continue;
-                deposit(A, yi * A.comp_w + xi, lum, cr, cg, cb, bw[k]);
+                deposit(A, tile, xi - S.tile_x0, yi - S.tile_y0, yi * A.comp_w + xi, lum, cr, cg, cb, bw[k]);
             }
         }
         else
@@ -131,7 +184,7 @@ __global__ void __launch_bounds__(kPsfThreads) psf_kernel(PsfArgs A)
                     const float dxr = (float)dx - ox;
                     const float wt = expf(-(dxr * dxr + dyr * dyr) * inv2) * inv_wsum;
                     if (wt < 1e-6f) continue;
-                    deposit(A, yi * A.comp_w + xi, lum, cr, cg, cb, wt);
+                    deposit(A, tile, xi - S.tile_x0, yi - S.tile_y0, yi * A.comp_w + xi, lum, cr, cg, cb, wt);
                 }
             }
         }
@@ -204,7 +257,10 @@ static int psf_render_impl(const gl_surface* surfaces, int n_surfaces, const gl_
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(d_src, sources, (size_t)n_sources * sizeof(gl_psf_source), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_grid, grid, (size_t)n_grid * sizeof(float2), cudaMemcpyHostToDevice, st);
-    const size_t smem = recs.size() * sizeof(SurfRec) + at.size() * sizeof(float);
+    // the CTA's source tile in shared memory when it fits (96 KB of tile)
+    const size_t tile_bytes = (size_t)(monochromatic ? 1 : 3) * tile_w * tile_h * sizeof(float);
+    const bool tile_smem = tile_bytes <= 96 * 1024;
+    const size_t smem = recs.size() * sizeof(SurfRec) + at.size() * sizeof(float) + (tile_smem ? tile_bytes + 16 : 0);
     if (e == cudaSuccess && smem > 48 * 1024)
         e = (cudaError_t)raise_smem_limit((const void*)psf_kernel, smem);
     if (e == cudaSuccess)
@@ -218,6 +274,7 @@ static int psf_render_impl(const gl_surface* surfaces, int n_surfaces, const gl_
         A.mono = monochromatic ? 1 : 0;
         A.sigma_px = splat_sigma_px; A.radius_px = splat_radius_px;
         A.out_r = d_out_r; A.out_g = d_out_g; A.out_b = d_out_b;
+        A.tile_smem = tile_smem ? 1 : 0;
         const dim3 g((unsigned)n_sources, (unsigned)((n_grid + kPsfThreads - 1) / kPsfThreads));
         psf_kernel<<<g, kPsfThreads, smem, st>>>(A);
         e = cudaGetLastError();
