@@ -588,10 +588,16 @@ def _serve_mix(args, pool, cfg, sb_on, seconds, dump, budget=SERVE_BUDGET):
                                         poisson_requests)
     reqs = poisson_requests(args.serve_rate, seconds, pool.keys(), seed=5, starburst=sb_on,
                             psf_frac=args.serve_psf_frac)
-    # warm: one request per lens
+    # warm: one flare request per lens, and one PSF atlas per lens on a 2 x 2
+    # source grid, which the mix never asks for (its 4 x 4 and 8 x 8 atlases
+    # find no pre-pass kept: each computes its own on first use)
     srv = FlareServer(pool, budget_bytes=SERVE_BUDGET, max_inflight=args.serve_slots, items_per_warp=8)
-    srv.run_trace([FlareRequest(lens_id=i, width=512, height=512, n_spec=8, ray_grid=32, field_deg=5.0, rid=i,
-                                starburst=sb_on) for i in pool])
+    warm = [FlareRequest(lens_id=i, width=512, height=512, n_spec=8, ray_grid=32, field_deg=5.0, rid=i,
+                         starburst=sb_on) for i in pool]
+    if args.serve_psf_frac > 0:
+        warm += [FlareRequest(lens_id=i, width=128, height=128, n_spec=8, ray_grid=32, field_deg=0.0,
+                              rid=len(pool) + i, kind="psf", psf_grid=2) for i in pool]
+    srv.run_trace(warm)
     torch.cuda.synchronize()
     warm_exec = srv.exec
     _progress("serving warm-up (starburst %s)" % sb_on)

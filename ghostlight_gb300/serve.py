@@ -340,6 +340,9 @@ class ResidentLens:
                                                int(config.aperture_blades), float(config.aperture_rotation),
                                                C.byref(h)), "lens_create")
         self._h = h
+        # host pre-pass cells and pupil grids of PSF atlases (psf_inputs'
+        # cache): they depend only on this lens and the atlas's sources
+        self.psf_cache: dict = {}
 
     @property
     def n_pairs(self) -> int:
@@ -430,7 +433,7 @@ def render_params(rl: ResidentLens, req: FlareRequest, correction, apply_correct
 # CUDA executor
 # ---------------------------------------------------------------------------
 class _Running:
-    __slots__ = ("req", "handle", "stream", "outs", "host", "event", "psf")
+    __slots__ = ("req", "handle", "stream", "outs", "host", "event", "psf", "prep")
 
 
 class CudaExecutor:
@@ -468,6 +471,7 @@ class CudaExecutor:
         self.streams = {lv: [torch.cuda.Stream(device=self.device, priority=lv) for _ in range(max_inflight)]
                         for lv in self.LEVELS}
         self.free_streams = {lv: list(v) for lv, v in self.streams.items()}
+        self._prep_pool = None                   # worker thread of the PSF host pre-passes
         self._pinned: Dict[tuple, list] = collections.defaultdict(list)
 
     def cta_items(self, req: FlareRequest) -> int:
@@ -535,7 +539,7 @@ class CudaExecutor:
                                                   len(sp), src.ctypes.data_as(P(gl_flare_source)), 1, C.byref(prm),
                                                   st, C.byref(h)), "request_create")
         run = _Running()
-        run.req, run.handle, run.stream, run.psf = req, h, (lv, stream), None
+        run.req, run.handle, run.stream, run.psf, run.prep = req, h, (lv, stream), None, None
         # the request renders into its own pool-allocated planes
         if self.lambda_chunks is not None:
             _native.check(self._lib.gl_request_set_lambda_split(h, min(int(self.lambda_chunks), req.n_spec)),
@@ -576,13 +580,36 @@ class CudaExecutor:
     def _start_psf(self, req: FlareRequest, rl: ResidentLens, lv, stream) -> _Running:
         """A PSF request: the host pre-pass, then the atlas on the request's
         stream (gl_psf_render_async: scratch from the device pool, no wait)
-        into a tensor allocated on that stream, copied out like a flare."""
-        from .psf_grid import psf_inputs, psf_launch
-        torch = self.torch
+        into a tensor allocated on that stream, copied out like a flare.
+
+        The pre-pass (float32 host traces, up to ~70 ms on a 30-surface lens)
+        is kept per resident lens and source grid.  One not yet kept runs on
+        a worker thread, so the request loop goes on admitting and completing
+        other requests meanwhile; done() launches the atlas once it is
+        ready."""
+        from .psf_grid import psf_inputs
         cfg, src = self.psf_config(req, rl)
-        inp = psf_inputs(src, rl.lens, cfg)
         run = _Running()
         run.req, run.handle, run.stream = req, None, (lv, stream)
+        run.psf = run.host = run.outs = run.event = None
+        run.prep = None
+        s7 = np.zeros((len(src), 7), np.float32)
+        s7[:, :src.shape[1]] = src
+        if ("cells", s7.tobytes(), int(getattr(cfg, "center_mode", 0))) in rl.psf_cache:
+            self._launch_psf(run, psf_inputs(src, rl.lens, cfg, rl.psf_cache))
+        else:
+            if self._prep_pool is None:
+                import concurrent.futures
+                self._prep_pool = concurrent.futures.ThreadPoolExecutor(max_workers=1,
+                                                                        thread_name_prefix="gl-psf-prepass")
+            run.prep = self._prep_pool.submit(psf_inputs, src, rl.lens, cfg, rl.psf_cache)
+        return run
+
+    def _launch_psf(self, run: _Running, inp: dict):
+        from .psf_grid import psf_launch
+        torch = self.torch
+        req = run.req
+        stream = run.stream[1]
         with torch.cuda.stream(stream):
             run.psf = torch.zeros((3, inp["comp_h"], inp["comp_w"]), dtype=torch.float32, device=self.device)
             psf_launch(inp, run.psf, stream.cuda_stream, ordered=True)
@@ -668,6 +695,13 @@ class CudaExecutor:
                 self.recycle(b)
 
     def done(self, run: _Running) -> bool:
+        if run.prep is not None:                  # a PSF pre-pass on the worker thread
+            if not run.prep.done():
+                return False
+            inp = run.prep.result()
+            run.prep = None
+            self._launch_psf(run, inp)
+            return False
         return run.event.query()
 
     def finish(self, run: _Running):

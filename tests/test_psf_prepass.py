@@ -64,3 +64,33 @@ def test_fixed_target_aims_the_chief_ray(pins):
         assert cells[k].status == 0
         assert abs(cells[k].chief_x_mm - src[k, 5]) < 2e-4 and abs(cells[k].chief_y_mm - src[k, 6]) < 2e-4
         assert cells[k].aim_residual_mm < 2e-4
+
+
+def test_kept_prepass_equals_a_fresh_one(pins):
+    """psf_inputs with a lens-owned cache (the serving path) returns the same
+    tile centres, sources and pupil grid as without one, and a second atlas
+    over the same sources reuses the kept pre-pass and grid."""
+    from ghostlight_gb300.config import PSFConfig
+    from ghostlight_gb300.psf_grid import psf_inputs
+    lens = _lens(pins)
+    cfg = PSFConfig(grid_nx=3, grid_ny=2, tile_w=32, tile_h=32, tile_extent_mm=0.3, spectral_samples=8,
+                    ray_grid=24)
+    xs = np.linspace(-0.2, 0.2, 3, dtype=np.float32)
+    src = np.array([[x, y, 1.0, 1.0, 1.0] for y in (-0.1, 0.1) for x in xs], np.float32)
+    cache = {}
+    fresh = psf_inputs(src, lens, cfg)
+    first = psf_inputs(src, lens, cfg, cache)
+    assert len(cache) == 2
+    kept_cells = [v for k, v in cache.items() if k[0] == "cells"][0]
+    again = psf_inputs(src, lens, cfg, cache)
+    assert again["cells"] is kept_cells and again["grid"] is first["grid"]
+    for got in (first, again):
+        for i in range(len(src)):
+            a, b = got["cells"][i], fresh["cells"][i]
+            assert (a.chief_x_mm, a.chief_y_mm, a.beam_ax, a.beam_ay) == (b.chief_x_mm, b.chief_y_mm, b.beam_ax,
+                                                                          b.beam_ay)
+            s, t = got["sources"][i], fresh["sources"][i]
+            assert bytes(s) == bytes(t)
+        np.testing.assert_array_equal(got["grid"], fresh["grid"])
+    other = psf_inputs(src[:4], lens, cfg, cache)     # other sources: a pre-pass of their own
+    assert len(cache) == 3 and other["n"] == 4
