@@ -76,30 +76,35 @@ __device__ __forceinline__ void flush_taps(float4* accum, int W, int H, int cx, 
 // nearer the vertex, which is the reference's root rule (trace_core.h:
 // 505-515); unlike b^2 - 4ac about the centre of curvature, this form loses
 // no precision for large radii or rays near the vertex.
+//
+// Every lane of the warp runs it (a lane whose ray is dead computes values
+// nobody reads): it returns whether the ray hits instead of leaving early, so
+// the lock-step walk pays for no divergent branches; the rare far-root case
+// is a warp-uniform branch.
 __device__ __forceinline__ bool sphere_hit(V3 o, V3 d, float z_s, float c, float& t_out, V3& q_out)
 {
-    if (fabsf(d.z) < 1e-12f) return false;
     const float t0 = (z_s - o.z) / d.z;
     const float px = o.x + d.x * t0, py = o.y + d.y * t0;
     const float A = c * (d.x * d.x + d.y * d.y + d.z * d.z);   // c |d|^2
     const float B = c * (px * d.x + py * d.y) - d.z;
     const float C = c * (px * px + py * py);
     const float disc = B * B - A * C;
-    if (disc < 0.0f) return false;
     const float den = B + copysignf(sqrtf(disc), B);
     const float ts = (den != 0.0f) ? -C / den : 0.0f;
     float t = t0 + ts;
-    if (!(t > 1e-6f))
+    bool ok = (fabsf(d.z) >= 1e-12f) & (disc >= 0.0f);
+    const bool near = t > 1e-6f;
+    if (__any_sync(kFull, ok & !near))
     {
         // the near root is behind the ray: the far root, if any, is the hit
-        if (!(A != 0.0f) || !(ts != 0.0f)) return false;
         const float tb = t0 + (C / A) / ts;
-        if (!(tb > 1e-6f)) return false;
-        t = tb;
+        const bool far = (A != 0.0f) & (ts != 0.0f) & (tb > 1e-6f);
+        ok = ok & (near | far);
+        t = near ? t : tb;
     }
     t_out = t;
     q_out = v3(o.x + d.x * t, o.y + d.y * t, o.z + d.z * t - z_s);
-    return true;
+    return ok;
 }
 
 __device__ __forceinline__ bool check_polygon(float hx, float hy, float h2, const SurfRec& s)
@@ -180,6 +185,11 @@ __device__ __forceinline__ HotRec make_hot(const SurfRec& s)
 // has three.  cos_2 >= 0 is the substrate-side cosine when the caller already
 // has it (a refraction's transmitted cosine: the film keeps n sin(theta), so
 // it is the same angle); cos_2 < 0 computes it here.
+// HAVE_COS2: cos_2 is the substrate-side cosine (a refraction's transmitted
+// cosine); otherwise it is computed here.  The film-TIR fallbacks to the bare
+// Fresnel reflectance are rare: they are taken as warp-uniform branches and
+// selected per lane (every lane of the warp calls this).
+template <bool HAVE_COS2>
 __device__ __forceinline__ float mgf2_reflectance(float cos_i, float n1, float n2, int layers, float ar_scale,
                                                   float kdelta, float cos_2)
 {
@@ -187,13 +197,13 @@ __device__ __forceinline__ float mgf2_reflectance(float cos_i, float n1, float n
     const float cn = 1.38f;
     const float a1 = n1 * (1.0f / cn);
     const float sin2_c = a1 * a1 * (1.0f - cos_i * cos_i);
-    if (sin2_c >= 1.0f) return fresnel_reflectance(cos_i, n1, n2);
     const float cos_c = sqrtf(1.0f - sin2_c);
-    if (cos_2 < 0.0f)
+    bool bare = sin2_c >= 1.0f;
+    if (!HAVE_COS2)
     {
         const float a2 = cn / n2;
         const float sin2_2 = a2 * a2 * (1.0f - cos_c * cos_c);
-        if (sin2_2 >= 1.0f) return fresnel_reflectance(cos_i, n1, n2);
+        bare = bare | (sin2_2 >= 1.0f);
         cos_2 = sqrtf(1.0f - sin2_2);
     }
     const float p1 = n1 * cos_i, pc = cn * cos_c, p2 = n2 * cos_2;
@@ -204,50 +214,63 @@ __device__ __forceinline__ float mgf2_reflectance(float cos_i, float n1, float n
     const float x = 2.0f * AC * BD * c2d;
     float R = (AD * AD + CB * CB + x) / (BD * BD + AC * AC + x);
     R = fminf(fmaxf(R, 0.0f), 1.0f);
-    return R * ar_scale;
+    R *= ar_scale;
+    if (__any_sync(kFull, bare))
+    {
+        const float Rb = fresnel_reflectance(cos_i, n1, n2);
+        R = bare ? Rb : R;
+    }
+    return R;
 }
 
 // Snell's law as refract_ray (trace_core.h:533-552), renormalised like it:
 // the walk's directions then stay unit to rounding over every interaction
 // (a drift in |d| would bias the next surface's root and the landing).
-// ci = -dot(nrm, d) >= 0; returns the transmitted cosine (for the coating),
-// or -1 on total internal reflection.
-__device__ __forceinline__ float refract_unit(V3& d, V3 nrm, float ci, float n1, float n2)
+// ci = -dot(nrm, d) >= 0; returns the transmitted cosine (for the coating)
+// and clears ok on total internal reflection.
+__device__ __forceinline__ float refract_unit(V3& d, V3 nrm, float ci, float n1, float n2, bool& ok)
 {
     const float nr = n1 / n2;
     const float s2t = nr * nr * (1.0f - ci * ci);
-    if (s2t >= 1.0f) return -1.0f;
+    ok = ok & (s2t < 1.0f);
     const float ct = sqrtf(1.0f - s2t);
     d = d * nr + nrm * (nr * ci - ct);
     d = d * rsqrtf(d.x * d.x + d.y * d.y + d.z * d.z);
     return ct;
 }
 
-// One surface interaction on the lane's ray; false when the ray died.
+// One surface interaction on the lane's ray; returns whether the ray lives
+// on.  Every lane of the warp runs it, whether or not its ray is still alive
+// (the walk is lock-step, so a lane leaving early saves no issue slot, only
+// adds branch and reconvergence instructions): the geometry of the common
+// path (untilted sphere or plane, round stop, single-layer coating) is
+// straight-line code whose tests fold into the result, and the caller
+// ignores the state of a lane whose ray died.  Branches are on the
+// surface's kind (the same for every lane) or warp-uniform votes; the
+// out-of-line weight models and bitmap stops, which index memory with the
+// ray's values, run only for lanes whose ray is alive.
 // WEIGHT = false skips the energy weight: whether a ray dies (missed,
 // clipped, TIR) is geometry only (trace_cuda.h sets the status from geometry
 // alone), so the off-sensor probe needs none of it.
 template <bool WEIGHT>
 __device__ __forceinline__ bool surface_step(V3& o, V3& d, const HotRec& h, const SurfRec& s, float lam,
                                              float kdelta, float n2, bool reflecting, float reflect_ior,
-                                             float& cur, float& w)
+                                             float& cur, float& w, bool alive)
 {
     V3 nrm, hit;
+    bool ok;
     if (!(h.bits & HB_GENERAL))
     {
         const float c = h.c;
         V3 q;
         float t;
-        if (!sphere_hit(o, d, h.z, c, t, q)) return false;
+        ok = alive & sphere_hit(o, d, h.z, c, t, q);
         const float hx = q.x * h.inv_aspect, hy = q.y;
         const float h2 = hx * hx + hy * hy;
-        if (!(h2 <= h.sa2)) return false;
+        ok = ok & (h2 <= h.sa2);
         // one test on the common path: plain circular / elliptical stops
-        if (h.bits & (HB_POLYGON | HB_IMAGE))
-        {
-            if ((h.bits & HB_POLYGON) ? !check_polygon(hx, hy, h2, s) : !image_aperture_ok(q.x, q.y, s))
-                return false;
-        }
+        if (h.bits & HB_POLYGON) ok = ok & check_polygon(hx, hy, h2, s);
+        else if ((h.bits & HB_IMAGE) && ok) ok = image_aperture_ok(q.x, q.y, s);
         // outward normal (c q_x, c q_y, c q_z - 1), turned to oppose the ray
         // (for a plane, c = 0, it is (0, 0, -1) as it stands)
         nrm = v3(c * q.x, c * q.y, c * q.z - 1.0f);
@@ -255,8 +278,8 @@ __device__ __forceinline__ bool surface_step(V3& o, V3& d, const HotRec& h, cons
     }
     else
     {
-        float t;
-        if (!intersect_general(o, d, s, t, nrm)) return false;
+        float t = 0.0f;
+        ok = alive && intersect_general(o, d, s, t, nrm);
         hit = o + d * t;
     }
     float ci = -dot(nrm, d);
@@ -268,8 +291,8 @@ __device__ __forceinline__ bool surface_step(V3& o, V3& d, const HotRec& h, cons
     {
         if (WEIGHT)
         {
-            w *= simple ? mgf2_reflectance(ci, n1, n2, h.ar_layers, h.ar_scale, kdelta, -1.0f)
-                        : weight_general(d, nrm, n1, n2, s, lam, true);
+            if (simple) w *= mgf2_reflectance<false>(ci, n1, n2, h.ar_layers, h.ar_scale, kdelta, -1.0f);
+            else if (ok) w *= weight_general(d, nrm, n1, n2, s, lam, true);
             if (h.bits & HB_ATTEN) w *= attenuator_general(hit, s);
         }
         d = d + nrm * (2.0f * ci);
@@ -279,17 +302,16 @@ __device__ __forceinline__ bool surface_step(V3& o, V3& d, const HotRec& h, cons
     else
     {
         const V3 d_in = d;
-        const float ct = refract_unit(d, nrm, ci, n1, n2);
-        if (ct < 0.0f) return false;
+        const float ct = refract_unit(d, nrm, ci, n1, n2, ok);
         if (WEIGHT)
         {
-            w *= simple ? 1.0f - mgf2_reflectance(ci, n1, n2, h.ar_layers, h.ar_scale, kdelta, ct)
-                        : weight_general(d_in, nrm, n1, n2, s, lam, false);
+            if (simple) w *= 1.0f - mgf2_reflectance<true>(ci, n1, n2, h.ar_layers, h.ar_scale, kdelta, ct);
+            else if (ok) w *= weight_general(d_in, nrm, n1, n2, s, lam, false);
             if (h.bits & HB_ATTEN) w *= attenuator_general(hit, s);
         }
         cur = n2;
     }
-    return true;
+    return ok;
 }
 
 // The three legs of trace_ghost_ray (trace.cpp:196-233) flattened into one
@@ -377,11 +399,10 @@ __device__ __forceinline__ void trace_warp(const RenderArgs& A, const SurfRec* l
             if (!(hr.bits & HB_ACTIVE)) continue;
             n2 = back ? bfl[s] : atl[s];
             const float rior = (back && refl) ? atl[a] : cur;
-            if (alive)
-            {
-                alive = surface_step<!PROBE>(o, d, hr, lens[s], sp.x, kdelta, n2, refl, rior, cur, w);
-                if (PROBE && !alive) kdead = k;
-            }
+            // every lane steps (see surface_step); a dead lane's state is not read
+            const bool ok = surface_step<!PROBE>(o, d, hr, lens[s], sp.x, kdelta, n2, refl, rior, cur, w, alive);
+            if (PROBE && alive && !ok) kdead = k;
+            alive = ok;
         }
         if (PROBE && A.death != nullptr && active)
             A.death[(size_t)pair * A.perm_stride + sidx] = (unsigned char)min(kdead, 255);

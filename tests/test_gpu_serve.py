@@ -224,3 +224,26 @@ def test_psf_request_matches_render_psf(pool):
         assert rel_l2(alone[r.rid].numpy(), wants[r.rid]) < 1e-6
         assert rel_l2(mix[r.rid].numpy(), wants[r.rid]) < 1e-6
         assert r.traced > 0
+
+
+def test_served_requests_match_fp64_oracle(pool):
+    """Every flare request of a concurrent mix (three lenses, several sizes,
+    wavelength counts, grids and fields, off-sensor cull on) against the FP64
+    oracle's render of the same pairs, grid, source and spectrum, colour
+    correction applied: relative L2 below 1e-3."""
+    from oracle import oracle as O
+    from ghostlight_gb300.flare import pupil_grid
+    from ghostlight_gb300.serve import _spectral
+    p, cfg = pool
+    reqs = _reqs()
+    got = _run_server(p, reqs)
+    for req in reqs:
+        rl = p[req.lens_id]
+        spec, corr = _spectral(req.n_spec, cfg)
+        grid = pupil_grid(rl.lens, req.ray_grid, 0, 0, 0, 0.0)
+        src = np.array([[math.radians(req.field_deg), 0.0, 1.0, 1.0, 1.0]], np.float32)
+        want = O.render(rl.lens.records(), rl.pairs, rl.boosts, src, [grid], spec, rl.sensor_half_w,
+                        rl.sensor_half_h, req.width, req.height, req.gain, fp64=True)
+        want = np.einsum("ij,jhw->ihw", corr.astype(np.float64), want)
+        assert np.abs(want).sum() > 0
+        assert rel_l2(got[req.rid].numpy(), want) < 1e-3, req

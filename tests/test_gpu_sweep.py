@@ -1,6 +1,6 @@
 """Source sweep as one CUDA graph: replay equals direct enqueue, each frame's
-ghost layer equals a plan render of its source, and the starburst lands on
-the source's image point."""
+ghost layer equals a plan render of its source and the FP64 oracle's render,
+and the starburst lands on the source's image point."""
 import math
 
 import numpy as np
@@ -83,3 +83,26 @@ def test_frames_equal_plan_renders_and_starburst_is_centred():
     y, x = np.unravel_index(np.argmax(g), g.shape)
     assert abs(x - cx) <= 1.0 and abs(y - cy) <= 1.0
     sw.close(); sb["plan"].close(); rl.close()
+
+
+def test_sweep_frames_match_fp64_oracle():
+    """Each replayed frame's ghost layer against the FP64 oracle's render of
+    the same lens, pairs, grid, spectrum and source (colour correction
+    applied): relative L2 below 1e-3."""
+    from oracle import oracle as O
+    from ghostlight_gb300.flare import pupil_grid
+    from ghostlight_gb300.serve import _spectral
+    rl, cfg, sw, src, _ = _setup(False)
+    sw.capture()
+    sw.replay()
+    torch.cuda.synchronize()
+    spec, corr = _spectral(sw.n_spec, cfg)
+    grid = pupil_grid(rl.lens, sw.ray_grid, 0, 0, 0, 0.0)
+    for k in range(sw.n_frames):
+        s = np.array([[src[k, 0], src[k, 1], 1.0, 1.0, 1.0]], np.float32)
+        want = O.render(rl.lens.records(), rl.pairs, rl.boosts, s, [grid], spec, rl.sensor_half_w,
+                        rl.sensor_half_h, sw.width, sw.height, 1000.0, fp64=True)
+        want = np.einsum("ij,jhw->ihw", corr.astype(np.float64), want)
+        assert np.abs(want).sum() > 0, k
+        assert rel_l2(sw.frame(k).cpu().numpy(), want) < 1e-3, k
+    sw.close(); rl.close()
