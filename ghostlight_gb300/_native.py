@@ -86,6 +86,7 @@ def _declare(lib):
     lib.gl_mdft_plan_execute3.argtypes = [vp, vp, vp, vp, vp, i, i, i, i, i, i, i, P(f), vp]
     lib.gl_sprite_plan_autocorr.argtypes = [vp, vp, i, vp, i, i, vp]
     lib.gl_mdft_plan_set_launch.argtypes = [vp, i]
+    lib.gl_mdft_plan_set_tile.argtypes = [vp, i]
     lib.gl_mdft_plan_set_lambda_range.argtypes = [vp, i, i]
     lib.gl_mdft_plan_execute2.argtypes = [vp, vp, vp, vp, vp, i, vp]
     lib.gl_build_pupil.argtypes = [P(gl_surface), i, i, f, i, f, vp, vp]

@@ -7,7 +7,8 @@ JSON file so a server starts tuned.  Knobs:
 
 * the ghost render: persistent work queue with 4..8 CTAs per SM, or one-shot
   CTAs of 1..8 32-sample items per warp (``GhostRenderPlan.set_launch``);
-* the starburst GEMMs: the persistent grid size (``MdftPlan.set_launch``).
+* the starburst GEMMs: the persistent grid size and the output tile width of
+  the second GEMM, 128 or 64 complex columns per unit (``MdftPlan.set_launch``).
 
 The splat has no tile to tune: each lane keeps its 2x2 footprint across the
 wavelength loop and flushes on change, so there is no shared-memory tile whose
@@ -25,8 +26,10 @@ GHOST_CANDIDATES = [(0, 0, 1), (0, 0, 2), (0, 0, 4), (0, 0, 8), (0, 0, 16), (0, 
                     (2, 0, 1), (4, 0, 1), (8, 0, 1)]
 
 
-def mdft_candidates(sms: int) -> List[int]:
-    return [0, max(1, (3 * sms) // 4), max(1, sms // 2)]
+def mdft_candidates(sms: int) -> List[tuple]:
+    """(CTAs, tile width) pairs: one CTA per SM with either tile, then fewer
+    CTAs with the default tile."""
+    return [(0, 128), (0, 64), (max(1, (3 * sms) // 4), 128), (max(1, sms // 2), 128)]
 
 
 class Tuner:
@@ -126,7 +129,7 @@ def tune_ghost_plan(plan, outs, stream=None, tuner: Optional[Tuner] = None, cand
 
 
 def tune_mdft_plan(plan, pupil, outs, stream=None, tuner: Optional[Tuner] = None, candidates=None):
-    """Pick and apply the GEMM grid of an MdftPlan."""
+    """Pick and apply the GEMM grid and output tile of an MdftPlan."""
     import torch
     t = tuner or default_tuner()
     sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count

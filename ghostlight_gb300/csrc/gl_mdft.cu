@@ -233,6 +233,7 @@ struct MdftArgs {
     int box;                          // 1: accumulate Re E (pixel-integrated form); 0: |E|^2
     float4 tint;                      // per-launch colour factor on the weights
     int lam_base;                     // first wavelength of this launch's range
+    int NBt;                          // step 2: output tiles per row of the frame (Kx / tile width)
 };
 
 template <int FORM>
@@ -269,13 +270,19 @@ __device__ __forceinline__ void store_split16(__nv_bfloat16* row, int n, int i0,
     d2[0] = h4[0]; d2[1] = h4[1];
 }
 
-template <int FORM, int STEP>
+// TN (step 2): complex output columns per unit, 128 or 64 (the autotuner's
+// tile-shape knob).  A 64-column unit stages three 64-row blocks of T' (8 KB
+// each, box rows 64 in tB) and issues N = 128 MMAs; its smaller stages allow
+// a three-deep pipeline, and twice the units spread a small frame over more
+// SMs.
+template <int FORM, int STEP, int TN = 128>
 __global__ void __launch_bounds__(kMdftThreads, 1) mdft_kernel(const __grid_constant__ CUtensorMap tA,
                                                               const __grid_constant__ CUtensorMap tB, MdftArgs args)
 {
-    constexpr int nB = (STEP == 2) ? 3 : 1;                      // B operand tiles per stage
-    constexpr int kStagesM = (STEP == 2) ? 2 : 4;
-    constexpr int kStageBytes = (2 + nB) * kOpTile;
+    static_assert(TN == 128 || TN == 64, "tile width");
+    constexpr int kBBytes = (STEP == 2) ? 3 * TN * 128 : kOpTile;   // B operand bytes per stage
+    constexpr int kStagesM = (STEP == 2) ? (TN == 128 ? 2 : 3) : 4;
+    constexpr int kStageBytes = 2 * kOpTile + kBBytes;
     constexpr int kbe = (FORM == 0) ? 64 : 32;                   // reduction elements per 128-byte row
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = align1024(smem_raw);
@@ -309,12 +316,12 @@ __global__ void __launch_bounds__(kMdftThreads, 1) mdft_kernel(const __grid_cons
         if (STEP == 2)
         {
             // wavelength-major: all output tiles of one wavelength, then the next
-            const int tiles = args.NBm * args.NB;
+            const int tiles = args.NBm * args.NBt;
             const int lr = u / tiles;               // wavelength within this launch's range
             lam = args.lam_base + lr;
             const int tile = u - lr * tiles;
-            mb = tile / args.NB;
-            xb = tile % args.NB;
+            mb = tile / args.NBt;
+            xb = tile % args.NBt;
         }
         else
         {
@@ -347,9 +354,14 @@ __global__ void __launch_bounds__(kMdftThreads, 1) mdft_kernel(const __grid_cons
                     tc::tma_load_2d(st + kOpTile, &tA, x, rowA + args.KA, &full[s]);
                     if (STEP == 2)
                     {
-                        const int rowB = ((lam * args.NB + xb) * 3) * 128;
+                        // rows [-Ti | Tr | Ti] of this tile's columns: T' holds them
+                        // in 128-row blocks, a 64-column tile takes one half of each
+                        const int xb128 = (TN == 128) ? xb : (xb >> 1);
+                        const int half = (TN == 128) ? 0 : (xb & 1) * 64;
+                        const int rowB = ((lam * args.NB + xb128) * 3) * 128 + half;
                         #pragma unroll
-                        for (int j = 0; j < 3; ++j) tc::tma_load_2d(st + (2 + j) * kOpTile, &tB, x, rowB + j * 128, &full[s]);
+                        for (int j = 0; j < 3; ++j)
+                            tc::tma_load_2d(st + 2 * kOpTile + j * TN * 128, &tB, x, rowB + j * 128, &full[s]);
                     }
                     else
                     {
@@ -367,7 +379,7 @@ __global__ void __launch_bounds__(kMdftThreads, 1) mdft_kernel(const __grid_cons
     {
         if (lane == 0)
         {
-            const uint32_t id256 = idesc_any<FORM>(128, 256);
+            const uint32_t id2 = idesc_any<FORM>(128, 2 * TN);
             const uint32_t id128 = idesc_any<FORM>(128, 128);
             int it = 0, ui = 0;
             bool stop = false;
@@ -387,13 +399,13 @@ __global__ void __launch_bounds__(kMdftThreads, 1) mdft_kernel(const __grid_cons
                     const uint64_t aI = tc::sw128_desc(tc::smem_u32(st + kOpTile));
                     if (STEP == 2)
                     {
-                        const uint64_t bRI = tc::sw128_desc(tc::smem_u32(st + 3 * kOpTile));   // [Tr | Ti]
-                        const uint64_t bNR = tc::sw128_desc(tc::smem_u32(st + 2 * kOpTile));   // [-Ti | Tr]
+                        const uint64_t bRI = tc::sw128_desc(tc::smem_u32(st + 2 * kOpTile + TN * 128));   // [Tr | Ti]
+                        const uint64_t bNR = tc::sw128_desc(tc::smem_u32(st + 2 * kOpTile));              // [-Ti | Tr]
                         #pragma unroll
                         for (int kk = 0; kk < 4; ++kk)
                         {
-                            mma_any<FORM>(d, aR + 2 * kk, bRI + 2 * kk, id256, (kb | kk) != 0);
-                            mma_any<FORM>(d, aI + 2 * kk, bNR + 2 * kk, id256, 1u);
+                            mma_any<FORM>(d, aR + 2 * kk, bRI + 2 * kk, id2, (kb | kk) != 0);
+                            mma_any<FORM>(d, aI + 2 * kk, bNR + 2 * kk, id2, 1u);
                         }
                     }
                     else
@@ -437,13 +449,13 @@ __global__ void __launch_bounds__(kMdftThreads, 1) mdft_kernel(const __grid_cons
                 const bool row_in = l < args.win_h;
                 const size_t orow = (size_t)(args.y0 + l) * (size_t)args.out_w + (size_t)args.x0;
                 #pragma unroll 1
-                for (int c = 0; c < 8; ++c)
+                for (int c = 0; c < TN / 16; ++c)
                 {
                     float re[16], im[16];
                     tc::tmem_ld16(ta + (uint32_t)(c * 16), re);
-                    tc::tmem_ld16(ta + 128u + (uint32_t)(c * 16), im);
+                    tc::tmem_ld16(ta + (uint32_t)TN + (uint32_t)(c * 16), im);
                     if (!ok || !row_in) continue;
-                    const int kc = xb * 128 + c * 16;
+                    const int kc = xb * TN + c * 16;
                     #pragma unroll
                     for (int j = 0; j < 16; j += 4)
                     {
@@ -821,8 +833,9 @@ struct MdftPlan {
     int box = 0;                // pixel-integrated form (the reference's MDFT engine)
     int lam0 = 0, lam1 = -1;    // wavelength range of the next executes (lam1 < 0: all)
     int ctas = 0;               // GEMM grid (0 = one CTA per SM)
+    int tile_n = 128;           // step-2 output tile width (complex columns): 128 or 64
     int* err = nullptr;
-    CUtensorMap t_wx, t_wy, t_mask, t_tp;
+    CUtensorMap t_wx, t_wy, t_mask, t_tp, t_tp64;
     int sms = 0;
 };
 
@@ -930,15 +943,18 @@ extern "C" int gl_mdft_plan_create3(int n, int Kx, int Ky, int n_lambda, const d
     // shared-memory opt-in once here, so execute enqueues kernels only (graph capture)
     {
         const int smem1 = 4 * 3 * kOpTile + 1024, smem2 = 2 * 5 * kOpTile + 1024;
+        const int smem2h = 3 * (2 * kOpTile + 3 * 64 * 128) + 1024;
         if (form == 0)
         {
             chk(cudaFuncSetAttribute(mdft_kernel<0, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem1));
             chk(cudaFuncSetAttribute(mdft_kernel<0, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem2));
+            chk(cudaFuncSetAttribute(mdft_kernel<0, 2, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem2h));
         }
         else if (form == 1)
         {
             chk(cudaFuncSetAttribute(mdft_kernel<1, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem1));
             chk(cudaFuncSetAttribute(mdft_kernel<1, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem2));
+            chk(cudaFuncSetAttribute(mdft_kernel<1, 2, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem2h));
         }
     }
     const CUtensorMapDataType dt = form == 0 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
@@ -950,6 +966,7 @@ extern "C" int gl_mdft_plan_create3(int n, int Kx, int Ky, int n_lambda, const d
         if (!rc) rc = make_tmap_2d(&p->t_wy, p->wy, dt, p->elem, (uint64_t)n_lambda * 2 * Ky, (uint64_t)p->Kp, 128, bc);
         if (!rc) rc = make_tmap_2d(&p->t_mask, p->mask, dt, p->elem, (uint64_t)n, (uint64_t)p->Kp, 128, bc);
         if (!rc) rc = make_tmap_2d(&p->t_tp, p->tprime, dt, p->elem, (uint64_t)n_lambda * NBx * 3 * 128, (uint64_t)p->Kp, 128, bc);
+        if (!rc) rc = make_tmap_2d(&p->t_tp64, p->tprime, dt, p->elem, (uint64_t)n_lambda * NBx * 3 * 128, (uint64_t)p->Kp, 64, bc);
     }
     if (e != cudaSuccess || rc)
     {
@@ -1015,6 +1032,7 @@ extern "C" int gl_mdft_plan_execute3(gl_mdft_plan* plan, const float* d_pupil, f
         GL_CUDA_TRY(cudaMemsetAsync(d_out_b, 0, npx * sizeof(float), st));
     }
     MdftArgs a;
+    a.NBt = NBx;
     a.KA = p->Kx; a.Kx = p->Kx; a.NBm = NBx;
     a.n = p->n; a.n_lambda = p->n_lambda; a.Kp = p->Kp;
     a.nkb = p->Kp / (p->form == 0 ? 64 : 32);
@@ -1031,8 +1049,11 @@ extern "C" int gl_mdft_plan_execute3(gl_mdft_plan* plan, const float* d_pupil, f
     const int g1 = std::min(a.n_units, gmax);
     MdftArgs a2 = a;
     a2.KA = p->Ky; a2.NBm = NBy;
-    a2.n_units = NBy * NBx * nl;                        // step 2: (lambda, output tile)
+    const bool half = p->tile_n == 64;
+    a2.NBt = p->Kx / p->tile_n;
+    a2.n_units = NBy * a2.NBt * nl;                     // step 2: (lambda, output tile)
     const int g2 = std::min(a2.n_units, gmax);
+    const size_t smem2h = 3 * (2 * (size_t)kOpTile + 3 * 64 * 128) + 1024;
     if (p->form == 2)
     {
         mdft_simt_step1<<<dim3(NI, NBx, nl), 256, 0, st>>>(static_cast<const float*>(p->wx),
@@ -1045,12 +1066,14 @@ extern "C" int gl_mdft_plan_execute3(gl_mdft_plan* plan, const float* d_pupil, f
     else if (p->form == 0)
     {
         mdft_kernel<0, 1><<<g1, kMdftThreads, smem1, st>>>(p->t_wx, p->t_mask, a);
-        mdft_kernel<0, 2><<<g2, kMdftThreads, smem2, st>>>(p->t_wy, p->t_tp, a2);
+        if (half) mdft_kernel<0, 2, 64><<<g2, kMdftThreads, smem2h, st>>>(p->t_wy, p->t_tp64, a2);
+        else mdft_kernel<0, 2><<<g2, kMdftThreads, smem2, st>>>(p->t_wy, p->t_tp, a2);
     }
     else
     {
         mdft_kernel<1, 1><<<g1, kMdftThreads, smem1, st>>>(p->t_wx, p->t_mask, a);
-        mdft_kernel<1, 2><<<g2, kMdftThreads, smem2, st>>>(p->t_wy, p->t_tp, a2);
+        if (half) mdft_kernel<1, 2, 64><<<g2, kMdftThreads, smem2h, st>>>(p->t_wy, p->t_tp64, a2);
+        else mdft_kernel<1, 2><<<g2, kMdftThreads, smem2, st>>>(p->t_wy, p->t_tp, a2);
     }
     GL_CUDA_TRY(cudaGetLastError());
     launches += 2;
@@ -1086,6 +1109,15 @@ extern "C" int gl_mdft_plan_set_launch(gl_mdft_plan* plan, int ctas)
     if (!plan || ctas < 0) return fail(GL_ERR_INVALID, "mdft_plan_set_launch: bad arguments");
     // one 192-thread CTA with ~161 KB of shared memory fits per SM
     plan->p->ctas = ctas == 0 ? 0 : std::min(ctas, plan->p->sms);
+    return GL_OK;
+}
+
+extern "C" int gl_mdft_plan_set_tile(gl_mdft_plan* plan, int tile_n)
+{
+    using namespace gl;
+    if (!plan || (tile_n != 64 && tile_n != 128))
+        return fail(GL_ERR_INVALID, "mdft_plan_set_tile: the tile width must be 64 or 128 output columns");
+    plan->p->tile_n = tile_n;
     return GL_OK;
 }
 

@@ -108,10 +108,15 @@ class MdftPlan:
         """Restrict the next executes to wavelengths [begin, end) ((0, -1): all)."""
         _native.check(self._lib.gl_mdft_plan_set_lambda_range(self._h, int(begin), int(end)), "mdft")
 
-    def set_launch(self, ctas: int = 0):
-        """GEMM grid of the tensor-core forms (0 = one CTA per SM)."""
+    def set_launch(self, ctas=0, tile: int = 128):
+        """GEMM grid of the tensor-core forms (0 = one CTA per SM) and the
+        output tile width of their second GEMM (128 or 64 complex columns);
+        ``ctas`` may also be a (ctas, tile) pair, as the autotuner passes it."""
+        if isinstance(ctas, (tuple, list)):
+            ctas, tile = ctas
         _native.check(self._lib.gl_mdft_plan_set_launch(self._h, int(ctas)), "mdft")
-        self.launch = int(ctas)
+        _native.check(self._lib.gl_mdft_plan_set_tile(self._h, int(tile)), "mdft")
+        self.launch = (int(ctas), int(tile))
 
     def execute_raw(self, pupil_ptr: int, r_ptr: int, g_ptr: int, b_ptr: int, stream=None, accumulate=False):
         """execute on raw device addresses (planes owned by another component,

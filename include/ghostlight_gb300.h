@@ -401,6 +401,13 @@ int gl_mdft_plan_create2(int n, int Kx, int Ky, int n_lambda, const double* scal
 int gl_mdft_plan_set_center(gl_mdft_plan* plan, double center_x, double center_y, void* stream);
 /* GEMM grid of the tcgen05 forms (0 = one CTA per SM); autotuner knob. */
 int gl_mdft_plan_set_launch(gl_mdft_plan* plan, int ctas);
+/* Output tile of the second GEMM (E = W_y T) of the tcgen05 forms, in
+ * complex output columns per unit: 128 (default; N = 256 MMAs, two pipeline
+ * stages) or 64 (N = 128 MMAs, three stages, twice the units, so a small
+ * frame spreads over more SMs); the autotuner's tile-shape knob.  No
+ * counterpart in the reference (its starburst contracts with SIMT dot
+ * products, mdft_render.cu:137-172).  Results agree to float rounding. */
+int gl_mdft_plan_set_tile(gl_mdft_plan* plan, int tile_n);
 /* Restrict the next executes to wavelengths [lam_begin, lam_end) (0, -1:
  * all): a large pattern enqueued as several short wavelength ranges (each
  * accumulating) frees its CTAs' SMs between the ranges, so a serving loop's

@@ -194,3 +194,39 @@ def test_mdft_wavelength_ranges_sum_to_the_whole(form):
     with pytest.raises(ValueError):
         plan.set_lambda_range(5, 9)
     plan.close()
+
+
+@pytest.mark.parametrize("form,tol", [("split_bf16", 1e-3), ("tf32", 2e-2)])
+def test_output_tile_widths_agree_and_match_oracle(form, tol):
+    """The second GEMM's output tile (128 or 64 complex columns per unit,
+    gl_mdft_plan_set_tile): both widths give the same frame to float rounding
+    (the same K blocks in the same order per output element) and match the
+    FP64 oracle, on a rectangular frame with a recentred pattern, a
+    wavelength range and the accumulate mode."""
+    from ghostlight_gb300.starburst import MdftPlan
+    from oracle import mdft_oracle as MO
+    n, Kx, Ky, L = 128, 384, 256, 5
+    A, sx, sy, w = _inputs(n, L)
+    plan = MdftPlan(n, (Kx, Ky), sx, sy, w, form, center_x=Kx / 2 - 7.25, center_y=Ky / 2 + 3.5)
+    dA = torch.from_numpy(A).cuda()
+    got = {}
+    for tile in (128, 64):
+        plan.set_launch(0, tile)
+        assert plan.launch == (0, tile)
+        outs = [torch.full((Ky, Kx), 0.5, device="cuda") for _ in range(3)]
+        plan.set_lambda_range(0, 2)
+        plan.execute(dA, *outs, accumulate=True)
+        plan.set_lambda_range(2, L)
+        plan.execute(dA, *outs, accumulate=True)
+        plan.set_lambda_range(0, -1)
+        torch.cuda.synchronize()
+        assert plan.status() == 0
+        got[tile] = np.stack([o.cpu().numpy() for o in outs]).astype(np.float64) - 0.5
+    want = MO.eform(A, (Kx, Ky), sx, sy, Kx / 2 - 7.25, Ky / 2 + 3.5, w)
+    for tile in (128, 64):
+        err = np.linalg.norm(got[tile] - want) / np.linalg.norm(want)
+        assert err < tol, (tile, err)
+    assert np.linalg.norm(got[64] - got[128]) / np.linalg.norm(got[128]) < 1e-6
+    with pytest.raises(ValueError):
+        plan.set_launch(0, 96)
+    plan.close()

@@ -50,8 +50,9 @@ def test_autocorrelation_matches_fp64():
     plan.close()
 
 
-@pytest.mark.parametrize("form,tol", [("split_bf16", 1e-4), ("tf32", 2e-2), ("fp32", 1e-5)])
-def test_pixel_integrated_mdft_matches_fp64(form, tol):
+@pytest.mark.parametrize("form,tol,tile", [("split_bf16", 1e-4, 128), ("split_bf16", 1e-4, 64), ("tf32", 2e-2, 128),
+                                           ("tf32", 2e-2, 64), ("fp32", 1e-5, 128)])
+def test_pixel_integrated_mdft_matches_fp64(form, tol, tile):
     from ghostlight_gb300.starburst import MdftPlan, SpritePlan, _round128
     from oracle import mdft_box_oracle as MB
     _, N, fill, pupil = _setup()
@@ -81,6 +82,7 @@ def test_pixel_integrated_mdft_matches_fp64(form, tol):
     knorm = (px_mm * px_mm) / (dx * dx) * gain
     K = _round128(2 * half + 1)
     plan = MdftPlan(n, (K, K), s, s, w, form, center_x=0.0, center_y=0.0, box=True, red_center=float(mc))
+    plan.set_launch(0, tile)                # output tile of the second GEMM: 128 or 64 columns
     out = [torch.zeros((H, W), dtype=torch.float32, device="cuda") for _ in range(3)]
     for (px, py, r, g, b) in sources:
         x0, x1 = max(0, int(math.floor(px)) - half), min(W, int(math.floor(px)) + half + 1)
