@@ -1155,15 +1155,17 @@ def roofline(res, plan):
 
 
 # FP32 operations per traced ray-wavelength (FADD + FMUL + 2 x FFMA, thread
-# level, predicated on) of the timed render kernel on this workload, measured
-# with ncu on one launch of the tuned shape
-# (smsp__sass_thread_inst_executed_op_{fadd,fmul,ffma}_pred_on.sum:
-# 4.926e9 + 20.971e9 + 2 x 18.993e9 = 6.388e10 FLOP over 6.007e7 traces)
-# and frozen as the algorithmic count.
+# level, predicated on) of the render kernel on this workload, measured with
+# ncu on one launch of the tuned shape while only the lanes of live rays ran
+# the step (smsp__sass_thread_inst_executed_op_{fadd,fmul,ffma}_pred_on.sum:
+# 4.926e9 + 20.971e9 + 2 x 18.993e9 = 6.388e10 FLOP over 6.007e7 traces),
+# and frozen as the algorithmic count.  The branch-free step now also runs
+# on the lanes of dead rays (work nobody reads: 7.5e10 counted FLOP per
+# launch), which the algorithmic count leaves out.
 FLOPS_PER_RAY_LAMBDA = 1063.5
 # DRAM bytes (read + write) of one render launch on this frame, from the same
-# capture (dram__bytes_read.sum + dram__bytes_write.sum: 41.03 + 3.09 MB).
-RENDER_DRAM_BYTES = 44.12e6
+# capture (dram__bytes_read.sum + dram__bytes_write.sum: 41.03 + 4.11 MB).
+RENDER_DRAM_BYTES = 45.15e6
 FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.070e9 / 1e12
 
 
