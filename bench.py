@@ -54,17 +54,18 @@ def _progress(what: str) -> None:
     print("[bench +%.1fs] %s" % (time.perf_counter() - _T0, what), file=sys.stderr, flush=True)
 
 
-def _workload():
-    """Seeded config-2 lens and its calibration (the reference's
-    calibrate_lens values for the same records, committed as a fixture)."""
+def _workload(name="cfg2_wide_angle_24"):
+    """Seeded config-2 lens (or another seeded fixture lens) and its
+    calibration (the reference's calibrate_lens values for the same records,
+    committed as a fixture)."""
     from ghostlight_gb300._abi import gl_surface
     from ghostlight_gb300.optics import OpticalSystem
     pins = np.load(GOLDEN / "ref_pins.npz")
-    raw = pins["cfg2_wide_angle_24/lens"]
+    raw = pins[name + "/lens"]
     recs = list((gl_surface * raw.shape[0]).from_buffer_copy(raw.tobytes()))
     meta = json.loads((GOLDEN / "ref_meta.json").read_text())
-    cal = meta["cfg2_wide_angle_24"]["calibration"]
-    return OpticalSystem.from_records(recs, name="cfg2_wide_angle_24"), cal
+    cal = meta[name]["calibration"]
+    return OpticalSystem.from_records(recs, name=name), cal
 
 
 def _config():
@@ -266,6 +267,11 @@ def run_gpu(args, rank, world):
     d2h = 3 * W * H * 4
 
     traced = plan.traced()            # traces of the last (timed) execute: deterministic per frame
+    cfg1 = None
+    if not args.quick:
+        with torch.cuda.stream(stream):
+            cfg1 = run_cfg1(args, dev, stream, timed)
+        _progress("configuration 1")
     cfg3 = frame_res = None
     if not args.quick or args.only == "cfg3":
         with torch.cuda.stream(stream):
@@ -308,11 +314,77 @@ def run_gpu(args, rank, world):
         "clocks": clk.summary(),
         "autotune": tuner.log,
     }
+    if cfg1 is not None:
+        res["cfg1"] = cfg1
     if cfg3 is not None:
         res["starburst_psf"] = cfg3
     if frame_res is not None:
         res["full_flare_frame"] = frame_res
     return res, plan, frame_host
+
+
+# ---- configuration 1: the plain small frame ------------------------------------
+def run_cfg1(args, dev, stream, timed):
+    """Configuration 1 on the GPU: the seeded 12-surface double Gauss (6-blade
+    stop), the 2-reflection pairs of the device culler at 1e-7 that do not
+    cross the stop, a 32^2 pupil grid, 8 wavelengths, a 10 deg source,
+    512^2 float32 RGB, the off-sensor cull on (as the reference arm's cfg1
+    CPU frame), batched (one graph) against the per-pair launches; and its
+    starburst, the split-BF16 matrix DFT of the device-built 256^2 stop
+    pupil to 512^2 at the same 8 wavelengths, alone and added to the frame
+    in the same graph."""
+    import torch
+    import ghostlight_gb300 as gl
+    from ghostlight_gb300.flare import GhostRenderPlan, filter_ghosts_device, pupil_grid, spectral_table
+    from ghostlight_gb300.prescriptions import stop_crossing
+    from ghostlight_gb300.starburst import MdftPlan, build_pupil
+    lens, cal = _workload("cfg1_double_gauss_12")
+    hw, hh = cal["sensor_half_w"], cal["sensor_half_h"]
+    fr = filter_ghosts_device(lens, hw, hh, gl.FlareConfig(min_ghost_intensity=1e-7))
+    keep = np.array([not stop_crossing(lens.records(), int(a), int(b)) for a, b in fr.pairs], bool)
+    pairs, boosts = fr.pairs[keep], fr.boosts[keep]
+    spec, corr = spectral_table(8)
+    grid = pupil_grid(lens, 32)
+    src = np.array([[math.radians(10.0), 0.0, 1.0, 1.0, 1.0]], np.float32)
+    W1 = H1 = 512
+    mk = lambda plain: GhostRenderPlan(lens, pairs, boosts, src, [grid], None, spec, corr, W1, H1, hw, hh, 1000.0,
+                                       apply_correction=True, plain_per_pair=plain, cull_dead_pairs=not plain)
+    plan, plain = mk(False), mk(True)
+    outs = torch.zeros((3, H1, W1), device=dev)
+    n_sb = 256
+    lam = spec[:, 0].astype(np.float64)
+    s = (1.0 / (2.0 * n_sb)) * 550.0 / lam
+    sb = MdftPlan(n_sb, W1, s, s, (spec[:, 1:4] / 1e3).astype(np.float32), "split_bf16",
+                  center_x=W1 / 2.0, center_y=H1 / 2.0)
+    pupil = build_pupil(lens, n_sb, 0.3)
+    for _ in range(2):
+        plan.execute(outs[0], outs[1], outs[2], stream=stream.cuda_stream)
+        sb.execute(pupil, outs[0], outs[1], outs[2], stream=stream.cuda_stream, accumulate=True)
+    stream.synchronize()
+    g_ghost, g_frame = torch.cuda.CUDAGraph(), torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g_ghost, stream=stream):
+        plan.execute(outs[0], outs[1], outs[2], stream=stream.cuda_stream)
+    with torch.cuda.graph(g_frame, stream=stream):
+        plan.execute(outs[0], outs[1], outs[2], stream=stream.cuda_stream)
+        sb.execute(pupil, outs[0], outs[1], outs[2], stream=stream.cuda_stream, accumulate=True)
+    steps, warm = max(args.steps, 10), max(args.warmup, 3)
+    t_ghost = timed(g_ghost.replay, steps, warm)
+    t_frame = timed(g_frame.replay, steps, warm)
+    t_sb = timed(lambda: sb.execute(pupil, outs[0], outs[1], outs[2], stream=stream.cuda_stream), steps, warm)
+    t_plain = timed(lambda: plain.execute(outs[0], outs[1], outs[2], stream=stream.cuda_stream), steps, warm)
+    traced = plan.traced()
+    status = sb.status()
+    plan.close(); plain.close(); sb.close()
+    fps = len(t_ghost) / sum(t_ghost)
+    plain_fps = len(t_plain) / sum(t_plain)
+    return {"workload": "cfg1: seeded 12-surface double Gauss, %d non-stop-crossing pairs (device culler at "
+                        "1e-7), 32^2 grid, 8 wavelengths, 10 deg, 512^2, off-sensor cull on; starburst: "
+                        "split-BF16 matrix DFT of the 256^2 stop pupil to 512^2 x 8 wavelengths" % len(pairs),
+            "ghost_frames_per_s": fps, "ghost_ms": 1e3 / fps, "ray_lambda_traces": traced,
+            "plain_frames_per_s": plain_fps, "speedup_batched_vs_plain": fps / plain_fps,
+            "starburst_ms": 1e3 * float(np.median(t_sb)), "starburst_status": status,
+            "frame_frames_per_s": len(t_frame) / sum(t_frame),
+            "l2": "flushed between timed steps"}
 
 
 # ---- starburst precision sweep + PSF/veil convolution (cfg3) -----------------

@@ -31,12 +31,16 @@ def test_device_trace_matches_reference_rays(pins, name):
         rays = torch.from_numpy(pins["%s/rays_%d/in" % (name, k)]).cuda()
         want = pins["%s/rays_%d/out" % (name, k)]
         got = gl.trace_rays(lens, rays, a, b).cpu().numpy()
-        agree = (got[:, 4] == want[:, 4]).mean()
-        assert agree >= 0.99, (name, k, agree)
+        # every ray's status equals the reference's (none of these rays meets
+        # a clear aperture within float rounding of its edge: their FP64
+        # statuses do not change when every clear radius grows or shrinks by
+        # 1e-5); landings within 5e-4 mm (measured at most 1.5e-4 mm, the
+        # float32 rounding of a walk in another operation order)
+        np.testing.assert_array_equal(got[:, 4], want[:, 4], err_msg="%s rays_%d status" % (name, k))
         ok = (got[:, 4] == 0) & (want[:, 4] == 0)
         if ok.any():
             d = np.abs(got[ok, :2].astype(np.float64) - want[ok, :2])
-            assert np.median(d) < 1e-3 and np.percentile(d, 99) < 5e-2, (name, k)
+            assert np.median(d) < 1e-4 and d.max() < 5e-4, (name, k, np.median(d), d.max())
             rw = np.abs(got[ok, 3] - want[ok, 3]) / np.maximum(np.abs(want[ok, 3]), 1e-30)
             assert np.median(rw) < 1e-4
         k += 1
