@@ -154,7 +154,11 @@ struct __align__(16) HotRec {
     float ar_scale;                 // 0.25^(ar_layers - 1): the extra AR layers of the SIMPLE model
     int pad;
 };
-enum HotBits { HB_ACTIVE = 1, HB_GENERAL = 2, HB_POLYGON = 4, HB_SIMPLE = 8, HB_ATTEN = 16, HB_IMAGE = 32 };
+// HB_FAST: the common surface — active, untilted sphere or plane, round or
+// elliptical stop, single-layer coating with at least one layer, no
+// attenuator — whose step is one straight-line path behind one test.
+enum HotBits { HB_ACTIVE = 1, HB_GENERAL = 2, HB_POLYGON = 4, HB_SIMPLE = 8, HB_ATTEN = 16, HB_IMAGE = 32,
+               HB_FAST = 64 };
 
 __device__ __forceinline__ HotRec make_hot(const SurfRec& s)
 {
@@ -167,6 +171,7 @@ __device__ __forceinline__ HotRec make_hot(const SurfRec& s)
              ((s.form != 0 || (s.flags & SF_TRANSFORMED)) ? HB_GENERAL : 0) |
              ((s.shape == 1) ? HB_POLYGON : 0) | ((s.coating == 0) ? HB_SIMPLE : 0) |
              ((s.coating == 4) ? HB_ATTEN : 0) | ((s.shape == 2) ? HB_IMAGE : 0);
+    if (h.bits == (HB_ACTIVE | HB_SIMPLE) && s.ar_layers >= 1) h.bits |= HB_FAST;
     h.ar_layers = s.ar_layers;
     h.ar_scale = 1.0f;
     for (int i = 1; i < s.ar_layers; ++i) h.ar_scale *= 0.25f;
@@ -189,11 +194,12 @@ __device__ __forceinline__ HotRec make_hot(const SurfRec& s)
 // cosine); otherwise it is computed here.  The film-TIR fallbacks to the bare
 // Fresnel reflectance are rare: they are taken as warp-uniform branches and
 // selected per lane (every lane of the warp calls this).
-template <bool HAVE_COS2>
+// LAYERED: the caller knows the surface has at least one layer.
+template <bool HAVE_COS2, bool LAYERED = false>
 __device__ __forceinline__ float mgf2_reflectance(float cos_i, float n1, float n2, int layers, float ar_scale,
                                                   float kdelta, float cos_2)
 {
-    if (layers <= 0) return fresnel_reflectance(cos_i, n1, n2);
+    if (!LAYERED && layers <= 0) return fresnel_reflectance(cos_i, n1, n2);
     const float cn = 1.38f;
     const float a1 = n1 * (1.0f / cn);
     const float sin2_c = a1 * a1 * (1.0f - cos_i * cos_i);
@@ -237,6 +243,40 @@ __device__ __forceinline__ float refract_unit(V3& d, V3 nrm, float ci, float n1,
     d = d * nr + nrm * (nr * ci - ct);
     d = d * rsqrtf(d.x * d.x + d.y * d.y + d.z * d.z);
     return ct;
+}
+
+// The step of an HB_FAST surface: the common path of surface_step below with
+// none of its per-kind tests (same arithmetic, same result).
+template <bool WEIGHT>
+__device__ __forceinline__ bool surface_step_fast(V3& o, V3& d, const HotRec& h, float kdelta, float n2,
+                                                  bool reflecting, float reflect_ior, float& cur, float& w,
+                                                  bool alive)
+{
+    const float c = h.c;
+    V3 q;
+    float t;
+    bool ok = alive & sphere_hit(o, d, h.z, c, t, q);
+    const float hx = q.x * h.inv_aspect, hy = q.y;
+    ok = ok & (hx * hx + hy * hy <= h.sa2);
+    V3 nrm = v3(c * q.x, c * q.y, c * q.z - 1.0f);
+    float ci = -dot(nrm, d);
+    if (ci < 0.0f) { nrm = -nrm; ci = -ci; }
+    o = v3(q.x, q.y, q.z + h.z);
+    const float n1 = cur;
+    if (reflecting)
+    {
+        if (WEIGHT) w *= mgf2_reflectance<false, true>(ci, n1, n2, h.ar_layers, h.ar_scale, kdelta, -1.0f);
+        d = d + nrm * (2.0f * ci);
+        d = d * rsqrtf(d.x * d.x + d.y * d.y + d.z * d.z);
+        cur = reflect_ior;
+    }
+    else
+    {
+        const float ct = refract_unit(d, nrm, ci, n1, n2, ok);
+        if (WEIGHT) w *= 1.0f - mgf2_reflectance<true, true>(ci, n1, n2, h.ar_layers, h.ar_scale, kdelta, ct);
+        cur = n2;
+    }
+    return ok;
 }
 
 // One surface interaction on the lane's ray; returns whether the ray lives
@@ -400,7 +440,9 @@ __device__ __forceinline__ void trace_warp(const RenderArgs& A, const SurfRec* l
             n2 = back ? bfl[s] : atl[s];
             const float rior = (back && refl) ? atl[a] : cur;
             // every lane steps (see surface_step); a dead lane's state is not read
-            const bool ok = surface_step<!PROBE>(o, d, hr, lens[s], sp.x, kdelta, n2, refl, rior, cur, w, alive);
+            const bool ok = (hr.bits & HB_FAST)
+                ? surface_step_fast<!PROBE>(o, d, hr, kdelta, n2, refl, rior, cur, w, alive)
+                : surface_step<!PROBE>(o, d, hr, lens[s], sp.x, kdelta, n2, refl, rior, cur, w, alive);
             if (PROBE && alive && !ok) kdead = k;
             alive = ok;
         }
