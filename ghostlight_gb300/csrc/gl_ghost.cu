@@ -436,13 +436,15 @@ __device__ __forceinline__ void trace_warp(const RenderArgs& A, const SurfRec* l
             else if (k < L2) { s = 2 * b - k;        refl = (s == a); back = true; }
             else             { s = a + 1 + (k - L2); refl = false; }
             const HotRec hr = hot[s];
-            if (!(hr.bits & HB_ACTIVE)) continue;
             n2 = back ? bfl[s] : atl[s];
             const float rior = (back && refl) ? atl[a] : cur;
-            // every lane steps (see surface_step); a dead lane's state is not read
-            const bool ok = (hr.bits & HB_FAST)
-                ? surface_step_fast<!PROBE>(o, d, hr, kdelta, n2, refl, rior, cur, w, alive)
-                : surface_step<!PROBE>(o, d, hr, lens[s], sp.x, kdelta, n2, refl, rior, cur, w, alive);
+            // every lane steps (see surface_step); a dead lane's state is not
+            // read; an inactive surface leaves the ray as it is
+            bool ok;
+            if (hr.bits & HB_FAST) ok = surface_step_fast<!PROBE>(o, d, hr, kdelta, n2, refl, rior, cur, w, alive);
+            else if (hr.bits & HB_ACTIVE)
+                ok = surface_step<!PROBE>(o, d, hr, lens[s], sp.x, kdelta, n2, refl, rior, cur, w, alive);
+            else continue;
             if (PROBE && alive && !ok) kdead = k;
             alive = ok;
         }
