@@ -537,16 +537,29 @@ def run_cfg3(args, dev, stream, flush, timed):
     stream.synchronize()
     splan.close()
     bsec, ssec = sum(ts_b) / len(ts_b), sum(ts_s) / len(ts_s)
-    # algorithmic bytes of the bake: pupil read 4 + row-FFT write 8 + column read 8 + PSF write 4
+    # HBM bytes of the bake: pupil read 4 + row-FFT write 8 + column read 8 + PSF write 4
     # + PSF read 4 per grid point, sprite write 12 per coarse texel
     bbytes = SN * SN * 28.0 + 12.0 * (SN // SDS) ** 2
+    # The wavelength bake reads the 16 MB PSF (L2-resident) through L1 with
+    # 4 bilinear 4-byte taps per fine texel and wavelength: its bound is the
+    # L1 load path, not HBM (ncu on the bake kernel: L1 72% busy, 4.09 GB of
+    # L1 loads and 16.8 MB of DRAM reads per launch).  Algorithmic tap bytes:
+    # (SN/ds)^2 coarse texels x ds^2 fine texels x wavelengths x 4 taps x 4 B,
+    # against the nominal L1 load bandwidth (128 B per clock per SM).
+    gbytes = float((SN // SDS) ** 2 * SDS * SDS * N_SPEC * 4 * 4)
+    l1_peak = 152 * 128 * 2.070e9 / 1e9
     sprite_res = {"grid": SN, "ds": SDS, "wavelengths": N_SPEC, "bake_ms": 1e3 * bsec, "splat_ms": 1e3 * ssec,
                   "splat_footprint_px": (2 * srx + 1) ** 2,
-                  "roofline_bake": {"bound": "hbm", "achieved": bbytes / bsec / 1e9, "peak": peaks["hbm_gbs"],
-                                    "unit": "GB/s", "frac": bbytes / bsec / 1e9 / peaks["hbm_gbs"],
-                                    "algorithmic_bytes": bbytes,
-                                    "note": "HBM bytes of the three passes; the wavelength bake's bilinear "
-                                            "gathers (31 x 4 L2 reads per fine texel) take most of the time"}}
+                  "roofline_bake": {"bound": "l1", "achieved": gbytes / bsec / 1e9, "peak": l1_peak,
+                                    "unit": "GB/s", "frac": gbytes / bsec / 1e9 / l1_peak,
+                                    "algorithmic_bytes": gbytes,
+                                    "peak_note": "nominal L1 load bandwidth: 152 SMs x 128 B x 2.07 GHz",
+                                    "hbm": {"bytes": bbytes, "achieved": bbytes / bsec / 1e9,
+                                            "frac": bbytes / bsec / 1e9 / peaks["hbm_gbs"]},
+                                    "note": "the whole bake (two FFT passes + the wavelength bake) is timed; "
+                                            "ncu: the bake kernel's L1 is 72% busy, its 4-byte taps spanning "
+                                            "several 32-byte sectors per warp (4.09 GB moved for 2.08 GB of "
+                                            "taps); HBM carries 1/250 of that"}}
     return {"autotune": tuner.log, "sprite": sprite_res,
             "workload": "512^2 9-blade curved-blade pupil (2 px AA, 0.5%% dust r 1-4 px) -> %d^2, %d wavelengths; "
                         "conv %dx%d x3 (*) %d^2 FP32" % (SB_K, N_SPEC, W, H, CONV_K),
