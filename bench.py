@@ -287,13 +287,8 @@ def run_gpu(args, rank, world):
             if not args.quick:
                 frame_res = run_full_frame(args, dev, stream, timed, plan, plain, sb_inputs, sb_inputs[4])
             sb_inputs[4].close()
-    sec = float(sum(t_batched))
-    if world > 1:
-        t = torch.tensor([sec], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        sec = float(t.item())
+    value, sec = replica_rate(float(sum(t_batched)), args.steps, world, dev)
     frames = args.steps * world
-    value = frames / sec
     ms_step = 1e3 * sec / args.steps
     rays_per_s = traced * frames / sec
     plain_fps = len(t_plain) / sum(t_plain)
@@ -329,6 +324,21 @@ def run_gpu(args, rank, world):
     if frame_res is not None:
         res["full_flare_frame"] = frame_res
     return res, plan, frame_host
+
+
+def replica_rate(sec, steps, world, device=None):
+    """Whole-job frames/s of `world` independent replicas (one rank per GPU,
+    no exchange on the data path): every rank timed `steps` frames in `sec`
+    seconds; the job's time is the slowest rank's (max over ranks, an
+    all-reduce over the initialised process group: NCCL on GPUs, gloo on the
+    host), and the job rendered steps x world frames.  Returns (frames/s,
+    job seconds)."""
+    if world > 1:
+        import torch
+        t = torch.tensor([float(sec)], dtype=torch.float64, device=device)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        sec = float(t.item())
+    return steps * world / sec, sec
 
 
 # ---- configuration 1: the plain small frame ------------------------------------
