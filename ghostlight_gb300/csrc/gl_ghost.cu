@@ -400,7 +400,7 @@ __device__ __forceinline__ void splat_ray(const RenderArgs& A, const PairDev& P,
 
 template <bool PROBE>
 __device__ __forceinline__ void trace_warp(const RenderArgs& A, const SurfRec* lens, const HotRec* hot,
-                                           const float* at, const float* bf, const float4* spec,
+                                           const float2* ab, const float4* spec,
                                            const float* kdel, const PairDev& P, const SourceDev& S,
                                            float2 uv, bool active, float* acc, int pair, int li0, int li1,
                                            int sidx)
@@ -420,8 +420,7 @@ __device__ __forceinline__ void trace_warp(const RenderArgs& A, const SurfRec* l
         ++n_lambda;
         const float4 sp = spec[li];
         const float kdelta = kdel[li];
-        const float* atl = at + li * n;
-        const float* bfl = bf + li * n;
+        const float2* abl = ab + li * n;
         V3 o = v3(uv.x * A.front_R + S.sdx, uv.y * A.front_R + S.sdy, A.start_z);
         V3 d = v3(S.dx, S.dy, S.dz);
         float w = 1.0f, cur = 1.0f;
@@ -436,8 +435,9 @@ __device__ __forceinline__ void trace_warp(const RenderArgs& A, const SurfRec* l
             else if (k < L2) { s = 2 * b - k;        refl = (s == a); back = true; }
             else             { s = a + 1 + (k - L2); refl = false; }
             const HotRec hr = hot[s];
-            n2 = back ? bfl[s] : atl[s];
-            const float rior = (back && refl) ? atl[a] : cur;
+            const float2 io = abl[s];
+            n2 = back ? io.y : io.x;
+            const float rior = (back && refl) ? abl[a].x : cur;
             // every lane steps (see surface_step); a dead lane's state is not
             // read; an inactive surface leaves the ray as it is
             bool ok;
@@ -509,10 +509,11 @@ __global__ void __launch_bounds__(kRenderThreads, kRenderMinBlocks) ghost_render
     extern __shared__ __align__(16) unsigned char smem_raw[];
     HotRec* hot = reinterpret_cast<HotRec*>(smem_raw);
     float4* spec = reinterpret_cast<float4*>(hot + A.n_surf);
-    float* kdel = reinterpret_cast<float*>(spec + A.n_spec);
-    float* at = kdel + A.n_spec;
-    float* bf = at + A.n_spec * A.n_surf;
-    SurfRec* lens = reinterpret_cast<SurfRec*>(bf + A.n_spec * A.n_surf);
+    // per (wavelength, surface): (IOR after the surface, IOR before it), one
+    // 8-byte shared load for either direction of the walk
+    float2* ab = reinterpret_cast<float2*>(spec + A.n_spec);
+    float* kdel = reinterpret_cast<float*>(ab + A.n_spec * A.n_surf);
+    SurfRec* lens = reinterpret_cast<SurfRec*>(kdel + A.n_spec);
     float* acc_base = reinterpret_cast<float*>(lens + A.n_surf);
     const int tid = threadIdx.x;
     float* acc = acc_base + tid * kAccStride;   // 13 floats per lane: conflict-free banks
@@ -528,7 +529,7 @@ __global__ void __launch_bounds__(kRenderThreads, kRenderMinBlocks) ghost_render
             kdel[i] = 2.0f * kPi * 1.38f * (550.0f / (4.0f * 1.38f)) / A.spec[i].x;
         }
         const int nt = A.n_spec * A.n_surf;
-        for (int i = tid; i < nt; i += blockDim.x) { at[i] = A.ior_at[i]; bf[i] = A.ior_bf[i]; }
+        for (int i = tid; i < nt; i += blockDim.x) ab[i] = make_float2(A.ior_at[i], A.ior_bf[i]);
     }
     __syncthreads();
     for (int i = tid; i < A.n_surf; i += blockDim.x) hot[i] = make_hot(lens[i]);
@@ -597,7 +598,7 @@ __global__ void __launch_bounds__(kRenderThreads, kRenderMinBlocks) ghost_render
         int sidx = w.z + lane;
         if (PROBE && A.perm != nullptr && active) sidx = A.perm[(size_t)w.x * A.perm_stride + sidx];
         const float2 uv = active ? A.samples[sidx] : make_float2(0.0f, 0.0f);
-        trace_warp<PROBE>(A, lens, hot, at, bf, spec, kdel, P, S, uv, active, acc, w.x, li0, li1, sidx);
+        trace_warp<PROBE>(A, lens, hot, ab, spec, kdel, P, S, uv, active, acc, w.x, li0, li1, sidx);
     }
 }
 
