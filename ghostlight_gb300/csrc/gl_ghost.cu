@@ -157,8 +157,9 @@ struct __align__(16) HotRec {
 // HB_FAST: the common surface — active, untilted sphere or plane, round or
 // elliptical stop, single-layer coating with at least one layer, no
 // attenuator — whose step is one straight-line path behind one test.
+// HB_ROUND: an HB_FAST surface whose stop is round (aspect 1).
 enum HotBits { HB_ACTIVE = 1, HB_GENERAL = 2, HB_POLYGON = 4, HB_SIMPLE = 8, HB_ATTEN = 16, HB_IMAGE = 32,
-               HB_FAST = 64 };
+               HB_FAST = 64, HB_ROUND = 128 };
 
 __device__ __forceinline__ HotRec make_hot(const SurfRec& s)
 {
@@ -171,7 +172,7 @@ __device__ __forceinline__ HotRec make_hot(const SurfRec& s)
              ((s.form != 0 || (s.flags & SF_TRANSFORMED)) ? HB_GENERAL : 0) |
              ((s.shape == 1) ? HB_POLYGON : 0) | ((s.coating == 0) ? HB_SIMPLE : 0) |
              ((s.coating == 4) ? HB_ATTEN : 0) | ((s.shape == 2) ? HB_IMAGE : 0);
-    if (h.bits == (HB_ACTIVE | HB_SIMPLE) && s.ar_layers >= 1) h.bits |= HB_FAST;
+    if (h.bits == (HB_ACTIVE | HB_SIMPLE) && s.ar_layers >= 1) h.bits |= HB_FAST | (s.aspect == 1.0f ? HB_ROUND : 0);
     h.ar_layers = s.ar_layers;
     h.ar_scale = 1.0f;
     for (int i = 1; i < s.ar_layers; ++i) h.ar_scale *= 0.25f;
@@ -247,16 +248,19 @@ __device__ __forceinline__ float refract_unit(V3& d, V3 nrm, float ci, float n1,
 
 // The step of an HB_FAST surface: the common path of surface_step below with
 // none of its per-kind tests (same arithmetic, same result).
-template <bool WEIGHT>
+// ROUND: the stop is round (no aspect scaling).  reflect_ior is read only
+// on a reflecting step: through ior_a (the IOR after surface a) when the walk
+// runs backward, else it is the current medium.
+template <bool WEIGHT, bool ROUND>
 __device__ __forceinline__ bool surface_step_fast(V3& o, V3& d, const HotRec& h, float kdelta, float n2,
-                                                  bool reflecting, float reflect_ior, float& cur, float& w,
-                                                  bool alive)
+                                                  bool reflecting, bool back, const float2* ior_a, float& cur,
+                                                  float& w, bool alive)
 {
     const float c = h.c;
     V3 q;
     float t;
     bool ok = alive & sphere_hit(o, d, h.z, c, t, q);
-    const float hx = q.x * h.inv_aspect, hy = q.y;
+    const float hx = ROUND ? q.x : q.x * h.inv_aspect, hy = q.y;
     ok = ok & (hx * hx + hy * hy <= h.sa2);
     V3 nrm = v3(c * q.x, c * q.y, c * q.z - 1.0f);
     float ci = -dot(nrm, d);
@@ -268,7 +272,7 @@ __device__ __forceinline__ bool surface_step_fast(V3& o, V3& d, const HotRec& h,
         if (WEIGHT) w *= mgf2_reflectance<false, true>(ci, n1, n2, h.ar_layers, h.ar_scale, kdelta, -1.0f);
         d = d + nrm * (2.0f * ci);
         d = d * rsqrtf(d.x * d.x + d.y * d.y + d.z * d.z);
-        cur = reflect_ior;
+        cur = back ? ior_a->x : cur;
     }
     else
     {
@@ -441,7 +445,10 @@ __device__ __forceinline__ void trace_warp(const RenderArgs& A, const SurfRec* l
             // every lane steps (see surface_step); a dead lane's state is not
             // read; an inactive surface leaves the ray as it is
             bool ok;
-            if (hr.bits & HB_FAST) ok = surface_step_fast<!PROBE>(o, d, hr, kdelta, n2, refl, rior, cur, w, alive);
+            if (hr.bits & HB_ROUND)
+                ok = surface_step_fast<!PROBE, true>(o, d, hr, kdelta, n2, refl, back, abl + a, cur, w, alive);
+            else if (hr.bits & HB_FAST)
+                ok = surface_step_fast<!PROBE, false>(o, d, hr, kdelta, n2, refl, back, abl + a, cur, w, alive);
             else if (hr.bits & HB_ACTIVE)
                 ok = surface_step<!PROBE>(o, d, hr, lens[s], sp.x, kdelta, n2, refl, rior, cur, w, alive);
             else continue;
