@@ -262,21 +262,30 @@ __device__ __forceinline__ bool surface_step_fast(V3& o, V3& d, const HotRec& h,
     bool ok = alive & sphere_hit(o, d, h.z, c, t, q);
     const float hx = ROUND ? q.x : q.x * h.inv_aspect, hy = q.y;
     ok = ok & (hx * hx + hy * hy <= h.sa2);
-    V3 nrm = v3(c * q.x, c * q.y, c * q.z - 1.0f);
-    float ci = -dot(nrm, d);
-    if (ci < 0.0f) { nrm = -nrm; ci = -ci; }
+    // The normal is not turned to oppose the ray: with cr = -nrm.d, ci = |cr|
+    // and sg the sign of cr, reflection d + (sg nrm)(2 ci) = d + nrm (2 cr)
+    // and Snell's nr d + (sg nrm)(nr ci - ct) = nr d + nrm (nr cr - sg ct),
+    // the signs cancelling exactly.
+    const V3 nrm = v3(c * q.x, c * q.y, c * q.z - 1.0f);
+    const float cr = -dot(nrm, d);
+    const float ci = fabsf(cr);
     o = v3(q.x, q.y, q.z + h.z);
     const float n1 = cur;
     if (reflecting)
     {
         if (WEIGHT) w *= mgf2_reflectance<false, true>(ci, n1, n2, h.ar_layers, h.ar_scale, kdelta, -1.0f);
-        d = d + nrm * (2.0f * ci);
+        d = d + nrm * (2.0f * cr);
         d = d * rsqrtf(d.x * d.x + d.y * d.y + d.z * d.z);
         cur = back ? ior_a->x : cur;
     }
     else
     {
-        const float ct = refract_unit(d, nrm, ci, n1, n2, ok);
+        const float nr = n1 / n2;
+        const float s2t = nr * nr * (1.0f - ci * ci);
+        ok = ok & (s2t < 1.0f);
+        const float ct = sqrtf(1.0f - s2t);
+        d = d * nr + nrm * fmaf(nr, cr, cr < 0.0f ? ct : -ct);
+        d = d * rsqrtf(d.x * d.x + d.y * d.y + d.z * d.z);
         if (WEIGHT) w *= 1.0f - mgf2_reflectance<true, true>(ci, n1, n2, h.ar_layers, h.ar_scale, kdelta, ct);
         cur = n2;
     }
