@@ -1267,8 +1267,8 @@ def roofline(res, plan):
 # launch), which the algorithmic count leaves out.
 FLOPS_PER_RAY_LAMBDA = 1063.5
 # DRAM bytes (read + write) of one render launch on this frame, from the same
-# capture (dram__bytes_read.sum + dram__bytes_write.sum: 41.03 + 4.11 MB).
-RENDER_DRAM_BYTES = 45.15e6
+# capture (dram__bytes_read.sum + dram__bytes_write.sum: 40.99 + 4.94 MB).
+RENDER_DRAM_BYTES = 45.93e6
 FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.070e9 / 1e12
 
 
