@@ -205,10 +205,12 @@ extern "C" int gl_gemm_bf16_tc(const void* d_a, const void* d_b, float* d_c, int
 // B' = [hi | lo | hi].  FORM 1 (TF32): FP32 operands, kind::tf32 MMAs.
 // Accumulation is FP32 in TMEM throughout.
 //
-// Complex products: step 2 keeps, per 128 output columns, the three row
-// blocks [-Ti | Tr | Ti] of T' next to each other in shared memory, so one
-// N = 256 MMA against [Tr | Ti] (A = Wr) and one against [-Ti | Tr] (A = Wi)
-// accumulate [Re E | Im E] together.
+// Complex products: T' holds, per 128 output columns, the two row blocks
+// [Tr | Ti]; step 2 stages them next to each other in shared memory and
+// accumulates two products with the same B operand, D1 = Wr [Tr | Ti] and
+// D2 = Wi [Tr | Ti] (N = 2 x tile width each), which its epilogue combines:
+// Re E = Wr Tr - Wi Ti = D1[Tr] - D2[Ti], Im E = Wr Ti + Wi Tr = D1[Ti] +
+// D2[Tr].
 // ===========================================================================
 namespace gl {
 namespace {
@@ -280,9 +282,12 @@ __global__ void __launch_bounds__(kMdftThreads, 1) mdft_kernel(const __grid_cons
                                                               const __grid_constant__ CUtensorMap tB, MdftArgs args)
 {
     static_assert(TN == 128 || TN == 64, "tile width");
-    constexpr int kBBytes = (STEP == 2) ? 3 * TN * 128 : kOpTile;   // B operand bytes per stage
-    constexpr int kStagesM = (STEP == 2) ? (TN == 128 ? 2 : 3) : 4;
+    constexpr int kBBytes = (STEP == 2) ? 2 * TN * 128 : kOpTile;   // B operand bytes per stage
+    constexpr int kStagesM = (STEP == 2) ? (TN == 128 ? 3 : 4) : 4;
     constexpr int kStageBytes = 2 * kOpTile + kBBytes;
+    // accumulator buffers in TMEM's 512 columns: a unit of step 2 takes
+    // 4 TN columns (D1 and D2), so the 128-column tile is single-buffered
+    constexpr int kAccBufs = (STEP == 2 && TN == 128) ? 1 : 2;
     constexpr int kbe = (FORM == 0) ? 64 : 32;                   // reduction elements per 128-byte row
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = align1024(smem_raw);
@@ -354,13 +359,13 @@ __global__ void __launch_bounds__(kMdftThreads, 1) mdft_kernel(const __grid_cons
                     tc::tma_load_2d(st + kOpTile, &tA, x, rowA + args.KA, &full[s]);
                     if (STEP == 2)
                     {
-                        // rows [-Ti | Tr | Ti] of this tile's columns: T' holds them
-                        // in 128-row blocks, a 64-column tile takes one half of each
+                        // rows [Tr | Ti] of this tile's columns: T' holds them in
+                        // 128-row blocks, a 64-column tile takes one half of each
                         const int xb128 = (TN == 128) ? xb : (xb >> 1);
                         const int half = (TN == 128) ? 0 : (xb & 1) * 64;
-                        const int rowB = ((lam * args.NB + xb128) * 3) * 128 + half;
+                        const int rowB = ((lam * args.NB + xb128) * 2) * 128 + half;
                         #pragma unroll
-                        for (int j = 0; j < 3; ++j)
+                        for (int j = 0; j < 2; ++j)
                             tc::tma_load_2d(st + 2 * kOpTile + j * TN * 128, &tB, x, rowB + j * 128, &full[s]);
                     }
                     else
@@ -385,8 +390,8 @@ __global__ void __launch_bounds__(kMdftThreads, 1) mdft_kernel(const __grid_cons
             bool stop = false;
             for (int u = u0; u < u1 && !stop; u += G, ++ui)
             {
-                const int b = ui & 1, ur = ui >> 1;
-                if (ui >= 2 && !tc::mbar_wait(&acc_empty[b], (ur - 1) & 1, err, tc::TC_TIMEOUT_ACC_FREE)) break;
+                const int b = ui % kAccBufs, ur = ui / kAccBufs;
+                if (ui >= kAccBufs && !tc::mbar_wait(&acc_empty[b], (ur - 1) & 1, err, tc::TC_TIMEOUT_ACC_FREE)) break;
                 tc::tc_fence_after();
                 const uint32_t d = tmem + (uint32_t)(b * 256);
                 for (int kb = 0; kb < args.nkb; ++kb, ++it)
@@ -399,13 +404,13 @@ __global__ void __launch_bounds__(kMdftThreads, 1) mdft_kernel(const __grid_cons
                     const uint64_t aI = tc::sw128_desc(tc::smem_u32(st + kOpTile));
                     if (STEP == 2)
                     {
-                        const uint64_t bRI = tc::sw128_desc(tc::smem_u32(st + 2 * kOpTile + TN * 128));   // [Tr | Ti]
-                        const uint64_t bNR = tc::sw128_desc(tc::smem_u32(st + 2 * kOpTile));              // [-Ti | Tr]
+                        // D1 = Wr [Tr | Ti] at d, D2 = Wi [Tr | Ti] at d + 2 TN
+                        const uint64_t bRI = tc::sw128_desc(tc::smem_u32(st + 2 * kOpTile));   // [Tr | Ti]
                         #pragma unroll
                         for (int kk = 0; kk < 4; ++kk)
                         {
                             mma_any<FORM>(d, aR + 2 * kk, bRI + 2 * kk, id2, (kb | kk) != 0);
-                            mma_any<FORM>(d, aI + 2 * kk, bNR + 2 * kk, id2, 1u);
+                            mma_any<FORM>(d + 2 * TN, aI + 2 * kk, bRI + 2 * kk, id2, (kb | kk) != 0);
                         }
                     }
                     else
@@ -437,7 +442,7 @@ __global__ void __launch_bounds__(kMdftThreads, 1) mdft_kernel(const __grid_cons
         {
             int lam, mb, xb;
             decode(u, lam, mb, xb);
-            const int b = ui & 1, ur = ui >> 1;
+            const int b = ui % kAccBufs, ur = ui / kAccBufs;
             const bool ok = tc::mbar_wait(&acc_full[b], ur & 1, err, tc::TC_TIMEOUT_ACC);
             tc::tc_fence_after();
             const uint32_t ta = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(b * 256);
@@ -451,9 +456,18 @@ __global__ void __launch_bounds__(kMdftThreads, 1) mdft_kernel(const __grid_cons
                 #pragma unroll 1
                 for (int c = 0; c < TN / 16; ++c)
                 {
-                    float re[16], im[16];
+                    // Re E = D1[Tr] - D2[Ti], Im E = D1[Ti] + D2[Tr]
+                    float re[16], im[16], u2[16], v2[16];
                     tc::tmem_ld16(ta + (uint32_t)(c * 16), re);
                     tc::tmem_ld16(ta + (uint32_t)TN + (uint32_t)(c * 16), im);
+                    tc::tmem_ld16(ta + (uint32_t)(2 * TN) + (uint32_t)(c * 16), u2);
+                    tc::tmem_ld16(ta + (uint32_t)(3 * TN) + (uint32_t)(c * 16), v2);
+                    #pragma unroll
+                    for (int j = 0; j < 16; ++j)
+                    {
+                        re[j] -= v2[j];
+                        im[j] += u2[j];
+                    }
                     if (!ok || !row_in) continue;
                     const int kc = xb * TN + c * 16;
                     #pragma unroll
@@ -487,9 +501,9 @@ __global__ void __launch_bounds__(kMdftThreads, 1) mdft_kernel(const __grid_cons
             }
             else
             {
-                // T' rows of this k: [-Ti | Tr | Ti] blocks of 128 rows.
+                // T' rows of this k: [Tr | Ti] blocks of 128 rows.
                 const int k = row;
-                const size_t blk = ((size_t)(lam * args.NB + mb) * 3) * 128;
+                const size_t blk = ((size_t)(lam * args.NB + mb) * 2) * 128;
                 #pragma unroll 1
                 for (int c = 0; c < 8; ++c)
                 {
@@ -501,22 +515,19 @@ __global__ void __launch_bounds__(kMdftThreads, 1) mdft_kernel(const __grid_cons
                     if (FORM == 0)
                     {
                         __nv_bfloat16* T = static_cast<__nv_bfloat16*>(args.tprime);
-                        store_split16(T + (blk + 0 * 128 + k) * (size_t)args.Kp, args.n, i0, im, -1.0f);
-                        store_split16(T + (blk + 1 * 128 + k) * (size_t)args.Kp, args.n, i0, re, 1.0f);
-                        store_split16(T + (blk + 2 * 128 + k) * (size_t)args.Kp, args.n, i0, im, 1.0f);
+                        store_split16(T + (blk + 0 * 128 + k) * (size_t)args.Kp, args.n, i0, re, 1.0f);
+                        store_split16(T + (blk + 1 * 128 + k) * (size_t)args.Kp, args.n, i0, im, 1.0f);
                     }
                     else
                     {
                         float* T = static_cast<float*>(args.tprime);
                         float* r0 = T + (blk + 0 * 128 + k) * (size_t)args.Kp + i0;
                         float* r1 = T + (blk + 1 * 128 + k) * (size_t)args.Kp + i0;
-                        float* r2 = T + (blk + 2 * 128 + k) * (size_t)args.Kp + i0;
                         #pragma unroll
                         for (int j = 0; j < 16; j += 4)
                         {
-                            *reinterpret_cast<float4*>(r0 + j) = make_float4(-im[j], -im[j + 1], -im[j + 2], -im[j + 3]);
-                            *reinterpret_cast<float4*>(r1 + j) = make_float4(re[j], re[j + 1], re[j + 2], re[j + 3]);
-                            *reinterpret_cast<float4*>(r2 + j) = make_float4(im[j], im[j + 1], im[j + 2], im[j + 3]);
+                            *reinterpret_cast<float4*>(r0 + j) = make_float4(re[j], re[j + 1], re[j + 2], re[j + 3]);
+                            *reinterpret_cast<float4*>(r1 + j) = make_float4(im[j], im[j + 1], im[j + 2], im[j + 3]);
                         }
                     }
                 }
@@ -942,8 +953,8 @@ extern "C" int gl_mdft_plan_create3(int n, int Kx, int Ky, int n_lambda, const d
     chk(cudaStreamSynchronize(st));
     // shared-memory opt-in once here, so execute enqueues kernels only (graph capture)
     {
-        const int smem1 = 4 * 3 * kOpTile + 1024, smem2 = 2 * 5 * kOpTile + 1024;
-        const int smem2h = 3 * (2 * kOpTile + 3 * 64 * 128) + 1024;
+        const int smem1 = 4 * 3 * kOpTile + 1024, smem2 = 3 * 4 * kOpTile + 1024;
+        const int smem2h = 4 * (2 * kOpTile + 2 * 64 * 128) + 1024;
         if (form == 0)
         {
             chk(cudaFuncSetAttribute(mdft_kernel<0, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem1));
@@ -1041,7 +1052,7 @@ extern "C" int gl_mdft_plan_execute3(gl_mdft_plan* plan, const float* d_pupil, f
     a.weights = p->weights; a.err = p->err;
     a.out_w = out_w; a.x0 = x0; a.y0 = y0; a.win_w = win_w; a.win_h = win_h; a.box = p->box;
     a.tint = tint_rgb ? make_float4(tint_rgb[0], tint_rgb[1], tint_rgb[2], 0.0f) : make_float4(1.0f, 1.0f, 1.0f, 0.0f);
-    const size_t smem1 = 4 * 3 * (size_t)kOpTile + 1024, smem2 = 2 * 5 * (size_t)kOpTile + 1024;
+    const size_t smem1 = 4 * 3 * (size_t)kOpTile + 1024, smem2 = 3 * 4 * (size_t)kOpTile + 1024;
     const int l0 = p->lam0, l1 = p->lam1 < 0 ? p->n_lambda : p->lam1, nl = l1 - l0;
     a.lam_base = l0;
     a.n_units = nl * NBx * NI;                          // step 1: (lambda, k block, pupil-row block)
@@ -1053,7 +1064,7 @@ extern "C" int gl_mdft_plan_execute3(gl_mdft_plan* plan, const float* d_pupil, f
     a2.NBt = p->Kx / p->tile_n;
     a2.n_units = NBy * a2.NBt * nl;                     // step 2: (lambda, output tile)
     const int g2 = std::min(a2.n_units, gmax);
-    const size_t smem2h = 3 * (2 * (size_t)kOpTile + 3 * 64 * 128) + 1024;
+    const size_t smem2h = 4 * (2 * (size_t)kOpTile + 2 * 64 * 128) + 1024;
     if (p->form == 2)
     {
         mdft_simt_step1<<<dim3(NI, NBx, nl), 256, 0, st>>>(static_cast<const float*>(p->wx),
