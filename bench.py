@@ -387,12 +387,17 @@ def run_cfg1(args, dev, stream, timed):
         sb.execute(pupil, outs[0], outs[1], outs[2], stream=stream.cuda_stream, accumulate=True)
     steps, warm = max(args.steps, 10), max(args.warmup, 3)
     t_ghost = timed(g_ghost.replay, steps, warm)
+    stream.synchronize()
+    got = outs.cpu().numpy().astype(np.float64)       # the ghost frame of the last timed replay
     t_frame = timed(g_frame.replay, steps, warm)
     t_sb = timed(lambda: sb.execute(pupil, outs[0], outs[1], outs[2], stream=stream.cuda_stream), steps, warm)
     t_plain = timed(lambda: plain.execute(outs[0], outs[1], outs[2], stream=stream.cuda_stream), steps, warm)
     traced = plan.traced()
     status = sb.status()
+    kept = plan.pair_hits() > 0
     plan.close(); plain.close(); sb.close()
+    # the frame and its inputs, for the FP64 check of the CPU leg (cfg1_parity)
+    _CFG1_CHECK[:] = [lens, pairs[kept], boosts[kept], src, grid, spec, corr, hw, hh, W1, H1, got]
     fps = len(t_ghost) / sum(t_ghost)
     plain_fps = len(t_plain) / sum(t_plain)
     return {"workload": "cfg1: seeded 12-surface double Gauss, %d non-stop-crossing pairs (device culler at "
@@ -403,6 +408,26 @@ def run_cfg1(args, dev, stream, timed):
             "starburst_ms": 1e3 * float(np.median(t_sb)), "starburst_status": status,
             "frame_frames_per_s": len(t_frame) / sum(t_frame),
             "l2": "flushed between timed steps"}
+
+
+_CFG1_CHECK: list = []
+
+
+def cfg1_parity():
+    """The CPU leg's check of the configuration-1 frame the GPU rendered in
+    its timed loop: the FP64 oracle's render of the same kept pairs, grid,
+    spectrum and colour correction; relative L2 and the largest per-pixel
+    error relative to the frame's peak."""
+    from oracle import oracle as O
+    lens, pairs, boosts, src, grid, spec, corr, hw, hh, W1, H1, got = _CFG1_CHECK
+    want = O.render(lens.records(), pairs, boosts, src, [grid], spec, hw, hh, W1, H1, 1000.0, fp64=True,
+                    n_threads=os.cpu_count() or 1)
+    want = np.einsum("ij,jhw->ihw", corr.astype(np.float64), want)
+    rel = float(np.linalg.norm(got - want) / max(np.linalg.norm(want), 1e-300))
+    mx = float(np.abs(got - want).max() / max(float(np.abs(want).max()), 1e-300))
+    return {"rel_l2": rel, "max_err_rel_peak": mx, "tolerance": 1e-3, "pass": rel <= 1e-3,
+            "against": "FP64 oracle, the %d pairs the off-sensor cull kept, 512^2 x 3 planes, same grid / spectral "
+                       "table / colour correction" % len(pairs)}
 
 
 # ---- starburst precision sweep + PSF/veil convolution (cfg3) -----------------
@@ -1223,6 +1248,8 @@ def main():
         lens, cal = _workload()
         if not (args.no_cpu_baseline or args.quick):
             res["cpu_baseline"], res["parity"] = cpu_baseline(plan, lens, cal, gpu_frame)
+            if _CFG1_CHECK and "cfg1" in res:
+                res["cfg1"]["parity"] = cfg1_parity()
             _progress("cpu baseline and FP64 parity")
         if not args.quick:
             res["anamorphic_sweep"] = run_sweep(args)
