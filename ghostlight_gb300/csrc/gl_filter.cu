@@ -51,6 +51,15 @@ bool same_probe(const ProbeOut& x, const ProbeOut& y)
     return std::memcmp(&x, &y, sizeof(ProbeOut)) == 0;
 }
 
+// One out-of-line copy of the trace for both kinds of probe ray: the IEEE
+// general step is large, and the launch is one wave whose time is one
+// divergent trace, so a single copy keeps its code in the instruction cache.
+__device__ __noinline__ TraceOut probe_trace(const SurfRec* lens, int n, const float* at, const float* bf, V3 o,
+                                              float lam, int a, int b)
+{
+    return trace_ghost(lens, n, at, bf, o, v3(0.0f, 0.0f, 1.0f), lam, a, b);
+}
+
 __global__ void __launch_bounds__(kProbeThreads)
 filter_probe_kernel(const SurfRec* __restrict__ recs, int n, const float* __restrict__ ior_at3,
                     const float* __restrict__ ior_bf3, const int2* __restrict__ pairs,
@@ -78,8 +87,7 @@ filter_probe_kernel(const SurfRec* __restrict__ recs, int n, const float* __rest
     ProbeOut* o = out + blockIdx.x;
     if (tid < 3)
     {
-        TraceOut r = trace_ghost(lens, n, at + tid * n, bf + tid * n, v3(0.0f, 0.0f, start_z),
-                                 v3(0.0f, 0.0f, 1.0f), lams[tid], p.x, p.y);
+        TraceOut r = probe_trace(lens, n, at + tid * n, bf + tid * n, v3(0.0f, 0.0f, start_z), lams[tid], p.x, p.y);
         o->w[tid] = r.w;
         o->wok[tid] = (r.status == 0);
     }
@@ -91,8 +99,7 @@ filter_probe_kernel(const SurfRec* __restrict__ recs, int n, const float* __rest
         int good = 0;
         if (!(u * u + v * v > 1.0f))
         {
-            TraceOut r = trace_ghost(lens, n, at + n, bf + n, v3(u * front_R, v * front_R, start_z),
-                                     v3(0.0f, 0.0f, 1.0f), 550.0f, p.x, p.y);
+            TraceOut r = probe_trace(lens, n, at + n, bf + n, v3(u * front_R, v * front_R, start_z), 550.0f, p.x, p.y);
             if (r.status == 0) { px[k] = r.x; py[k] = r.y; good = 1; }
         }
         ok[k] = good;
