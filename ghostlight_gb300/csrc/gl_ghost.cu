@@ -196,10 +196,13 @@ __device__ __forceinline__ HotRec make_hot(const SurfRec& s)
 // Fresnel reflectance are rare: they are taken as warp-uniform branches and
 // selected per lane (every lane of the warp calls this).
 // LAYERED: the caller knows the surface has at least one layer.
+// Returns R before the extra layers' scale, which it leaves in `scale` (1 for
+// the bare Fresnel fallbacks), so a refraction's weight 1 - scale R is one FMA.
 template <bool HAVE_COS2, bool LAYERED = false>
 __device__ __forceinline__ float mgf2_reflectance(float cos_i, float n1, float n2, int layers, float ar_scale,
-                                                  float kdelta, float cos_2)
+                                                  float kdelta, float cos_2, float& scale)
 {
+    scale = 1.0f;
     if (!LAYERED && layers <= 0) return fresnel_reflectance(cos_i, n1, n2);
     const float cn = 1.38f;
     const float a1 = n1 * (1.0f / cn);
@@ -221,11 +224,12 @@ __device__ __forceinline__ float mgf2_reflectance(float cos_i, float n1, float n
     const float x = 2.0f * AC * BD * c2d;
     float R = (AD * AD + CB * CB + x) / (BD * BD + AC * AC + x);
     R = fminf(fmaxf(R, 0.0f), 1.0f);
-    R *= ar_scale;
+    scale = ar_scale;
     if (__any_sync(kFull, bare))
     {
         const float Rb = fresnel_reflectance(cos_i, n1, n2);
         R = bare ? Rb : R;
+        scale = bare ? 1.0f : ar_scale;
     }
     return R;
 }
@@ -273,7 +277,12 @@ __device__ __forceinline__ bool surface_step_fast(V3& o, V3& d, const HotRec& h,
     const float n1 = cur;
     if (reflecting)
     {
-        if (WEIGHT) w *= mgf2_reflectance<false, true>(ci, n1, n2, h.ar_layers, h.ar_scale, kdelta, -1.0f);
+        if (WEIGHT)
+        {
+            float sc;
+            const float R = mgf2_reflectance<false, true>(ci, n1, n2, h.ar_layers, h.ar_scale, kdelta, -1.0f, sc);
+            w *= R * sc;
+        }
         d = d + nrm * (2.0f * cr);
         d = d * rsqrtf(d.x * d.x + d.y * d.y + d.z * d.z);
         cur = back ? ior_a->x : cur;
@@ -286,7 +295,12 @@ __device__ __forceinline__ bool surface_step_fast(V3& o, V3& d, const HotRec& h,
         const float ct = sqrtf(1.0f - s2t);
         d = d * nr + nrm * fmaf(nr, cr, cr < 0.0f ? ct : -ct);
         d = d * rsqrtf(d.x * d.x + d.y * d.y + d.z * d.z);
-        if (WEIGHT) w *= 1.0f - mgf2_reflectance<true, true>(ci, n1, n2, h.ar_layers, h.ar_scale, kdelta, ct);
+        if (WEIGHT)
+        {
+            float sc;
+            const float R = mgf2_reflectance<true, true>(ci, n1, n2, h.ar_layers, h.ar_scale, kdelta, ct, sc);
+            w *= fmaf(-R, sc, 1.0f);
+        }
         cur = n2;
     }
     return ok;
@@ -344,7 +358,12 @@ __device__ __forceinline__ bool surface_step(V3& o, V3& d, const HotRec& h, cons
     {
         if (WEIGHT)
         {
-            if (simple) w *= mgf2_reflectance<false>(ci, n1, n2, h.ar_layers, h.ar_scale, kdelta, -1.0f);
+            if (simple)
+            {
+                float sc;
+                const float R = mgf2_reflectance<false>(ci, n1, n2, h.ar_layers, h.ar_scale, kdelta, -1.0f, sc);
+                w *= R * sc;
+            }
             else if (ok) w *= weight_general(d, nrm, n1, n2, s, lam, true);
             if (h.bits & HB_ATTEN) w *= attenuator_general(hit, s);
         }
@@ -358,7 +377,12 @@ __device__ __forceinline__ bool surface_step(V3& o, V3& d, const HotRec& h, cons
         const float ct = refract_unit(d, nrm, ci, n1, n2, ok);
         if (WEIGHT)
         {
-            if (simple) w *= 1.0f - mgf2_reflectance<true>(ci, n1, n2, h.ar_layers, h.ar_scale, kdelta, ct);
+            if (simple)
+            {
+                float sc;
+                const float R = mgf2_reflectance<true>(ci, n1, n2, h.ar_layers, h.ar_scale, kdelta, ct, sc);
+                w *= fmaf(-R, sc, 1.0f);
+            }
             else if (ok) w *= weight_general(d_in, nrm, n1, n2, s, lam, false);
             if (h.bits & HB_ATTEN) w *= attenuator_general(hit, s);
         }
