@@ -728,6 +728,7 @@ def _serve_mix(args, pool, cfg, sb_on, seconds, dump, budget=SERVE_BUDGET):
     srv.run_trace(warm)
     torch.cuda.synchronize()
     warm_exec = srv.exec
+    warm_exec.close()
     _progress("serving warm-up (starburst %s)" % sb_on)
     srv = FlareServer(pool, budget_bytes=budget, max_inflight=args.serve_slots, items_per_warp=8,
                       policy=args.serve_policy)
@@ -802,6 +803,7 @@ def _serve_mix(args, pool, cfg, sb_on, seconds, dump, budget=SERVE_BUDGET):
     serial_req_s = len(ts) / sum(ts)
     _progress("serving serial sample")
     served_req_s = len(reqs) / wall
+    srv.exec.close()
     if sb_on:
         srv.exec.sprites.close()
     return {"workload": "Poisson %.0f req/s for %.0f s (%d requests), %d resident lenses of 8-30 surfaces, "

@@ -512,6 +512,12 @@ class CudaExecutor:
             return lst.pop()
         return self.torch.empty(shape, dtype=self.torch.float32, pin_memory=True)
 
+    def close(self):
+        """Stop the PSF pre-pass worker (after the pre-passes it holds)."""
+        if self._prep_pool is not None:
+            self._prep_pool.shutdown(wait=True)
+            self._prep_pool = None
+
     def recycle(self, host):
         if host is not None:
             self._pinned[tuple(host.shape)].append(host)
@@ -785,6 +791,11 @@ class FlareServer:
 
     def idle(self) -> bool:
         return not self.running and not self.sched.pending
+
+    def close(self):
+        """Release the executor's host workers (the resident lenses stay)."""
+        if hasattr(self.exec, "close"):
+            self.exec.close()
 
     def run_trace(self, requests: List[FlareRequest], poll_s: float = 2e-4) -> List[FlareRequest]:
         """Replay requests at their arrival times (seconds from now) and
