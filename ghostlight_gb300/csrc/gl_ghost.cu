@@ -89,8 +89,12 @@ __device__ __forceinline__ bool sphere_hit(V3 o, V3 d, float z_s, float c, float
     const float B = c * (px * d.x + py * d.y) - d.z;
     const float C = c * (px * px + py * py);
     const float disc = B * B - A * C;
+    // den = B + sign(B) sqrt(disc) vanishes only when B = 0 and disc = 0,
+    // i.e. A C = 0: A = 0 is a plane, whose B = -d_z, and C = 0 puts the
+    // vertex-plane point on the axis, where B = -d_z too; with |d_z| >= 1e-12
+    // neither can happen, so a live ray never divides by zero here
     const float den = B + copysignf(sqrtf(disc), B);
-    const float ts = (den != 0.0f) ? -C / den : 0.0f;
+    const float ts = -C / den;
     float t = t0 + ts;
     bool ok = (fabsf(d.z) >= 1e-12f) & (disc >= 0.0f);
     const bool near = t > 1e-6f;
