@@ -191,7 +191,7 @@ extern "C" int gl_gemm_bf16_tc(const void* d_a, const void* d_b, float* d_c, int
 
 // ===========================================================================
 // Matrix-DFT starburst, field form:  E_l = W_y(l) A W_x(l)^T,  I_l = |E_l|^2,
-// out_c = sum_l w_c(l) I_l   (the benchmark spec's form of mdft_render.cu's
+// out_c = sum_l w_c(l) I_l   (the field form of mdft_render.cu's
 // per-wavelength triple product, evaluated on the tensor cores).
 //
 //   W_x[k][j] = exp(-2 pi i s_x(l) (j - c_j)(k - c_x)),  same for y.

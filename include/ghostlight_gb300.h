@@ -371,7 +371,7 @@ int gl_ghost_plan_destroy(gl_ghost_plan* plan);
  * mdft_render.cu:137-172).  Synchronous. */
 int gl_gemm_bf16_tc(const void* d_a, const void* d_b, float* d_c, int M, int N, int K, void* stream);
 
-/* Matrix-DFT starburst in field form (the benchmark spec's E = W_y A W_x^T of
+/* Matrix-DFT starburst in field form (E = W_y A W_x^T, the field form of
  * mdft_render.cu's per-wavelength triple product): for each wavelength l,
  *   W_x[k][j] = exp(-2 pi i scale_x[l] (j - (n-1)/2)(k - center_x)),
  *   E_l = W_y A W_x^T  (K_out x K_out),  out_c += weights_rgb[3l+c] |E_l|^2.

@@ -3,7 +3,7 @@
 Field form: E_l = W_y A W_x^T with
 W[k][j] = exp(-2 pi i s_l (j - (n-1)/2)(k - c)), I_l = |E_l|^2,
 out_c = sum_l w_c(l) I_l — the per-wavelength triple product of the
-reference's mdft_render.cu:156-173 in the benchmark spec's field form.  Rows and
+reference's mdft_render.cu:156-173 in its field form.  Rows and
 columns can be restricted to a window so full-size outputs are checked on
 sub-windows.
 """

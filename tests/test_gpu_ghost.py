@@ -1,8 +1,8 @@
 """GPU parity of the flare path: device culler, device trace, batched
 render, against the reference's recorded outputs and the FP64 oracle.
 
-Tolerances (stated by the benchmark spec): ghost set and pupil mask bit-exact;
-FP32 images within 1e-3 relative L2 of the FP64 oracle.
+Tolerances (the flare path's parity bar): ghost set and pupil mask
+bit-exact; FP32 images within 1e-3 relative L2 of the FP64 oracle.
 """
 import numpy as np
 import pytest

@@ -10,7 +10,7 @@ drop-in call surface with nothing precomputed but the lens: the source
 position is solved to a field angle, the ghost set filtered and culled on the
 device, exactly as the reference's render_point_flare does.
 
-Tolerance: relative L2 <= 1e-3 against the golden (the benchmark spec's image
+Tolerance: relative L2 <= 1e-3 against the golden (the flare path's image
 bar); the reference's goldens themselves carry the GPU's atomic-reorder noise
 of < 1 ppm of peak and were stored to 15 mantissa bits (< 3.1e-5 relative).
 A ghost image that misses the bar may do so only by rays that land within
