@@ -944,8 +944,8 @@ def run_sweep(args):
 
 
 def cpu_baseline(plan, lens, cal, gpu_frame):
-    """The CPU leg, timed on the host cores and used as the checker of the
-    timed frame:
+    """The CPU leg, timed on the host cores and used as the FP64 parity
+    reference of the timed frame:
 
     * timing: the reference's own code (oracle/_ref, built from the staged
       reference sources: its filter, grids and trace_ghost_ray in the

@@ -507,10 +507,10 @@ def read_lens(path, images=None) -> Tuple[List[gl_surface], str, float, List[Tup
     major = int(ver.get("major", 0)) if isinstance(ver, dict) else 0
     minor = int(ver.get("minor", 0)) if isinstance(ver, dict) else 0
     if major != LENS_FORMAT_MAJOR:
-        _fail(path, "unsupported lens format major version %d (this build reads version %d only)."
+        _fail(path, "unsupported lens format major version %d (this library reads version %d only)."
               % (major, LENS_FORMAT_MAJOR))
     if minor > LENS_FORMAT_MINOR:
-        warnings.warn("%s: lens format minor version %d is newer than this build understands (%d); unknown "
+        warnings.warn("%s: lens format minor version %d is newer than this library understands (%d); unknown "
                       "fields will be ignored." % (path, minor, LENS_FORMAT_MINOR))
     name, focal = "", f32(0.0)
     meta = j.get("metadata")
@@ -603,7 +603,7 @@ def read_lens(path, images=None) -> Tuple[List[gl_surface], str, float, List[Tup
         tid = K.bake_layers(surfaces, idx, layer_stacks[idx])
         K.reset_coating(surfaces[idx], K.SPECTRAL_ANGULAR, tid)
     for idx, what in notes:
-        warnings.warn("%s: surface %d: %s is not supported by this build" % (path, idx, what))
+        warnings.warn("%s: surface %d: %s is not supported by this library" % (path, idx, what))
     return surfaces, name, float(focal), notes
 
 

@@ -223,7 +223,7 @@ class OpticalSystem:
             self.surfaces.append(s if isinstance(s, Surface) else Surface(s))
         self._calib = None
         self._calib_key = None
-        self.unsupported = []           # (surface index, feature) a lens file used that this build lacks
+        self.unsupported = []           # (surface index, feature) a lens file used that this library lacks
         self.source_path = None
 
     @classmethod

@@ -1,7 +1,7 @@
 /*
  * gl_oracle.c — CPU oracle of the flare path.  TEST INFRASTRUCTURE ONLY: only
  * tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg load it, as
- * the checker; the product never does.
+ * the parity reference; the product never does.
  *
  * gl_oracle_impl.h restates the reference trace (JaydenB/ghostlight
  * ghostlight/src/trace.cpp, trace_core.h, fresnel.h) and is instantiated for

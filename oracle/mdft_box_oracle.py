@@ -1,7 +1,7 @@
 """FP64 restatement of the reference's matrix-DFT starburst engine.
 
-TEST INFRASTRUCTURE ONLY (the checker of the device form; nothing in the
-product imports it).  It follows ghostlight/src/mdft_render.cu:199-340:
+TEST INFRASTRUCTURE ONLY (the parity reference of the device form; nothing
+in the product imports it).  It follows ghostlight/src/mdft_render.cu:199-340:
 
 1. C, the compact pupil autocorrelation: G = fft2(|fft2(A)|^2), the lags
    |l| <= mc = ceil(fill N) + 4 (:233-235) read at (l mod N), conjugated

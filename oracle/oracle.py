@@ -1,7 +1,8 @@
 """ctypes wrapper of the C oracle (oracle/gl_oracle.c).
 
 TEST INFRASTRUCTURE ONLY — used by tests/, __graft_entry__.smoke() and
-bench.py's cpu_baseline leg as the checker / CPU baseline.  The product
+bench.py's cpu_baseline leg as the reference for parity and the CPU
+baseline.  The product
 (ghostlight_gb300) never imports it.
 """
 from __future__ import annotations

@@ -8,8 +8,8 @@ oracle/ref_driver.cpp.  Three things are written to ``--out``:
 
 * ``refgpu_selfcheck.json`` — the sm_103a build against the reference's own
   stored goldens (validation/goldens, recorded with CUDA 13.2), by max
-  difference in ppm of peak, to show that this build of the reference is the
-  reference;
+  difference in ppm of peak, to show that this compile of the reference
+  reproduces the reference;
 * ``refgpu_images.npz`` + ``refgpu_meta.json`` — its images of the seeded
   configuration-1, -2 and -4 lenses with deterministic sampling
   (concentration off), and its veil and starburst layers (matrix-DFT and
